@@ -1,0 +1,220 @@
+/*
+ * sns_gpu.h -- C ABI of libsns_gpu.so, the GB300 (sm_103a) implementation of
+ * the SMR-RK3 time step of NaokiHori/SimpleNavierStokesSolver.
+ *
+ * The structures below have the reference's exact member order and types, so
+ * the reference's own driver, logging, save and statistics code
+ * (src/main.c, src/logging.c, src/save.c, src/statistics/) compiles against
+ * them unchanged. The hot-path entry points keep the reference's names and
+ * signatures; each comment names the reference interface it replaces.
+ *
+ * Ownership and residency. fluid_init / temperature_init allocate the host
+ * arrays of the structure (reference layouts, include/arrays/*.h) and a device
+ * mirror that holds the authoritative state from then on. The hot-path calls
+ * only enqueue GPU work on the solver's CUDA stream; the host arrays are
+ * refreshed by sns_sync_to_host (call it before logging/saving/statistics)
+ * and pushed to the device by sns_sync_to_device (after writing into them,
+ * e.g. when loading a restart).
+ *
+ * Errors. Every int-returning call returns SNS_OK (0) on success and a
+ * nonzero SNS_ERR_* code otherwise (the reference returns 0 unconditionally
+ * and aborts on allocation failure, src/common.c:8-15); sns_last_error()
+ * returns a message. Constructors return NULL on failure.
+ *
+ * Scope: one MPI rank (parallel->mpisize == 1), one GPU, jtot a power of two,
+ * itot >= 2. All arithmetic is IEEE binary64 without contraction, in the
+ * reference's operation order: results equal the reference's bit for bit on
+ * the same host (same libm for the host-side grid set-up).
+ */
+#ifndef SNS_GPU_H
+#define SNS_GPU_H
+
+#include <stdbool.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ types */
+/* include/structure.h:4-7 */
+typedef struct param_t_ param_t;
+typedef struct parallel_t_ parallel_t;
+typedef struct fluid_t_ fluid_t;
+typedef struct temperature_t_ temperature_t;
+
+/* include/param.h:10-13 */
+#define RKSTEPMAX 3
+#define LX 1.
+
+/* include/param.h:15-25 */
+typedef struct rkcoef_t_ {
+  double alpha;
+  double beta;
+  double gamma;
+} rkcoef_t;
+
+typedef struct schedule_t_ {
+  double rate;
+  double after;
+  double next;
+} schedule_t;
+
+/* include/param.h:28-54 (member order and types kept for ABI compatibility) */
+struct param_t_ {
+  bool load_flow_field;
+  char *dirname_restart;
+  bool with_temperature;
+  bool with_thermal_forcing;
+  int itot, jtot;
+  double lx, ly;
+  double stretch;
+  double *xf, *xc;
+  double *dxf, *dxc;
+  double *yf, *yc;
+  double dy;
+  double Ra, Pr;
+  rkcoef_t rkcoefs[3];
+  double time, dt;
+  int step, implicitx, implicity;
+  double expimp_wtimes[2][2];
+  double timemax, wtimemax;
+  schedule_t log, save, stat;
+};
+
+/* include/parallel.h:10-13 */
+struct parallel_t_ {
+  int mpisize, mpirank;
+  int ymrank, yprank;
+};
+
+/* include/fluid.h:8-13 */
+struct fluid_t_ {
+  double *ux, *uy;
+  double *p, *psi;
+  double *srcuxa, *srcuxb, *srcuxg;
+  double *srcuya, *srcuyb, *srcuyg;
+};
+
+/* include/temperature.h:8-12 */
+struct temperature_t_ {
+  double *temp;
+  double *tempforcex;
+  double *srctempa, *srctempb, *srctempg;
+};
+
+/* include/temperature.h:22-23 */
+#define TEMP_XM +0.5
+#define TEMP_XP -0.5
+
+/* ------------------------------------------------------------ status codes */
+#define SNS_OK 0
+#define SNS_ERR_ARG 1         /* NULL or inconsistent argument */
+#define SNS_ERR_UNSUPPORTED 2 /* mpisize != 1, jtot not a power of two, ... */
+#define SNS_ERR_CUDA 3        /* CUDA launch or runtime error */
+#define SNS_ERR_OOM 4         /* device or host allocation failed */
+#define SNS_ERR_STATE 5       /* call out of order (e.g. object already finalised) */
+
+/* ----------------------------------------------- reference hot-path entries */
+/* include/fluid.h:15 (src/fluid/init.c:85-92): allocates the structure, its
+ * host arrays and the device mirror; u = p = 0 with the reference's
+ * boundary values. Restart loading (param->load_flow_field) is not done here:
+ * write the loaded fields into the host arrays and call sns_sync_to_device. */
+extern fluid_t *fluid_init(const param_t *param, const parallel_t *parallel);
+/* include/fluid.h:16 (src/fluid/finalise.c) */
+extern int fluid_finalise(fluid_t *fluid);
+
+/* include/fluid.h:19-21 (src/fluid/boundary_conditions.c:6-55). Apply the
+ * reference's single-rank halo and wall rules in place to the host array
+ * passed (O(itot + jtot) host work). The device copy never stores halo or
+ * wall values (they are implied by index logic in every kernel), so these
+ * calls do not touch the device state. */
+extern int fluid_update_boundaries_ux(const param_t *param, const parallel_t *parallel, double *ux);
+extern int fluid_update_boundaries_uy(const param_t *param, const parallel_t *parallel, double *uy);
+extern int fluid_update_boundaries_p(const param_t *param, const parallel_t *parallel, double *p);
+
+/* include/fluid.h:23 (src/fluid/update_velocity.c:490-498): momentum sources
+ * and RK3 / Crank-Nicolson prediction of ux, uy */
+extern int fluid_update_velocity(const param_t *param, const parallel_t *parallel, const int rkstep,
+                                 fluid_t *fluid, const temperature_t *temperature);
+/* include/fluid.h:24 (src/fluid/compute_potential.c:15-168): Poisson solve for
+ * the scalar potential psi (real DFT along y, tridiagonal along x) */
+extern int fluid_compute_potential(const param_t *param, const parallel_t *parallel, const int rkstep,
+                                   fluid_t *fluid);
+/* include/fluid.h:25 (src/fluid/correct_velocity.c:6-42) */
+extern int fluid_correct_velocity(const param_t *param, const parallel_t *parallel, const int rkstep,
+                                  fluid_t *fluid);
+/* include/fluid.h:26 (src/fluid/update_pressure.c:7-60) */
+extern int fluid_update_pressure(const param_t *param, const parallel_t *parallel, const int rkstep,
+                                 fluid_t *fluid);
+
+/* include/temperature.h:14 (src/temperature/init.c:48-55): linear profile plus
+ * the reference's rand() noise (call srand(0) first, as parallel_init does for
+ * rank 0, src/parallel/init.c:25, to reproduce the reference's initial field) */
+extern temperature_t *temperature_init(const param_t *param, const parallel_t *parallel);
+/* include/temperature.h:15 */
+extern int temperature_finalise(temperature_t *temperature);
+/* include/temperature.h:17 (src/temperature/force.c:6-32): buoyancy from the
+ * current temperature, consumed by the next fluid_update_velocity */
+extern int temperature_compute_force(const param_t *param, const parallel_t *parallel,
+                                     temperature_t *temperature);
+/* include/temperature.h:18 (src/temperature/update.c:233-238) */
+extern int temperature_update_temp(const param_t *param, const parallel_t *parallel, const int rkstep,
+                                   const fluid_t *fluid, temperature_t *temperature);
+/* include/temperature.h:20 (src/temperature/boundary_conditions.c:6-21), same
+ * convention as fluid_update_boundaries_* */
+extern int temperature_update_boundaries_temp(const param_t *param, const parallel_t *parallel,
+                                              double *temp);
+
+/* include/param.h:59 (src/param/decide_dt.c:11-101): advective limit from a
+ * device reduction over ux, uy; diffusive limits and the EXP/IMP choice from
+ * param->expimp_wtimes on the host. Blocks until the reduction is done. */
+extern int param_decide_dt(param_t *param, const parallel_t *parallel, const fluid_t *fluid);
+
+/* ------------------------------------------------------------ sns helpers */
+/* param_t built from arguments instead of environment variables; grid and RK
+ * coefficients as src/param/init.c:124-213 (uniform grid when
+ * stretch >= itot/2, clipped Chebyshev otherwise). expimp_wtimes defaults to
+ * {{1,2},{2,3}} (explicit preferred when dt limits tie). */
+extern param_t *sns_param_create(int itot, int jtot, double ly, double stretch, double Ra, double Pr,
+                                 int with_temperature, int with_thermal_forcing);
+extern int sns_param_destroy(param_t *param);
+/* single-rank parallel_t {1, 0, 0, 0}; also calls srand(0) like
+ * src/parallel/init.c:25 does on rank 0 */
+extern parallel_t *sns_parallel_create(void);
+extern int sns_parallel_destroy(parallel_t *parallel);
+
+/* device -> host arrays (reference layouts, halos filled by the reference's
+ * rules); either pointer may be NULL. Blocks until the copies are done. */
+extern int sns_sync_to_host(const param_t *param, fluid_t *fluid, temperature_t *temperature);
+/* host arrays -> device (interior values are taken; halos are implied) */
+extern int sns_sync_to_device(const param_t *param, fluid_t *fluid, temperature_t *temperature);
+/* waits for all GPU work queued for this fluid's solver */
+extern int sns_synchronize(const fluid_t *fluid);
+/* the CUDA stream (cudaStream_t) the solver enqueues on */
+extern void *sns_stream(const fluid_t *fluid);
+
+/* one full time step's three RK substages (src/main.c:79-101) with the dt and
+ * scheme currently in param, using fused kernels; with_temperature honoured */
+extern int sns_integrate(const param_t *param, const parallel_t *parallel, fluid_t *fluid,
+                         temperature_t *temperature);
+/* nsteps of { param_decide_dt; sns_integrate; step += 1; time += dt }
+ * (src/main.c:28-35 without logging/saving/statistics) */
+extern int sns_run(param_t *param, const parallel_t *parallel, fluid_t *fluid, temperature_t *temperature,
+                   int nsteps);
+
+/* message of the last error on this thread ("" if none) */
+extern const char *sns_last_error(void);
+/* number of kernel launches issued by this process so far */
+extern long long sns_kernel_launches(void);
+/* struct layout as compiled into the library, for binding checks: writes up to
+ * n values -- sizeof(param_t), offsetof(param_t, itot / dy / rkcoefs / time /
+ * dt / step / expimp_wtimes / timemax / log / stat), sizeof(parallel_t),
+ * sizeof(fluid_t), offsetof(fluid_t, srcuyg), sizeof(temperature_t) -- and
+ * returns how many it wrote (15) */
+extern int sns_abi_layout(size_t *out, int n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SNS_GPU_H */

@@ -1,0 +1,135 @@
+"""ctypes binding of libsns_gpu.so (include/sns_gpu.h).
+
+The structures mirror the C layouts exactly (which mirror the reference's
+include/param.h, parallel.h, fluid.h, temperature.h). Loading the library
+needs no GPU; every compute entry point needs one. There is no fallback: if
+the library is missing, importing this module raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import POINTER, c_bool, c_char_p, c_double, c_int, c_longlong, c_size_t, c_void_p
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "_lib", "libsns_gpu.so")
+
+SNS_OK = 0
+SNS_ERR_ARG = 1
+SNS_ERR_UNSUPPORTED = 2
+SNS_ERR_CUDA = 3
+SNS_ERR_OOM = 4
+SNS_ERR_STATE = 5
+
+_PD = POINTER(c_double)
+
+
+class RkCoef(ctypes.Structure):
+    _fields_ = [("alpha", c_double), ("beta", c_double), ("gamma", c_double)]
+
+
+class Schedule(ctypes.Structure):
+    _fields_ = [("rate", c_double), ("after", c_double), ("next", c_double)]
+
+
+class Param(ctypes.Structure):
+    """param_t (include/param.h:28-54 of the reference)."""
+
+    _fields_ = [
+        ("load_flow_field", c_bool), ("dirname_restart", c_char_p),
+        ("with_temperature", c_bool), ("with_thermal_forcing", c_bool),
+        ("itot", c_int), ("jtot", c_int), ("lx", c_double), ("ly", c_double),
+        ("stretch", c_double), ("xf", _PD), ("xc", _PD), ("dxf", _PD), ("dxc", _PD),
+        ("yf", _PD), ("yc", _PD), ("dy", c_double), ("Ra", c_double), ("Pr", c_double),
+        ("rkcoefs", RkCoef * 3), ("time", c_double), ("dt", c_double),
+        ("step", c_int), ("implicitx", c_int), ("implicity", c_int),
+        ("expimp_wtimes", (c_double * 2) * 2), ("timemax", c_double), ("wtimemax", c_double),
+        ("log", Schedule), ("save", Schedule), ("stat", Schedule),
+    ]
+
+
+class Parallel(ctypes.Structure):
+    """parallel_t (include/parallel.h:10-13)."""
+
+    _fields_ = [("mpisize", c_int), ("mpirank", c_int), ("ymrank", c_int), ("yprank", c_int)]
+
+
+class Fluid(ctypes.Structure):
+    """fluid_t (include/fluid.h:8-13)."""
+
+    _fields_ = [("ux", _PD), ("uy", _PD), ("p", _PD), ("psi", _PD),
+                ("srcuxa", _PD), ("srcuxb", _PD), ("srcuxg", _PD),
+                ("srcuya", _PD), ("srcuyb", _PD), ("srcuyg", _PD)]
+
+
+class Temperature(ctypes.Structure):
+    """temperature_t (include/temperature.h:8-12)."""
+
+    _fields_ = [("temp", _PD), ("tempforcex", _PD), ("srctempa", _PD), ("srctempb", _PD), ("srctempg", _PD)]
+
+
+PP, PL, PF, PT = POINTER(Param), POINTER(Parallel), POINTER(Fluid), POINTER(Temperature)
+
+# name -> (restype, argtypes)
+PROTOTYPES = {
+    "fluid_init": (PF, [PP, PL]),
+    "fluid_finalise": (c_int, [PF]),
+    "fluid_update_boundaries_ux": (c_int, [PP, PL, _PD]),
+    "fluid_update_boundaries_uy": (c_int, [PP, PL, _PD]),
+    "fluid_update_boundaries_p": (c_int, [PP, PL, _PD]),
+    "fluid_update_velocity": (c_int, [PP, PL, c_int, PF, PT]),
+    "fluid_compute_potential": (c_int, [PP, PL, c_int, PF]),
+    "fluid_correct_velocity": (c_int, [PP, PL, c_int, PF]),
+    "fluid_update_pressure": (c_int, [PP, PL, c_int, PF]),
+    "temperature_init": (PT, [PP, PL]),
+    "temperature_finalise": (c_int, [PT]),
+    "temperature_compute_force": (c_int, [PP, PL, PT]),
+    "temperature_update_temp": (c_int, [PP, PL, c_int, PF, PT]),
+    "temperature_update_boundaries_temp": (c_int, [PP, PL, _PD]),
+    "param_decide_dt": (c_int, [PP, PL, PF]),
+    "sns_param_create": (PP, [c_int, c_int, c_double, c_double, c_double, c_double, c_int, c_int]),
+    "sns_param_destroy": (c_int, [PP]),
+    "sns_parallel_create": (PL, []),
+    "sns_parallel_destroy": (c_int, [PL]),
+    "sns_sync_to_host": (c_int, [PP, PF, PT]),
+    "sns_sync_to_device": (c_int, [PP, PF, PT]),
+    "sns_synchronize": (c_int, [PF]),
+    "sns_stream": (c_void_p, [PF]),
+    "sns_integrate": (c_int, [PP, PL, PF, PT]),
+    "sns_run": (c_int, [PP, PL, PF, PT, c_int]),
+    "sns_last_error": (c_char_p, []),
+    "sns_kernel_launches": (c_longlong, []),
+    "sns_abi_layout": (c_int, [POINTER(c_size_t), c_int]),
+}
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with simplenavierstokessolver_gb300/build.py "
+                               "(or __graft_entry__.build()); there is no CPU fallback")
+        l = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in PROTOTYPES.items():
+            fn = getattr(l, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = l
+    return _lib
+
+
+def last_error() -> str:
+    return (lib().sns_last_error() or b"").decode(errors="replace")
+
+
+class SnsError(RuntimeError):
+    def __init__(self, code: int, what: str):
+        super().__init__(f"{what} failed with status {code}: {last_error()}")
+        self.code = code
+
+
+def check(code: int, what: str) -> None:
+    if code != SNS_OK:
+        raise SnsError(code, what)

@@ -1,0 +1,776 @@
+// Plain FP64 path of the SMR-RK3 step on GB300 (sm_103a).
+//
+// Compiled with --fmad=false: every expression below is evaluated with the
+// same IEEE binary64 operations, in the same order, as the reference's C
+// (cited per kernel), so results are bit-identical to it. Divisions by grid
+// spacings become multiplications by exact reciprocals only when every such
+// spacing is a power of two (DevGrid::rcp), where both give the same
+// correctly rounded result.
+//
+// On GB300 the FP64 pipe (~0.5 Tops/s) rather than HBM bounds this path, so
+// the kernels minimise FP64 instructions: y-face quantities are carried from
+// row to row by each thread, RHS-independent Thomas factors are precomputed,
+// and the implicit-source terms (exactly zero in the explicit scheme) are not
+// evaluated.
+#include <cfloat>
+#include <cstdint>
+
+#include "sns_internal.h"
+
+namespace sns {
+namespace {
+
+template <bool RCP>
+__device__ __forceinline__ double dv(double a, double d, double rd) {
+  if constexpr (RCP) {
+    return a * rd;
+  } else {
+    return a / d;
+  }
+}
+
+__device__ __forceinline__ int wrap_up(int y, int ny) { return y + 1 == ny ? 0 : y + 1; }
+__device__ __forceinline__ int wrap_dn(int y, int ny) { return y == 0 ? ny - 1 : y - 1; }
+
+constexpr int kRows = 16;  // rows marched by one thread in the stencil kernels
+
+// ---------------------------------------------------------------- temperature
+struct TempArgs {
+  DevGrid g;
+  StageScalars s;
+  const double *t_in;
+  double *t_out, *at, *qt;
+  const double *ux, *uy;
+};
+
+// src/temperature/update.c:11-87 (sources) and :114-122, :221-226 (RK3 update)
+template <int IMPX, int IMPY, bool RCP>
+__global__ void __launch_bounds__(128) k_temp(const TempArgs a) {
+  const int nx = a.g.nx, ny = a.g.ny;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= nx) return;
+  const int y0 = blockIdx.y * kRows;
+  const int y1 = min(y0 + kRows, ny);
+  const double *T = a.t_in;
+  const double dcm = a.g.dxc[x], dcp = a.g.dxc[x + 1], df = a.g.dxf[x];
+  const double rcm = a.g.rdxc[x], rcp = a.g.rdxc[x + 1], rf = a.g.rdxf[x];
+  const double cm = a.g.c_cm[x], cp = a.g.c_cp[x];
+  const double dy = a.g.dy, rdy = a.g.rdy, kappa = a.s.kappa;
+  const bool left = x == 0, right = x == nx - 1;
+  double tc = T[(size_t)y0 * nx + x];
+  // y-face between rows y0-1 and y0 (periodic halo, src/temperature/boundary_conditions.c:13-14)
+  double gym = dv<RCP>(tc - T[(size_t)wrap_dn(y0, ny) * nx + x], dy, rdy);
+  double pym = (0.5 * a.uy[(size_t)y0 * nx + x]) * gym;
+  for (int y = y0; y < y1; ++y) {
+    const int yp = wrap_up(y, ny);
+    const size_t r = (size_t)y * nx + x;
+    const double tp = T[(size_t)yp * nx + x];
+    const double tl = left ? kTempXm : T[r - 1];
+    const double tr = right ? kTempXp : T[r + 1];
+    const double gxm = dv<RCP>(tc - tl, dcm, rcm);
+    const double gxp = dv<RCP>(tr - tc, dcp, rcp);
+    const double gyp = dv<RCP>(tp - tc, dy, rdy);
+    const double pyp = (0.5 * a.uy[(size_t)yp * nx + x]) * gyp;
+    const double uxm = a.ux[r];
+    const double uxp = right ? 0.0 : a.ux[r + 1];
+    const double adv1 = -((cm * uxm) * gxm) - ((cp * uxp) * gxp);
+    const double adv2 = -pym - pyp;
+    const double dif1 = dv<RCP>(kappa * (gxp - gxm), df, rf);
+    const double dif2 = dv<RCP>(kappa * (gyp - gym), dy, rdy);
+    double A = adv1 + adv2;
+    if (!IMPX) A = A + dif1;
+    if (!IMPY) A = A + dif2;
+    double q = a.s.adt * A;
+    if (a.s.has_b) q = q + a.s.bdt * a.at[r];
+    if (IMPX || IMPY) {
+      const double G = (IMPX && IMPY) ? dif1 + dif2 : (IMPX ? dif1 : dif2);
+      q = q + a.s.gdt * G;
+    }
+    a.at[r] = A;
+    if (IMPX || IMPY) {
+      a.qt[r] = q;
+    } else {
+      a.t_out[r] = tc + q;
+    }
+    tc = tp;
+    gym = gyp;
+    pym = pyp;
+  }
+}
+
+// ------------------------------------------------------------------ velocity
+struct VelArgs {
+  DevGrid g;
+  StageScalars s;
+  const double *ux, *uy, *p, *tf;  // tf: temperature the buoyancy is taken from (nullptr: none)
+  double *ux_out, *uy_out, *aux, *auy, *qx, *qy;
+};
+
+// src/fluid/update_velocity.c:11-104 (ux sources), :106-192 (uy sources),
+// :219-230 / :371-381 (RK3 increments) and :436-441 / :580-585 (update).
+template <int IMPX, int IMPY, bool RCP>
+__global__ void __launch_bounds__(128) k_vel(const VelArgs a) {
+  const int nx = a.g.nx, ny = a.g.ny;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= nx) return;
+  const int y0 = blockIdx.y * kRows;
+  const int y1 = min(y0 + kRows, ny);
+  const bool left = x == 0, right = x == nx - 1;
+  const bool has_ux = x >= 1;  // ux is updated for i = 2..itot
+  const double dy = a.g.dy, rdy = a.g.rdy, nu = a.s.nu;
+  // ux at i = x+1: DXF(i-1), DXF(i), DXC(i); uy at i = x+1: DXC(i), DXC(i+1), DXF(i)
+  const double uf_m = has_ux ? a.g.dxf[x - 1] : 1.0, uf_p = a.g.dxf[x], uc_c = a.g.dxc[x];
+  const double ruf_m = has_ux ? a.g.rdxf[x - 1] : 1.0, ruf_p = a.g.rdxf[x], ruc_c = a.g.rdxc[x];
+  const double fm = a.g.c_fm[x], fp = a.g.c_fp[x];
+  const double vc_m = a.g.dxc[x], vc_p = a.g.dxc[x + 1], vf_c = a.g.dxf[x];
+  const double rvc_m = a.g.rdxc[x], rvc_p = a.g.rdxc[x + 1], rvf_c = a.g.rdxf[x];
+  const double cm = a.g.c_cm[x], cp = a.g.c_cp[x];
+  const double *ux = a.ux, *uy = a.uy, *p = a.p;
+
+  const int ym = wrap_dn(y0, ny);
+  const size_t r0 = (size_t)y0 * nx + x, rm = (size_t)ym * nx + x;
+  double u0 = ux[r0], u1 = right ? 0.0 : ux[r0 + 1];
+  double um0 = ux[rm], um1 = right ? 0.0 : ux[rm + 1];
+  double v0 = uy[r0];
+  double vl = left ? 0.0 : uy[r0 - 1];
+  double pm = p[rm];
+  // y-faces between rows y0-1 and y0
+  double gym_u = dv<RCP>(u0 - um0, dy, rdy);
+  double pym_u = 0.0;
+  if (has_ux) pym_u = (0.5 * (fm * vl + fp * v0)) * gym_u;
+  const double vm = uy[rm];
+  double gym_v = dv<RCP>(v0 - vm, dy, rdy);
+  double pym_v = (0.5 * (0.5 * vm + 0.5 * v0)) * gym_v;
+
+  for (int y = y0; y < y1; ++y) {
+    const int yp = wrap_up(y, ny);
+    const size_t r = (size_t)y * nx + x, rp = (size_t)yp * nx + x;
+    const double u0n = ux[rp];
+    const double u1n = right ? 0.0 : ux[rp + 1];
+    const double v0n = uy[rp];
+    const double vln = left ? 0.0 : uy[rp - 1];
+    const double vr = right ? 0.0 : uy[r + 1];
+    const double pc = p[r];
+    // ---- ux(i, j), i = x+1 >= 2
+    if (has_ux) {
+      const double ul = ux[r - 1];
+      const double gxm = dv<RCP>(u0 - ul, uf_m, ruf_m);
+      const double gxp = dv<RCP>(u1 - u0, uf_p, ruf_p);
+      const double gyp = dv<RCP>(u0n - u0, dy, rdy);
+      const double vxm = 0.5 * ul + 0.5 * u0;
+      const double vxp = 0.5 * u0 + 0.5 * u1;
+      const double adv1 = -((fm * vxm) * gxm) - ((fp * vxp) * gxp);
+      const double pyp = (0.5 * (fm * vln + fp * v0n)) * gyp;
+      const double adv2 = -pym_u - pyp;
+      const double dif1 = dv<RCP>(nu * (gxp - gxm), uc_c, ruc_c);
+      const double dif2 = dv<RCP>(nu * (gyp - gym_u), dy, rdy);
+      const double pre = -dv<RCP>(pc - p[r - 1], uc_c, ruc_c);
+      double A = adv1 + adv2;
+      if (!IMPX) A = A + dif1;
+      if (!IMPY) A = A + dif2;
+      if (a.tf) A = A + (0.5 * a.tf[r - 1] + 0.5 * a.tf[r]);
+      double G;
+      if (IMPX && IMPY) {
+        G = (dif1 + dif2) + pre;
+      } else if (IMPX) {
+        G = dif1 + pre;
+      } else if (IMPY) {
+        G = dif2 + pre;
+      } else {
+        G = pre;
+      }
+      double q = a.s.adt * A;
+      if (a.s.has_b) q = q + a.s.bdt * a.aux[r];
+      q = q + a.s.gdt * G;
+      a.aux[r] = A;
+      if (IMPX || IMPY) {
+        a.qx[r] = q;
+      } else {
+        a.ux_out[r] = u0 + q;
+      }
+      gym_u = gyp;
+      pym_u = pyp;
+    }
+    // ---- uy(i, j), i = x+1 >= 1
+    {
+      const double gxm = dv<RCP>(v0 - vl, vc_m, rvc_m);
+      const double gxp = dv<RCP>(vr - v0, vc_p, rvc_p);
+      const double gyp = dv<RCP>(v0n - v0, dy, rdy);
+      const double wxm = 0.5 * um0 + 0.5 * u0;
+      const double wxp = 0.5 * um1 + 0.5 * u1;
+      const double adv1 = -((cm * wxm) * gxm) - ((cp * wxp) * gxp);
+      const double pyp = (0.5 * (0.5 * v0 + 0.5 * v0n)) * gyp;
+      const double adv2 = -pym_v - pyp;
+      const double dif1 = dv<RCP>(nu * (gxp - gxm), vf_c, rvf_c);
+      const double dif2 = dv<RCP>(nu * (gyp - gym_v), dy, rdy);
+      const double pre = -dv<RCP>(pc - pm, dy, rdy);
+      double A = adv1 + adv2;
+      if (!IMPX) A = A + dif1;
+      if (!IMPY) A = A + dif2;
+      double G;
+      if (IMPX && IMPY) {
+        G = (dif1 + dif2) + pre;
+      } else if (IMPX) {
+        G = dif1 + pre;
+      } else if (IMPY) {
+        G = dif2 + pre;
+      } else {
+        G = pre;
+      }
+      double q = a.s.adt * A;
+      if (a.s.has_b) q = q + a.s.bdt * a.auy[r];
+      q = q + a.s.gdt * G;
+      a.auy[r] = A;
+      if (IMPX || IMPY) {
+        a.qy[r] = q;
+      } else {
+        a.uy_out[r] = v0 + q;
+      }
+      gym_v = gyp;
+      pym_v = pyp;
+    }
+    um0 = u0;
+    um1 = u1;
+    u0 = u0n;
+    u1 = u1n;
+    v0 = v0n;
+    vl = vln;
+    pm = pc;
+  }
+}
+
+// ------------------------------------------------------- Crank-Nicolson solves
+// src/linalg.c:9-30 applied per row along x; factors are shared by all rows.
+// mode 0: rows x = 0..nx-1, first row divides by d0 (T: update.c:150-157, uy:
+//         update_velocity.c:509-516)
+// mode 1: ux rows x = 1..nx-1 of the (itot+1)-system whose rows 0 and itot are
+//         identity rows with zero right-hand side (update_velocity.c:249-253)
+__global__ void k_solve_x(int nx, int ny, LineFactors f, int mode, double *q) {
+  const int y = blockIdx.x * blockDim.x + threadIdx.x;
+  if (y >= ny) return;
+  double *row = q + (size_t)y * nx;
+  double prev;
+  int x0;
+  if (mode == 0) {
+    prev = row[0] / f.d0;
+    row[0] = prev;
+    x0 = 1;
+  } else {
+    prev = 0.0;
+    x0 = 1;
+  }
+  for (int x = x0; x < nx; ++x) {
+    double v;
+    if (f.zero[x]) {
+      v = 0.0;
+    } else {
+      v = f.inv[x] * (row[x] - f.l[x] * prev);
+    }
+    row[x] = v;
+    prev = v;
+  }
+  // mode 1: the identity row itot+1 is zero, so row itot-1 is final already
+  const int xlo = mode == 0 ? 0 : 1;
+  double next = prev;
+  for (int x = nx - 2; x >= xlo; --x) {
+    const double v = row[x] - f.up[x] * next;
+    row[x] = v;
+    next = v;
+  }
+}
+
+// src/linalg.c:52-108 applied per column along y (periodic), coalesced across x.
+__global__ void k_solve_y(int nx, int ny, PeriodicFactors f, int first_col, double *q) {
+  const int x = first_col + blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= nx) return;
+  const int n = ny;
+  double *col = q + x;
+  const size_t s = (size_t)nx;
+  const LineFactors &sub = f.sub;
+  double prev = col[0] / sub.d0;
+  col[0] = prev;
+  for (int y = 1; y < n - 1; ++y) {
+    double v;
+    if (sub.zero[y]) {
+      v = 0.0;
+    } else {
+      v = sub.inv[y] * (col[y * s] - sub.l[y] * prev);
+    }
+    col[y * s] = v;
+    prev = v;
+  }
+  double next = prev;
+  for (int y = n - 3; y >= 0; --y) {
+    const double v = col[y * s] - sub.up[y] * next;
+    col[y * s] = v;
+    next = v;
+  }
+  const double q00 = col[0], q0l = col[(size_t)(n - 2) * s];
+  const double last = (col[(size_t)(n - 1) * s] - f.u_last * q00 - f.l_last * q0l) / f.den;
+  col[(size_t)(n - 1) * s] = last;
+  for (int y = 0; y <= n - 2; ++y) col[y * s] = col[y * s] + last * f.q1[y];
+}
+
+__global__ void k_add_increment(int nx, int ny, int kind, const double *in, const double *q, double *out) {
+  const size_t n = (size_t)nx * ny;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < n; k += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(k % nx);
+    if (kind == 1 && x == 0) continue;
+    out[k] = in[k] + q[k];
+  }
+}
+
+// ------------------------------------------------------------------- Poisson
+struct PoissonArgs {
+  DevGrid g;
+  StageScalars s;
+  const double *ux, *uy;
+  double2 *spec;
+  double *psi;
+  int cols;  // x columns per block
+};
+
+// slot of element idx before the in-place decimation-in-time stages: digit
+// reversal over the stage radices (2 first when log2(M) is odd, then 4s)
+__device__ __forceinline__ int fft_slot(int idx, int M, int nst, int first2) {
+  int rest = idx, span = M, slot = 0;
+  for (int s = nst - 1; s >= 0; --s) {
+    if (s == 0 && first2) {
+      span >>= 1;
+      slot += (rest & 1) * span;
+      rest >>= 1;
+    } else {
+      span >>= 2;
+      slot += (rest & 3) * span;
+      rest >>= 2;
+    }
+  }
+  return slot;
+}
+
+// One in-place DIT stage on `cols` columns of length M held in shared memory;
+// the same floating-point operations as dit_stage() of the CPU FFT.
+template <bool FWD>
+__device__ __forceinline__ void fft_stages(double2 *z, int cols, int M, int N, int nst, int first2,
+                                           const double2 *tw) {
+  int L = 1, lg = 0;
+  for (int st = 0; st < nst; ++st) {
+    const int R = (st == 0 && first2) ? 2 : 4;
+    const int span = R * L, tstep = N / span, nb = M / R;
+    for (int b = threadIdx.x; b < cols * nb; b += blockDim.x) {
+      const int c = b / nb, bb = b - c * nb;
+      const int k = bb & (L - 1);
+      const int base = c * M + (bb >> lg) * span + k;
+      double vr[4], vi[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        if (r < R) {
+          const double2 v = z[base + r * L];
+          vr[r] = v.x;
+          vi[r] = v.y;
+        }
+      }
+      if (L > 1) {
+#pragma unroll
+        for (int r = 1; r < 4; ++r) {
+          if (r < R) {
+            const double2 w = tw[r * k * tstep];
+            const double xr = vr[r], xi = vi[r];
+            if (FWD) {
+              vr[r] = xr * w.x - xi * w.y;
+              vi[r] = xr * w.y + xi * w.x;
+            } else {
+              vr[r] = xr * w.x + xi * w.y;
+              vi[r] = xi * w.x - xr * w.y;
+            }
+          }
+        }
+      }
+      if (R == 2) {
+        z[base] = make_double2(vr[0] + vr[1], vi[0] + vi[1]);
+        z[base + L] = make_double2(vr[0] - vr[1], vi[0] - vi[1]);
+      } else {
+        const double t0r = vr[0] + vr[2], t0i = vi[0] + vi[2];
+        const double t1r = vr[0] - vr[2], t1i = vi[0] - vi[2];
+        const double t2r = vr[1] + vr[3], t2i = vi[1] + vi[3];
+        const double t3r = vr[1] - vr[3], t3i = vi[1] - vi[3];
+        const double sr = FWD ? t3i : -t3i;
+        const double si = FWD ? -t3r : t3r;
+        z[base] = make_double2(t0r + t2r, t0i + t2i);
+        z[base + L] = make_double2(t1r + sr, t1i + si);
+        z[base + 2 * L] = make_double2(t0r - t2r, t0i - t2i);
+        z[base + 3 * L] = make_double2(t1r - sr, t1i - si);
+      }
+    }
+    __syncthreads();
+    L *= R;
+    lg += (R == 2) ? 1 : 2;
+  }
+}
+
+// src/fluid/compute_potential.c:69-92: right-hand side (div u*)/(gamma dt)
+// and its real DFT along y (forward, FFTW conventions).
+template <bool RCP>
+__global__ void __launch_bounds__(256) k_poisson_fwd(const PoissonArgs a) {
+  extern __shared__ double2 z[];
+  const int nx = a.g.nx, ny = a.g.ny, M = ny / 2, C = a.cols;
+  const int x0 = blockIdx.x * C;
+  double *zd = reinterpret_cast<double *>(z);
+  const double dy = a.g.dy, rdy = a.g.rdy;
+  for (int e = threadIdx.x; e < C * ny; e += blockDim.x) {
+    const int c = e % C, y = e / C, x = x0 + c;
+    double d = 0.0;
+    if (x < nx) {
+      const size_t r = (size_t)y * nx + x;
+      const double uxm = a.ux[r];
+      const double uxp = x == nx - 1 ? 0.0 : a.ux[r + 1];
+      const double uym = a.uy[r];
+      const double uyp = a.uy[(size_t)wrap_up(y, ny) * nx + x];
+      d = a.s.rgdt * (dv<RCP>(uxp - uxm, a.g.dxf[x], a.g.rdxf[x]) + dv<RCP>(uyp - uym, dy, rdy));
+    }
+    zd[2 * (c * M + fft_slot(y >> 1, M, a.g.fft_nst, a.g.fft_first2)) + (y & 1)] = d;
+  }
+  __syncthreads();
+  const double2 *tw = reinterpret_cast<const double2 *>(a.g.tw);
+  fft_stages<true>(z, C, M, ny, a.g.fft_nst, a.g.fft_first2, tw);
+  const int half = M / 2 + 1;
+  for (int e = threadIdx.x; e < C * half; e += blockDim.x) {
+    const int c = e / half, k = e - c * half, x = x0 + c;
+    if (x >= nx) continue;
+    double2 *out = a.spec + (size_t)x * a.g.jpitch;
+    const double2 *zc = z + c * M;
+    if (k == 0) {
+      const double2 z0 = zc[0];
+      out[0] = make_double2(z0.x + z0.y, 0.0);
+      out[M] = make_double2(z0.x - z0.y, 0.0);
+    } else {
+      const double2 A = zc[k], B = zc[M - k];
+      const double sre = A.x + B.x, dim = A.y - B.y, dre = A.x - B.x, sim = A.y + B.y;
+      const double er = 0.5 * sre, ei = 0.5 * dim;
+      const double orr = 0.5 * sim, oi = -(0.5 * dre);
+      const double2 w = tw[k];
+      const double wor = w.x * orr - w.y * oi;
+      const double woi = w.x * oi + w.y * orr;
+      out[k] = make_double2(er + wor, ei + woi);
+      if (2 * k != M) out[M - k] = make_double2(er - wor, woi - ei);
+    }
+  }
+}
+
+// src/fluid/compute_potential.c:109-136: per Fourier mode, Thomas along x with
+// the complex right-hand side (real and imaginary parts share the factors).
+__global__ void k_poisson_tri(const DevGrid g, double2 *spec) {
+  const int J = blockIdx.x * blockDim.x + threadIdx.x;
+  if (J >= g.nh) return;
+  const int nx = g.nx;
+  const size_t jp = (size_t)g.jpitch;
+  double2 *col = spec + J;
+  const double d0 = g.pd0[J];
+  double2 prev = col[0];
+  prev.x = prev.x / d0;
+  prev.y = prev.y / d0;
+  col[0] = prev;
+  for (int x = 1; x < nx; ++x) {
+    const size_t f = (size_t)x * jp + J;
+    double2 v = col[(size_t)x * jp];
+    if (g.pzero[f]) {
+      v.x = 0.0;
+      v.y = 0.0;
+    } else {
+      const double inv = g.pinv[f], l = g.pl[x];
+      v.x = inv * (v.x - l * prev.x);
+      v.y = inv * (v.y - l * prev.y);
+    }
+    col[(size_t)x * jp] = v;
+    prev = v;
+  }
+  double2 next = prev;
+  for (int x = nx - 2; x >= 0; --x) {
+    const double u = g.pup[(size_t)x * jp + J];
+    double2 v = col[(size_t)x * jp];
+    v.x = v.x - u * next.x;
+    v.y = v.y - u * next.y;
+    col[(size_t)x * jp] = v;
+    next = v;
+  }
+}
+
+// src/fluid/compute_potential.c:146-157: inverse real DFT along y and the
+// 1/jtot normalisation, psi on the interior (halo and walls implied).
+__global__ void __launch_bounds__(256) k_poisson_bwd(const PoissonArgs a) {
+  extern __shared__ double2 z[];
+  const int nx = a.g.nx, ny = a.g.ny, M = ny / 2, C = a.cols;
+  const int x0 = blockIdx.x * C;
+  const double2 *tw = reinterpret_cast<const double2 *>(a.g.tw);
+  const int half = M / 2 + 1;
+  for (int e = threadIdx.x; e < C * half; e += blockDim.x) {
+    const int c = e / half, k = e - c * half, x = x0 + c;
+    double2 *zc = z + c * M;
+    if (x >= nx) {
+      zc[fft_slot(k, M, a.g.fft_nst, a.g.fft_first2)] = make_double2(0.0, 0.0);
+      if (k > 0) zc[fft_slot(M - k, M, a.g.fft_nst, a.g.fft_first2)] = make_double2(0.0, 0.0);
+      continue;
+    }
+    const double2 *in = a.spec + (size_t)x * a.g.jpitch;
+    if (k == 0) {
+      const double x0r = in[0].x, xmr = in[M].x;
+      zc[0] = make_double2(x0r + xmr, x0r - xmr);
+    } else {
+      const double2 A = in[k], B = in[M - k];
+      const double er = A.x + B.x, ei = A.y - B.y, dr = A.x - B.x, di = A.y + B.y;
+      const double2 w = tw[k];
+      const double orr = dr * w.x + di * w.y;
+      const double oi = di * w.x - dr * w.y;
+      zc[fft_slot(k, M, a.g.fft_nst, a.g.fft_first2)] = make_double2(er - oi, ei + orr);
+      if (2 * k != M) zc[fft_slot(M - k, M, a.g.fft_nst, a.g.fft_first2)] = make_double2(er + oi, orr - ei);
+    }
+  }
+  __syncthreads();
+  fft_stages<false>(z, C, M, ny, a.g.fft_nst, a.g.fft_first2, tw);
+  const double *zd = reinterpret_cast<const double *>(z);
+  for (int e = threadIdx.x; e < C * ny; e += blockDim.x) {
+    const int c = e % C, y = e / C, x = x0 + c;
+    if (x >= nx) continue;
+    a.psi[(size_t)y * nx + x] = zd[2 * (c * M + (y >> 1)) + (y & 1)] * a.s.rny;
+  }
+}
+
+// ------------------------------------------------ correction and pressure
+struct CorrArgs {
+  DevGrid g;
+  StageScalars s;
+  const double *psi;
+  double *ux, *uy, *p;
+  unsigned long long *colmax, *uymax;
+};
+
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+  // |v| as an order-preserving key; NaN counts as 0 (fmax(NaN, small) = small
+  // in src/param/decide_dt.c:147,155)
+  const double a = fabs(v);
+  return a == a ? (unsigned long long)__double_as_longlong(a) : 0ull;
+}
+
+// src/fluid/correct_velocity.c:6-42 and src/fluid/update_pressure.c:7-60, per
+// cell in the reference's order; with colmax set, also max |ux| per column and
+// max |uy| for the next src/param/decide_dt.c (exact: division is monotonic).
+template <int IMPX, int IMPY, bool RCP, bool CORR, bool PRES>
+__global__ void __launch_bounds__(128) k_corr(const CorrArgs a) {
+  const int nx = a.g.nx, ny = a.g.ny;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= nx) return;
+  const int y0 = blockIdx.y * kRows;
+  const int y1 = min(y0 + kRows, ny);
+  const double gdt = a.s.gdt, dy = a.g.dy, rdy = a.g.rdy;
+  const double dxi = a.g.dxi[x];
+  const double dcm = a.g.dxc[x], dcp = a.g.dxc[x + 1], df = a.g.dxf[x];
+  const double rcm = a.g.rdxc[x], rcp = a.g.rdxc[x + 1], rf = a.g.rdxf[x];
+  const bool left = x == 0, right = x == nx - 1;
+  const double *psi = a.psi;
+  double sm = psi[(size_t)wrap_dn(y0, ny) * nx + x];
+  unsigned long long mx = 0ull, my = 0ull;
+  for (int y = y0; y < y1; ++y) {
+    const size_t r = (size_t)y * nx + x;
+    const double sc = psi[r];
+    const double sl = left ? sc : psi[r - 1];  // Neumann psi(0) = psi(1)
+    if (CORR) {
+      if (!left) {
+        const double u = a.ux[r] - ((gdt * (sc - sl)) * dxi);
+        a.ux[r] = u;
+        mx = max(mx, abs_bits(u));
+      }
+      const double v = a.uy[r] - dv<RCP>(gdt * (sc - sm), dy, rdy);
+      a.uy[r] = v;
+      my = max(my, abs_bits(v));
+    }
+    if (PRES) {
+      double pv = a.p[r] + sc;
+      if (IMPX) {
+        const double sr = right ? sc : psi[r + 1];  // Neumann psi(nx+1) = psi(nx)
+        const double gm = dv<RCP>(sc - sl, dcm, rcm);
+        const double gp = dv<RCP>(sr - sc, dcp, rcp);
+        pv = pv + a.s.pcorr * dv<RCP>(gp - gm, df, rf);
+      }
+      if (IMPY) {
+        const double sn = psi[(size_t)wrap_up(y, ny) * nx + x];
+        const double gm = dv<RCP>(sc - sm, dy, rdy);
+        const double gp = dv<RCP>(sn - sc, dy, rdy);
+        pv = pv + a.s.pcorr * dv<RCP>(gp - gm, dy, rdy);
+      }
+      a.p[r] = pv;
+    }
+    sm = sc;
+  }
+  if (CORR && a.colmax) {
+    if (!left) atomicMax(a.colmax + x, mx);
+    atomicMax(a.uymax, my);
+  }
+}
+
+__global__ void k_umax(int nx, int ny, const double *ux, const double *uy, unsigned long long *colmax,
+                       unsigned long long *uymax) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= nx) return;
+  const int y0 = blockIdx.y * kRows;
+  const int y1 = min(y0 + kRows, ny);
+  unsigned long long mx = 0ull, my = 0ull;
+  for (int y = y0; y < y1; ++y) {
+    const size_t r = (size_t)y * nx + x;
+    if (x >= 1) mx = max(mx, abs_bits(ux[r]));
+    my = max(my, abs_bits(uy[r]));
+  }
+  if (x >= 1) atomicMax(colmax + x, mx);
+  atomicMax(uymax, my);
+}
+
+dim3 march_grid(const DevGrid &g) { return dim3((g.nx + 127) / 128, (g.ny + kRows - 1) / kRows); }
+
+int poisson_cols(const DevGrid &g) {
+  // enough blocks to cover the SMs at least twice, at most 64 KiB of shared memory each
+  int c = 1;
+  while (c < 16 && (size_t)(2 * c) * g.ny * sizeof(double) <= 65536 && g.nx / (2 * c) >= 304) c *= 2;
+  return c;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------- launches
+cudaError_t launch_temp_update(const DevGrid &g, const StageScalars &s, int impx, int impy,
+                               const double *t_in, double *t_out, double *at, double *qt,
+                               const double *ux, const double *uy, cudaStream_t st) {
+  const TempArgs a{g, s, t_in, t_out, at, qt, ux, uy};
+  const dim3 grid = march_grid(g), block(128);
+#define SNS_T(X, Y, R) k_temp<X, Y, R><<<grid, block, 0, st>>>(a)
+  if (g.rcp) {
+    if (impx && impy) SNS_T(1, 1, true);
+    else if (impx) SNS_T(1, 0, true);
+    else if (impy) SNS_T(0, 1, true);
+    else SNS_T(0, 0, true);
+  } else {
+    if (impx && impy) SNS_T(1, 1, false);
+    else if (impx) SNS_T(1, 0, false);
+    else if (impy) SNS_T(0, 1, false);
+    else SNS_T(0, 0, false);
+  }
+#undef SNS_T
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_velocity_update(const DevGrid &g, const StageScalars &s, int impx, int impy,
+                                   const double *ux, const double *uy, const double *p, const double *tforce,
+                                   double *ux_out, double *uy_out, double *aux, double *auy,
+                                   double *qx, double *qy, cudaStream_t st) {
+  const VelArgs a{g, s, ux, uy, p, tforce, ux_out, uy_out, aux, auy, qx, qy};
+  const dim3 grid = march_grid(g), block(128);
+#define SNS_V(X, Y, R) k_vel<X, Y, R><<<grid, block, 0, st>>>(a)
+  if (g.rcp) {
+    if (impx && impy) SNS_V(1, 1, true);
+    else if (impx) SNS_V(1, 0, true);
+    else if (impy) SNS_V(0, 1, true);
+    else SNS_V(0, 0, true);
+  } else {
+    if (impx && impy) SNS_V(1, 1, false);
+    else if (impx) SNS_V(1, 0, false);
+    else if (impy) SNS_V(0, 1, false);
+    else SNS_V(0, 0, false);
+  }
+#undef SNS_V
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_solve_x(const DevGrid &g, const LineFactors &f, int mode, double *q, cudaStream_t st) {
+  k_solve_x<<<(g.ny + 127) / 128, 128, 0, st>>>(g.nx, g.ny, f, mode, q);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_solve_y(const DevGrid &g, const PeriodicFactors &f, int first_col, double *q, cudaStream_t st) {
+  const int cols = g.nx - first_col;
+  k_solve_y<<<(cols + 127) / 128, 128, 0, st>>>(g.nx, g.ny, f, first_col, q);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_add_increment(const DevGrid &g, int kind, const double *in, const double *q, double *out,
+                                 cudaStream_t st) {
+  const size_t n = (size_t)g.nx * g.ny;
+  const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
+  k_add_increment<<<blocks, 256, 0, st>>>(g.nx, g.ny, kind, in, q, out);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_poisson(const DevGrid &g, const StageScalars &s, const double *ux, const double *uy,
+                           double2 *spec, double *psi, cudaStream_t st) {
+  const int C = poisson_cols(g);
+  const PoissonArgs a{g, s, ux, uy, spec, psi, C};
+  const size_t smem = (size_t)C * g.ny * sizeof(double);
+  const int blocks = (g.nx + C - 1) / C;
+  static bool attr_set = false;
+  if (!attr_set) {
+    const int lim = 160 * 1024;
+    cudaFuncSetAttribute(k_poisson_fwd<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaFuncSetAttribute(k_poisson_fwd<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    cudaFuncSetAttribute(k_poisson_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    attr_set = true;
+  }
+  if (g.rcp) {
+    k_poisson_fwd<true><<<blocks, 256, smem, st>>>(a);
+  } else {
+    k_poisson_fwd<false><<<blocks, 256, smem, st>>>(a);
+  }
+  k_poisson_tri<<<(g.nh + 63) / 64, 64, 0, st>>>(g, spec);
+  k_poisson_bwd<<<blocks, 256, smem, st>>>(a);
+  count_launches(3);
+  return cudaGetLastError();
+}
+
+template <bool CORR, bool PRES>
+static cudaError_t launch_corr_t(const DevGrid &g, const StageScalars &s, int impx, int impy, const double *psi,
+                                 double *ux, double *uy, double *p, unsigned long long *colmax,
+                                 unsigned long long *uymax, cudaStream_t st) {
+  const CorrArgs a{g, s, psi, ux, uy, p, colmax, uymax};
+  const dim3 grid = march_grid(g), block(128);
+#define SNS_C(X, Y, R) k_corr<X, Y, R, CORR, PRES><<<grid, block, 0, st>>>(a)
+  if (g.rcp) {
+    if (impx && impy) SNS_C(1, 1, true);
+    else if (impx) SNS_C(1, 0, true);
+    else if (impy) SNS_C(0, 1, true);
+    else SNS_C(0, 0, true);
+  } else {
+    if (impx && impy) SNS_C(1, 1, false);
+    else if (impx) SNS_C(1, 0, false);
+    else if (impy) SNS_C(0, 1, false);
+    else SNS_C(0, 0, false);
+  }
+#undef SNS_C
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_correct(const DevGrid &g, const StageScalars &s, const double *psi, double *ux, double *uy,
+                           cudaStream_t st) {
+  return launch_corr_t<true, false>(g, s, 0, 0, psi, ux, uy, nullptr, nullptr, nullptr, st);
+}
+
+cudaError_t launch_pressure(const DevGrid &g, const StageScalars &s, int impx, int impy, const double *psi,
+                            double *p, cudaStream_t st) {
+  return launch_corr_t<false, true>(g, s, impx, impy, psi, nullptr, nullptr, p, nullptr, nullptr, st);
+}
+
+cudaError_t launch_correct_pressure(const DevGrid &g, const StageScalars &s, int impx, int impy,
+                                    const double *psi, double *ux, double *uy, double *p,
+                                    unsigned long long *colmax, unsigned long long *uymax, cudaStream_t st) {
+  return launch_corr_t<true, true>(g, s, impx, impy, psi, ux, uy, p, colmax, uymax, st);
+}
+
+cudaError_t launch_umax(const DevGrid &g, const double *ux, const double *uy, unsigned long long *colmax,
+                        unsigned long long *uymax, cudaStream_t st) {
+  k_umax<<<march_grid(g), 128, 0, st>>>(g.nx, g.ny, ux, uy, colmax, uymax);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+}  // namespace sns

@@ -1,0 +1,1174 @@
+// Host side of libsns_gpu.so: the C ABI declared in include/sns_gpu.h.
+//
+// Everything computed here that feeds the kernels (grid metrics, Thomas
+// factors, Poisson eigenvalues, FFT twiddles, RK scalars) uses the
+// reference's expressions in its operation order; this file must be compiled
+// without floating-point contraction (-ffp-contract=off), which the build
+// recipe enforces.
+#include <cfloat>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstddef>
+#include <cstring>
+
+#include <algorithm>
+#include <atomic>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "sns_gpu.h"
+#include "sns_internal.h"
+
+namespace sns {
+
+static std::atomic<long long> g_launches{0};
+void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+static thread_local std::string g_error;
+
+static int fail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_error = buf;
+  return code;
+}
+
+#define SNS_CUDA(call)                                                                       \
+  do {                                                                                       \
+    cudaError_t e_ = (call);                                                                 \
+    if (e_ != cudaSuccess)                                                                   \
+      return fail(SNS_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+constexpr double kPi = 3.1415926535897932;  // include/common.h:7
+constexpr uint64_t kFluidMagic = 0x534e53464c554944ull;  // "SNSFLUID"
+constexpr uint64_t kTempMagic = 0x534e5354454d5045ull;   // "SNSTEMPE"
+
+static bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+static bool is_pow2_double(double v) {
+  if (!(v > 0.0) || !std::isfinite(v)) return false;
+  int e;
+  return std::frexp(v, &e) == 0.5;
+}
+
+// ------------------------------------------------------------------- context
+struct Context {
+  const param_t *param = nullptr;
+  int refs = 0;
+  int nx = 0, ny = 0;
+  cudaStream_t stream = nullptr;
+  DevGrid g{};
+  std::vector<void *> allocs;
+  std::vector<double> dxf, dxc;  // host copies of the reference arrays (0-based)
+  double *staging = nullptr;     // pinned, nx*ny doubles
+  unsigned long long *red_host = nullptr;  // pinned, nx+1 words
+  // factors for the implicit solves: device buffer + host mirror
+  double *fac = nullptr;
+  size_t fac_words = 0;
+};
+
+static std::mutex g_mu;
+static std::vector<Context *> g_contexts;
+
+struct FluidExt {
+  fluid_t pub;  // first member: fluid_t* and FluidExt* coincide
+  uint64_t magic;
+  Context *ctx;
+  Fields f;
+};
+
+struct TempExt {
+  temperature_t pub;
+  uint64_t magic;
+  Context *ctx;
+  TempFields f;
+  int cur;   // buffer holding the current temperature
+  int snap;  // buffer the buoyancy refers to; -1 forcing off, -2 never computed
+};
+
+static FluidExt *as_fluid(const fluid_t *f) {
+  auto *e = reinterpret_cast<FluidExt *>(const_cast<fluid_t *>(f));
+  return (e && e->magic == kFluidMagic) ? e : nullptr;
+}
+static TempExt *as_temp(const temperature_t *t) {
+  auto *e = reinterpret_cast<TempExt *>(const_cast<temperature_t *>(t));
+  return (e && e->magic == kTempMagic) ? e : nullptr;
+}
+
+template <typename T>
+static int dev_alloc(Context *c, T **p, size_t count) {
+  void *ptr = nullptr;
+  cudaError_t e = cudaMalloc(&ptr, std::max<size_t>(count, 1) * sizeof(T));
+  if (e != cudaSuccess) return fail(SNS_ERR_OOM, "cudaMalloc(%zu bytes): %s", count * sizeof(T), cudaGetErrorString(e));
+  c->allocs.push_back(ptr);
+  *p = static_cast<T *>(ptr);
+  return SNS_OK;
+}
+
+template <typename T>
+static int upload(Context *c, const T **dst, const std::vector<T> &src) {
+  T *p = nullptr;
+  if (int rc = dev_alloc(c, &p, src.size())) return rc;
+  SNS_CUDA(cudaMemcpy(p, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
+  *dst = p;
+  return SNS_OK;
+}
+
+// Thomas forward elimination of a constant matrix (src/linalg.c:11-24): the
+// RHS-independent part, stored so that the device repeats only the RHS work.
+static void factorize(int n, const double *l, const double *d, const double *u, double *inv, double *up,
+                      uint8_t *zero) {
+  up[0] = u[0] / d[0];
+  inv[0] = 0.0;
+  zero[0] = 0;
+  for (int i = 1; i <= n - 1; i++) {
+    double v = d[i] - l[i] * up[i - 1];
+    if (std::fabs(v) < DBL_EPSILON) {
+      up[i] = 0.;
+      inv[i] = 0.;
+      zero[i] = 1;
+    } else {
+      v = 1. / v;
+      up[i] = v * u[i];
+      inv[i] = v;
+      zero[i] = 0;
+    }
+  }
+}
+
+// same twiddle rule as the CPU FFT: exp(-2 pi i t/n), exact at multiples of
+// pi/2, libm cos/sin only on [0, pi/4]
+static void twiddle(int n, int t, double *re, double *im) {
+  const long t4 = 4L * t;
+  const long q = t4 / n;
+  const long r = t4 - q * (long)n;
+  double c, s;
+  if (2 * r <= n) {
+    const double a = (3.14159265358979323846 * (double)r) / (2.0 * (double)n);
+    c = std::cos(a);
+    s = std::sin(a);
+  } else {
+    const double a = (3.14159265358979323846 * (double)(n - r)) / (2.0 * (double)n);
+    c = std::sin(a);
+    s = std::cos(a);
+  }
+  double cq, sq;
+  switch (q & 3) {
+    case 0: cq = c; sq = s; break;
+    case 1: cq = -s; sq = c; break;
+    case 2: cq = -c; sq = -s; break;
+    default: cq = s; sq = -c; break;
+  }
+  *re = cq;
+  *im = -sq;
+}
+
+static void destroy_context(Context *c) {
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (void *p : c->allocs) cudaFree(p);
+  c->allocs.clear();
+  if (c->staging) cudaFreeHost(c->staging);
+  if (c->red_host) cudaFreeHost(c->red_host);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+static int build_context(Context *c, const param_t *param) {
+  const int nx = param->itot, ny = param->jtot;
+  c->param = param;
+  c->nx = nx;
+  c->ny = ny;
+  SNS_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  c->dxf.assign(param->dxf, param->dxf + nx);
+  c->dxc.assign(param->dxc, param->dxc + nx + 1);
+  DevGrid &g = c->g;
+  g.nx = nx;
+  g.ny = ny;
+  g.nh = ny / 2 + 1;
+  g.jpitch = (g.nh + 15) / 16 * 16;
+  g.dy = param->dy;
+  bool rcp = is_pow2_double(param->dy);
+  for (double v : c->dxf) rcp = rcp && is_pow2_double(v);
+  for (double v : c->dxc) rcp = rcp && is_pow2_double(v);
+  g.rcp = rcp;
+  g.rdy = 1.0 / param->dy;
+  const double *dxf = param->dxf, *dxc = param->dxc;
+  auto DXF = [&](int i) { return dxf[i - 1]; };
+  auto DXC = [&](int i) { return dxc[i - 1]; };
+  std::vector<double> rdxf(nx), rdxc(nx + 1), dxi(nx + 1), ccm(nx), ccp(nx), cfm(nx), cfp(nx), pl(nx);
+  for (int i = 1; i <= nx; i++) {
+    rdxf[i - 1] = 1.0 / DXF(i);
+    ccm[i - 1] = DXC(i) / (2. * DXF(i));      // src/temperature/update.c:44, update_velocity.c:242
+    ccp[i - 1] = DXC(i + 1) / (2. * DXF(i));  // src/temperature/update.c:45, update_velocity.c:243
+    if (i >= 2) {
+      cfm[i - 1] = DXF(i - 1) / (2. * DXC(i));  // src/fluid/update_velocity.c:148
+      cfp[i - 1] = DXF(i) / (2. * DXC(i));      // src/fluid/update_velocity.c:149
+    }
+    pl[i - 1] = 1. / DXC(i) / DXF(i);  // src/fluid/compute_potential.c:118
+  }
+  for (int i = 1; i <= nx + 1; i++) {
+    rdxc[i - 1] = 1.0 / DXC(i);
+    dxi[i - 1] = 1. / DXC(i);  // src/fluid/correct_velocity.c:13
+  }
+  int rc = SNS_OK;
+  if ((rc = upload(c, &g.dxf, c->dxf)) || (rc = upload(c, &g.dxc, c->dxc)) || (rc = upload(c, &g.rdxf, rdxf)) ||
+      (rc = upload(c, &g.rdxc, rdxc)) || (rc = upload(c, &g.dxi, dxi)) || (rc = upload(c, &g.c_cm, ccm)) ||
+      (rc = upload(c, &g.c_cp, ccp)) || (rc = upload(c, &g.c_fm, cfm)) || (rc = upload(c, &g.c_fp, cfp)) ||
+      (rc = upload(c, &g.pl, pl)))
+    return rc;
+  // Poisson factors per mode J (src/fluid/compute_potential.c:109-127)
+  const int nh = g.nh;
+  const size_t jp = (size_t)g.jpitch;
+  std::vector<double> pinv((size_t)nx * jp, 0.0), pup((size_t)nx * jp, 0.0), pd0(nh);
+  std::vector<uint8_t> pzero((size_t)nx * jp, 0);
+  {
+    std::vector<double> l(nx), d(nx), u(nx), inv(nx), up(nx);
+    std::vector<uint8_t> zero(nx);
+    const double dy = param->dy;
+    for (int J = 0; J < nh; J++) {
+      const double eig = -4. / pow(dy, 2.) * pow(sin(kPi * (J) / (1. * ny)), 2.);
+      for (int i = 1; i <= nx; i++) {
+        l[i - 1] = 1. / DXC(i) / DXF(i);
+        u[i - 1] = 1. / DXC(i + 1) / DXF(i);
+      }
+      for (int i = 1; i <= nx; i++) d[i - 1] = -l[i - 1] - u[i - 1] + eig;
+      d[0] += l[0];
+      d[nx - 1] += u[nx - 1];
+      factorize(nx, l.data(), d.data(), u.data(), inv.data(), up.data(), zero.data());
+      pd0[J] = d[0];
+      for (int x = 0; x < nx; x++) {
+        pinv[(size_t)x * jp + J] = inv[x];
+        pup[(size_t)x * jp + J] = up[x];
+        pzero[(size_t)x * jp + J] = zero[x];
+      }
+    }
+  }
+  if ((rc = upload(c, &g.pinv, pinv)) || (rc = upload(c, &g.pup, pup)) || (rc = upload(c, &g.pzero, pzero)) ||
+      (rc = upload(c, &g.pd0, pd0)))
+    return rc;
+  std::vector<double> tw(2 * (size_t)ny);
+  for (int t = 0; t < ny; t++) twiddle(ny, t, &tw[2 * t], &tw[2 * t + 1]);
+  if ((rc = upload(c, &g.tw, tw))) return rc;
+  int p = 0;
+  while ((1 << p) < ny / 2) p++;
+  g.fft_first2 = p & 1;
+  g.fft_nst = (p & 1) + p / 2;
+  SNS_CUDA(cudaMallocHost(&c->staging, sizeof(double) * (size_t)nx * ny));
+  SNS_CUDA(cudaMallocHost(&c->red_host, sizeof(unsigned long long) * (size_t)(nx + 1)));
+  return SNS_OK;
+}
+
+static int check_inputs(const param_t *param, const parallel_t *parallel) {
+  if (!param || !parallel) return fail(SNS_ERR_ARG, "param and parallel must not be NULL");
+  if (parallel->mpisize != 1)
+    return fail(SNS_ERR_UNSUPPORTED, "single-rank only (mpisize=%d); one GPU holds the whole domain", parallel->mpisize);
+  if (param->itot < 2) return fail(SNS_ERR_UNSUPPORTED, "itot=%d < 2", param->itot);
+  if (param->jtot < 2 || !is_pow2(param->jtot) || param->jtot > 16384)
+    return fail(SNS_ERR_UNSUPPORTED, "jtot=%d must be a power of two in [2, 16384] (real FFT along y)", param->jtot);
+  if (!param->dxf || !param->dxc) return fail(SNS_ERR_ARG, "param grid arrays are NULL");
+  return SNS_OK;
+}
+
+static Context *acquire_context(const param_t *param) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  for (Context *c : g_contexts)
+    if (c->param == param && c->nx == param->itot && c->ny == param->jtot) {
+      c->refs++;
+      return c;
+    }
+  Context *c = new Context();
+  if (build_context(c, param) != SNS_OK) {
+    std::string keep = g_error;
+    destroy_context(c);
+    g_error = keep;
+    return nullptr;
+  }
+  c->refs = 1;
+  g_contexts.push_back(c);
+  return c;
+}
+
+static void release_context(Context *c) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  if (--c->refs > 0) return;
+  g_contexts.erase(std::remove(g_contexts.begin(), g_contexts.end(), c), g_contexts.end());
+  destroy_context(c);
+}
+
+// ------------------------------------------------- host boundary rules
+// single-rank forms of src/fluid/boundary_conditions.c:6-55 and
+// src/temperature/boundary_conditions.c:6-21 on reference-layout host arrays
+static void host_bc_ux(int nx, int ny, double *ux) {
+  auto UX = [&](int i, int j) -> double & { return ux[(size_t)j * (nx + 1) + (i - 1)]; };
+  for (int i = 2; i <= nx; i++) {
+    UX(i, 0) = UX(i, ny);
+    UX(i, ny + 1) = UX(i, 1);
+  }
+  for (int j = 0; j <= ny + 1; j++) {
+    UX(1, j) = 0.;
+    UX(nx + 1, j) = 0.;
+  }
+}
+static void host_bc_uy(int nx, int ny, double *uy) {
+  auto UY = [&](int i, int j) -> double & { return uy[(size_t)j * (nx + 2) + i]; };
+  for (int i = 1; i <= nx; i++) {
+    UY(i, 0) = UY(i, ny);
+    UY(i, ny + 1) = UY(i, 1);
+  }
+  for (int j = 0; j <= ny + 1; j++) {
+    UY(0, j) = 0.;
+    UY(nx + 1, j) = 0.;
+  }
+}
+static void host_bc_p(int nx, int ny, double *p) {
+  auto P = [&](int i, int j) -> double & { return p[(size_t)j * (nx + 2) + i]; };
+  for (int i = 1; i <= nx; i++) {
+    P(i, 0) = P(i, ny);
+    P(i, ny + 1) = P(i, 1);
+  }
+  for (int j = 0; j <= ny + 1; j++) {
+    P(0, j) = P(1, j);
+    P(nx + 1, j) = P(nx, j);
+  }
+}
+static void host_bc_temp(int nx, int ny, double *t) {
+  auto T = [&](int i, int j) -> double & { return t[(size_t)j * (nx + 2) + i]; };
+  for (int i = 1; i <= nx; i++) {
+    T(i, 0) = T(i, ny);
+    T(i, ny + 1) = T(i, 1);
+  }
+  for (int j = 1; j <= ny; j++) {
+    T(0, j) = TEMP_XM;
+    T(nx + 1, j) = TEMP_XP;
+  }
+}
+
+// -------------------------------------------------- dense <-> reference layout
+// dense interior (x fastest, ny rows) from/to a reference-layout array whose
+// rows have `width` entries and whose interior column x sits at offset `off`
+static int fetch(Context *c, const double *dev) {
+  SNS_CUDA(cudaMemcpyAsync(c->staging, dev, sizeof(double) * (size_t)c->nx * c->ny, cudaMemcpyDeviceToHost,
+                           c->stream));
+  SNS_CUDA(cudaStreamSynchronize(c->stream));
+  return SNS_OK;
+}
+
+static int download(Context *c, const double *dev, double *host, int width, int off, int first_x) {
+  const int nx = c->nx, ny = c->ny;
+  if (int rc = fetch(c, dev)) return rc;
+  for (int y = 0; y < ny; y++)
+    std::memcpy(host + (size_t)(y + 1) * width + off + first_x, c->staging + (size_t)y * nx + first_x,
+                sizeof(double) * (nx - first_x));
+  return SNS_OK;
+}
+
+static int upload_field(Context *c, double *dev, const double *host, int width, int off, int first_x) {
+  const int nx = c->nx, ny = c->ny;
+  SNS_CUDA(cudaStreamSynchronize(c->stream));
+  for (int y = 0; y < ny; y++) {
+    double *row = c->staging + (size_t)y * nx;
+    if (first_x > 0) std::memset(row, 0, sizeof(double) * first_x);
+    std::memcpy(row + first_x, host + (size_t)(y + 1) * width + off + first_x, sizeof(double) * (nx - first_x));
+  }
+  SNS_CUDA(cudaMemcpyAsync(dev, c->staging, sizeof(double) * (size_t)nx * ny, cudaMemcpyHostToDevice, c->stream));
+  SNS_CUDA(cudaStreamSynchronize(c->stream));
+  return SNS_OK;
+}
+
+// sources: srcux* rows of itot-1 entries for i = 2..itot, srcuy*/srctemp* rows of itot
+static int download_src(Context *c, const double *dev, double *host, int is_ux) {
+  const int nx = c->nx, ny = c->ny;
+  SNS_CUDA(cudaMemcpyAsync(c->staging, dev, sizeof(double) * (size_t)nx * ny, cudaMemcpyDeviceToHost, c->stream));
+  SNS_CUDA(cudaStreamSynchronize(c->stream));
+  const int w = is_ux ? nx - 1 : nx, x0 = is_ux ? 1 : 0;
+  for (int y = 0; y < ny; y++) std::memcpy(host + (size_t)y * w, c->staging + (size_t)y * nx + x0, sizeof(double) * w);
+  return SNS_OK;
+}
+
+static int upload_src(Context *c, double *dev, const double *host, int is_ux) {
+  const int nx = c->nx, ny = c->ny;
+  SNS_CUDA(cudaStreamSynchronize(c->stream));
+  const int w = is_ux ? nx - 1 : nx, x0 = is_ux ? 1 : 0;
+  for (int y = 0; y < ny; y++) {
+    double *row = c->staging + (size_t)y * nx;
+    if (x0) row[0] = 0.0;
+    std::memcpy(row + x0, host + (size_t)y * w, sizeof(double) * w);
+  }
+  SNS_CUDA(cudaMemcpyAsync(dev, c->staging, sizeof(double) * (size_t)nx * ny, cudaMemcpyHostToDevice, c->stream));
+  SNS_CUDA(cudaStreamSynchronize(c->stream));
+  return SNS_OK;
+}
+
+// -------------------------------------------------------------- RK scalars
+static StageScalars stage_scalars(const param_t *param, int rk) {
+  StageScalars s{};
+  const double alpha = param->rkcoefs[rk].alpha, beta = param->rkcoefs[rk].beta, gamma = param->rkcoefs[rk].gamma;
+  const double dt = param->dt, Ra = param->Ra, Pr = param->Pr;
+  s.adt = alpha * dt;
+  s.bdt = beta * dt;
+  s.gdt = gamma * dt;
+  s.has_b = beta != 0.0;
+  s.kappa = 1. / sqrt(Pr) / sqrt(Ra);  // src/temperature/update.c:65
+  s.nu = sqrt(Pr) / sqrt(Ra);          // src/fluid/update_velocity.c:171
+  s.rgdt = 1. / (gamma * dt);          // src/fluid/compute_potential.c:81
+  s.rny = 1.0 / param->jtot;           // exact: jtot is a power of two
+  const double Re = sqrt(Ra) / sqrt(Pr);  // src/fluid/update_pressure.c:19
+  s.pcorr = -(gamma * dt) / (2. * Re);    // src/fluid/update_pressure.c:37
+  return s;
+}
+
+// ------------------------------------------------- implicit-solve factors
+// Factor buffer layout (doubles): [l | inv | up | zero-as-bytes] per system.
+struct HostFactors {
+  std::vector<double> l, inv, up;
+  std::vector<uint8_t> zero;
+  double d0 = 0;
+};
+
+static void x_system(const param_t *param, int rk, int kind, HostFactors &hf) {
+  // kind 0: temperature (src/temperature/update.c:141-149), n = itot
+  // kind 1: ux (src/fluid/update_velocity.c:249-264), n = itot+1 with identity end rows
+  // kind 2: uy (src/fluid/update_velocity.c:500-508), n = itot
+  const int nx = param->itot;
+  const double *dxf = param->dxf, *dxc = param->dxc;
+  auto DXF = [&](int i) { return dxf[i - 1]; };
+  auto DXC = [&](int i) { return dxc[i - 1]; };
+  const double gamma = param->rkcoefs[rk].gamma, dt = param->dt, Ra = param->Ra, Pr = param->Pr;
+  const int n = kind == 1 ? nx + 1 : nx;
+  std::vector<double> l(n), d(n), u(n);
+  for (int i = 1; i <= n; i++) {
+    if (kind == 1 && (i == 1 || i == nx + 1)) {
+      l[i - 1] = 0.;
+      u[i - 1] = 0.;
+      d[i - 1] = 1.;
+      continue;
+    }
+    double pf, cm, cp;
+    if (kind == 0) {
+      pf = (gamma * dt) / (2. * sqrt(Pr) * sqrt(Ra));
+      cm = 1. / DXF(i) / DXC(i);
+      cp = 1. / DXF(i) / DXC(i + 1);
+    } else if (kind == 1) {
+      pf = (gamma * dt * sqrt(Pr)) / (2. * sqrt(Ra));
+      cm = 1. / DXC(i) / DXF(i - 1);
+      cp = 1. / DXC(i) / DXF(i);
+    } else {
+      pf = (gamma * dt * sqrt(Pr)) / (2. * sqrt(Ra));
+      cm = 1. / DXF(i) / DXC(i);
+      cp = 1. / DXF(i) / DXC(i + 1);
+    }
+    const double c0 = -cm - cp;
+    l[i - 1] = -pf * cm;
+    u[i - 1] = -pf * cp;
+    d[i - 1] = 1. - pf * c0;
+  }
+  hf.l = l;
+  hf.inv.assign(n, 0.);
+  hf.up.assign(n, 0.);
+  hf.zero.assign(n, 0);
+  factorize(n, l.data(), d.data(), u.data(), hf.inv.data(), hf.up.data(), hf.zero.data());
+  hf.d0 = d[0];
+}
+
+// src/linalg.c:52-108 with the constant y matrix of src/temperature/update.c:189-197
+// (temperature, is_temp) or src/fluid/update_velocity.c:404-412 (velocity)
+static void y_system(const param_t *param, int rk, int is_temp, HostFactors &sub, std::vector<double> &q1,
+                     double &l_last, double &u_last, double &den) {
+  const int n = param->jtot;
+  const double gamma = param->rkcoefs[rk].gamma, dt = param->dt, Ra = param->Ra, Pr = param->Pr, dy = param->dy;
+  const double pf = is_temp ? (gamma * dt) / (2. * sqrt(Pr) * sqrt(Ra)) : (gamma * dt * sqrt(Pr)) / (2. * sqrt(Ra));
+  std::vector<double> l(n), d(n), u(n);
+  for (int j = 0; j < n; j++) {
+    const double cm = 1. / dy / dy, cp = 1. / dy / dy;
+    const double c0 = -cm - cp;
+    l[j] = -pf * cm;
+    u[j] = -pf * cp;
+    d[j] = 1. - pf * c0;
+  }
+  const int m = n - 1;
+  sub.l.assign(l.begin(), l.begin() + m);
+  sub.inv.assign(m, 0.);
+  sub.up.assign(m, 0.);
+  sub.zero.assign(m, 0);
+  factorize(m, l.data(), d.data(), u.data(), sub.inv.data(), sub.up.data(), sub.zero.data());
+  sub.d0 = d[0];
+  // second small system: RHS (-l[0], 0, ..., 0, -u[n-2]) (src/linalg.c:75-87), full Thomas
+  q1.assign(m, 0.);
+  for (int i = 0; i < m; i++) q1[i] = i == 0 ? -l[i] : i == m - 1 ? -u[i] : 0.;
+  {
+    std::vector<double> ll(l.begin(), l.begin() + m), dd(d.begin(), d.begin() + m), uu(u.begin(), u.begin() + m);
+    uu[0] = uu[0] / dd[0];
+    q1[0] = q1[0] / dd[0];
+    for (int i = 1; i <= m - 1; i++) {
+      double v = dd[i] - ll[i] * uu[i - 1];
+      if (std::fabs(v) < DBL_EPSILON) {
+        uu[i] = 0.;
+        q1[i] = 0.;
+      } else {
+        v = 1. / v;
+        uu[i] = v * uu[i];
+        q1[i] = v * (q1[i] - ll[i] * q1[i - 1]);
+      }
+    }
+    for (int i = m - 2; i >= 0; i--) q1[i] -= uu[i] * q1[i + 1];
+  }
+  l_last = l[n - 1];
+  u_last = u[n - 1];
+  den = (d[n - 1] + u[n - 1] * q1[0] + l[n - 1] * q1[n - 2]);
+}
+
+// copies factor arrays into the context's device buffer at word offset `off`
+static int push_factors(Context *c, const HostFactors &hf, size_t off, LineFactors &lf) {
+  const size_t n = hf.l.size();
+  std::vector<double> buf(4 * n, 0.0);
+  std::memcpy(&buf[0], hf.l.data(), n * sizeof(double));
+  std::memcpy(&buf[n], hf.inv.data(), n * sizeof(double));
+  std::memcpy(&buf[2 * n], hf.up.data(), n * sizeof(double));
+  std::memcpy(&buf[3 * n], hf.zero.data(), n);
+  SNS_CUDA(cudaMemcpyAsync(c->fac + off, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  lf.n = (int)n;
+  lf.l = c->fac + off;
+  lf.inv = c->fac + off + n;
+  lf.up = c->fac + off + 2 * n;
+  lf.zero = reinterpret_cast<const uint8_t *>(c->fac + off + 3 * n);
+  lf.d0 = hf.d0;
+  return SNS_OK;
+}
+
+static int ensure_factor_buffer(Context *c) {
+  const size_t need = 4 * (size_t)(c->nx + 1) + 5 * (size_t)c->ny + 16;
+  if (c->fac_words >= need) return SNS_OK;
+  if (int rc = dev_alloc(c, &c->fac, need)) return rc;
+  c->fac_words = need;
+  return SNS_OK;
+}
+
+static int implicit_x(Context *c, const param_t *param, int rk, int kind, double *q) {
+  HostFactors hf;
+  x_system(param, rk, kind, hf);
+  LineFactors lf{};
+  if (int rc = push_factors(c, hf, 0, lf)) return rc;
+  SNS_CUDA(launch_solve_x(c->g, lf, kind == 1 ? 1 : 0, q, c->stream));
+  return SNS_OK;
+}
+
+static int implicit_y(Context *c, const param_t *param, int rk, int is_temp, int first_col, double *q) {
+  HostFactors sub;
+  std::vector<double> q1;
+  PeriodicFactors pf{};
+  y_system(param, rk, is_temp, sub, q1, pf.l_last, pf.u_last, pf.den);
+  const size_t off = 4 * (size_t)(c->nx + 1);
+  if (int rc = push_factors(c, sub, off, pf.sub)) return rc;
+  const size_t qoff = off + 4 * sub.l.size();
+  SNS_CUDA(cudaMemcpyAsync(c->fac + qoff, q1.data(), q1.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  pf.q1 = c->fac + qoff;
+  SNS_CUDA(launch_solve_y(c->g, pf, first_col, q, c->stream));
+  return SNS_OK;
+}
+
+static int ensure_implicit_buffers(FluidExt *fe) {
+  Context *c = fe->ctx;
+  const size_t n = (size_t)c->nx * c->ny;
+  if (int rc = ensure_factor_buffer(c)) return rc;
+  if (!fe->f.qx) {
+    if (int rc = dev_alloc(c, &fe->f.qx, n)) return rc;
+    if (int rc = dev_alloc(c, &fe->f.qy, n)) return rc;
+  }
+  return SNS_OK;
+}
+
+// ------------------------------------------------------------ operations
+static int do_temp_update(const param_t *param, int rk, FluidExt *fe, TempExt *te) {
+  Context *c = te->ctx;
+  int out = 0;
+  while (out == te->cur || out == te->snap) out++;
+  const int impx = param->implicitx, impy = param->implicity;
+  const StageScalars s = stage_scalars(param, rk);
+  if (impx || impy) {
+    if (int rc = ensure_factor_buffer(c)) return rc;
+    if (!te->f.qt)
+      if (int rc = dev_alloc(c, &te->f.qt, (size_t)c->nx * c->ny)) return rc;
+  }
+  SNS_CUDA(launch_temp_update(c->g, s, impx, impy, te->f.t[te->cur], te->f.t[out], te->f.at, te->f.qt, fe->f.ux,
+                              fe->f.uy, c->stream));
+  if (impx || impy) {
+    if (impx)
+      if (int rc = implicit_x(c, param, rk, 0, te->f.qt)) return rc;
+    if (impy)
+      if (int rc = implicit_y(c, param, rk, 1, 0, te->f.qt)) return rc;
+    SNS_CUDA(launch_add_increment(c->g, 0, te->f.t[te->cur], te->f.qt, te->f.t[out], c->stream));
+  }
+  te->cur = out;
+  return SNS_OK;
+}
+
+static int do_velocity_update(const param_t *param, int rk, FluidExt *fe, const TempExt *te) {
+  Context *c = fe->ctx;
+  const int impx = param->implicitx, impy = param->implicity;
+  const StageScalars s = stage_scalars(param, rk);
+  if (impx || impy)
+    if (int rc = ensure_implicit_buffers(fe)) return rc;
+  const double *tf = (te && te->snap >= 0) ? te->f.t[te->snap] : nullptr;
+  Fields &f = fe->f;
+  SNS_CUDA(launch_velocity_update(c->g, s, impx, impy, f.ux, f.uy, f.p, tf, f.ux_alt, f.uy_alt, f.aux, f.auy, f.qx,
+                                  f.qy, c->stream));
+  if (impx || impy) {
+    if (impx) {
+      if (int rc = implicit_x(c, param, rk, 1, f.qx)) return rc;
+      if (int rc = implicit_x(c, param, rk, 2, f.qy)) return rc;
+    }
+    if (impy) {
+      if (int rc = implicit_y(c, param, rk, 0, 1, f.qx)) return rc;
+      if (int rc = implicit_y(c, param, rk, 0, 0, f.qy)) return rc;
+    }
+    SNS_CUDA(launch_add_increment(c->g, 1, f.ux, f.qx, f.ux_alt, c->stream));
+    SNS_CUDA(launch_add_increment(c->g, 0, f.uy, f.qy, f.uy_alt, c->stream));
+  }
+  std::swap(f.ux, f.ux_alt);
+  std::swap(f.uy, f.uy_alt);
+  return SNS_OK;
+}
+
+// dt from the reduction results (src/param/decide_dt.c:11-101)
+static void finish_decide_dt(param_t *param, const Context *c) {
+  const double safe_factors[2] = {0.7, 0.9};
+  const int nx = c->nx;
+  const double Ra = param->Ra, Pr = param->Pr;
+  const double diffusivity = fmax(sqrt(Pr) / sqrt(Ra), 1. / sqrt(Pr) / sqrt(Ra));
+  const double lx = param->lx;
+  const double *dxc = param->dxc;
+  const double dy = param->dy;
+  const double small = 1.e-8;
+  double dt_adv = 5.e-2;
+  // min_j DXC(i)/max(|ux(i,j)|, small) = DXC(i)/max(max_j |ux(i,j)|, small):
+  // IEEE division is monotonic in the divisor, so this is the reference's value
+  for (int i = 2; i <= nx; i++) {
+    double m;
+    std::memcpy(&m, &c->red_host[i - 1], sizeof m);
+    const double vel = fmax(m, small);
+    dt_adv = fmin(dt_adv, dxc[i - 1] / vel);
+  }
+  {
+    double m;
+    std::memcpy(&m, &c->red_host[nx], sizeof m);
+    const double vel = fmax(m, small);
+    dt_adv = fmin(dt_adv, dy / vel);
+  }
+  dt_adv *= safe_factors[0];
+  double dx = lx;
+  for (int i = 2; i <= nx; i++) dx = fmin(dx, dxc[i - 1]);
+  double dt_dif_x = 0.25 / diffusivity * pow(dx, 2.);
+  double dt_dif_y = 0.25 / diffusivity * pow(dy, 2.);
+  dt_dif_x *= safe_factors[1];
+  dt_dif_y *= safe_factors[1];
+  double dt = 1.e-2;
+  double optimal_wtime = DBL_MAX;
+  int bx = -1, by = -1;
+  for (int implicity = 0; implicity < 2; implicity++) {
+    for (int implicitx = 0; implicitx < 2; implicitx++) {
+      const double cand = implicitx ? implicity ? dt_adv : fmin(dt_adv, dt_dif_y)
+                                    : implicity ? fmin(dt_adv, dt_dif_x) : fmin(dt_adv, fmin(dt_dif_x, dt_dif_y));
+      const double niter = 1. / cand;
+      const double wtime = param->expimp_wtimes[implicity][implicitx] * niter;
+      if (wtime < optimal_wtime) {
+        dt = cand;
+        optimal_wtime = wtime;
+        bx = implicitx;
+        by = implicity;
+      }
+    }
+  }
+  param->implicitx = bx;
+  param->implicity = by;
+  param->dt = dt;
+}
+
+static int reduce_to_host(Context *c, Fields &f, bool launch) {
+  if (launch) {
+    SNS_CUDA(cudaMemsetAsync(f.colmax, 0, sizeof(unsigned long long) * (c->nx + 1), c->stream));
+    SNS_CUDA(launch_umax(c->g, f.ux, f.uy, f.colmax, f.uymax, c->stream));
+  }
+  SNS_CUDA(cudaMemcpyAsync(c->red_host, f.colmax, sizeof(unsigned long long) * (c->nx + 1), cudaMemcpyDeviceToHost,
+                           c->stream));
+  SNS_CUDA(cudaStreamSynchronize(c->stream));
+  return SNS_OK;
+}
+
+}  // namespace sns
+
+using namespace sns;
+
+// =========================================================== C ABI
+extern "C" {
+
+const char *sns_last_error(void) { return g_error.c_str(); }
+long long sns_kernel_launches(void) { return g_launches.load(); }
+
+int sns_abi_layout(size_t *out, int n) {
+  const size_t v[] = {sizeof(param_t),          offsetof(param_t, itot),    offsetof(param_t, dy),
+                      offsetof(param_t, rkcoefs), offsetof(param_t, time),  offsetof(param_t, dt),
+                      offsetof(param_t, step),  offsetof(param_t, expimp_wtimes), offsetof(param_t, timemax),
+                      offsetof(param_t, log),   offsetof(param_t, stat),    sizeof(parallel_t),
+                      sizeof(fluid_t),          offsetof(fluid_t, srcuyg),  sizeof(temperature_t)};
+  const int m = (int)(sizeof v / sizeof v[0]);
+  for (int k = 0; k < m && k < n; k++) out[k] = v[k];
+  return m;
+}
+
+param_t *sns_param_create(int itot, int jtot, double ly, double stretch_in, double Ra, double Pr,
+                          int with_temperature, int with_thermal_forcing) {
+  if (itot < 2 || jtot < 2) {
+    fail(SNS_ERR_ARG, "itot=%d jtot=%d", itot, jtot);
+    return nullptr;
+  }
+  param_t *param = static_cast<param_t *>(calloc(1, sizeof(param_t)));
+  if (!param) return nullptr;
+  param->load_flow_field = false;
+  param->with_temperature = with_temperature != 0;
+  param->with_thermal_forcing = with_thermal_forcing != 0;
+  param->timemax = 2.0e+2;
+  param->wtimemax = 6.0e+2;
+  param->itot = itot;
+  param->jtot = jtot;
+  param->lx = LX;
+  param->ly = ly;
+  param->stretch = stretch_in;
+  param->Ra = Ra;
+  param->Pr = Pr;
+  // src/param/init.c:124-195
+  param->xf = static_cast<double *>(calloc(itot + 1, sizeof(double)));
+  param->xc = static_cast<double *>(calloc(itot + 2, sizeof(double)));
+  param->dxf = static_cast<double *>(calloc(itot, sizeof(double)));
+  param->dxc = static_cast<double *>(calloc(itot + 1, sizeof(double)));
+  param->yf = static_cast<double *>(calloc(jtot + 1, sizeof(double)));
+  param->yc = static_cast<double *>(calloc(jtot, sizeof(double)));
+  double *xf = param->xf, *xc = param->xc, *dxf = param->dxf, *dxc = param->dxc;
+  const double lx = param->lx;
+  int stretch = (int)param->stretch;
+  if (stretch < 0) stretch = 0;
+  if (stretch >= itot / 2) {
+    const double dx = lx / itot;
+    for (int i = 1; i <= itot + 1; i++) xf[i - 1] = 1. * (i - 1) * dx;
+  } else {
+    for (int i = 1; i <= itot + 1; i++) xf[i - 1] = cos(kPi * (1. * (i - 1) + stretch) / (itot + 2. * stretch));
+    const double mn = xf[0], mx = xf[itot];
+    for (int i = 1; i <= itot + 1; i++) xf[i - 1] = lx * (xf[i - 1] - mn) / (mx - mn);
+  }
+  xf[0] = 0.;
+  xf[itot] = lx;
+  for (int i = 1; i <= itot; i++) dxf[i - 1] = xf[i] - xf[i - 1];
+  xc[0] = xf[0];
+  for (int i = 1; i <= itot; i++) xc[i] = 0.5 * (xf[i - 1] + xf[i]);
+  xc[itot + 1] = xf[itot];
+  for (int i = 1; i <= itot + 1; i++) dxc[i - 1] = xc[i] - xc[i - 1];
+  param->dy = ly / jtot;
+  for (int j = 1; j <= jtot + 1; j++) param->yf[j - 1] = 1. * (j - 1) * param->dy;
+  for (int j = 1; j <= jtot; j++) param->yc[j - 1] = 0.5 * (2 * j - 1) * param->dy;
+  // src/param/init.c:197-213
+  param->rkcoefs[0].alpha = 32. / 60.;
+  param->rkcoefs[0].beta = 0. / 60.;
+  param->rkcoefs[1].alpha = 25. / 60.;
+  param->rkcoefs[1].beta = -17. / 60.;
+  param->rkcoefs[2].alpha = 45. / 60.;
+  param->rkcoefs[2].beta = -25. / 60.;
+  for (int rk = 0; rk < RKSTEPMAX; rk++) param->rkcoefs[rk].gamma = param->rkcoefs[rk].alpha + param->rkcoefs[rk].beta;
+  param->expimp_wtimes[0][0] = 1.;
+  param->expimp_wtimes[0][1] = 2.;
+  param->expimp_wtimes[1][0] = 2.;
+  param->expimp_wtimes[1][1] = 3.;
+  return param;
+}
+
+int sns_param_destroy(param_t *param) {
+  if (!param) return SNS_OK;
+  free(param->xf);
+  free(param->xc);
+  free(param->dxf);
+  free(param->dxc);
+  free(param->yf);
+  free(param->yc);
+  free(param);
+  return SNS_OK;
+}
+
+parallel_t *sns_parallel_create(void) {
+  parallel_t *p = static_cast<parallel_t *>(calloc(1, sizeof(parallel_t)));
+  if (!p) return nullptr;
+  p->mpisize = 1;
+  p->mpirank = 0;
+  p->ymrank = 0;
+  p->yprank = 0;
+  srand(0);  // src/parallel/init.c:25 on rank 0
+  return p;
+}
+
+int sns_parallel_destroy(parallel_t *parallel) {
+  free(parallel);
+  return SNS_OK;
+}
+
+fluid_t *fluid_init(const param_t *param, const parallel_t *parallel) {
+  if (check_inputs(param, parallel) != SNS_OK) return nullptr;
+  Context *c = acquire_context(param);
+  if (!c) return nullptr;
+  FluidExt *fe = static_cast<FluidExt *>(calloc(1, sizeof(FluidExt)));
+  const int nx = param->itot, ny = param->jtot;
+  const size_t nu = (size_t)(nx + 1) * (ny + 2), nc = (size_t)(nx + 2) * (ny + 2);
+  const size_t sx = (size_t)(nx - 1) * ny, sc = (size_t)nx * ny;
+  fe->magic = kFluidMagic;
+  fe->ctx = c;
+  fluid_t &h = fe->pub;
+  h.ux = static_cast<double *>(calloc(nu, sizeof(double)));
+  h.uy = static_cast<double *>(calloc(nc, sizeof(double)));
+  h.p = static_cast<double *>(calloc(nc, sizeof(double)));
+  h.psi = static_cast<double *>(calloc(nc, sizeof(double)));
+  h.srcuxa = static_cast<double *>(calloc(sx, sizeof(double)));
+  h.srcuxb = static_cast<double *>(calloc(sx, sizeof(double)));
+  h.srcuxg = static_cast<double *>(calloc(sx, sizeof(double)));
+  h.srcuya = static_cast<double *>(calloc(sc, sizeof(double)));
+  h.srcuyb = static_cast<double *>(calloc(sc, sizeof(double)));
+  h.srcuyg = static_cast<double *>(calloc(sc, sizeof(double)));
+  Fields &f = fe->f;
+  const size_t n = sc;
+  int rc = SNS_OK;
+  if ((rc = dev_alloc(c, &f.ux, n)) || (rc = dev_alloc(c, &f.uy, n)) || (rc = dev_alloc(c, &f.ux_alt, n)) ||
+      (rc = dev_alloc(c, &f.uy_alt, n)) || (rc = dev_alloc(c, &f.p, n)) || (rc = dev_alloc(c, &f.psi, n)) ||
+      (rc = dev_alloc(c, &f.aux, n)) || (rc = dev_alloc(c, &f.auy, n)) ||
+      (rc = dev_alloc(c, &f.spec, (size_t)nx * c->g.jpitch)) || (rc = dev_alloc(c, &f.colmax, (size_t)nx + 1))) {
+    fluid_finalise(&fe->pub);
+    return nullptr;
+  }
+  f.uymax = f.colmax + nx;
+  for (double *d : {f.ux, f.uy, f.ux_alt, f.uy_alt, f.p, f.psi, f.aux, f.auy}) cudaMemsetAsync(d, 0, n * sizeof(double), c->stream);
+  cudaMemsetAsync(f.spec, 0, (size_t)nx * c->g.jpitch * sizeof(double2), c->stream);
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess) {
+    fail(SNS_ERR_CUDA, "fluid_init: %s", cudaGetErrorString(cudaGetLastError()));
+    fluid_finalise(&fe->pub);
+    return nullptr;
+  }
+  // src/fluid/init.c:52-81: zero fields with boundary and halo values
+  host_bc_ux(nx, ny, h.ux);
+  host_bc_uy(nx, ny, h.uy);
+  host_bc_p(nx, ny, h.p);
+  return &fe->pub;
+}
+
+int fluid_finalise(fluid_t *fluid) {
+  FluidExt *fe = as_fluid(fluid);
+  if (!fe) return fail(SNS_ERR_ARG, "fluid_finalise: not a fluid_t from fluid_init");
+  fluid_t &h = fe->pub;
+  for (double *p : {h.ux, h.uy, h.p, h.psi, h.srcuxa, h.srcuxb, h.srcuxg, h.srcuya, h.srcuyb, h.srcuyg}) free(p);
+  Context *c = fe->ctx;
+  if (c) {
+    cudaStreamSynchronize(c->stream);
+    std::lock_guard<std::mutex> lk(g_mu);
+    // this object's device arrays
+    std::vector<void *> mine = {fe->f.ux, fe->f.uy, fe->f.ux_alt, fe->f.uy_alt, fe->f.p, fe->f.psi,
+                                fe->f.aux, fe->f.auy, fe->f.spec, fe->f.colmax, fe->f.qx, fe->f.qy};
+    for (void *p : mine) {
+      if (!p) continue;
+      auto it = std::find(c->allocs.begin(), c->allocs.end(), p);
+      if (it != c->allocs.end()) {
+        cudaFree(p);
+        c->allocs.erase(it);
+      }
+    }
+  }
+  fe->magic = 0;
+  free(fe);
+  if (c) release_context(c);
+  return SNS_OK;
+}
+
+temperature_t *temperature_init(const param_t *param, const parallel_t *parallel) {
+  if (check_inputs(param, parallel) != SNS_OK) return nullptr;
+  Context *c = acquire_context(param);
+  if (!c) return nullptr;
+  TempExt *te = static_cast<TempExt *>(calloc(1, sizeof(TempExt)));
+  const int nx = param->itot, ny = param->jtot;
+  const size_t nc = (size_t)(nx + 2) * (ny + 2), sx = (size_t)(nx - 1) * ny, sc = (size_t)nx * ny;
+  te->magic = kTempMagic;
+  te->ctx = c;
+  te->cur = 0;
+  te->snap = -2;
+  temperature_t &h = te->pub;
+  h.temp = static_cast<double *>(calloc(nc, sizeof(double)));
+  h.tempforcex = static_cast<double *>(calloc(sx, sizeof(double)));
+  h.srctempa = static_cast<double *>(calloc(sc, sizeof(double)));
+  h.srctempb = static_cast<double *>(calloc(sc, sizeof(double)));
+  h.srctempg = static_cast<double *>(calloc(sc, sizeof(double)));
+  // src/temperature/init.c:30-41: linear profile + rand() noise
+  {
+    const double factor = 0.1;
+    const double *xc = param->xc;
+    for (int j = 1; j <= ny; j++)
+      for (int i = 1; i <= nx; i++) {
+        const double x = xc[i];
+        const double r = -0.5 + 1. * rand() / RAND_MAX;
+        h.temp[(size_t)j * (nx + 2) + i] = (TEMP_XP - TEMP_XM) * x + TEMP_XM + factor * r;
+      }
+    host_bc_temp(nx, ny, h.temp);
+  }
+  int rc = SNS_OK;
+  for (int k = 0; k < 3 && rc == SNS_OK; k++) rc = dev_alloc(c, &te->f.t[k], sc);
+  if (rc == SNS_OK) rc = dev_alloc(c, &te->f.at, sc);
+  if (rc != SNS_OK) {
+    temperature_finalise(&te->pub);
+    return nullptr;
+  }
+  for (int k = 0; k < 3; k++) cudaMemsetAsync(te->f.t[k], 0, sc * sizeof(double), c->stream);
+  cudaMemsetAsync(te->f.at, 0, sc * sizeof(double), c->stream);
+  if (upload_field(c, te->f.t[0], h.temp, nx + 2, 1, 0) != SNS_OK) {
+    temperature_finalise(&te->pub);
+    return nullptr;
+  }
+  return &te->pub;
+}
+
+int temperature_finalise(temperature_t *temperature) {
+  TempExt *te = as_temp(temperature);
+  if (!te) return fail(SNS_ERR_ARG, "temperature_finalise: not a temperature_t from temperature_init");
+  temperature_t &h = te->pub;
+  for (double *p : {h.temp, h.tempforcex, h.srctempa, h.srctempb, h.srctempg}) free(p);
+  Context *c = te->ctx;
+  if (c) {
+    cudaStreamSynchronize(c->stream);
+    std::lock_guard<std::mutex> lk(g_mu);
+    std::vector<void *> mine = {te->f.t[0], te->f.t[1], te->f.t[2], te->f.at, te->f.qt};
+    for (void *p : mine) {
+      if (!p) continue;
+      auto it = std::find(c->allocs.begin(), c->allocs.end(), p);
+      if (it != c->allocs.end()) {
+        cudaFree(p);
+        c->allocs.erase(it);
+      }
+    }
+  }
+  te->magic = 0;
+  free(te);
+  if (c) release_context(c);
+  return SNS_OK;
+}
+
+int fluid_update_boundaries_ux(const param_t *param, const parallel_t *parallel, double *ux) {
+  if (!param || !ux) return fail(SNS_ERR_ARG, "NULL argument");
+  (void)parallel;
+  host_bc_ux(param->itot, param->jtot, ux);
+  return SNS_OK;
+}
+
+int fluid_update_boundaries_uy(const param_t *param, const parallel_t *parallel, double *uy) {
+  if (!param || !uy) return fail(SNS_ERR_ARG, "NULL argument");
+  (void)parallel;
+  host_bc_uy(param->itot, param->jtot, uy);
+  return SNS_OK;
+}
+
+int fluid_update_boundaries_p(const param_t *param, const parallel_t *parallel, double *p) {
+  if (!param || !p) return fail(SNS_ERR_ARG, "NULL argument");
+  (void)parallel;
+  host_bc_p(param->itot, param->jtot, p);
+  return SNS_OK;
+}
+
+int temperature_update_boundaries_temp(const param_t *param, const parallel_t *parallel, double *temp) {
+  if (!param || !temp) return fail(SNS_ERR_ARG, "NULL argument");
+  (void)parallel;
+  host_bc_temp(param->itot, param->jtot, temp);
+  return SNS_OK;
+}
+
+int temperature_compute_force(const param_t *param, const parallel_t *parallel, temperature_t *temperature) {
+  TempExt *te = as_temp(temperature);
+  if (!param || !parallel || !te) return fail(SNS_ERR_ARG, "temperature_compute_force: bad argument");
+  te->snap = param->with_thermal_forcing ? te->cur : -1;
+  return SNS_OK;
+}
+
+int temperature_update_temp(const param_t *param, const parallel_t *parallel, const int rkstep, const fluid_t *fluid,
+                            temperature_t *temperature) {
+  TempExt *te = as_temp(temperature);
+  FluidExt *fe = as_fluid(fluid);
+  if (!param || !parallel || !te || !fe || rkstep < 0 || rkstep >= RKSTEPMAX)
+    return fail(SNS_ERR_ARG, "temperature_update_temp: bad argument");
+  return do_temp_update(param, rkstep, fe, te);
+}
+
+int fluid_update_velocity(const param_t *param, const parallel_t *parallel, const int rkstep, fluid_t *fluid,
+                          const temperature_t *temperature) {
+  FluidExt *fe = as_fluid(fluid);
+  if (!param || !parallel || !fe || rkstep < 0 || rkstep >= RKSTEPMAX)
+    return fail(SNS_ERR_ARG, "fluid_update_velocity: bad argument");
+  const TempExt *te = temperature ? as_temp(temperature) : nullptr;
+  return do_velocity_update(param, rkstep, fe, te);
+}
+
+int fluid_compute_potential(const param_t *param, const parallel_t *parallel, const int rkstep, fluid_t *fluid) {
+  FluidExt *fe = as_fluid(fluid);
+  if (!param || !parallel || !fe || rkstep < 0 || rkstep >= RKSTEPMAX)
+    return fail(SNS_ERR_ARG, "fluid_compute_potential: bad argument");
+  Context *c = fe->ctx;
+  SNS_CUDA(launch_poisson(c->g, stage_scalars(param, rkstep), fe->f.ux, fe->f.uy, fe->f.spec, fe->f.psi, c->stream));
+  return SNS_OK;
+}
+
+int fluid_correct_velocity(const param_t *param, const parallel_t *parallel, const int rkstep, fluid_t *fluid) {
+  FluidExt *fe = as_fluid(fluid);
+  if (!param || !parallel || !fe || rkstep < 0 || rkstep >= RKSTEPMAX)
+    return fail(SNS_ERR_ARG, "fluid_correct_velocity: bad argument");
+  Context *c = fe->ctx;
+  SNS_CUDA(launch_correct(c->g, stage_scalars(param, rkstep), fe->f.psi, fe->f.ux, fe->f.uy, c->stream));
+  return SNS_OK;
+}
+
+int fluid_update_pressure(const param_t *param, const parallel_t *parallel, const int rkstep, fluid_t *fluid) {
+  FluidExt *fe = as_fluid(fluid);
+  if (!param || !parallel || !fe || rkstep < 0 || rkstep >= RKSTEPMAX)
+    return fail(SNS_ERR_ARG, "fluid_update_pressure: bad argument");
+  Context *c = fe->ctx;
+  SNS_CUDA(launch_pressure(c->g, stage_scalars(param, rkstep), param->implicitx, param->implicity, fe->f.psi,
+                           fe->f.p, c->stream));
+  return SNS_OK;
+}
+
+int param_decide_dt(param_t *param, const parallel_t *parallel, const fluid_t *fluid) {
+  FluidExt *fe = as_fluid(fluid);
+  if (!param || !parallel || !fe) return fail(SNS_ERR_ARG, "param_decide_dt: bad argument");
+  if (int rc = reduce_to_host(fe->ctx, fe->f, true)) return rc;
+  finish_decide_dt(param, fe->ctx);
+  return SNS_OK;
+}
+
+int sns_sync_to_host(const param_t *param, fluid_t *fluid, temperature_t *temperature) {
+  if (!param) return fail(SNS_ERR_ARG, "sns_sync_to_host: NULL param");
+  const int nx = param->itot, ny = param->jtot;
+  if (fluid) {
+    FluidExt *fe = as_fluid(fluid);
+    if (!fe) return fail(SNS_ERR_ARG, "sns_sync_to_host: foreign fluid_t");
+    Context *c = fe->ctx;
+    fluid_t &h = fe->pub;
+    int rc = SNS_OK;
+    if ((rc = download(c, fe->f.ux, h.ux, nx + 1, 0, 1)) || (rc = download(c, fe->f.uy, h.uy, nx + 2, 1, 0)) ||
+        (rc = download(c, fe->f.p, h.p, nx + 2, 1, 0)) || (rc = download(c, fe->f.psi, h.psi, nx + 2, 1, 0)) ||
+        (rc = download_src(c, fe->f.aux, h.srcuxa, 1)) || (rc = download_src(c, fe->f.auy, h.srcuya, 0)))
+      return rc;
+    host_bc_ux(nx, ny, h.ux);
+    host_bc_uy(nx, ny, h.uy);
+    host_bc_p(nx, ny, h.p);
+    host_bc_p(nx, ny, h.psi);
+  }
+  if (temperature) {
+    TempExt *te = as_temp(temperature);
+    if (!te) return fail(SNS_ERR_ARG, "sns_sync_to_host: foreign temperature_t");
+    Context *c = te->ctx;
+    temperature_t &h = te->pub;
+    int rc = SNS_OK;
+    if ((rc = download(c, te->f.t[te->cur], h.temp, nx + 2, 1, 0)) || (rc = download_src(c, te->f.at, h.srctempa, 0)))
+      return rc;
+    host_bc_temp(nx, ny, h.temp);
+    if (te->snap >= 0) {
+      // tempforcex (src/temperature/force.c:17-23) from the snapshot buffer
+      if (int rc2 = fetch(c, te->f.t[te->snap])) return rc2;
+      for (int j = 1; j <= ny; j++)
+        for (int i = 2; i <= nx; i++) {
+          const double tm = c->staging[(size_t)(j - 1) * nx + (i - 2)], tp = c->staging[(size_t)(j - 1) * nx + (i - 1)];
+          h.tempforcex[(size_t)(j - 1) * (nx - 1) + (i - 2)] = 0.5 * tm + 0.5 * tp;
+        }
+    }
+  }
+  return SNS_OK;
+}
+
+int sns_sync_to_device(const param_t *param, fluid_t *fluid, temperature_t *temperature) {
+  if (!param) return fail(SNS_ERR_ARG, "sns_sync_to_device: NULL param");
+  const int nx = param->itot;
+  if (fluid) {
+    FluidExt *fe = as_fluid(fluid);
+    if (!fe) return fail(SNS_ERR_ARG, "sns_sync_to_device: foreign fluid_t");
+    Context *c = fe->ctx;
+    fluid_t &h = fe->pub;
+    int rc = SNS_OK;
+    if ((rc = upload_field(c, fe->f.ux, h.ux, nx + 1, 0, 1)) || (rc = upload_field(c, fe->f.uy, h.uy, nx + 2, 1, 0)) ||
+        (rc = upload_field(c, fe->f.p, h.p, nx + 2, 1, 0)) || (rc = upload_field(c, fe->f.psi, h.psi, nx + 2, 1, 0)) ||
+        (rc = upload_src(c, fe->f.aux, h.srcuxa, 1)) || (rc = upload_src(c, fe->f.auy, h.srcuya, 0)))
+      return rc;
+  }
+  if (temperature) {
+    TempExt *te = as_temp(temperature);
+    if (!te) return fail(SNS_ERR_ARG, "sns_sync_to_device: foreign temperature_t");
+    Context *c = te->ctx;
+    temperature_t &h = te->pub;
+    te->cur = 0;
+    te->snap = -2;
+    int rc = SNS_OK;
+    if ((rc = upload_field(c, te->f.t[0], h.temp, nx + 2, 1, 0)) || (rc = upload_src(c, te->f.at, h.srctempa, 0)))
+      return rc;
+  }
+  return SNS_OK;
+}
+
+int sns_synchronize(const fluid_t *fluid) {
+  FluidExt *fe = as_fluid(fluid);
+  if (!fe) return fail(SNS_ERR_ARG, "sns_synchronize: bad fluid");
+  SNS_CUDA(cudaStreamSynchronize(fe->ctx->stream));
+  return SNS_OK;
+}
+
+void *sns_stream(const fluid_t *fluid) {
+  FluidExt *fe = as_fluid(fluid);
+  return fe ? (void *)fe->ctx->stream : nullptr;
+}
+
+static int integrate_impl(const param_t *param, FluidExt *fe, TempExt *te, bool reduce_last) {
+  Context *c = fe->ctx;
+  Fields &f = fe->f;
+  for (int rk = 0; rk < RKSTEPMAX; rk++) {
+    if (param->with_temperature && te) {
+      te->snap = param->with_thermal_forcing ? te->cur : -1;
+      if (int rc = do_temp_update(param, rk, fe, te)) return rc;
+    }
+    if (int rc = do_velocity_update(param, rk, fe, te)) return rc;
+    const StageScalars s = stage_scalars(param, rk);
+    SNS_CUDA(launch_poisson(c->g, s, f.ux, f.uy, f.spec, f.psi, c->stream));
+    const bool red = reduce_last && rk == RKSTEPMAX - 1;
+    if (red) SNS_CUDA(cudaMemsetAsync(f.colmax, 0, sizeof(unsigned long long) * (c->nx + 1), c->stream));
+    SNS_CUDA(launch_correct_pressure(c->g, s, param->implicitx, param->implicity, f.psi, f.ux, f.uy, f.p,
+                                     red ? f.colmax : nullptr, red ? f.uymax : nullptr, c->stream));
+  }
+  return SNS_OK;
+}
+
+int sns_integrate(const param_t *param, const parallel_t *parallel, fluid_t *fluid, temperature_t *temperature) {
+  FluidExt *fe = as_fluid(fluid);
+  if (!param || !parallel || !fe) return fail(SNS_ERR_ARG, "sns_integrate: bad argument");
+  if (parallel->mpisize != 1) return fail(SNS_ERR_UNSUPPORTED, "single-rank only");
+  TempExt *te = temperature ? as_temp(temperature) : nullptr;
+  return integrate_impl(param, fe, te, false);
+}
+
+int sns_run(param_t *param, const parallel_t *parallel, fluid_t *fluid, temperature_t *temperature, int nsteps) {
+  FluidExt *fe = as_fluid(fluid);
+  if (!param || !parallel || !fe || nsteps < 0) return fail(SNS_ERR_ARG, "sns_run: bad argument");
+  if (parallel->mpisize != 1) return fail(SNS_ERR_UNSUPPORTED, "single-rank only");
+  TempExt *te = temperature ? as_temp(temperature) : nullptr;
+  Context *c = fe->ctx;
+  bool have_reduction = false;
+  for (int s = 0; s < nsteps; s++) {
+    if (int rc = reduce_to_host(c, fe->f, !have_reduction)) return rc;
+    finish_decide_dt(param, c);
+    if (int rc = integrate_impl(param, fe, te, true)) return rc;
+    have_reduction = true;
+    param->step += 1;
+    param->time += param->dt;
+  }
+  SNS_CUDA(cudaStreamSynchronize(c->stream));
+  return SNS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,130 @@
+// Internal declarations shared by the host-side C ABI (sns_api.cpp) and the
+// CUDA kernels. Not part of the public interface.
+//
+// Device layout ("dense"): every field is ny rows by nx columns, x fastest,
+// element (i, j) of the reference (1-based, include/arrays/*.h) at
+// [(j-1)*nx + (i-1)]. No halo rows or columns are stored:
+//   * y is periodic, so row j=0 is row ny and row ny+1 is row 1 (index wrap);
+//   * wall values are implied by index logic: ux(1) = ux(nx+1) = 0 (ux(1) is
+//     stored, always zero), uy(0) = uy(nx+1) = 0, p and psi Neumann
+//     (p(0) = p(1), p(nx+1) = p(nx)), T(0) = +0.5, T(nx+1) = -0.5.
+// The Poisson spectrum is stored x-major: mode J of column i at
+// [(i-1)*jpitch + J] as double2, so line solves along x for fixed J read
+// consecutive J across a warp.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace sns {
+
+constexpr double kTempXm = +0.5;  // include/temperature.h:22
+constexpr double kTempXp = -0.5;  // include/temperature.h:23
+
+// Grid metrics on the device, all indexed by x = i-1.
+struct DevGrid {
+  int nx, ny, nh, jpitch;  // nh = ny/2 + 1 Fourier modes; jpitch >= nh
+  bool rcp;                // every metric divisor is a power of two
+  double dy, rdy;
+  const double *dxf;    // [nx]    DXF(i)
+  const double *dxc;    // [nx+1]  DXC(i), i = 1..nx+1
+  const double *rdxf;   // [nx]    1/DXF(i) (exact when rcp)
+  const double *rdxc;   // [nx+1]  1/DXC(i) (exact when rcp)
+  const double *dxi;    // [nx+1]  1./DXC(i) as src/fluid/correct_velocity.c:13
+  const double *c_cm;   // [nx]    DXC(i)/(2.*DXF(i))     (T and uy advection)
+  const double *c_cp;   // [nx]    DXC(i+1)/(2.*DXF(i))
+  const double *c_fm;   // [nx]    DXF(i-1)/(2.*DXC(i))   (ux advection, i >= 2)
+  const double *c_fp;   // [nx]    DXF(i)/(2.*DXC(i))
+  // Poisson: Thomas factors of the per-mode x-systems (src/fluid/compute_potential.c:109-136)
+  const double *pl;     // [nx]            lower diagonal 1./DXC(i)/DXF(i)
+  const double *pd0;    // [nh]            first pivot per mode
+  const double *pinv;   // [nx * jpitch]   1./pivot
+  const double *pup;    // [nx * jpitch]   normalised upper diagonal
+  const uint8_t *pzero; // [nx * jpitch]   1 where |pivot| < DBL_EPSILON (row forced to 0)
+  const double *tw;     // [2*ny]          twiddles exp(-2 pi i t/ny), t < ny
+  int fft_nst;          // stages of the length-ny/2 complex FFT
+  int fft_first2;       // first stage radix 2 (else all radix 4)
+};
+
+// Factors of one constant-matrix Thomas system shared by all lines, uploaded
+// per substage for the Crank-Nicolson solves (src/linalg.c:9-30).
+struct LineFactors {
+  int n;
+  const double *l;      // [n] lower diagonal
+  const double *inv;    // [n] 1./pivot (row 0 unused when first_div)
+  const double *up;     // [n] normalised upper diagonal
+  const uint8_t *zero;  // [n]
+  double d0;            // first pivot (first_div mode)
+};
+
+// Periodic y system (src/linalg.c:52-108): Thomas factors of the (n-1)
+// sub-system, the RHS-independent second solution q1 and the closure.
+struct PeriodicFactors {
+  LineFactors sub;     // size n-1, first_div mode
+  const double *q1;    // [n-1]
+  double l_last, u_last, den;  // l[n-1], u[n-1], d[n-1] + u[n-1]*q1[0] + l[n-1]*q1[n-2]
+};
+
+// RK substage scalars, computed on the host exactly as the reference does.
+struct StageScalars {
+  double adt, bdt, gdt;  // alpha*dt, beta*dt, gamma*dt
+  bool has_b;            // beta != 0 (beta*dt*srcb contributes)
+  double kappa;          // 1./sqrt(Pr)/sqrt(Ra)   (temperature diffusion)
+  double nu;             // sqrt(Pr)/sqrt(Ra)      (momentum diffusion)
+  double rgdt;           // 1./(gamma*dt)          (Poisson right-hand side)
+  double rny;            // 1/jtot when jtot is a power of two
+  double pcorr;          // -(gamma*dt)/(2.*Re)    (pressure correction, implicit)
+};
+
+struct Fields {
+  double *ux, *uy;             // current velocity (dense)
+  double *ux_alt, *uy_alt;     // prediction targets (swapped after update)
+  double *p, *psi;
+  double *aux, *auy;           // explicit RK sources srcuxa / srcuya (dense, in place)
+  double *qx, *qy;             // increments for the implicit paths
+  double2 *spec;               // Poisson spectrum [nx * jpitch]
+  unsigned long long *colmax;  // [nx] max |ux| per column (bit patterns)
+  unsigned long long *uymax;   // [1]
+};
+
+struct TempFields {
+  double *t[3];   // rotation of temperature buffers
+  double *at;     // srctempa (dense)
+  double *qt;     // increment for the implicit paths
+};
+
+// ---------------------------------------------------------------- launches
+// All return cudaGetLastError() of their launches.
+cudaError_t launch_temp_update(const DevGrid &g, const StageScalars &s, int impx, int impy,
+                               const double *t_in, double *t_out, double *at, double *qt,
+                               const double *ux, const double *uy, cudaStream_t st);
+cudaError_t launch_velocity_update(const DevGrid &g, const StageScalars &s, int impx, int impy,
+                                   const double *ux, const double *uy, const double *p, const double *tforce,
+                                   double *ux_out, double *uy_out, double *aux, double *auy,
+                                   double *qx, double *qy, cudaStream_t st);
+// x-direction Crank-Nicolson solve on q rows, then field += q into out
+// (mode 0: first row divides by d0 (T, uy); mode 1: ux rows 2..nx with a zero row before)
+cudaError_t launch_solve_x(const DevGrid &g, const LineFactors &f, int mode, double *q, cudaStream_t st);
+cudaError_t launch_solve_y(const DevGrid &g, const PeriodicFactors &f, int first_col, double *q, cudaStream_t st);
+// out = in + q on the interior (kind 0: T/uy all x; kind 1: ux x >= 1)
+cudaError_t launch_add_increment(const DevGrid &g, int kind, const double *in, const double *q, double *out,
+                                 cudaStream_t st);
+cudaError_t launch_poisson(const DevGrid &g, const StageScalars &s, const double *ux, const double *uy,
+                           double2 *spec, double *psi, cudaStream_t st);
+cudaError_t launch_correct(const DevGrid &g, const StageScalars &s, const double *psi, double *ux, double *uy,
+                           cudaStream_t st);
+cudaError_t launch_pressure(const DevGrid &g, const StageScalars &s, int impx, int impy, const double *psi,
+                            double *p, cudaStream_t st);
+// correct + pressure in one pass; with colmax non-null also the max-|u| reduction for the next dt
+cudaError_t launch_correct_pressure(const DevGrid &g, const StageScalars &s, int impx, int impy,
+                                    const double *psi, double *ux, double *uy, double *p,
+                                    unsigned long long *colmax, unsigned long long *uymax, cudaStream_t st);
+cudaError_t launch_umax(const DevGrid &g, const double *ux, const double *uy, unsigned long long *colmax,
+                        unsigned long long *uymax, cudaStream_t st);
+
+// counts kernel launches (process-wide)
+void count_launches(long long n);
+
+}  // namespace sns
