@@ -1,0 +1,386 @@
+"""Benchmark of the SMR-RK3 time step on GB300.
+
+Workload (default): 2D Rayleigh-Benard, 512 x 1024 uniform staggered grid,
+lx = 1, ly = 2, Ra = 1e9, Pr = 1, u = p = 0 and T = linear profile + uniform
+noise in [-0.05, 0.05] (the reference's own initial condition), dt and the
+explicit/implicit choice from param_decide_dt every step. One bench "step" is
+one solver time step: the device max-|u| reduction and dt decision plus the
+three RK substages (temperature, momentum, Poisson, projection, pressure).
+
+Arms:
+  default          the plain FP64 GPU path of libsns_gpu.so (bit-identical to the
+                   reference); inputs resident in HBM; per-step CUDA events on the
+                   solver's stream; L2 flushed (256 MiB write) between timed steps.
+  --impl reference the CPU oracle (the reference's algorithm restated in C, bit
+                   identical to it) on all host cores, same workload and metric.
+
+The JSON line also carries the per-kernel roofline of the dominant kernel
+(CUDA events around each launch, a second pass of the same steps), the CPU
+baseline, an end-to-end number through the C ABI with host buffers, kernel
+launch counts and the SM clocks sampled during the timed region.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+# FP64 instruction rate of this GPU (DADD = DMUL = DFMA issue rate), measured with
+# a pipe-saturating loop of independent FP64 ops on a GB300 (see the FP64 profile
+# summary under profiles/)
+MEASURED_FP64_GOPS = 503.6
+
+# algorithmic DRAM bytes per cell per launch (FP64, explicit scheme) and FP64
+# instructions per cell, per kernel, from the kernels' loads/stores and
+# arithmetic (beta != 0 substages; rk=0 skips one 8-byte read and two FP64 ops)
+KERNEL_MODEL = {
+    # name: (bytes per cell, fp64 ops per cell)
+    "temperature_update": (48.0, 27.0),
+    "velocity_update": (80.0, 81.0),
+    "poisson_forward_fft": (24.0, None),
+    "poisson_tridiagonal": (40.0, 5.0),
+    "poisson_inverse_fft": (16.0, None),
+    "correct_and_pressure": (56.0, 9.0),
+    "max_velocity": (16.0, 0.0),
+}
+
+
+def fft_ops_per_cell(ny: int, forward: bool) -> float:
+    """FP64 instructions per real sample of one length-ny real FFT as the
+    kernels perform it (radix-2 first stage if log2(ny/2) is odd, radix-4
+    stages with twiddles after the first, split step), plus the divergence
+    (forward) or the 1/ny scaling (inverse)."""
+    m = ny // 2
+    p = m.bit_length() - 1
+    stages = ([2] if p % 2 else []) + [4] * (p // 2)
+    ops, L = 0.0, 1
+    for s, r in enumerate(stages):
+        nb = m // r
+        per = (4 if r == 2 else 16) + ((r - 1) * 6 if L > 1 else 0)
+        ops += nb * per
+        L *= r
+    ops += (m // 2) * 18 + 2  # split step pairs
+    per_sample = ops / ny
+    return per_sample + (6.0 if forward else 1.0)
+
+
+def load_peaks():
+    try:
+        with open(PEAKS_PATH) as fh:
+            pk = json.load(fh)
+        return float(pk["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm), "power_w_max": max(power) if power else None}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo", init_method="env://")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(value: float, world: int) -> float:
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ----------------------------------------------------------------- CPU arms
+def cpu_oracle_rate(cfg, seconds: float, threads: int, min_steps: int = 2):
+    """cell-steps/s of the CPU oracle on a bounded sample of the workload"""
+    from oracle.bindings import OracleCase
+
+    o = OracleCase(cfg, threads=threads)
+    o.run(1)  # warm-up (page-in, first-touch)
+    n, t0 = 0, time.perf_counter()
+    while n < min_steps or time.perf_counter() - t0 < seconds:
+        o.run(1)
+        n += 1
+    el = time.perf_counter() - t0
+    o.close()
+    return cfg.itot * cfg.jtot * n / el, n, el
+
+
+def reference_arm(args, world, rank):
+    from oracle.build import build as build_oracle
+    from oracle.bindings import Config
+
+    if rank != 0:
+        return 0
+    build_oracle()
+    cfg = Config(args.nx, args.ny, ly=2.0, Ra=args.Ra, Pr=args.Pr)
+    threads = os.cpu_count() or 1
+    from oracle.bindings import OracleCase
+
+    o = OracleCase(cfg, threads=threads)
+    for _ in range(args.warmup):
+        o.run(1)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        o.run(1)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    value = cfg.itot * cfg.jtot * args.steps / total
+    line = {
+        "metric": "cell-steps/s (plain FP64 SMR-RK3 step)", "value": value, "unit": "cell-steps/s",
+        "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (reference initial condition, srand(0))",
+        "config": workload_config(args),
+        "cpu_baseline": {"value": value, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} time steps of {args.nx}x{args.ny} after {args.warmup} warm-up"},
+        "e2e": {"value": value, "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def workload_config(args):
+    return {"workload": f"rayleigh_benard_{args.nx}x{args.ny}_Ra{args.Ra:g}_Pr{args.Pr:g}_plain_fp64",
+            "nx": args.nx, "ny": args.ny, "lx": 1.0, "ly": 2.0, "Ra": args.Ra, "Pr": args.Pr,
+            "grid": "uniform", "scheme": "explicit x / explicit y (chosen by param_decide_dt)",
+            "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas only"}
+
+
+# ----------------------------------------------------------------- GPU arm
+def gpu_arm(args, world, rank, local):
+    import torch
+
+    from simplenavierstokessolver_gb300.build import build as build_lib
+
+    build_lib()
+    torch.cuda.set_device(local)
+    from simplenavierstokessolver_gb300 import Case, kernel_launches
+    from simplenavierstokessolver_gb300 import _native as N
+
+    lib = N.lib()
+    case = Case(args.nx, args.ny, ly=2.0, Ra=args.Ra, Pr=args.Pr)
+    stream = torch.cuda.ExternalStream(case.stream())
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    cells = args.nx * args.ny
+
+    def flush_l2():
+        with torch.cuda.stream(stream):
+            flush.zero_()
+
+    for _ in range(args.warmup):
+        case.run(1)
+        flush_l2()
+    torch.cuda.synchronize()
+
+    # ---- pass A: headline, uninstrumented
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    launches0 = kernel_launches()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for a, b in ev:
+        a.record(stream)
+        case.run(1)
+        b.record(stream)
+        flush_l2()
+    torch.cuda.synchronize()
+    barrier(world)
+    launches = kernel_launches() - launches0
+    clk = clocks.stop()
+    ms = sum(a.elapsed_time(b) for a, b in ev)
+    ms = max_over_ranks(ms, world)
+    value = cells * args.steps * world / (ms * 1e-3)
+
+    # ---- pass B: per-kernel device times (events around each launch)
+    lib.sns_profile(case.fluid, 1)
+    for _ in range(args.steps):
+        case.run(1)
+        flush_l2()
+    kinds = 16
+    kms = (N.c_double * kinds)()
+    kcnt = (N.c_longlong * kinds)()
+    nk = lib.sns_profile_read(case.fluid, kms, kcnt, kinds)
+    lib.sns_profile(case.fluid, 0)
+    kernels = {}
+    total_k = sum(kms[k] for k in range(nk))
+    for k in range(nk):
+        if kcnt[k]:
+            name = lib.sns_profile_kind_name(k).decode()
+            kernels[name] = {"launches": int(kcnt[k]), "ms": kms[k], "avg_us": 1e3 * kms[k] / kcnt[k],
+                             "share": kms[k] / total_k if total_k else None}
+    dom = max(kernels, key=lambda n: kernels[n]["ms"])
+    peak, peak_kind = load_peaks()
+    bpc, opc = KERNEL_MODEL.get(dom, (None, None))
+    if dom == "poisson_forward_fft":
+        opc = fft_ops_per_cell(args.ny, True)
+    if dom == "poisson_inverse_fft":
+        opc = fft_ops_per_cell(args.ny, False)
+    avg_s = kernels[dom]["avg_us"] * 1e-6
+    achieved = bpc * cells / avg_s / 1e9 if bpc else None
+    roofline = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak if achieved else None, "traffic": None,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
+                "algorithmic_bytes_per_launch": bpc * cells if bpc else None,
+                "note": "FP64-pipe bound on GB300: see fp64_roofline"}
+    fp64 = None
+    if opc:
+        ach = opc * cells / avg_s / 1e9
+        fp64 = {"kernel": dom, "achieved": ach, "peak": MEASURED_FP64_GOPS, "unit": "Gop/s (FP64 instructions)",
+                "frac": ach / MEASURED_FP64_GOPS, "ops_per_cell": opc}
+
+    # ---- end to end through the C ABI with host buffers
+    # each step: host arrays -> device (sns_sync_to_device), the reference-named
+    # calls of one time step (param_decide_dt + 3 x integrate sequence), device ->
+    # host arrays (sns_sync_to_host)
+    e2e_steps = max(2, min(args.steps, 10))
+    host = case.host_arrays()
+    case.sync_to_host()
+    h2d = sum(host[k].size * 8 for k in ("ux", "uy", "p", "psi", "temp", "srcuxa", "srcuya", "srctempa"))
+    d2h = h2d + host["temp"].size * 8  # + the buoyancy snapshot for tempforcex
+    torch.cuda.synchronize()
+    barrier(world)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        case.sync_to_device()
+        case.run_calls(1)
+        case.sync_to_host()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    e2e = {"value": cells * e2e_steps * world / e2e_s, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h, "steps": e2e_steps,
+           "path": "sns_sync_to_device + reference-named calls (param_decide_dt, temperature_*, fluid_*) "
+                   "+ sns_sync_to_host per step"}
+    case.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        from oracle.build import build as build_oracle
+        from oracle.bindings import Config
+
+        build_oracle()
+        threads = os.cpu_count() or 1
+        rate, n, el = cpu_oracle_rate(Config(args.nx, args.ny, ly=2.0, Ra=args.Ra, Pr=args.Pr), args.cpu_seconds,
+                                      threads)
+        cpu = {"value": rate, "unit": "cell-steps/s", "cores": threads, "kind": "port",
+               "sample": f"{n} time steps of {args.nx}x{args.ny} in {el:.1f} s on {threads} threads "
+                         "(CPU oracle, bit-identical to the reference)"}
+
+    if rank == 0:
+        line = {
+            "metric": "cell-steps/s (plain FP64 SMR-RK3 step)", "value": value, "unit": "cell-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (reference initial condition, srand(0))", "config": workload_config(args),
+            "roofline": roofline, "fp64_roofline": fp64, "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": int(launches), "clocks": clk,
+        }
+        print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--nx", type=int, default=512)
+    ap.add_argument("--ny", type=int, default=1024)
+    ap.add_argument("--Ra", type=float, default=1e9)
+    ap.add_argument("--Pr", type=float, default=1.0)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        return reference_arm(args, world, rank)
+    return gpu_arm(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

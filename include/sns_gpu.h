@@ -203,6 +203,16 @@ extern int sns_integrate(const param_t *param, const parallel_t *parallel, fluid
 extern int sns_run(param_t *param, const parallel_t *parallel, fluid_t *fluid, temperature_t *temperature,
                    int nsteps);
 
+/* per-kernel device time: with profiling enabled every kernel launched for
+ * this solver is bracketed by CUDA events on its stream. sns_profile(f, 1)
+ * resets the totals and starts, sns_profile(f, 0) stops. sns_profile_read
+ * fills ms[k] (summed milliseconds) and count[k] (launches) for the first n
+ * kernel kinds and returns the number of kinds; sns_profile_kind_name names
+ * kind k. */
+extern int sns_profile(const fluid_t *fluid, int enable);
+extern int sns_profile_read(const fluid_t *fluid, double *ms, long long *count, int n);
+extern const char *sns_profile_kind_name(int kind);
+
 /* message of the last error on this thread ("" if none) */
 extern const char *sns_last_error(void);
 /* number of kernel launches issued by this process so far */

@@ -100,6 +100,9 @@ PROTOTYPES = {
     "sns_last_error": (c_char_p, []),
     "sns_kernel_launches": (c_longlong, []),
     "sns_abi_layout": (c_int, [POINTER(c_size_t), c_int]),
+    "sns_profile": (c_int, [PF, c_int]),
+    "sns_profile_read": (c_int, [PF, POINTER(c_double), POINTER(c_longlong), c_int]),
+    "sns_profile_kind_name": (c_char_p, [c_int]),
 }
 
 _lib = None

@@ -702,12 +702,9 @@ cudaError_t launch_add_increment(const DevGrid &g, int kind, const double *in, c
   return cudaGetLastError();
 }
 
-cudaError_t launch_poisson(const DevGrid &g, const StageScalars &s, const double *ux, const double *uy,
-                           double2 *spec, double *psi, cudaStream_t st) {
+static int poisson_setup(const DevGrid &g, size_t *smem) {
   const int C = poisson_cols(g);
-  const PoissonArgs a{g, s, ux, uy, spec, psi, C};
-  const size_t smem = (size_t)C * g.ny * sizeof(double);
-  const int blocks = (g.nx + C - 1) / C;
+  *smem = (size_t)C * g.ny * sizeof(double);
   static bool attr_set = false;
   if (!attr_set) {
     const int lim = 160 * 1024;
@@ -716,14 +713,38 @@ cudaError_t launch_poisson(const DevGrid &g, const StageScalars &s, const double
     cudaFuncSetAttribute(k_poisson_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     attr_set = true;
   }
+  return C;
+}
+
+cudaError_t launch_poisson_fwd(const DevGrid &g, const StageScalars &s, const double *ux, const double *uy,
+                               double2 *spec, cudaStream_t st) {
+  size_t smem;
+  const int C = poisson_setup(g, &smem);
+  const PoissonArgs a{g, s, ux, uy, spec, nullptr, C};
+  const int blocks = (g.nx + C - 1) / C;
   if (g.rcp) {
     k_poisson_fwd<true><<<blocks, 256, smem, st>>>(a);
   } else {
     k_poisson_fwd<false><<<blocks, 256, smem, st>>>(a);
   }
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_poisson_tri(const DevGrid &g, double2 *spec, cudaStream_t st) {
   k_poisson_tri<<<(g.nh + 63) / 64, 64, 0, st>>>(g, spec);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_poisson_bwd(const DevGrid &g, const StageScalars &s, const double2 *spec, double *psi,
+                               cudaStream_t st) {
+  size_t smem;
+  const int C = poisson_setup(g, &smem);
+  const PoissonArgs a{g, s, nullptr, nullptr, const_cast<double2 *>(spec), psi, C};
+  const int blocks = (g.nx + C - 1) / C;
   k_poisson_bwd<<<blocks, 256, smem, st>>>(a);
-  count_launches(3);
+  count_launches(1);
   return cudaGetLastError();
 }
 

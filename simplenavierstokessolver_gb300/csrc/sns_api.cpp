@@ -71,6 +71,54 @@ struct Context {
   // factors for the implicit solves: device buffer + host mirror
   double *fac = nullptr;
   size_t fac_words = 0;
+  // optional per-launch event timing (sns_profile)
+  bool prof = false;
+  std::vector<cudaEvent_t> prof_ev;  // two per slot
+  std::vector<int> prof_kind;
+  size_t prof_used = 0;
+  double prof_ms[K_NUM_KINDS] = {};
+  long long prof_n[K_NUM_KINDS] = {};
+};
+
+static void prof_collect(Context *c) {
+  if (c->prof_used == 0) return;
+  cudaStreamSynchronize(c->stream);
+  for (size_t k = 0; k < c->prof_used; k++) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c->prof_ev[2 * k], c->prof_ev[2 * k + 1]) == cudaSuccess) {
+      c->prof_ms[c->prof_kind[k]] += ms;
+      c->prof_n[c->prof_kind[k]] += 1;
+    }
+  }
+  c->prof_used = 0;
+}
+
+// brackets the launches of one kernel with events on the solver's stream
+// when profiling is on; no work at all otherwise
+struct Prof {
+  Context *c;
+  long idx = -1;
+  Prof(Context *c_, int kind) : c(c_) {
+    if (!c->prof) return;
+    if (c->prof_used >= 2048) prof_collect(c);
+    if (2 * (c->prof_used + 1) > c->prof_ev.size()) {
+      cudaEvent_t a, b;
+      if (cudaEventCreate(&a) != cudaSuccess) return;
+      if (cudaEventCreate(&b) != cudaSuccess) {
+        cudaEventDestroy(a);
+        return;
+      }
+      c->prof_ev.push_back(a);
+      c->prof_ev.push_back(b);
+      c->prof_kind.push_back(0);
+    }
+    idx = (long)c->prof_used++;
+    c->prof_kind[idx] = kind;
+    cudaEventRecord(c->prof_ev[2 * idx], c->stream);
+  }
+  ~Prof() {
+    if (idx >= 0) cudaEventRecord(c->prof_ev[2 * idx + 1], c->stream);
+  }
 };
 
 static std::mutex g_mu;
@@ -171,6 +219,8 @@ static void twiddle(int n, int t, double *re, double *im) {
 
 static void destroy_context(Context *c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
+  for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);
+  c->prof_ev.clear();
   for (void *p : c->allocs) cudaFree(p);
   c->allocs.clear();
   if (c->staging) cudaFreeHost(c->staging);
@@ -554,6 +604,7 @@ static int implicit_x(Context *c, const param_t *param, int rk, int kind, double
   x_system(param, rk, kind, hf);
   LineFactors lf{};
   if (int rc = push_factors(c, hf, 0, lf)) return rc;
+  Prof pf(c, K_SOLVE_X);
   SNS_CUDA(launch_solve_x(c->g, lf, kind == 1 ? 1 : 0, q, c->stream));
   return SNS_OK;
 }
@@ -568,6 +619,7 @@ static int implicit_y(Context *c, const param_t *param, int rk, int is_temp, int
   const size_t qoff = off + 4 * sub.l.size();
   SNS_CUDA(cudaMemcpyAsync(c->fac + qoff, q1.data(), q1.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   pf.q1 = c->fac + qoff;
+  Prof pr(c, K_SOLVE_Y);
   SNS_CUDA(launch_solve_y(c->g, pf, first_col, q, c->stream));
   return SNS_OK;
 }
@@ -595,13 +647,17 @@ static int do_temp_update(const param_t *param, int rk, FluidExt *fe, TempExt *t
     if (!te->f.qt)
       if (int rc = dev_alloc(c, &te->f.qt, (size_t)c->nx * c->ny)) return rc;
   }
-  SNS_CUDA(launch_temp_update(c->g, s, impx, impy, te->f.t[te->cur], te->f.t[out], te->f.at, te->f.qt, fe->f.ux,
-                              fe->f.uy, c->stream));
+  {
+    Prof pf(c, K_TEMP);
+    SNS_CUDA(launch_temp_update(c->g, s, impx, impy, te->f.t[te->cur], te->f.t[out], te->f.at, te->f.qt, fe->f.ux,
+                                fe->f.uy, c->stream));
+  }
   if (impx || impy) {
     if (impx)
       if (int rc = implicit_x(c, param, rk, 0, te->f.qt)) return rc;
     if (impy)
       if (int rc = implicit_y(c, param, rk, 1, 0, te->f.qt)) return rc;
+    Prof pf(c, K_ADD_INC);
     SNS_CUDA(launch_add_increment(c->g, 0, te->f.t[te->cur], te->f.qt, te->f.t[out], c->stream));
   }
   te->cur = out;
@@ -616,8 +672,11 @@ static int do_velocity_update(const param_t *param, int rk, FluidExt *fe, const 
     if (int rc = ensure_implicit_buffers(fe)) return rc;
   const double *tf = (te && te->snap >= 0) ? te->f.t[te->snap] : nullptr;
   Fields &f = fe->f;
-  SNS_CUDA(launch_velocity_update(c->g, s, impx, impy, f.ux, f.uy, f.p, tf, f.ux_alt, f.uy_alt, f.aux, f.auy, f.qx,
-                                  f.qy, c->stream));
+  {
+    Prof pf(c, K_VEL);
+    SNS_CUDA(launch_velocity_update(c->g, s, impx, impy, f.ux, f.uy, f.p, tf, f.ux_alt, f.uy_alt, f.aux, f.auy,
+                                    f.qx, f.qy, c->stream));
+  }
   if (impx || impy) {
     if (impx) {
       if (int rc = implicit_x(c, param, rk, 1, f.qx)) return rc;
@@ -627,11 +686,28 @@ static int do_velocity_update(const param_t *param, int rk, FluidExt *fe, const 
       if (int rc = implicit_y(c, param, rk, 0, 1, f.qx)) return rc;
       if (int rc = implicit_y(c, param, rk, 0, 0, f.qy)) return rc;
     }
+    Prof pf(c, K_ADD_INC);
     SNS_CUDA(launch_add_increment(c->g, 1, f.ux, f.qx, f.ux_alt, c->stream));
     SNS_CUDA(launch_add_increment(c->g, 0, f.uy, f.qy, f.uy_alt, c->stream));
   }
   std::swap(f.ux, f.ux_alt);
   std::swap(f.uy, f.uy_alt);
+  return SNS_OK;
+}
+
+static int poisson(Context *c, const StageScalars &s, Fields &f) {
+  {
+    Prof pf(c, K_POI_FWD);
+    SNS_CUDA(launch_poisson_fwd(c->g, s, f.ux, f.uy, f.spec, c->stream));
+  }
+  {
+    Prof pf(c, K_POI_TRI);
+    SNS_CUDA(launch_poisson_tri(c->g, f.spec, c->stream));
+  }
+  {
+    Prof pf(c, K_POI_BWD);
+    SNS_CUDA(launch_poisson_bwd(c->g, s, f.spec, f.psi, c->stream));
+  }
   return SNS_OK;
 }
 
@@ -692,6 +768,7 @@ static void finish_decide_dt(param_t *param, const Context *c) {
 static int reduce_to_host(Context *c, Fields &f, bool launch) {
   if (launch) {
     SNS_CUDA(cudaMemsetAsync(f.colmax, 0, sizeof(unsigned long long) * (c->nx + 1), c->stream));
+    Prof pf(c, K_UMAX);
     SNS_CUDA(launch_umax(c->g, f.ux, f.uy, f.colmax, f.uymax, c->stream));
   }
   SNS_CUDA(cudaMemcpyAsync(c->red_host, f.colmax, sizeof(unsigned long long) * (c->nx + 1), cudaMemcpyDeviceToHost,
@@ -1014,7 +1091,7 @@ int fluid_compute_potential(const param_t *param, const parallel_t *parallel, co
   if (!param || !parallel || !fe || rkstep < 0 || rkstep >= RKSTEPMAX)
     return fail(SNS_ERR_ARG, "fluid_compute_potential: bad argument");
   Context *c = fe->ctx;
-  SNS_CUDA(launch_poisson(c->g, stage_scalars(param, rkstep), fe->f.ux, fe->f.uy, fe->f.spec, fe->f.psi, c->stream));
+  if (int rc = poisson(c, stage_scalars(param, rkstep), fe->f)) return rc;
   return SNS_OK;
 }
 
@@ -1023,6 +1100,7 @@ int fluid_correct_velocity(const param_t *param, const parallel_t *parallel, con
   if (!param || !parallel || !fe || rkstep < 0 || rkstep >= RKSTEPMAX)
     return fail(SNS_ERR_ARG, "fluid_correct_velocity: bad argument");
   Context *c = fe->ctx;
+  Prof pf(c, K_CORR);
   SNS_CUDA(launch_correct(c->g, stage_scalars(param, rkstep), fe->f.psi, fe->f.ux, fe->f.uy, c->stream));
   return SNS_OK;
 }
@@ -1032,6 +1110,7 @@ int fluid_update_pressure(const param_t *param, const parallel_t *parallel, cons
   if (!param || !parallel || !fe || rkstep < 0 || rkstep >= RKSTEPMAX)
     return fail(SNS_ERR_ARG, "fluid_update_pressure: bad argument");
   Context *c = fe->ctx;
+  Prof pf(c, K_PRES);
   SNS_CUDA(launch_pressure(c->g, stage_scalars(param, rkstep), param->implicitx, param->implicity, fe->f.psi,
                            fe->f.p, c->stream));
   return SNS_OK;
@@ -1113,6 +1192,42 @@ int sns_sync_to_device(const param_t *param, fluid_t *fluid, temperature_t *temp
   return SNS_OK;
 }
 
+static const char *kKindNames[K_NUM_KINDS] = {
+    "temperature_update", "velocity_update", "poisson_forward_fft", "poisson_tridiagonal", "poisson_inverse_fft",
+    "correct_and_pressure", "correct_velocity", "update_pressure", "max_velocity", "cn_solve_x", "cn_solve_y",
+    "add_increment"};
+
+int sns_profile(const fluid_t *fluid, int enable) {
+  FluidExt *fe = as_fluid(fluid);
+  if (!fe) return fail(SNS_ERR_ARG, "sns_profile: bad fluid");
+  Context *c = fe->ctx;
+  prof_collect(c);
+  if (enable) {
+    for (int k = 0; k < K_NUM_KINDS; k++) {
+      c->prof_ms[k] = 0.0;
+      c->prof_n[k] = 0;
+    }
+  }
+  c->prof = enable != 0;
+  return SNS_OK;
+}
+
+int sns_profile_read(const fluid_t *fluid, double *ms, long long *count, int n) {
+  FluidExt *fe = as_fluid(fluid);
+  if (!fe || !ms || !count) return fail(SNS_ERR_ARG, "sns_profile_read: bad argument");
+  Context *c = fe->ctx;
+  prof_collect(c);
+  for (int k = 0; k < n && k < K_NUM_KINDS; k++) {
+    ms[k] = c->prof_ms[k];
+    count[k] = c->prof_n[k];
+  }
+  return K_NUM_KINDS;
+}
+
+const char *sns_profile_kind_name(int kind) {
+  return (kind >= 0 && kind < K_NUM_KINDS) ? kKindNames[kind] : "";
+}
+
 int sns_synchronize(const fluid_t *fluid) {
   FluidExt *fe = as_fluid(fluid);
   if (!fe) return fail(SNS_ERR_ARG, "sns_synchronize: bad fluid");
@@ -1135,9 +1250,10 @@ static int integrate_impl(const param_t *param, FluidExt *fe, TempExt *te, bool 
     }
     if (int rc = do_velocity_update(param, rk, fe, te)) return rc;
     const StageScalars s = stage_scalars(param, rk);
-    SNS_CUDA(launch_poisson(c->g, s, f.ux, f.uy, f.spec, f.psi, c->stream));
+    if (int rc = poisson(c, s, f)) return rc;
     const bool red = reduce_last && rk == RKSTEPMAX - 1;
     if (red) SNS_CUDA(cudaMemsetAsync(f.colmax, 0, sizeof(unsigned long long) * (c->nx + 1), c->stream));
+    Prof pf(c, K_CORR_PRES);
     SNS_CUDA(launch_correct_pressure(c->g, s, param->implicitx, param->implicity, f.psi, f.ux, f.uy, f.p,
                                      red ? f.colmax : nullptr, red ? f.uymax : nullptr, c->stream));
   }

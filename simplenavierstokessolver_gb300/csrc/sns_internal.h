@@ -111,8 +111,11 @@ cudaError_t launch_solve_y(const DevGrid &g, const PeriodicFactors &f, int first
 // out = in + q on the interior (kind 0: T/uy all x; kind 1: ux x >= 1)
 cudaError_t launch_add_increment(const DevGrid &g, int kind, const double *in, const double *q, double *out,
                                  cudaStream_t st);
-cudaError_t launch_poisson(const DevGrid &g, const StageScalars &s, const double *ux, const double *uy,
-                           double2 *spec, double *psi, cudaStream_t st);
+cudaError_t launch_poisson_fwd(const DevGrid &g, const StageScalars &s, const double *ux, const double *uy,
+                               double2 *spec, cudaStream_t st);
+cudaError_t launch_poisson_tri(const DevGrid &g, double2 *spec, cudaStream_t st);
+cudaError_t launch_poisson_bwd(const DevGrid &g, const StageScalars &s, const double2 *spec, double *psi,
+                               cudaStream_t st);
 cudaError_t launch_correct(const DevGrid &g, const StageScalars &s, const double *psi, double *ux, double *uy,
                            cudaStream_t st);
 cudaError_t launch_pressure(const DevGrid &g, const StageScalars &s, int impx, int impy, const double *psi,
@@ -123,6 +126,12 @@ cudaError_t launch_correct_pressure(const DevGrid &g, const StageScalars &s, int
                                     unsigned long long *colmax, unsigned long long *uymax, cudaStream_t st);
 cudaError_t launch_umax(const DevGrid &g, const double *ux, const double *uy, unsigned long long *colmax,
                         unsigned long long *uymax, cudaStream_t st);
+
+// kernel kinds for the optional per-launch event timing (sns_profile_*)
+enum KernelKind {
+  K_TEMP = 0, K_VEL, K_POI_FWD, K_POI_TRI, K_POI_BWD, K_CORR_PRES, K_CORR, K_PRES, K_UMAX, K_SOLVE_X, K_SOLVE_Y,
+  K_ADD_INC, K_NUM_KINDS
+};
 
 // counts kernel launches (process-wide)
 void count_launches(long long n);

@@ -61,7 +61,13 @@ def test_golden_cases(name, fused):
         if meta["seeded"]:
             for x in (o, c):
                 x.set_state(g["init_ux"], g["init_uy"], g["init_p"], g["init_temp"])
-        assert_bitwise(c.get_state(), o.get_state(), ("ux", "uy", "p", "temp"), "initial state")
+            # seeded arrays carry arbitrary halo values; the reference overwrites
+            # them at the first boundary call of the first substage
+            o.call("update_boundaries")
+        # with the temperature uncoupled the reference never applies its wall
+        # and halo rules to it, so only its interior is defined
+        fields = FIELDS if cfg.with_temperature else ("ux", "uy", "p", "psi")
+        assert_bitwise(c.get_state(), o.get_state(), [k for k in fields if k != "psi"], "initial state")
         if fused:
             c.run(meta["steps"])
         else:
@@ -69,9 +75,10 @@ def test_golden_cases(name, fused):
         o.run(meta["steps"])
         sg, so = c.get_state(), o.get_state()
         assert c.get_dt() == o.get_dt()
-        assert_bitwise(sg, so, FIELDS, name)
+        assert_bitwise(sg, so, fields, name)
+        assert np.array_equal(sg["temp"][1:-1, 1:-1], so["temp"][1:-1, 1:-1])
         assert_bitwise(c.get_sources(), o.get_sources(), ("srcuxa", "srcuya", "srctempa"), name)
-        for k in FIELDS:
+        for k in fields:
             err = rel_l2(sg[k], g[f"final_{k}"])
             assert err <= REL_TOL or (platform.machine() == "x86_64" and np.array_equal(sg[k], g[f"final_{k}"])), \
                 f"{k}: rel L2 {err:.3e} vs the reference's fixture"
