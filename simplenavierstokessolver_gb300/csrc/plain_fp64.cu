@@ -260,12 +260,8 @@ __global__ void k_solve_x(int nx, int ny, LineFactors f, int mode, double *q) {
     x0 = 1;
   }
   for (int x = x0; x < nx; ++x) {
-    double v;
-    if (f.zero[x]) {
-      v = 0.0;
-    } else {
-      v = f.inv[x] * (row[x] - f.l[x] * prev);
-    }
+    const double inv = f.inv[x];
+    const double v = inv == 0.0 ? 0.0 : inv * (row[x] - f.l[x] * prev);
     row[x] = v;
     prev = v;
   }
@@ -290,12 +286,8 @@ __global__ void k_solve_y(int nx, int ny, PeriodicFactors f, int first_col, doub
   double prev = col[0] / sub.d0;
   col[0] = prev;
   for (int y = 1; y < n - 1; ++y) {
-    double v;
-    if (sub.zero[y]) {
-      v = 0.0;
-    } else {
-      v = sub.inv[y] * (col[y * s] - sub.l[y] * prev);
-    }
+    const double inv = sub.inv[y];
+    const double v = inv == 0.0 ? 0.0 : inv * (col[y * s] - sub.l[y] * prev);
     col[y * s] = v;
     prev = v;
   }
@@ -457,41 +449,109 @@ __global__ void __launch_bounds__(256) k_poisson_fwd(const PoissonArgs a) {
   }
 }
 
+// Register chunk of one line for the software-pipelined Thomas sweeps: the
+// loads of the next chunk are issued before the dependent arithmetic of the
+// current one, so each sweep pays about one memory latency in total instead
+// of one per element.
+constexpr int kTriChunk = 8;
+struct TriChunk {
+  double2 v[kTriChunk];
+  double f[kTriChunk];  // 1/pivot (forward) or normalised upper diagonal (backward)
+  double l[kTriChunk];
+};
+
+__device__ __forceinline__ void tri_load_fwd(TriChunk &c, const double2 *col, const double *inv, const double *pl,
+                                             int x0, int nx, size_t jp) {
+#pragma unroll
+  for (int k = 0; k < kTriChunk; ++k) {
+    const int x = x0 + k;
+    if (x < nx) {
+      c.v[k] = col[(size_t)x * jp];
+      c.f[k] = inv[(size_t)x * jp];
+      c.l[k] = pl[x];
+    }
+  }
+}
+
+// forward elimination step of src/linalg.c:35-44; a zero 1/pivot marks the
+// |pivot| < DBL_EPSILON rows, which the reference sets to 0
+__device__ __forceinline__ void tri_run_fwd(TriChunk &c, double2 *col, int x0, int nx, size_t jp, double2 &prev) {
+#pragma unroll
+  for (int k = 0; k < kTriChunk; ++k) {
+    const int x = x0 + k;
+    if (x < nx) {
+      double2 v = c.v[k];
+      const double inv = c.f[k], l = c.l[k];
+      if (inv == 0.0) {
+        v.x = 0.0;
+        v.y = 0.0;
+      } else {
+        v.x = inv * (v.x - l * prev.x);
+        v.y = inv * (v.y - l * prev.y);
+      }
+      col[(size_t)x * jp] = v;
+      prev = v;
+    }
+  }
+}
+
+__device__ __forceinline__ void tri_load_bwd(TriChunk &c, const double2 *col, const double *up, int x0, size_t jp) {
+#pragma unroll
+  for (int k = 0; k < kTriChunk; ++k) {
+    const int x = x0 - k;
+    if (x >= 0) {
+      c.v[k] = col[(size_t)x * jp];
+      c.f[k] = up[(size_t)x * jp];
+    }
+  }
+}
+
+// back substitution of src/linalg.c:46-48
+__device__ __forceinline__ void tri_run_bwd(TriChunk &c, double2 *col, int x0, size_t jp, double2 &next) {
+#pragma unroll
+  for (int k = 0; k < kTriChunk; ++k) {
+    const int x = x0 - k;
+    if (x >= 0) {
+      double2 v = c.v[k];
+      const double u = c.f[k];
+      v.x = v.x - u * next.x;
+      v.y = v.y - u * next.y;
+      col[(size_t)x * jp] = v;
+      next = v;
+    }
+  }
+}
+
 // src/fluid/compute_potential.c:109-136: per Fourier mode, Thomas along x with
-// the complex right-hand side (real and imaginary parts share the factors).
-__global__ void k_poisson_tri(const DevGrid g, double2 *spec) {
+// the complex right-hand side (real and imaginary parts share the factors),
+// one thread per mode; a warp reads 32 consecutive modes (coalesced).
+__global__ void __launch_bounds__(32) k_poisson_tri(const DevGrid g, double2 *spec) {
   const int J = blockIdx.x * blockDim.x + threadIdx.x;
   if (J >= g.nh) return;
   const int nx = g.nx;
   const size_t jp = (size_t)g.jpitch;
   double2 *col = spec + J;
+  const double *inv = g.pinv + J, *up = g.pup + J;
   const double d0 = g.pd0[J];
   double2 prev = col[0];
   prev.x = prev.x / d0;
   prev.y = prev.y / d0;
   col[0] = prev;
-  for (int x = 1; x < nx; ++x) {
-    const size_t f = (size_t)x * jp + J;
-    double2 v = col[(size_t)x * jp];
-    if (g.pzero[f]) {
-      v.x = 0.0;
-      v.y = 0.0;
-    } else {
-      const double inv = g.pinv[f], l = g.pl[x];
-      v.x = inv * (v.x - l * prev.x);
-      v.y = inv * (v.y - l * prev.y);
-    }
-    col[(size_t)x * jp] = v;
-    prev = v;
+  TriChunk a, b;
+  tri_load_fwd(a, col, inv, g.pl, 1, nx, jp);
+  for (int x0 = 1; x0 < nx; x0 += 2 * kTriChunk) {
+    tri_load_fwd(b, col, inv, g.pl, x0 + kTriChunk, nx, jp);
+    tri_run_fwd(a, col, x0, nx, jp, prev);
+    tri_load_fwd(a, col, inv, g.pl, x0 + 2 * kTriChunk, nx, jp);
+    tri_run_fwd(b, col, x0 + kTriChunk, nx, jp, prev);
   }
   double2 next = prev;
-  for (int x = nx - 2; x >= 0; --x) {
-    const double u = g.pup[(size_t)x * jp + J];
-    double2 v = col[(size_t)x * jp];
-    v.x = v.x - u * next.x;
-    v.y = v.y - u * next.y;
-    col[(size_t)x * jp] = v;
-    next = v;
+  tri_load_bwd(a, col, up, nx - 2, jp);
+  for (int x0 = nx - 2; x0 >= 0; x0 -= 2 * kTriChunk) {
+    tri_load_bwd(b, col, up, x0 - kTriChunk, jp);
+    tri_run_bwd(a, col, x0, jp, next);
+    tri_load_bwd(a, col, up, x0 - 2 * kTriChunk, jp);
+    tri_run_bwd(b, col, x0 - kTriChunk, jp, next);
   }
 }
 
@@ -551,79 +611,94 @@ __device__ __forceinline__ unsigned long long abs_bits(double v) {
   return a == a ? (unsigned long long)__double_as_longlong(a) : 0ull;
 }
 
+constexpr int kCorrRows = 4;  // rows per thread in the (memory-latency bound) correction kernels
+
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, off));
+  return v;
+}
+
 // src/fluid/correct_velocity.c:6-42 and src/fluid/update_pressure.c:7-60, per
 // cell in the reference's order; with colmax set, also max |ux| per column and
 // max |uy| for the next src/param/decide_dt.c (exact: division is monotonic).
+// Every lane of a block stays alive to the warp reduction (blockDim is a
+// multiple of 32); lanes past the last column only contribute zero.
 template <int IMPX, int IMPY, bool RCP, bool CORR, bool PRES>
 __global__ void __launch_bounds__(128) k_corr(const CorrArgs a) {
   const int nx = a.g.nx, ny = a.g.ny;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= nx) return;
-  const int y0 = blockIdx.y * kRows;
-  const int y1 = min(y0 + kRows, ny);
-  const double gdt = a.s.gdt, dy = a.g.dy, rdy = a.g.rdy;
-  const double dxi = a.g.dxi[x];
-  const double dcm = a.g.dxc[x], dcp = a.g.dxc[x + 1], df = a.g.dxf[x];
-  const double rcm = a.g.rdxc[x], rcp = a.g.rdxc[x + 1], rf = a.g.rdxf[x];
-  const bool left = x == 0, right = x == nx - 1;
-  const double *psi = a.psi;
-  double sm = psi[(size_t)wrap_dn(y0, ny) * nx + x];
+  const bool live = x < nx;
   unsigned long long mx = 0ull, my = 0ull;
-  for (int y = y0; y < y1; ++y) {
-    const size_t r = (size_t)y * nx + x;
-    const double sc = psi[r];
-    const double sl = left ? sc : psi[r - 1];  // Neumann psi(0) = psi(1)
-    if (CORR) {
-      if (!left) {
-        const double u = a.ux[r] - ((gdt * (sc - sl)) * dxi);
-        a.ux[r] = u;
-        mx = max(mx, abs_bits(u));
+  if (live) {
+    const int y0 = blockIdx.y * kCorrRows;
+    const int y1 = min(y0 + kCorrRows, ny);
+    const double gdt = a.s.gdt, dy = a.g.dy, rdy = a.g.rdy;
+    const double dxi = a.g.dxi[x];
+    const double dcm = a.g.dxc[x], dcp = a.g.dxc[x + 1], df = a.g.dxf[x];
+    const double rcm = a.g.rdxc[x], rcp = a.g.rdxc[x + 1], rf = a.g.rdxf[x];
+    const bool left = x == 0, right = x == nx - 1;
+    const double *psi = a.psi;
+    double sm = psi[(size_t)wrap_dn(y0, ny) * nx + x];
+    for (int y = y0; y < y1; ++y) {
+      const size_t r = (size_t)y * nx + x;
+      const double sc = psi[r];
+      const double sl = left ? sc : psi[r - 1];  // Neumann psi(0) = psi(1)
+      if (CORR) {
+        if (!left) {
+          const double u = a.ux[r] - ((gdt * (sc - sl)) * dxi);
+          a.ux[r] = u;
+          mx = max(mx, abs_bits(u));
+        }
+        const double v = a.uy[r] - dv<RCP>(gdt * (sc - sm), dy, rdy);
+        a.uy[r] = v;
+        my = max(my, abs_bits(v));
       }
-      const double v = a.uy[r] - dv<RCP>(gdt * (sc - sm), dy, rdy);
-      a.uy[r] = v;
-      my = max(my, abs_bits(v));
+      if (PRES) {
+        double pv = a.p[r] + sc;
+        if (IMPX) {
+          const double sr = right ? sc : psi[r + 1];  // Neumann psi(nx+1) = psi(nx)
+          const double gm = dv<RCP>(sc - sl, dcm, rcm);
+          const double gp = dv<RCP>(sr - sc, dcp, rcp);
+          pv = pv + a.s.pcorr * dv<RCP>(gp - gm, df, rf);
+        }
+        if (IMPY) {
+          const double sn = psi[(size_t)wrap_up(y, ny) * nx + x];
+          const double gm = dv<RCP>(sc - sm, dy, rdy);
+          const double gp = dv<RCP>(sn - sc, dy, rdy);
+          pv = pv + a.s.pcorr * dv<RCP>(gp - gm, dy, rdy);
+        }
+        a.p[r] = pv;
+      }
+      sm = sc;
     }
-    if (PRES) {
-      double pv = a.p[r] + sc;
-      if (IMPX) {
-        const double sr = right ? sc : psi[r + 1];  // Neumann psi(nx+1) = psi(nx)
-        const double gm = dv<RCP>(sc - sl, dcm, rcm);
-        const double gp = dv<RCP>(sr - sc, dcp, rcp);
-        pv = pv + a.s.pcorr * dv<RCP>(gp - gm, df, rf);
-      }
-      if (IMPY) {
-        const double sn = psi[(size_t)wrap_up(y, ny) * nx + x];
-        const double gm = dv<RCP>(sc - sm, dy, rdy);
-        const double gp = dv<RCP>(sn - sc, dy, rdy);
-        pv = pv + a.s.pcorr * dv<RCP>(gp - gm, dy, rdy);
-      }
-      a.p[r] = pv;
-    }
-    sm = sc;
   }
   if (CORR && a.colmax) {
-    if (!left) atomicMax(a.colmax + x, mx);
-    atomicMax(a.uymax, my);
+    if (live && x >= 1) atomicMax(a.colmax + x, mx);
+    my = warp_max_u64(my);
+    if ((threadIdx.x & 31) == 0) atomicMax(a.uymax, my);
   }
 }
 
-__global__ void k_umax(int nx, int ny, const double *ux, const double *uy, unsigned long long *colmax,
-                       unsigned long long *uymax) {
+__global__ void __launch_bounds__(128) k_umax(int nx, int ny, const double *ux, const double *uy,
+                                              unsigned long long *colmax, unsigned long long *uymax) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= nx) return;
-  const int y0 = blockIdx.y * kRows;
-  const int y1 = min(y0 + kRows, ny);
   unsigned long long mx = 0ull, my = 0ull;
-  for (int y = y0; y < y1; ++y) {
-    const size_t r = (size_t)y * nx + x;
-    if (x >= 1) mx = max(mx, abs_bits(ux[r]));
-    my = max(my, abs_bits(uy[r]));
+  if (x < nx) {
+    const int y0 = blockIdx.y * kRows;
+    const int y1 = min(y0 + kRows, ny);
+    for (int y = y0; y < y1; ++y) {
+      const size_t r = (size_t)y * nx + x;
+      if (x >= 1) mx = max(mx, abs_bits(ux[r]));
+      my = max(my, abs_bits(uy[r]));
+    }
+    if (x >= 1) atomicMax(colmax + x, mx);
   }
-  if (x >= 1) atomicMax(colmax + x, mx);
-  atomicMax(uymax, my);
+  my = warp_max_u64(my);
+  if ((threadIdx.x & 31) == 0) atomicMax(uymax, my);
 }
 
-dim3 march_grid(const DevGrid &g) { return dim3((g.nx + 127) / 128, (g.ny + kRows - 1) / kRows); }
+dim3 march_grid(const DevGrid &g, int rows = kRows) { return dim3((g.nx + 127) / 128, (g.ny + rows - 1) / rows); }
 
 int poisson_cols(const DevGrid &g) {
   // enough blocks to cover the SMs at least twice, at most 64 KiB of shared memory each
@@ -753,7 +828,7 @@ static cudaError_t launch_corr_t(const DevGrid &g, const StageScalars &s, int im
                                  double *ux, double *uy, double *p, unsigned long long *colmax,
                                  unsigned long long *uymax, cudaStream_t st) {
   const CorrArgs a{g, s, psi, ux, uy, p, colmax, uymax};
-  const dim3 grid = march_grid(g), block(128);
+  const dim3 grid = march_grid(g, kCorrRows), block(128);
 #define SNS_C(X, Y, R) k_corr<X, Y, R, CORR, PRES><<<grid, block, 0, st>>>(a)
   if (g.rcp) {
     if (impx && impy) SNS_C(1, 1, true);

@@ -276,7 +276,6 @@ static int build_context(Context *c, const param_t *param) {
   const int nh = g.nh;
   const size_t jp = (size_t)g.jpitch;
   std::vector<double> pinv((size_t)nx * jp, 0.0), pup((size_t)nx * jp, 0.0), pd0(nh);
-  std::vector<uint8_t> pzero((size_t)nx * jp, 0);
   {
     std::vector<double> l(nx), d(nx), u(nx), inv(nx), up(nx);
     std::vector<uint8_t> zero(nx);
@@ -295,12 +294,10 @@ static int build_context(Context *c, const param_t *param) {
       for (int x = 0; x < nx; x++) {
         pinv[(size_t)x * jp + J] = inv[x];
         pup[(size_t)x * jp + J] = up[x];
-        pzero[(size_t)x * jp + J] = zero[x];
       }
     }
   }
-  if ((rc = upload(c, &g.pinv, pinv)) || (rc = upload(c, &g.pup, pup)) || (rc = upload(c, &g.pzero, pzero)) ||
-      (rc = upload(c, &g.pd0, pd0)))
+  if ((rc = upload(c, &g.pinv, pinv)) || (rc = upload(c, &g.pup, pup)) || (rc = upload(c, &g.pd0, pd0)))
     return rc;
   std::vector<double> tw(2 * (size_t)ny);
   for (int t = 0; t < ny; t++) twiddle(ny, t, &tw[2 * t], &tw[2 * t + 1]);
@@ -576,17 +573,15 @@ static void y_system(const param_t *param, int rk, int is_temp, HostFactors &sub
 // copies factor arrays into the context's device buffer at word offset `off`
 static int push_factors(Context *c, const HostFactors &hf, size_t off, LineFactors &lf) {
   const size_t n = hf.l.size();
-  std::vector<double> buf(4 * n, 0.0);
+  std::vector<double> buf(3 * n, 0.0);
   std::memcpy(&buf[0], hf.l.data(), n * sizeof(double));
-  std::memcpy(&buf[n], hf.inv.data(), n * sizeof(double));
+  std::memcpy(&buf[n], hf.inv.data(), n * sizeof(double));  // 0 marks |pivot| < DBL_EPSILON rows
   std::memcpy(&buf[2 * n], hf.up.data(), n * sizeof(double));
-  std::memcpy(&buf[3 * n], hf.zero.data(), n);
   SNS_CUDA(cudaMemcpyAsync(c->fac + off, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   lf.n = (int)n;
   lf.l = c->fac + off;
   lf.inv = c->fac + off + n;
   lf.up = c->fac + off + 2 * n;
-  lf.zero = reinterpret_cast<const uint8_t *>(c->fac + off + 3 * n);
   lf.d0 = hf.d0;
   return SNS_OK;
 }

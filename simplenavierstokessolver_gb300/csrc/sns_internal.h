@@ -40,9 +40,8 @@ struct DevGrid {
   // Poisson: Thomas factors of the per-mode x-systems (src/fluid/compute_potential.c:109-136)
   const double *pl;     // [nx]            lower diagonal 1./DXC(i)/DXF(i)
   const double *pd0;    // [nh]            first pivot per mode
-  const double *pinv;   // [nx * jpitch]   1./pivot
+  const double *pinv;   // [nx * jpitch]   1./pivot; 0 where |pivot| < DBL_EPSILON (row forced to 0)
   const double *pup;    // [nx * jpitch]   normalised upper diagonal
-  const uint8_t *pzero; // [nx * jpitch]   1 where |pivot| < DBL_EPSILON (row forced to 0)
   const double *tw;     // [2*ny]          twiddles exp(-2 pi i t/ny), t < ny
   int fft_nst;          // stages of the length-ny/2 complex FFT
   int fft_first2;       // first stage radix 2 (else all radix 4)
@@ -53,10 +52,10 @@ struct DevGrid {
 struct LineFactors {
   int n;
   const double *l;      // [n] lower diagonal
-  const double *inv;    // [n] 1./pivot (row 0 unused when first_div)
+  const double *inv;    // [n] 1./pivot, 0 where |pivot| < DBL_EPSILON (row forced to 0);
+                        //     row 0 unused (first row divides by d0)
   const double *up;     // [n] normalised upper diagonal
-  const uint8_t *zero;  // [n]
-  double d0;            // first pivot (first_div mode)
+  double d0;            // first pivot
 };
 
 // Periodic y system (src/linalg.c:52-108): Thomas factors of the (n-1)
