@@ -807,7 +807,7 @@ cudaError_t launch_poisson_fwd(const DevGrid &g, const StageScalars &s, const do
 }
 
 cudaError_t launch_poisson_tri(const DevGrid &g, double2 *spec, cudaStream_t st) {
-  k_poisson_tri<<<(g.nh + 63) / 64, 64, 0, st>>>(g, spec);
+  k_poisson_tri<<<(g.nh + 31) / 32, 32, 0, st>>>(g, spec);
   count_launches(1);
   return cudaGetLastError();
 }
