@@ -449,110 +449,129 @@ __global__ void __launch_bounds__(256) k_poisson_fwd(const PoissonArgs a) {
   }
 }
 
-// Register chunk of one line for the software-pipelined Thomas sweeps: the
-// loads of the next chunk are issued before the dependent arithmetic of the
-// current one, so each sweep pays about one memory latency in total instead
-// of one per element.
-constexpr int kTriChunk = 8;
-struct TriChunk {
-  double2 v[kTriChunk];
-  double f[kTriChunk];  // 1/pivot (forward) or normalised upper diagonal (backward)
-  double l[kTriChunk];
+// Thomas sweeps with a per-thread shared-memory prefetch ring. Only
+// jtot/2+1 lines exist (17 warps at jtot = 1024), so no other warp can hide
+// the L2 latency of a serial recurrence; instead every thread keeps
+// kTriDepth chunks of kTriStage elements of its own line in flight with
+// cp.async, and the dependent arithmetic reads shared memory. Each thread
+// touches only its own ring slots, so no barrier is needed beyond the
+// initial staging of the lower diagonal.
+constexpr int kTriStage = 8;
+constexpr int kTriDepth = 8;
+constexpr int kTriMaxNx = 16384;  // lower diagonal staged in shared memory (itot limit)
+
+struct TriRing {
+  double2 v[kTriDepth][kTriStage][32];
+  double f[kTriDepth][kTriStage][32];
 };
 
-__device__ __forceinline__ void tri_load_fwd(TriChunk &c, const double2 *col, const double *inv, const double *pl,
-                                             int x0, int nx, size_t jp) {
-#pragma unroll
-  for (int k = 0; k < kTriChunk; ++k) {
-    const int x = x0 + k;
-    if (x < nx) {
-      c.v[k] = col[(size_t)x * jp];
-      c.f[k] = inv[(size_t)x * jp];
-      c.l[k] = pl[x];
-    }
-  }
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-// forward elimination step of src/linalg.c:35-44; a zero 1/pivot marks the
-// |pivot| < DBL_EPSILON rows, which the reference sets to 0
-__device__ __forceinline__ void tri_run_fwd(TriChunk &c, double2 *col, int x0, int nx, size_t jp, double2 &prev) {
+// stage `chunk` of this thread's line: elements x = x0 + dir*k, k < kTriStage,
+// that lie in [lo, hi]; always commits one group so the group count stays regular
+__device__ __forceinline__ void tri_issue(TriRing &R, int slot, const double2 *col, const double *fac, int x0, int dir,
+                                          int lo, int hi, size_t jp, int lane) {
 #pragma unroll
-  for (int k = 0; k < kTriChunk; ++k) {
-    const int x = x0 + k;
-    if (x < nx) {
-      double2 v = c.v[k];
-      const double inv = c.f[k], l = c.l[k];
-      if (inv == 0.0) {
-        v.x = 0.0;
-        v.y = 0.0;
-      } else {
-        v.x = inv * (v.x - l * prev.x);
-        v.y = inv * (v.y - l * prev.y);
-      }
-      col[(size_t)x * jp] = v;
-      prev = v;
+  for (int k = 0; k < kTriStage; ++k) {
+    const int x = x0 + dir * k;
+    if (x >= lo && x <= hi) {
+      cp_async16(&R.v[slot][k][lane], col + (size_t)x * jp);
+      cp_async8(&R.f[slot][k][lane], fac + (size_t)x * jp);
     }
   }
-}
-
-__device__ __forceinline__ void tri_load_bwd(TriChunk &c, const double2 *col, const double *up, int x0, size_t jp) {
-#pragma unroll
-  for (int k = 0; k < kTriChunk; ++k) {
-    const int x = x0 - k;
-    if (x >= 0) {
-      c.v[k] = col[(size_t)x * jp];
-      c.f[k] = up[(size_t)x * jp];
-    }
-  }
-}
-
-// back substitution of src/linalg.c:46-48
-__device__ __forceinline__ void tri_run_bwd(TriChunk &c, double2 *col, int x0, size_t jp, double2 &next) {
-#pragma unroll
-  for (int k = 0; k < kTriChunk; ++k) {
-    const int x = x0 - k;
-    if (x >= 0) {
-      double2 v = c.v[k];
-      const double u = c.f[k];
-      v.x = v.x - u * next.x;
-      v.y = v.y - u * next.y;
-      col[(size_t)x * jp] = v;
-      next = v;
-    }
-  }
+  cp_async_commit();
 }
 
 // src/fluid/compute_potential.c:109-136: per Fourier mode, Thomas along x with
 // the complex right-hand side (real and imaginary parts share the factors),
-// one thread per mode; a warp reads 32 consecutive modes (coalesced).
+// one thread per mode; a warp covers 32 consecutive modes, so every staged
+// element comes from one contiguous 512-byte row segment.
 __global__ void __launch_bounds__(32) k_poisson_tri(const DevGrid g, double2 *spec) {
-  const int J = blockIdx.x * blockDim.x + threadIdx.x;
-  if (J >= g.nh) return;
+  extern __shared__ double tri_smem[];
+  TriRing &R = *reinterpret_cast<TriRing *>(tri_smem);
+  double *pl = tri_smem + sizeof(TriRing) / sizeof(double);
+  const int lane = threadIdx.x;
   const int nx = g.nx;
+  for (int x = lane; x < nx; x += 32) pl[x] = g.pl[x];
+  __syncwarp();
+  const int J = blockIdx.x * 32 + lane;
+  if (J >= g.nh) return;
   const size_t jp = (size_t)g.jpitch;
   double2 *col = spec + J;
   const double *inv = g.pinv + J, *up = g.pup + J;
+  // ---- forward elimination, x = 1..nx-1 (src/linalg.c:33-45)
   const double d0 = g.pd0[J];
   double2 prev = col[0];
   prev.x = prev.x / d0;
   prev.y = prev.y / d0;
   col[0] = prev;
-  TriChunk a, b;
-  tri_load_fwd(a, col, inv, g.pl, 1, nx, jp);
-  for (int x0 = 1; x0 < nx; x0 += 2 * kTriChunk) {
-    tri_load_fwd(b, col, inv, g.pl, x0 + kTriChunk, nx, jp);
-    tri_run_fwd(a, col, x0, nx, jp, prev);
-    tri_load_fwd(a, col, inv, g.pl, x0 + 2 * kTriChunk, nx, jp);
-    tri_run_fwd(b, col, x0 + kTriChunk, nx, jp, prev);
+  const int nfwd = (nx - 1 + kTriStage - 1) / kTriStage;
+#pragma unroll 1
+  for (int c = 0; c < kTriDepth - 1; ++c) tri_issue(R, c, col, inv, 1 + c * kTriStage, 1, 1, nx - 1, jp, lane);
+#pragma unroll 1
+  for (int c = 0; c < nfwd; ++c) {
+    const int ahead = c + kTriDepth - 1;
+    tri_issue(R, ahead % kTriDepth, col, inv, 1 + ahead * kTriStage, 1, 1, nx - 1, jp, lane);
+    cp_async_wait<kTriDepth - 1>();
+    const int slot = c % kTriDepth;
+#pragma unroll
+    for (int k = 0; k < kTriStage; ++k) {
+      const int x = 1 + c * kTriStage + k;
+      if (x < nx) {
+        double2 v = R.v[slot][k][lane];
+        const double iv = R.f[slot][k][lane], l = pl[x];
+        if (iv == 0.0) {  // |pivot| < DBL_EPSILON: the reference sets the row to 0
+          v.x = 0.0;
+          v.y = 0.0;
+        } else {
+          v.x = iv * (v.x - l * prev.x);
+          v.y = iv * (v.y - l * prev.y);
+        }
+        col[(size_t)x * jp] = v;
+        prev = v;
+      }
+    }
   }
+  cp_async_wait<0>();
+  __threadfence_block();  // the back substitution re-reads values stored above
+  // ---- back substitution, x = nx-2..0 (src/linalg.c:46-48)
   double2 next = prev;
-  tri_load_bwd(a, col, up, nx - 2, jp);
-  for (int x0 = nx - 2; x0 >= 0; x0 -= 2 * kTriChunk) {
-    tri_load_bwd(b, col, up, x0 - kTriChunk, jp);
-    tri_run_bwd(a, col, x0, jp, next);
-    tri_load_bwd(a, col, up, x0 - 2 * kTriChunk, jp);
-    tri_run_bwd(b, col, x0 - kTriChunk, jp, next);
+  const int nbwd = (nx - 1 + kTriStage - 1) / kTriStage;
+#pragma unroll 1
+  for (int c = 0; c < kTriDepth - 1; ++c)
+    tri_issue(R, c, col, up, nx - 2 - c * kTriStage, -1, 0, nx - 2, jp, lane);
+#pragma unroll 1
+  for (int c = 0; c < nbwd; ++c) {
+    const int ahead = c + kTriDepth - 1;
+    tri_issue(R, ahead % kTriDepth, col, up, nx - 2 - ahead * kTriStage, -1, 0, nx - 2, jp, lane);
+    cp_async_wait<kTriDepth - 1>();
+    const int slot = c % kTriDepth;
+#pragma unroll
+    for (int k = 0; k < kTriStage; ++k) {
+      const int x = nx - 2 - c * kTriStage - k;
+      if (x >= 0) {
+        double2 v = R.v[slot][k][lane];
+        const double u = R.f[slot][k][lane];
+        v.x = v.x - u * next.x;
+        v.y = v.y - u * next.y;
+        col[(size_t)x * jp] = v;
+        next = v;
+      }
+    }
   }
+  cp_async_wait<0>();
 }
 
 // src/fluid/compute_potential.c:146-157: inverse real DFT along y and the
@@ -807,7 +826,14 @@ cudaError_t launch_poisson_fwd(const DevGrid &g, const StageScalars &s, const do
 }
 
 cudaError_t launch_poisson_tri(const DevGrid &g, double2 *spec, cudaStream_t st) {
-  k_poisson_tri<<<(g.nh + 31) / 32, 32, 0, st>>>(g, spec);
+  static bool attr = false;
+  const size_t smem = sizeof(TriRing) + sizeof(double) * (size_t)g.nx;
+  if (!attr) {
+    cudaFuncSetAttribute(k_poisson_tri, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(sizeof(TriRing) + sizeof(double) * (size_t)kTriMaxNx));
+    attr = true;
+  }
+  k_poisson_tri<<<(g.nh + 31) / 32, 32, smem, st>>>(g, spec);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -315,7 +315,8 @@ static int check_inputs(const param_t *param, const parallel_t *parallel) {
   if (!param || !parallel) return fail(SNS_ERR_ARG, "param and parallel must not be NULL");
   if (parallel->mpisize != 1)
     return fail(SNS_ERR_UNSUPPORTED, "single-rank only (mpisize=%d); one GPU holds the whole domain", parallel->mpisize);
-  if (param->itot < 2) return fail(SNS_ERR_UNSUPPORTED, "itot=%d < 2", param->itot);
+  if (param->itot < 2 || param->itot > 16384)
+    return fail(SNS_ERR_UNSUPPORTED, "itot=%d outside [2, 16384]", param->itot);
   if (param->jtot < 2 || !is_pow2(param->jtot) || param->jtot > 16384)
     return fail(SNS_ERR_UNSUPPORTED, "jtot=%d must be a power of two in [2, 16384] (real FFT along y)", param->jtot);
   if (!param->dxf || !param->dxc) return fail(SNS_ERR_ARG, "param grid arrays are NULL");
