@@ -32,7 +32,8 @@ __device__ __forceinline__ double dv(double a, double d, double rd) {
 __device__ __forceinline__ int wrap_up(int y, int ny) { return y + 1 == ny ? 0 : y + 1; }
 __device__ __forceinline__ int wrap_dn(int y, int ny) { return y == 0 ? ny - 1 : y - 1; }
 
-constexpr int kRows = 16;  // rows marched by one thread in the stencil kernels
+constexpr int kRows = 8;     // rows marched by one thread in the stencil kernels
+constexpr int kBlockX = 64;  // columns per block: ~6-7 blocks per SM at 512 x 1024 for load balance
 
 // ---------------------------------------------------------------- temperature
 struct TempArgs {
@@ -449,26 +450,25 @@ __global__ void __launch_bounds__(256) k_poisson_fwd(const PoissonArgs a) {
   }
 }
 
-// Thomas sweeps with a per-thread shared-memory prefetch ring. Only
-// jtot/2+1 lines exist (17 warps at jtot = 1024), so no other warp can hide
-// the L2 latency of a serial recurrence; instead every thread keeps
-// kTriDepth chunks of kTriStage elements of its own line in flight with
-// cp.async, and the dependent arithmetic reads shared memory. Each thread
-// touches only its own ring slots, so no barrier is needed beyond the
-// initial staging of the lower diagonal.
+// Thomas sweeps of the Poisson modes. On this GPU an FP64 warp instruction
+// occupies the sub-partition's FP64 pipe for the same time whether 1 or 32
+// lanes are active, and the recurrence is serial in x, so the sweep is bound
+// by the FP64 instructions one warp issues per element. Each warp therefore
+// carries one component (real or imaginary) of 32 modes -- 3 FP64
+// instructions per element forward, 2 backward -- and the two components of
+// a mode run in different blocks (different SMs). The zero-pivot test reads
+// the bits of 1/pivot with integer instructions. A per-thread cp.async ring
+// keeps kTriDepth chunks of the line in flight; each thread touches only its
+// own ring slots.
 constexpr int kTriStage = 8;
 constexpr int kTriDepth = 8;
 constexpr int kTriMaxNx = 16384;  // lower diagonal staged in shared memory (itot limit)
 
 struct TriRing {
-  double2 v[kTriDepth][kTriStage][32];
+  double v[kTriDepth][kTriStage][32];
   double f[kTriDepth][kTriStage][32];
 };
 
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
-}
 __device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
   const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
@@ -479,25 +479,25 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-// stage `chunk` of this thread's line: elements x = x0 + dir*k, k < kTriStage,
-// that lie in [lo, hi]; always commits one group so the group count stays regular
-__device__ __forceinline__ void tri_issue(TriRing &R, int slot, const double2 *col, const double *fac, int x0, int dir,
-                                          int lo, int hi, size_t jp, int lane) {
+// stage elements x = x0 + dir*k (k < kTriStage) lying in [lo, hi]; always
+// commits one group so that the group count stays regular
+__device__ __forceinline__ void tri_issue(TriRing &R, int slot, const double *val, const double *fac, int x0,
+                                          int dir, int lo, int hi, size_t vs, size_t fs, int lane) {
 #pragma unroll
   for (int k = 0; k < kTriStage; ++k) {
     const int x = x0 + dir * k;
     if (x >= lo && x <= hi) {
-      cp_async16(&R.v[slot][k][lane], col + (size_t)x * jp);
-      cp_async8(&R.f[slot][k][lane], fac + (size_t)x * jp);
+      cp_async8(&R.v[slot][k][lane], val + (size_t)x * vs);
+      cp_async8(&R.f[slot][k][lane], fac + (size_t)x * fs);
     }
   }
   cp_async_commit();
 }
 
-// src/fluid/compute_potential.c:109-136: per Fourier mode, Thomas along x with
-// the complex right-hand side (real and imaginary parts share the factors),
-// one thread per mode; a warp covers 32 consecutive modes, so every staged
-// element comes from one contiguous 512-byte row segment.
+// src/fluid/compute_potential.c:109-136 with src/linalg.c:32-50: per Fourier
+// mode, Thomas along x with the complex right-hand side; real and imaginary
+// parts undergo identical real operations (real matrix), so they are solved
+// as independent real lines. blockIdx.y selects the component.
 __global__ void __launch_bounds__(32) k_poisson_tri(const DevGrid g, double2 *spec) {
   extern __shared__ double tri_smem[];
   TriRing &R = *reinterpret_cast<TriRing *>(tri_smem);
@@ -509,37 +509,30 @@ __global__ void __launch_bounds__(32) k_poisson_tri(const DevGrid g, double2 *sp
   const int J = blockIdx.x * 32 + lane;
   if (J >= g.nh) return;
   const size_t jp = (size_t)g.jpitch;
-  double2 *col = spec + J;
+  double *col = reinterpret_cast<double *>(spec + J) + blockIdx.y;  // stride 2*jp doubles per x
+  const size_t vs = 2 * jp;
   const double *inv = g.pinv + J, *up = g.pup + J;
   // ---- forward elimination, x = 1..nx-1 (src/linalg.c:33-45)
-  const double d0 = g.pd0[J];
-  double2 prev = col[0];
-  prev.x = prev.x / d0;
-  prev.y = prev.y / d0;
+  double prev = col[0] / g.pd0[J];
   col[0] = prev;
-  const int nfwd = (nx - 1 + kTriStage - 1) / kTriStage;
+  const int nel = nx - 1;
+  const int nchunk = (nel + kTriStage - 1) / kTriStage;
 #pragma unroll 1
-  for (int c = 0; c < kTriDepth - 1; ++c) tri_issue(R, c, col, inv, 1 + c * kTriStage, 1, 1, nx - 1, jp, lane);
+  for (int c = 0; c < kTriDepth - 1; ++c) tri_issue(R, c, col, inv, 1 + c * kTriStage, 1, 1, nx - 1, vs, jp, lane);
 #pragma unroll 1
-  for (int c = 0; c < nfwd; ++c) {
+  for (int c = 0; c < nchunk; ++c) {
     const int ahead = c + kTriDepth - 1;
-    tri_issue(R, ahead % kTriDepth, col, inv, 1 + ahead * kTriStage, 1, 1, nx - 1, jp, lane);
+    tri_issue(R, ahead % kTriDepth, col, inv, 1 + ahead * kTriStage, 1, 1, nx - 1, vs, jp, lane);
     cp_async_wait<kTriDepth - 1>();
     const int slot = c % kTriDepth;
 #pragma unroll
     for (int k = 0; k < kTriStage; ++k) {
       const int x = 1 + c * kTriStage + k;
       if (x < nx) {
-        double2 v = R.v[slot][k][lane];
-        const double iv = R.f[slot][k][lane], l = pl[x];
-        if (iv == 0.0) {  // |pivot| < DBL_EPSILON: the reference sets the row to 0
-          v.x = 0.0;
-          v.y = 0.0;
-        } else {
-          v.x = iv * (v.x - l * prev.x);
-          v.y = iv * (v.y - l * prev.y);
-        }
-        col[(size_t)x * jp] = v;
+        const double iv = R.f[slot][k][lane];
+        // |pivot| < DBL_EPSILON rows carry 1/pivot = +0: the reference sets them to 0
+        const double v = __double_as_longlong(iv) == 0 ? 0.0 : iv * (R.v[slot][k][lane] - pl[x] * prev);
+        col[(size_t)x * vs] = v;
         prev = v;
       }
     }
@@ -547,26 +540,22 @@ __global__ void __launch_bounds__(32) k_poisson_tri(const DevGrid g, double2 *sp
   cp_async_wait<0>();
   __threadfence_block();  // the back substitution re-reads values stored above
   // ---- back substitution, x = nx-2..0 (src/linalg.c:46-48)
-  double2 next = prev;
-  const int nbwd = (nx - 1 + kTriStage - 1) / kTriStage;
+  double next = prev;
 #pragma unroll 1
   for (int c = 0; c < kTriDepth - 1; ++c)
-    tri_issue(R, c, col, up, nx - 2 - c * kTriStage, -1, 0, nx - 2, jp, lane);
+    tri_issue(R, c, col, up, nx - 2 - c * kTriStage, -1, 0, nx - 2, vs, jp, lane);
 #pragma unroll 1
-  for (int c = 0; c < nbwd; ++c) {
+  for (int c = 0; c < nchunk; ++c) {
     const int ahead = c + kTriDepth - 1;
-    tri_issue(R, ahead % kTriDepth, col, up, nx - 2 - ahead * kTriStage, -1, 0, nx - 2, jp, lane);
+    tri_issue(R, ahead % kTriDepth, col, up, nx - 2 - ahead * kTriStage, -1, 0, nx - 2, vs, jp, lane);
     cp_async_wait<kTriDepth - 1>();
     const int slot = c % kTriDepth;
 #pragma unroll
     for (int k = 0; k < kTriStage; ++k) {
       const int x = nx - 2 - c * kTriStage - k;
       if (x >= 0) {
-        double2 v = R.v[slot][k][lane];
-        const double u = R.f[slot][k][lane];
-        v.x = v.x - u * next.x;
-        v.y = v.y - u * next.y;
-        col[(size_t)x * jp] = v;
+        const double v = R.v[slot][k][lane] - R.f[slot][k][lane] * next;
+        col[(size_t)x * vs] = v;
         next = v;
       }
     }
@@ -625,9 +614,10 @@ struct CorrArgs {
 
 __device__ __forceinline__ unsigned long long abs_bits(double v) {
   // |v| as an order-preserving key; NaN counts as 0 (fmax(NaN, small) = small
-  // in src/param/decide_dt.c:147,155)
-  const double a = fabs(v);
-  return a == a ? (unsigned long long)__double_as_longlong(a) : 0ull;
+  // in src/param/decide_dt.c:147,155). Integer operations only: an FP64
+  // compare would occupy the (slow) FP64 pipe.
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+  return b > 0x7ff0000000000000ull ? 0ull : b;
 }
 
 constexpr int kCorrRows = 4;  // rows per thread in the (memory-latency bound) correction kernels
@@ -717,7 +707,15 @@ __global__ void __launch_bounds__(128) k_umax(int nx, int ny, const double *ux, 
   if ((threadIdx.x & 31) == 0) atomicMax(uymax, my);
 }
 
-dim3 march_grid(const DevGrid &g, int rows = kRows) { return dim3((g.nx + 127) / 128, (g.ny + rows - 1) / rows); }
+dim3 march_grid(const DevGrid &g, int rows = kRows) {
+  return dim3((g.nx + kBlockX - 1) / kBlockX, (g.ny + rows - 1) / rows);
+}
+
+// one thread per radix-4 butterfly of a stage, 64..256 per block
+int poisson_threads(const DevGrid &g, int cols) {
+  const int b = cols * (g.ny / 2) / 4;
+  return b <= 64 ? 64 : b >= 256 ? 256 : (b + 31) / 32 * 32;
+}
 
 int poisson_cols(const DevGrid &g) {
   // enough blocks to cover the SMs at least twice, at most 64 KiB of shared memory each
@@ -733,7 +731,7 @@ cudaError_t launch_temp_update(const DevGrid &g, const StageScalars &s, int impx
                                const double *t_in, double *t_out, double *at, double *qt,
                                const double *ux, const double *uy, cudaStream_t st) {
   const TempArgs a{g, s, t_in, t_out, at, qt, ux, uy};
-  const dim3 grid = march_grid(g), block(128);
+  const dim3 grid = march_grid(g), block(kBlockX);
 #define SNS_T(X, Y, R) k_temp<X, Y, R><<<grid, block, 0, st>>>(a)
   if (g.rcp) {
     if (impx && impy) SNS_T(1, 1, true);
@@ -756,7 +754,7 @@ cudaError_t launch_velocity_update(const DevGrid &g, const StageScalars &s, int 
                                    double *ux_out, double *uy_out, double *aux, double *auy,
                                    double *qx, double *qy, cudaStream_t st) {
   const VelArgs a{g, s, ux, uy, p, tforce, ux_out, uy_out, aux, auy, qx, qy};
-  const dim3 grid = march_grid(g), block(128);
+  const dim3 grid = march_grid(g), block(kBlockX);
 #define SNS_V(X, Y, R) k_vel<X, Y, R><<<grid, block, 0, st>>>(a)
   if (g.rcp) {
     if (impx && impy) SNS_V(1, 1, true);
@@ -817,9 +815,9 @@ cudaError_t launch_poisson_fwd(const DevGrid &g, const StageScalars &s, const do
   const PoissonArgs a{g, s, ux, uy, spec, nullptr, C};
   const int blocks = (g.nx + C - 1) / C;
   if (g.rcp) {
-    k_poisson_fwd<true><<<blocks, 256, smem, st>>>(a);
+    k_poisson_fwd<true><<<blocks, poisson_threads(g, C), smem, st>>>(a);
   } else {
-    k_poisson_fwd<false><<<blocks, 256, smem, st>>>(a);
+    k_poisson_fwd<false><<<blocks, poisson_threads(g, C), smem, st>>>(a);
   }
   count_launches(1);
   return cudaGetLastError();
@@ -833,7 +831,7 @@ cudaError_t launch_poisson_tri(const DevGrid &g, double2 *spec, cudaStream_t st)
                          (int)(sizeof(TriRing) + sizeof(double) * (size_t)kTriMaxNx));
     attr = true;
   }
-  k_poisson_tri<<<(g.nh + 31) / 32, 32, smem, st>>>(g, spec);
+  k_poisson_tri<<<dim3((g.nh + 31) / 32, 2), 32, smem, st>>>(g, spec);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -844,7 +842,7 @@ cudaError_t launch_poisson_bwd(const DevGrid &g, const StageScalars &s, const do
   const int C = poisson_setup(g, &smem);
   const PoissonArgs a{g, s, nullptr, nullptr, const_cast<double2 *>(spec), psi, C};
   const int blocks = (g.nx + C - 1) / C;
-  k_poisson_bwd<<<blocks, 256, smem, st>>>(a);
+  k_poisson_bwd<<<blocks, poisson_threads(g, C), smem, st>>>(a);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -854,7 +852,7 @@ static cudaError_t launch_corr_t(const DevGrid &g, const StageScalars &s, int im
                                  double *ux, double *uy, double *p, unsigned long long *colmax,
                                  unsigned long long *uymax, cudaStream_t st) {
   const CorrArgs a{g, s, psi, ux, uy, p, colmax, uymax};
-  const dim3 grid = march_grid(g, kCorrRows), block(128);
+  const dim3 grid = march_grid(g, kCorrRows), block(kBlockX);
 #define SNS_C(X, Y, R) k_corr<X, Y, R, CORR, PRES><<<grid, block, 0, st>>>(a)
   if (g.rcp) {
     if (impx && impy) SNS_C(1, 1, true);
@@ -890,7 +888,7 @@ cudaError_t launch_correct_pressure(const DevGrid &g, const StageScalars &s, int
 
 cudaError_t launch_umax(const DevGrid &g, const double *ux, const double *uy, unsigned long long *colmax,
                         unsigned long long *uymax, cudaStream_t st) {
-  k_umax<<<march_grid(g), 128, 0, st>>>(g.nx, g.ny, ux, uy, colmax, uymax);
+  k_umax<<<march_grid(g), kBlockX, 0, st>>>(g.nx, g.ny, ux, uy, colmax, uymax);
   count_launches(1);
   return cudaGetLastError();
 }
