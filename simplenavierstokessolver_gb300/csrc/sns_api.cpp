@@ -19,6 +19,7 @@
 #include <string>
 #include <vector>
 
+#include "host_common.h"
 #include "sns_gpu.h"
 #include "sns_internal.h"
 
@@ -46,7 +47,6 @@ static int fail(int code, const char *fmt, ...) {
       return fail(SNS_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
   } while (0)
 
-constexpr double kPi = 3.1415926535897932;  // include/common.h:7
 constexpr uint64_t kFluidMagic = 0x534e53464c554944ull;  // "SNSFLUID"
 constexpr uint64_t kTempMagic = 0x534e5354454d5045ull;   // "SNSTEMPE"
 
@@ -168,55 +168,6 @@ static int upload(Context *c, const T **dst, const std::vector<T> &src) {
   return SNS_OK;
 }
 
-// Thomas forward elimination of a constant matrix (src/linalg.c:11-24): the
-// RHS-independent part, stored so that the device repeats only the RHS work.
-static void factorize(int n, const double *l, const double *d, const double *u, double *inv, double *up,
-                      uint8_t *zero) {
-  up[0] = u[0] / d[0];
-  inv[0] = 0.0;
-  zero[0] = 0;
-  for (int i = 1; i <= n - 1; i++) {
-    double v = d[i] - l[i] * up[i - 1];
-    if (std::fabs(v) < DBL_EPSILON) {
-      up[i] = 0.;
-      inv[i] = 0.;
-      zero[i] = 1;
-    } else {
-      v = 1. / v;
-      up[i] = v * u[i];
-      inv[i] = v;
-      zero[i] = 0;
-    }
-  }
-}
-
-// same twiddle rule as the CPU FFT: exp(-2 pi i t/n), exact at multiples of
-// pi/2, libm cos/sin only on [0, pi/4]
-static void twiddle(int n, int t, double *re, double *im) {
-  const long t4 = 4L * t;
-  const long q = t4 / n;
-  const long r = t4 - q * (long)n;
-  double c, s;
-  if (2 * r <= n) {
-    const double a = (3.14159265358979323846 * (double)r) / (2.0 * (double)n);
-    c = std::cos(a);
-    s = std::sin(a);
-  } else {
-    const double a = (3.14159265358979323846 * (double)(n - r)) / (2.0 * (double)n);
-    c = std::sin(a);
-    s = std::cos(a);
-  }
-  double cq, sq;
-  switch (q & 3) {
-    case 0: cq = c; sq = s; break;
-    case 1: cq = -s; sq = c; break;
-    case 2: cq = -c; sq = -s; break;
-    default: cq = s; sq = -c; break;
-  }
-  *re = cq;
-  *im = -sq;
-}
-
 static void destroy_context(Context *c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);
@@ -278,10 +229,9 @@ static int build_context(Context *c, const param_t *param) {
   std::vector<double> pinv((size_t)nx * jp, 0.0), pup((size_t)nx * jp, 0.0), pd0(nh);
   {
     std::vector<double> l(nx), d(nx), u(nx), inv(nx), up(nx);
-    std::vector<uint8_t> zero(nx);
     const double dy = param->dy;
     for (int J = 0; J < nh; J++) {
-      const double eig = -4. / pow(dy, 2.) * pow(sin(kPi * (J) / (1. * ny)), 2.);
+      const double eig = poisson_eigenvalue(dy, ny, J);
       for (int i = 1; i <= nx; i++) {
         l[i - 1] = 1. / DXC(i) / DXF(i);
         u[i - 1] = 1. / DXC(i + 1) / DXF(i);
@@ -289,7 +239,7 @@ static int build_context(Context *c, const param_t *param) {
       for (int i = 1; i <= nx; i++) d[i - 1] = -l[i - 1] - u[i - 1] + eig;
       d[0] += l[0];
       d[nx - 1] += u[nx - 1];
-      factorize(nx, l.data(), d.data(), u.data(), inv.data(), up.data(), zero.data());
+      factorize(nx, l.data(), d.data(), u.data(), inv.data(), up.data());
       pd0[J] = d[0];
       for (int x = 0; x < nx; x++) {
         pinv[(size_t)x * jp + J] = inv[x];
@@ -299,13 +249,9 @@ static int build_context(Context *c, const param_t *param) {
   }
   if ((rc = upload(c, &g.pinv, pinv)) || (rc = upload(c, &g.pup, pup)) || (rc = upload(c, &g.pd0, pd0)))
     return rc;
-  std::vector<double> tw(2 * (size_t)ny);
-  for (int t = 0; t < ny; t++) twiddle(ny, t, &tw[2 * t], &tw[2 * t + 1]);
+  const std::vector<double> tw = twiddle_table(ny);
   if ((rc = upload(c, &g.tw, tw))) return rc;
-  int p = 0;
-  while ((1 << p) < ny / 2) p++;
-  g.fft_first2 = p & 1;
-  g.fft_nst = (p & 1) + p / 2;
+  fft_layout(ny, &g.fft_nst, &g.fft_first2);
   SNS_CUDA(cudaMallocHost(&c->staging, sizeof(double) * (size_t)nx * ny));
   SNS_CUDA(cudaMallocHost(&c->red_host, sizeof(unsigned long long) * (size_t)(nx + 1)));
   return SNS_OK;
@@ -475,7 +421,6 @@ static StageScalars stage_scalars(const param_t *param, int rk) {
 // Factor buffer layout (doubles): [l | inv | up | zero-as-bytes] per system.
 struct HostFactors {
   std::vector<double> l, inv, up;
-  std::vector<uint8_t> zero;
   double d0 = 0;
 };
 
@@ -519,8 +464,7 @@ static void x_system(const param_t *param, int rk, int kind, HostFactors &hf) {
   hf.l = l;
   hf.inv.assign(n, 0.);
   hf.up.assign(n, 0.);
-  hf.zero.assign(n, 0);
-  factorize(n, l.data(), d.data(), u.data(), hf.inv.data(), hf.up.data(), hf.zero.data());
+  factorize(n, l.data(), d.data(), u.data(), hf.inv.data(), hf.up.data());
   hf.d0 = d[0];
 }
 
@@ -543,8 +487,7 @@ static void y_system(const param_t *param, int rk, int is_temp, HostFactors &sub
   sub.l.assign(l.begin(), l.begin() + m);
   sub.inv.assign(m, 0.);
   sub.up.assign(m, 0.);
-  sub.zero.assign(m, 0);
-  factorize(m, l.data(), d.data(), u.data(), sub.inv.data(), sub.up.data(), sub.zero.data());
+  factorize(m, l.data(), d.data(), u.data(), sub.inv.data(), sub.up.data());
   sub.d0 = d[0];
   // second small system: RHS (-l[0], 0, ..., 0, -u[n-2]) (src/linalg.c:75-87), full Thomas
   q1.assign(m, 0.);
@@ -821,28 +764,8 @@ param_t *sns_param_create(int itot, int jtot, double ly, double stretch_in, doub
   param->dxc = static_cast<double *>(calloc(itot + 1, sizeof(double)));
   param->yf = static_cast<double *>(calloc(jtot + 1, sizeof(double)));
   param->yc = static_cast<double *>(calloc(jtot, sizeof(double)));
-  double *xf = param->xf, *xc = param->xc, *dxf = param->dxf, *dxc = param->dxc;
-  const double lx = param->lx;
-  int stretch = (int)param->stretch;
-  if (stretch < 0) stretch = 0;
-  if (stretch >= itot / 2) {
-    const double dx = lx / itot;
-    for (int i = 1; i <= itot + 1; i++) xf[i - 1] = 1. * (i - 1) * dx;
-  } else {
-    for (int i = 1; i <= itot + 1; i++) xf[i - 1] = cos(kPi * (1. * (i - 1) + stretch) / (itot + 2. * stretch));
-    const double mn = xf[0], mx = xf[itot];
-    for (int i = 1; i <= itot + 1; i++) xf[i - 1] = lx * (xf[i - 1] - mn) / (mx - mn);
-  }
-  xf[0] = 0.;
-  xf[itot] = lx;
-  for (int i = 1; i <= itot; i++) dxf[i - 1] = xf[i] - xf[i - 1];
-  xc[0] = xf[0];
-  for (int i = 1; i <= itot; i++) xc[i] = 0.5 * (xf[i - 1] + xf[i]);
-  xc[itot + 1] = xf[itot];
-  for (int i = 1; i <= itot + 1; i++) dxc[i - 1] = xc[i] - xc[i - 1];
-  param->dy = ly / jtot;
-  for (int j = 1; j <= jtot + 1; j++) param->yf[j - 1] = 1. * (j - 1) * param->dy;
-  for (int j = 1; j <= jtot; j++) param->yc[j - 1] = 0.5 * (2 * j - 1) * param->dy;
+  make_grid(itot, jtot, param->lx, ly, stretch_in, param->xf, param->xc, param->dxf, param->dxc, param->yf, param->yc,
+            &param->dy);
   // src/param/init.c:197-213
   param->rkcoefs[0].alpha = 32. / 60.;
   param->rkcoefs[0].beta = 0. / 60.;
