@@ -1,0 +1,86 @@
+/*
+ * sns_batch.h -- C ABI of the batched precision form of libsns_gpu.so.
+ *
+ * Many independent Rayleigh-Benard cases of uneven grid size and Ra/Pr
+ * advance together: every kernel launch of a time step covers all resident
+ * cases (work lists of (case, tile) units), and the step is replayed as one
+ * CUDA graph. Stencils, RK3 updates and halo traffic run in FP32; the Poisson
+ * solve (real DFT along y, tridiagonal along x), the divergence, the pressure
+ * and the scalar potential stay FP64. Results therefore differ from the
+ * reference by round-off growth, not bit for bit (the plain path of
+ * sns_gpu.h is the bit-exact drop-in).
+ *
+ * Scheme: the reference's SMR-RK3 step (src/main.c:79-101) with explicit
+ * diffusion in both directions; dt per case from the reference's advective
+ * limit (src/param/decide_dt.c:35-50) and the explicit diffusive limits, or a
+ * fixed dt. No reference counterpart exists for the batching itself: the
+ * reference runs one case per MPI job.
+ *
+ * Memory: one device arena of the size given at creation; a case is admitted
+ * only if its footprint (sns_batch_case_bytes) fits, so admission control
+ * by HBM footprint is a call away. Fields stay device-resident until read.
+ *
+ * Limits: jtot a power of two in [8, 8192]; itot a multiple of 32 in
+ * [64, 4096]; lx = 1.
+ */
+#ifndef SNS_BATCH_H
+#define SNS_BATCH_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct sns_batch sns_batch;
+
+typedef struct sns_case_desc {
+  int itot, jtot;            /* cells in x (wall-bounded) and y (periodic) */
+  double ly;                 /* domain height in y; lx is 1 */
+  double stretch;            /* >= itot/2: uniform x grid, else clipped Chebyshev (src/param/init.c:148-166) */
+  double Ra, Pr;
+  int with_temperature, with_thermal_forcing;
+  long long steps;           /* steps after which the case is complete (0: never) */
+  unsigned long long seed;   /* 0: the reference's own initial noise (srand(0); rand()),
+                                else SplitMix64(seed) uniform noise in [-0.05, 0.05] */
+  double fixed_dt;           /* > 0: use this dt every step instead of the CFL decision */
+} sns_case_desc;
+
+/* a batch with a device arena of hbm_bytes and room for max_cases cases */
+extern sns_batch *sns_batch_create(size_t hbm_bytes, int max_cases);
+extern int sns_batch_destroy(sns_batch *batch);
+/* arena bytes one case of this description occupies */
+extern size_t sns_batch_case_bytes(const sns_case_desc *desc);
+/* free arena bytes (largest contiguous block) */
+extern size_t sns_batch_free_bytes(const sns_batch *batch);
+/* admits a case; temp_init: optional initial temperature in the reference's
+ * (jtot+2) x (itot+2) layout (interior used). Fails with SNS_ERR_OOM when it
+ * does not fit, SNS_ERR_UNSUPPORTED for sizes outside the limits. */
+extern int sns_batch_add(sns_batch *batch, const sns_case_desc *desc, const double *temp_init, int *slot);
+/* releases a case's slot and arena memory (waits for queued work first) */
+extern int sns_batch_remove(sns_batch *batch, int slot);
+/* every resident, unfinished case advances nsteps time steps; enqueued on the
+ * batch's stream, returns without waiting */
+extern int sns_batch_step(sns_batch *batch, int nsteps);
+extern int sns_batch_synchronize(sns_batch *batch);
+extern void *sns_batch_stream(const sns_batch *batch);
+/* state of one case in the reference's layouts, as FP64 (halos and walls
+ * filled by the reference's rules); any pointer may be NULL. Waits. */
+extern int sns_batch_state(sns_batch *batch, int slot, double *ux, double *uy, double *p, double *psi,
+                           double *temp);
+/* time, dt of the next step, completed steps, done flag (steps reached). Waits. */
+extern int sns_batch_case_status(sns_batch *batch, int slot, double *time, double *dt, long long *step, int *done);
+/* number of resident cases; their slots written to slots[0..max) */
+extern int sns_batch_cases(const sns_batch *batch, int *slots, int max);
+/* cells summed over resident unfinished cases (the host knows every case's
+ * step count: each sns_batch_step step advances every unfinished case once) */
+extern long long sns_batch_active_cells(const sns_batch *batch);
+/* the initial temperature a case of this description starts from, in the
+ * reference's (jtot+2) x (itot+2) layout (for checking against other solvers) */
+extern int sns_batch_initial_temperature(const sns_case_desc *desc, double *temp);
+/* errors of these calls are reported by sns_last_error() (include/sns_gpu.h) */
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SNS_BATCH_H */

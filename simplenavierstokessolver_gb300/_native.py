@@ -68,7 +68,16 @@ class Temperature(ctypes.Structure):
     _fields_ = [("temp", _PD), ("tempforcex", _PD), ("srctempa", _PD), ("srctempb", _PD), ("srctempg", _PD)]
 
 
+class CaseDesc(ctypes.Structure):
+    """sns_case_desc (include/sns_batch.h)."""
+
+    _fields_ = [("itot", c_int), ("jtot", c_int), ("ly", c_double), ("stretch", c_double), ("Ra", c_double),
+                ("Pr", c_double), ("with_temperature", c_int), ("with_thermal_forcing", c_int),
+                ("steps", c_longlong), ("seed", ctypes.c_ulonglong), ("fixed_dt", c_double)]
+
+
 PP, PL, PF, PT = POINTER(Param), POINTER(Parallel), POINTER(Fluid), POINTER(Temperature)
+PCD = POINTER(CaseDesc)
 
 # name -> (restype, argtypes)
 PROTOTYPES = {
@@ -103,6 +112,21 @@ PROTOTYPES = {
     "sns_profile": (c_int, [PF, c_int]),
     "sns_profile_read": (c_int, [PF, POINTER(c_double), POINTER(c_longlong), c_int]),
     "sns_profile_kind_name": (c_char_p, [c_int]),
+    # include/sns_batch.h
+    "sns_batch_create": (c_void_p, [c_size_t, c_int]),
+    "sns_batch_destroy": (c_int, [c_void_p]),
+    "sns_batch_case_bytes": (c_size_t, [PCD]),
+    "sns_batch_free_bytes": (c_size_t, [c_void_p]),
+    "sns_batch_add": (c_int, [c_void_p, PCD, _PD, POINTER(c_int)]),
+    "sns_batch_remove": (c_int, [c_void_p, c_int]),
+    "sns_batch_step": (c_int, [c_void_p, c_int]),
+    "sns_batch_synchronize": (c_int, [c_void_p]),
+    "sns_batch_stream": (c_void_p, [c_void_p]),
+    "sns_batch_state": (c_int, [c_void_p, c_int, _PD, _PD, _PD, _PD, _PD]),
+    "sns_batch_case_status": (c_int, [c_void_p, c_int, _PD, _PD, POINTER(c_longlong), POINTER(c_int)]),
+    "sns_batch_cases": (c_int, [c_void_p, POINTER(c_int), c_int]),
+    "sns_batch_active_cells": (c_longlong, [c_void_p]),
+    "sns_batch_initial_temperature": (c_int, [PCD, _PD]),
 }
 
 _lib = None

@@ -36,7 +36,9 @@ def cuda_home() -> str:
 # translation unit -> extra flags. fmad=false: bit-identical FP64 path.
 UNITS = {
     "plain_fp64.cu": ["--fmad=false"],
+    "batch_fp32.cu": [],
     "sns_api.cpp": [],
+    "batch_api.cpp": [],
 }
 
 

@@ -1,0 +1,759 @@
+// Host side of the batched FP32-stencil / FP64-Poisson engine (include/sns_batch.h).
+//
+// A batch owns one device arena. Each admitted case gets one contiguous
+// block of it (first fit, coalescing free list), a slot in the device case
+// table and work items in the per-phase work lists. One time step of every
+// resident case is a fixed sequence of 16 launches, captured once per case
+// set into a CUDA graph and replayed per step; every case carries its own dt,
+// time, step count and buffer parity in the device table, so cases of
+// different age and size share the launches.
+#include <cfloat>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "batch_internal.h"
+#include "host_common.h"
+#include "sns_batch.h"
+#include "sns_gpu.h"
+
+namespace sns {
+
+static int bfail(int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  record_error(buf);
+  return code;
+}
+
+#define BCUDA(call)                                                                                     \
+  do {                                                                                                  \
+    cudaError_t e_ = (call);                                                                            \
+    if (e_ != cudaSuccess)                                                                              \
+      return bfail(SNS_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_));    \
+  } while (0)
+
+static size_t align256(size_t v) { return (v + 255) / 256 * 256; }
+
+// byte layout of one case inside its arena block
+struct CaseLayout {
+  size_t rdxf_f, rdxc_f, ccm_f, ccp_f, cfm_f, cfp_f;
+  size_t rdxf, rdxc, dxi, tw, lo, hi, pfac;
+  size_t ux[2], uy[2], t[2], aux, auy, at, p, psi, spec;
+  size_t total;
+  size_t pstride;
+};
+
+static CaseLayout layout_for(int nx, int ny) {
+  CaseLayout L{};
+  const int nh = ny / 2 + 1;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off += align256(bytes);
+    return o;
+  };
+  const size_t cells = (size_t)nx * ny;
+  L.rdxf_f = take(sizeof(float) * nx);
+  L.rdxc_f = take(sizeof(float) * (nx + 1));
+  L.ccm_f = take(sizeof(float) * nx);
+  L.ccp_f = take(sizeof(float) * nx);
+  L.cfm_f = take(sizeof(float) * nx);
+  L.cfp_f = take(sizeof(float) * nx);
+  L.rdxf = take(sizeof(double) * nx);
+  L.rdxc = take(sizeof(double) * (nx + 1));
+  L.dxi = take(sizeof(double) * (nx + 1));
+  L.tw = take(sizeof(double) * 2 * ny);
+  L.lo = take(sizeof(double) * nx);
+  L.hi = take(sizeof(double) * nx);
+  L.pstride = 4 * (size_t)nx + 2 * kPcrLevels * kSeg + kSeg;
+  L.pfac = take(sizeof(double) * L.pstride * nh);
+  for (int k = 0; k < 2; k++) {
+    L.ux[k] = take(sizeof(float) * cells);
+    L.uy[k] = take(sizeof(float) * cells);
+    L.t[k] = take(sizeof(float) * cells);
+  }
+  L.aux = take(sizeof(float) * cells);
+  L.auy = take(sizeof(float) * cells);
+  L.at = take(sizeof(float) * cells);
+  L.p = take(sizeof(double) * cells);
+  L.psi = take(sizeof(double) * cells);
+  L.spec = take(sizeof(double2) * (size_t)nh * nx);
+  L.total = off;
+  return L;
+}
+
+static int check_desc(const sns_case_desc *d) {
+  if (!d) return bfail(SNS_ERR_ARG, "NULL case description");
+  if (d->jtot < 8 || d->jtot > 8192 || (d->jtot & (d->jtot - 1)))
+    return bfail(SNS_ERR_UNSUPPORTED, "jtot=%d must be a power of two in [8, 8192]", d->jtot);
+  if (d->itot < 64 || d->itot > 4096 || d->itot % kSeg)
+    return bfail(SNS_ERR_UNSUPPORTED, "itot=%d must be a multiple of %d in [64, 4096]", d->itot, kSeg);
+  if (!(d->Ra > 0) || !(d->Pr > 0) || !(d->ly > 0)) return bfail(SNS_ERR_ARG, "Ra, Pr and ly must be positive");
+  return SNS_OK;
+}
+
+// SplitMix64 (Steele, Lea, Flood 2014), the seeded noise of sns_case_desc
+static inline unsigned long long splitmix64(unsigned long long &state) {
+  unsigned long long z = (state += 0x9e3779b97f4a7c15ull);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+// initial temperature in the reference's (jtot+2) x (itot+2) layout:
+// T = (TEMP_XP - TEMP_XM) x + TEMP_XM + 0.1 r (src/temperature/init.c:30-41)
+static void initial_temperature(const sns_case_desc *d, const double *xc, double *temp) {
+  const int nx = d->itot, ny = d->jtot;
+  std::memset(temp, 0, sizeof(double) * (size_t)(nx + 2) * (ny + 2));
+  unsigned long long st = d->seed;
+  if (d->seed == 0) srand(0);
+  for (int j = 1; j <= ny; j++)
+    for (int i = 1; i <= nx; i++) {
+      const double x = xc[i];
+      double r;
+      if (d->seed == 0) {
+        r = -0.5 + 1. * rand() / RAND_MAX;
+      } else {
+        r = (double)(splitmix64(st) >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+      }
+      temp[(size_t)j * (nx + 2) + i] = (TEMP_XP - TEMP_XM) * x + TEMP_XM + 0.1 * r;
+    }
+  for (int j = 1; j <= ny; j++) {
+    temp[(size_t)j * (nx + 2)] = TEMP_XM;
+    temp[(size_t)j * (nx + 2) + nx + 1] = TEMP_XP;
+  }
+  for (int i = 1; i <= nx; i++) {
+    temp[i] = temp[(size_t)ny * (nx + 2) + i];
+    temp[(size_t)(ny + 1) * (nx + 2) + i] = temp[(size_t)(nx + 2) + i];
+  }
+}
+
+// Partition-method factors of the per-mode Poisson lines (see batch_fp32.cu):
+// rows i = 0..n-1, sub-diagonal a_i (a_0 = 0), super-diagonal c_i
+// (c_{n-1} = 0), diagonal d_i = -a_i - c_i + eig with the reference's Neumann
+// closure (src/fluid/compute_potential.c:116-127).
+static void mode_factors(int n, const double *a, const double *c, const double *l_raw, const double *u_raw, double eig,
+                         bool pin_last, double *out) {
+  const int m = n / kSeg;
+  std::vector<double> d(n);
+  for (int i = 0; i < n; i++) d[i] = -l_raw[i] - u_raw[i] + eig;
+  d[0] += l_raw[0];
+  d[n - 1] += u_raw[n - 1];
+  double *inv = out, *up = out + n, *v = out + 2 * n, *w = out + 3 * n;
+  double *alpha = out + 4 * n, *beta = alpha + kPcrLevels * kSeg, *rD = beta + kPcrLevels * kSeg;
+  std::fill(out, out + 4 * n, 0.0);
+  std::vector<double> L(kSeg), D(kSeg), U(kSeg);
+  for (int k = 0; k < kSeg; k++) {
+    const int s = k * m, e = s + m - 1;
+    // interior block rows s..e-1
+    inv[s] = 1.0 / d[s];
+    up[s] = c[s] * inv[s];
+    for (int i = s + 1; i < e; i++) {
+      inv[i] = 1.0 / (d[i] - a[i] * up[i - 1]);
+      up[i] = c[i] * inv[i];
+    }
+    auto solve = [&](std::vector<double> &r) {  // r over rows s..e-1 (index i - s)
+      r[0] *= inv[s];
+      for (int i = s + 1; i < e; i++) r[i - s] = inv[i] * (r[i - s] - a[i] * r[i - s - 1]);
+      for (int i = e - 2; i >= s; i--) r[i - s] -= up[i] * r[i - s + 1];
+    };
+    std::vector<double> rv(m - 1, 0.0), rw(m - 1, 0.0);
+    rv[0] = -a[s];
+    rw[m - 2] = -c[e - 1];
+    solve(rv);
+    solve(rw);
+    for (int i = s; i < e; i++) {
+      v[i] = rv[i - s];
+      w[i] = rw[i - s];
+    }
+  }
+  for (int k = 0; k < kSeg; k++) {
+    const int s = k * m, e = s + m - 1;
+    const double ae = a[e], ce = c[e];
+    L[k] = ae * v[e - 1];
+    D[k] = ae * w[e - 1] + d[e];
+    U[k] = 0.0;
+    if (k < kSeg - 1) {
+      const int s1 = s + m;
+      D[k] += ce * v[s1];
+      U[k] = ce * w[s1];
+    }
+  }
+  if (pin_last) {  // singular mean mode: x_{n-1} = 0 (the reference's zero last pivot)
+    L[kSeg - 1] = 0.0;
+    D[kSeg - 1] = 1.0;
+    U[kSeg - 1] = 0.0;
+  }
+  for (int lev = 0; lev < kPcrLevels; lev++) {
+    const int dd = 1 << lev;
+    std::vector<double> L2(kSeg), D2(kSeg), U2(kSeg);
+    for (int k = 0; k < kSeg; k++) {
+      const double al = k - dd >= 0 ? -L[k] / D[k - dd] : 0.0;
+      const double be = k + dd < kSeg ? -U[k] / D[k + dd] : 0.0;
+      alpha[lev * kSeg + k] = al;
+      beta[lev * kSeg + k] = be;
+      L2[k] = k - dd >= 0 ? al * L[k - dd] : 0.0;
+      U2[k] = k + dd < kSeg ? be * U[k + dd] : 0.0;
+      D2[k] = D[k] + (k - dd >= 0 ? al * U[k - dd] : 0.0) + (k + dd < kSeg ? be * L[k + dd] : 0.0);
+    }
+    L = L2;
+    D = D2;
+    U = U2;
+  }
+  for (int k = 0; k < kSeg; k++) rD[k] = 1.0 / D[k];
+}
+
+struct CaseHost {
+  bool used = false;
+  sns_case_desc d{};
+  size_t off = 0, bytes = 0;
+  long long steps_done = 0;  // host mirror: every unfinished case advances one step per batch step
+  int fcols = 1;
+};
+
+}  // namespace sns
+
+using namespace sns;
+
+struct sns_batch {
+  cudaStream_t stream = nullptr;
+  char *arena = nullptr;
+  size_t arena_bytes = 0;
+  std::map<size_t, size_t> free_blocks;  // offset -> size
+  int max_cases = 0;
+  std::vector<CaseHost> hc;
+  std::vector<BCase> table;  // host copies of the static part of each slot
+  BCase *d_cases = nullptr;
+  BTile *d_tiles = nullptr;
+  BCols *d_cols = nullptr;
+  BModes *d_modes = nullptr;
+  size_t cap_tiles = 0, cap_cols = 0, cap_modes = 0;
+  int ntiles = 0, ncols = 0, nmodes = 0;
+  size_t fft_smem = 0;
+  int fft_threads = 64;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  bool dirty = true;
+  double rk_a[3] = {32. / 60., 25. / 60., 45. / 60.};
+  double rk_b[3] = {0. / 60., -17. / 60., -25. / 60.};
+  double *staging = nullptr;  // pinned
+  size_t staging_bytes = 0;
+  std::mutex mu;
+};
+
+static bool arena_alloc(sns_batch *b, size_t bytes, size_t *off) {
+  for (auto it = b->free_blocks.begin(); it != b->free_blocks.end(); ++it) {
+    if (it->second >= bytes) {
+      *off = it->first;
+      const size_t rest = it->second - bytes;
+      const size_t noff = it->first + bytes;
+      b->free_blocks.erase(it);
+      if (rest) b->free_blocks[noff] = rest;
+      return true;
+    }
+  }
+  return false;
+}
+
+static void arena_free(sns_batch *b, size_t off, size_t bytes) {
+  auto it = b->free_blocks.emplace(off, bytes).first;
+  auto next = std::next(it);
+  if (next != b->free_blocks.end() && it->first + it->second == next->first) {
+    it->second += next->second;
+    b->free_blocks.erase(next);
+  }
+  if (it != b->free_blocks.begin()) {
+    auto prev = std::prev(it);
+    if (prev->first + prev->second == it->first) {
+      prev->second += it->second;
+      b->free_blocks.erase(it);
+    }
+  }
+}
+
+template <typename T>
+static int ensure_device_list(T **ptr, size_t *cap, size_t need) {
+  if (need <= *cap) return SNS_OK;
+  if (*ptr) cudaFree(*ptr);
+  *ptr = nullptr;
+  const size_t n = std::max<size_t>(need, 2 * *cap);
+  BCUDA(cudaMalloc((void **)ptr, sizeof(T) * n));
+  *cap = n;
+  return SNS_OK;
+}
+
+// work lists for the current case set and the graph of one step
+static int rebuild(sns_batch *b) {
+  std::vector<BTile> tiles;
+  std::vector<BCols> cols;
+  std::vector<BModes> modes;
+  size_t smem = 0;
+  int threads = 64;
+  for (int c = 0; c < b->max_cases; c++) {
+    const CaseHost &h = b->hc[c];
+    if (!h.used) continue;
+    if (h.d.steps > 0 && h.steps_done >= h.d.steps) continue;
+    const int nx = h.d.itot, ny = h.d.jtot, nh = ny / 2 + 1;
+    for (int y0 = 0; y0 < ny; y0 += kBTileY)
+      for (int x0 = 0; x0 < nx; x0 += kBTileX) tiles.push_back({c, x0, y0});
+    for (int x0 = 0; x0 < nx; x0 += h.fcols) cols.push_back({c, x0});
+    for (int j0 = 0; j0 < nh; j0 += kBModesPerBlock) modes.push_back({c, j0});
+    smem = std::max(smem, sizeof(double) * (size_t)h.fcols * ny);
+    threads = std::max(threads, std::min(256, (h.fcols * (ny / 2) / 4 + 31) / 32 * 32));
+  }
+  if (int rc = ensure_device_list(&b->d_tiles, &b->cap_tiles, std::max<size_t>(tiles.size(), 1))) return rc;
+  if (int rc = ensure_device_list(&b->d_cols, &b->cap_cols, std::max<size_t>(cols.size(), 1))) return rc;
+  if (int rc = ensure_device_list(&b->d_modes, &b->cap_modes, std::max<size_t>(modes.size(), 1))) return rc;
+  if (!tiles.empty())
+    BCUDA(cudaMemcpyAsync(b->d_tiles, tiles.data(), sizeof(BTile) * tiles.size(), cudaMemcpyHostToDevice, b->stream));
+  if (!cols.empty())
+    BCUDA(cudaMemcpyAsync(b->d_cols, cols.data(), sizeof(BCols) * cols.size(), cudaMemcpyHostToDevice, b->stream));
+  if (!modes.empty())
+    BCUDA(cudaMemcpyAsync(b->d_modes, modes.data(), sizeof(BModes) * modes.size(), cudaMemcpyHostToDevice,
+                          b->stream));
+  b->ntiles = (int)tiles.size();
+  b->ncols = (int)cols.size();
+  b->nmodes = (int)modes.size();
+  b->fft_smem = smem;
+  b->fft_threads = threads;
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    b->exec = nullptr;
+  }
+  if (b->graph) {
+    cudaGraphDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  BCUDA(cudaStreamSynchronize(b->stream));
+  // one time step: three substages of five phases, then the per-case dt update
+  BCUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t err = cudaSuccess;
+  for (int rk = 0; rk < 3 && err == cudaSuccess; rk++) {
+    if ((err = launch_batch_stencil(b->d_cases, b->d_tiles, b->ntiles, rk, b->stream)) != cudaSuccess) break;
+    if ((err = launch_batch_fwd(b->d_cases, b->d_cols, b->ncols, rk, b->fft_smem, b->fft_threads, b->stream)) !=
+        cudaSuccess)
+      break;
+    if ((err = launch_batch_tri(b->d_cases, b->d_modes, b->nmodes, b->stream)) != cudaSuccess) break;
+    if ((err = launch_batch_bwd(b->d_cases, b->d_cols, b->ncols, b->fft_smem, b->fft_threads, b->stream)) !=
+        cudaSuccess)
+      break;
+    if ((err = launch_batch_corr(b->d_cases, b->d_tiles, b->ntiles, rk, b->stream)) != cudaSuccess) break;
+  }
+  if (err == cudaSuccess) err = launch_batch_dt(b->d_cases, b->max_cases, b->rk_a, b->rk_b, b->stream);
+  cudaGraph_t g = nullptr;
+  cudaError_t e2 = cudaStreamEndCapture(b->stream, &g);
+  if (err != cudaSuccess) return bfail(SNS_ERR_CUDA, "capturing the batch step: %s", cudaGetErrorString(err));
+  if (e2 != cudaSuccess) return bfail(SNS_ERR_CUDA, "capturing the batch step: %s", cudaGetErrorString(e2));
+  b->graph = g;
+  BCUDA(cudaGraphInstantiate(&b->exec, g, 0));
+  b->dirty = false;
+  return SNS_OK;
+}
+
+extern "C" {
+
+size_t sns_batch_case_bytes(const sns_case_desc *desc) {
+  if (check_desc(desc) != SNS_OK) return 0;
+  return layout_for(desc->itot, desc->jtot).total;
+}
+
+sns_batch *sns_batch_create(size_t hbm_bytes, int max_cases) {
+  if (max_cases <= 0 || hbm_bytes < (1u << 20)) {
+    bfail(SNS_ERR_ARG, "sns_batch_create: need max_cases > 0 and at least 1 MiB");
+    return nullptr;
+  }
+  sns_batch *b = new sns_batch();
+  b->max_cases = max_cases;
+  b->hc.resize(max_cases);
+  b->table.resize(max_cases);
+  for (BCase &t : b->table) {
+    std::memset(&t, 0, sizeof(BCase));
+    t.done = 1;  // empty slots are skipped by every kernel
+  }
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      batch_kernels_init() != cudaSuccess || cudaMalloc((void **)&b->arena, hbm_bytes) != cudaSuccess ||
+      cudaMalloc((void **)&b->d_cases, sizeof(BCase) * max_cases) != cudaSuccess ||
+      cudaMemcpy(b->d_cases, b->table.data(), sizeof(BCase) * max_cases, cudaMemcpyHostToDevice) != cudaSuccess) {
+    bfail(SNS_ERR_OOM, "sns_batch_create: %s", cudaGetErrorString(cudaGetLastError()));
+    sns_batch_destroy(b);
+    return nullptr;
+  }
+  b->arena_bytes = hbm_bytes;
+  b->free_blocks[0] = hbm_bytes;
+  return b;
+}
+
+int sns_batch_destroy(sns_batch *b) {
+  if (!b) return SNS_OK;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  cudaFree(b->arena);
+  cudaFree(b->d_cases);
+  cudaFree(b->d_tiles);
+  cudaFree(b->d_cols);
+  cudaFree(b->d_modes);
+  if (b->staging) cudaFreeHost(b->staging);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return SNS_OK;
+}
+
+size_t sns_batch_free_bytes(const sns_batch *b) {
+  if (!b) return 0;
+  size_t best = 0;
+  for (const auto &kv : b->free_blocks) best = std::max(best, kv.second);
+  return best;
+}
+
+void *sns_batch_stream(const sns_batch *b) { return b ? (void *)b->stream : nullptr; }
+
+int sns_batch_initial_temperature(const sns_case_desc *desc, double *temp) {
+  if (int rc = check_desc(desc)) return rc;
+  if (!temp) return bfail(SNS_ERR_ARG, "NULL output");
+  const int nx = desc->itot, ny = desc->jtot;
+  std::vector<double> xf(nx + 1), xc(nx + 2), dxf(nx), dxc(nx + 1);
+  double dy;
+  make_grid(nx, ny, 1.0, desc->ly, desc->stretch, xf.data(), xc.data(), dxf.data(), dxc.data(), nullptr, nullptr, &dy);
+  initial_temperature(desc, xc.data(), temp);
+  return SNS_OK;
+}
+
+int sns_batch_add(sns_batch *b, const sns_case_desc *d, const double *temp_init, int *slot_out) {
+  if (!b) return bfail(SNS_ERR_ARG, "NULL batch");
+  if (int rc = check_desc(d)) return rc;
+  std::lock_guard<std::mutex> lk(b->mu);
+  int slot = -1;
+  for (int c = 0; c < b->max_cases; c++)
+    if (!b->hc[c].used) {
+      slot = c;
+      break;
+    }
+  if (slot < 0) return bfail(SNS_ERR_OOM, "batch full (%d cases)", b->max_cases);
+  const int nx = d->itot, ny = d->jtot, nh = ny / 2 + 1;
+  const CaseLayout L = layout_for(nx, ny);
+  size_t off;
+  if (!arena_alloc(b, L.total, &off))
+    return bfail(SNS_ERR_OOM, "case needs %zu bytes, largest free block %zu", L.total, sns_batch_free_bytes(b));
+  char *base = b->arena + off;
+  // ---- grid and metrics (src/param/init.c:124-195)
+  std::vector<double> xf(nx + 1), xc(nx + 2), dxf(nx), dxc(nx + 1);
+  double dy;
+  make_grid(nx, ny, 1.0, d->ly, d->stretch, xf.data(), xc.data(), dxf.data(), dxc.data(), nullptr, nullptr, &dy);
+  auto DXF = [&](int i) { return dxf[i - 1]; };
+  auto DXC = [&](int i) { return dxc[i - 1]; };
+  std::vector<float> rdxf_f(nx), rdxc_f(nx + 1), ccm(nx), ccp(nx), cfm(nx, 0.f), cfp(nx, 0.f);
+  std::vector<double> rdxf(nx), rdxc(nx + 1), dxi(nx + 1), lo(nx), hi(nx), l_raw(nx), u_raw(nx);
+  for (int i = 1; i <= nx; i++) {
+    rdxf[i - 1] = 1.0 / DXF(i);
+    rdxf_f[i - 1] = (float)rdxf[i - 1];
+    ccm[i - 1] = (float)(DXC(i) / (2. * DXF(i)));
+    ccp[i - 1] = (float)(DXC(i + 1) / (2. * DXF(i)));
+    if (i >= 2) {
+      cfm[i - 1] = (float)(DXF(i - 1) / (2. * DXC(i)));
+      cfp[i - 1] = (float)(DXF(i) / (2. * DXC(i)));
+    }
+    l_raw[i - 1] = 1. / DXC(i) / DXF(i);
+    u_raw[i - 1] = 1. / DXC(i + 1) / DXF(i);
+    lo[i - 1] = i > 1 ? l_raw[i - 1] : 0.0;
+    hi[i - 1] = i < nx ? u_raw[i - 1] : 0.0;
+  }
+  for (int i = 1; i <= nx + 1; i++) {
+    rdxc[i - 1] = 1.0 / DXC(i);
+    rdxc_f[i - 1] = (float)rdxc[i - 1];
+    dxi[i - 1] = 1. / DXC(i);
+  }
+  std::vector<double> pfac(L.pstride * nh);
+  for (int J = 0; J < nh; J++)
+    mode_factors(nx, lo.data(), hi.data(), l_raw.data(), u_raw.data(), poisson_eigenvalue(dy, ny, J), J == 0,
+                 pfac.data() + L.pstride * J);
+  const std::vector<double> tw = twiddle_table(ny);
+  std::vector<double> temp((size_t)(nx + 2) * (ny + 2));
+  if (temp_init) {
+    std::memcpy(temp.data(), temp_init, sizeof(double) * temp.size());
+  } else {
+    initial_temperature(d, xc.data(), temp.data());
+  }
+  std::vector<float> t_dense((size_t)nx * ny);
+  for (int j = 1; j <= ny; j++)
+    for (int i = 1; i <= nx; i++) t_dense[(size_t)(j - 1) * nx + (i - 1)] = (float)temp[(size_t)j * (nx + 2) + i];
+  auto put = [&](size_t o, const void *src, size_t bytes) {
+    return cudaMemcpyAsync(base + o, src, bytes, cudaMemcpyHostToDevice, b->stream);
+  };
+  const size_t cells = (size_t)nx * ny;
+  cudaError_t e = cudaSuccess;
+  auto chk = [&](cudaError_t x) {
+    if (e == cudaSuccess) e = x;
+  };
+  chk(put(L.rdxf_f, rdxf_f.data(), sizeof(float) * nx));
+  chk(put(L.rdxc_f, rdxc_f.data(), sizeof(float) * (nx + 1)));
+  chk(put(L.ccm_f, ccm.data(), sizeof(float) * nx));
+  chk(put(L.ccp_f, ccp.data(), sizeof(float) * nx));
+  chk(put(L.cfm_f, cfm.data(), sizeof(float) * nx));
+  chk(put(L.cfp_f, cfp.data(), sizeof(float) * nx));
+  chk(put(L.rdxf, rdxf.data(), sizeof(double) * nx));
+  chk(put(L.rdxc, rdxc.data(), sizeof(double) * (nx + 1)));
+  chk(put(L.dxi, dxi.data(), sizeof(double) * (nx + 1)));
+  chk(put(L.tw, tw.data(), sizeof(double) * tw.size()));
+  chk(put(L.lo, lo.data(), sizeof(double) * nx));
+  chk(put(L.hi, hi.data(), sizeof(double) * nx));
+  chk(put(L.pfac, pfac.data(), sizeof(double) * pfac.size()));
+  for (int k = 0; k < 2; k++) {
+    chk(cudaMemsetAsync(base + L.ux[k], 0, sizeof(float) * cells, b->stream));
+    chk(cudaMemsetAsync(base + L.uy[k], 0, sizeof(float) * cells, b->stream));
+  }
+  chk(put(L.t[0], t_dense.data(), sizeof(float) * cells));
+  chk(cudaMemsetAsync(base + L.t[1], 0, sizeof(float) * cells, b->stream));
+  for (size_t o : {L.aux, L.auy, L.at}) chk(cudaMemsetAsync(base + o, 0, sizeof(float) * cells, b->stream));
+  chk(cudaMemsetAsync(base + L.p, 0, sizeof(double) * cells, b->stream));
+  chk(cudaMemsetAsync(base + L.psi, 0, sizeof(double) * cells, b->stream));
+  chk(cudaMemsetAsync(base + L.spec, 0, sizeof(double2) * (size_t)nh * nx, b->stream));
+  // ---- table entry
+  BCase t;
+  std::memset(&t, 0, sizeof t);
+  t.nx = nx;
+  t.ny = ny;
+  t.nh = nh;
+  fft_layout(ny, &t.fft_nst, &t.fft_first2);
+  int fc = std::min(8192 / ny, nx / 128);
+  fc = std::max(1, std::min(8, fc));
+  t.fcols = fc;
+  t.with_t = d->with_temperature ? 1 : 0;
+  t.with_force = d->with_thermal_forcing ? 1 : 0;
+  t.seg = nx / kSeg;
+  t.dy = dy;
+  t.rdy = 1.0 / dy;
+  t.rdy_f = (float)t.rdy;
+  t.kappa_f = (float)(1. / sqrt(d->Pr) / sqrt(d->Ra));
+  t.nu_f = (float)(sqrt(d->Pr) / sqrt(d->Ra));
+  {  // explicit diffusive limits (src/param/decide_dt.c:62-74)
+    const double diffusivity = fmax(sqrt(d->Pr) / sqrt(d->Ra), 1. / sqrt(d->Pr) / sqrt(d->Ra));
+    double dx = 1.0;
+    for (int i = 2; i <= nx; i++) dx = fmin(dx, DXC(i));
+    const double ddx = 0.25 / diffusivity * pow(dx, 2.) * 0.9, ddy = 0.25 / diffusivity * pow(dy, 2.) * 0.9;
+    t.dt_dif = fmin(ddx, ddy);
+  }
+  t.fixed_dt = d->fixed_dt;
+  t.target_steps = d->steps;
+  t.rdxf_f = reinterpret_cast<const float *>(base + L.rdxf_f);
+  t.rdxc_f = reinterpret_cast<const float *>(base + L.rdxc_f);
+  t.ccm_f = reinterpret_cast<const float *>(base + L.ccm_f);
+  t.ccp_f = reinterpret_cast<const float *>(base + L.ccp_f);
+  t.cfm_f = reinterpret_cast<const float *>(base + L.cfm_f);
+  t.cfp_f = reinterpret_cast<const float *>(base + L.cfp_f);
+  t.rdxf = reinterpret_cast<const double *>(base + L.rdxf);
+  t.rdxc = reinterpret_cast<const double *>(base + L.rdxc);
+  t.dxi = reinterpret_cast<const double *>(base + L.dxi);
+  t.tw = reinterpret_cast<const double *>(base + L.tw);
+  t.lo = reinterpret_cast<const double *>(base + L.lo);
+  t.hi = reinterpret_cast<const double *>(base + L.hi);
+  t.pfac = reinterpret_cast<const double *>(base + L.pfac);
+  t.pstride = L.pstride;
+  for (int k = 0; k < 2; k++) {
+    t.ux[k] = reinterpret_cast<float *>(base + L.ux[k]);
+    t.uy[k] = reinterpret_cast<float *>(base + L.uy[k]);
+    t.t[k] = reinterpret_cast<float *>(base + L.t[k]);
+  }
+  t.aux = reinterpret_cast<float *>(base + L.aux);
+  t.auy = reinterpret_cast<float *>(base + L.auy);
+  t.at = reinterpret_cast<float *>(base + L.at);
+  t.p = reinterpret_cast<double *>(base + L.p);
+  t.psi = reinterpret_cast<double *>(base + L.psi);
+  t.spec = reinterpret_cast<double2 *>(base + L.spec);
+  t.par = 0;
+  t.done = 0;
+  t.step = 0;
+  t.time = 0.0;
+  // first dt from u = 0: advective limit 0.7 * 0.05 (src/param/decide_dt.c:42)
+  t.dt = d->fixed_dt > 0 ? d->fixed_dt : fmin(5.e-2 * 0.7, t.dt_dif);
+  for (int k = 0; k < 3; k++) {
+    t.adt[k] = b->rk_a[k] * t.dt;
+    t.bdt[k] = b->rk_b[k] * t.dt;
+    t.gdt[k] = (b->rk_a[k] + b->rk_b[k]) * t.dt;
+    t.rgdt[k] = 1. / t.gdt[k];
+  }
+  chk(cudaMemcpyAsync(b->d_cases + slot, &t, sizeof(BCase), cudaMemcpyHostToDevice, b->stream));
+  chk(cudaStreamSynchronize(b->stream));  // host staging vectors die at return
+  if (e != cudaSuccess) {
+    arena_free(b, off, L.total);
+    return bfail(SNS_ERR_CUDA, "sns_batch_add: %s", cudaGetErrorString(e));
+  }
+  b->table[slot] = t;
+  CaseHost &h = b->hc[slot];
+  h.used = true;
+  h.d = *d;
+  h.off = off;
+  h.bytes = L.total;
+  h.steps_done = 0;
+  h.fcols = fc;
+  b->dirty = true;
+  if (slot_out) *slot_out = slot;
+  return SNS_OK;
+}
+
+int sns_batch_remove(sns_batch *b, int slot) {
+  if (!b || slot < 0 || slot >= b->max_cases || !b->hc[slot].used) return bfail(SNS_ERR_ARG, "bad slot");
+  std::lock_guard<std::mutex> lk(b->mu);
+  BCUDA(cudaStreamSynchronize(b->stream));
+  BCase empty;
+  std::memset(&empty, 0, sizeof empty);
+  empty.done = 1;
+  BCUDA(cudaMemcpy(b->d_cases + slot, &empty, sizeof(BCase), cudaMemcpyHostToDevice));
+  b->table[slot] = empty;
+  arena_free(b, b->hc[slot].off, b->hc[slot].bytes);
+  b->hc[slot] = CaseHost();
+  b->dirty = true;
+  return SNS_OK;
+}
+
+int sns_batch_step(sns_batch *b, int nsteps) {
+  if (!b || nsteps < 0) return bfail(SNS_ERR_ARG, "sns_batch_step: bad argument");
+  std::lock_guard<std::mutex> lk(b->mu);
+  for (int s = 0; s < nsteps; s++) {
+    if (b->dirty)
+      if (int rc = rebuild(b)) return rc;
+    if (b->ntiles == 0) break;
+    BCUDA(cudaGraphLaunch(b->exec, b->stream));
+    count_launches(16);
+    bool finished_one = false;
+    for (CaseHost &h : b->hc) {
+      if (!h.used || (h.d.steps > 0 && h.steps_done >= h.d.steps)) continue;
+      h.steps_done++;
+      if (h.d.steps > 0 && h.steps_done >= h.d.steps) finished_one = true;
+    }
+    if (finished_one) b->dirty = true;  // drop finished cases from the work lists
+  }
+  return SNS_OK;
+}
+
+int sns_batch_synchronize(sns_batch *b) {
+  if (!b) return bfail(SNS_ERR_ARG, "NULL batch");
+  BCUDA(cudaStreamSynchronize(b->stream));
+  return SNS_OK;
+}
+
+int sns_batch_cases(const sns_batch *b, int *slots, int max) {
+  if (!b) return 0;
+  int n = 0;
+  for (int c = 0; c < b->max_cases; c++)
+    if (b->hc[c].used) {
+      if (slots && n < max) slots[n] = c;
+      n++;
+    }
+  return n;
+}
+
+long long sns_batch_active_cells(const sns_batch *b) {
+  if (!b) return 0;
+  long long cells = 0;
+  for (const CaseHost &h : b->hc)
+    if (h.used && !(h.d.steps > 0 && h.steps_done >= h.d.steps)) cells += (long long)h.d.itot * h.d.jtot;
+  return cells;
+}
+
+int sns_batch_case_status(sns_batch *b, int slot, double *time, double *dt, long long *step, int *done) {
+  if (!b || slot < 0 || slot >= b->max_cases || !b->hc[slot].used) return bfail(SNS_ERR_ARG, "bad slot");
+  BCase t;
+  BCUDA(cudaStreamSynchronize(b->stream));
+  BCUDA(cudaMemcpy(&t, b->d_cases + slot, sizeof(BCase), cudaMemcpyDeviceToHost));
+  if (time) *time = t.time;
+  if (dt) *dt = t.dt;
+  if (step) *step = t.step;
+  if (done) *done = t.done;
+  return SNS_OK;
+}
+
+int sns_batch_state(sns_batch *b, int slot, double *ux, double *uy, double *p, double *psi, double *temp) {
+  if (!b || slot < 0 || slot >= b->max_cases || !b->hc[slot].used) return bfail(SNS_ERR_ARG, "bad slot");
+  std::lock_guard<std::mutex> lk(b->mu);
+  BCase t;
+  BCUDA(cudaStreamSynchronize(b->stream));
+  BCUDA(cudaMemcpy(&t, b->d_cases + slot, sizeof(BCase), cudaMemcpyDeviceToHost));
+  const int nx = t.nx, ny = t.ny;
+  const size_t cells = (size_t)nx * ny;
+  if (b->staging_bytes < sizeof(double) * cells) {
+    if (b->staging) cudaFreeHost(b->staging);
+    b->staging = nullptr;
+    BCUDA(cudaMallocHost((void **)&b->staging, sizeof(double) * cells));
+    b->staging_bytes = sizeof(double) * cells;
+  }
+  const int cur = t.par;
+  auto fetch_f = [&](const float *src, std::vector<double> &dst) -> int {
+    BCUDA(cudaMemcpy(b->staging, src, sizeof(float) * cells, cudaMemcpyDeviceToHost));
+    const float *f = reinterpret_cast<const float *>(b->staging);
+    dst.resize(cells);
+    for (size_t k = 0; k < cells; k++) dst[k] = f[k];
+    return SNS_OK;
+  };
+  auto fetch_d = [&](const double *src, std::vector<double> &dst) -> int {
+    BCUDA(cudaMemcpy(b->staging, src, sizeof(double) * cells, cudaMemcpyDeviceToHost));
+    dst.assign(b->staging, b->staging + cells);
+    return SNS_OK;
+  };
+  std::vector<double> v;
+  if (ux) {
+    if (int rc = fetch_f(t.ux[cur], v)) return rc;
+    std::memset(ux, 0, sizeof(double) * (size_t)(nx + 1) * (ny + 2));
+    for (int j = 1; j <= ny; j++)
+      for (int i = 2; i <= nx; i++) ux[(size_t)j * (nx + 1) + (i - 1)] = v[(size_t)(j - 1) * nx + (i - 1)];
+    for (int i = 2; i <= nx; i++) {
+      ux[i - 1] = ux[(size_t)ny * (nx + 1) + (i - 1)];
+      ux[(size_t)(ny + 1) * (nx + 1) + (i - 1)] = ux[(size_t)(nx + 1) + (i - 1)];
+    }
+  }
+  auto centred = [&](std::vector<double> &src, double *dst, int wall_mode) {
+    // wall_mode 0: zero walls (uy), 1: Neumann (p, psi), 2: temperature walls
+    std::memset(dst, 0, sizeof(double) * (size_t)(nx + 2) * (ny + 2));
+    for (int j = 1; j <= ny; j++)
+      for (int i = 1; i <= nx; i++) dst[(size_t)j * (nx + 2) + i] = src[(size_t)(j - 1) * nx + (i - 1)];
+    for (int i = 1; i <= nx; i++) {
+      dst[i] = dst[(size_t)ny * (nx + 2) + i];
+      dst[(size_t)(ny + 1) * (nx + 2) + i] = dst[(size_t)(nx + 2) + i];
+    }
+    const int j0 = wall_mode == 2 ? 1 : 0, j1 = wall_mode == 2 ? ny : ny + 1;
+    for (int j = j0; j <= j1; j++) {
+      double *row = dst + (size_t)j * (nx + 2);
+      if (wall_mode == 0) {
+        row[0] = 0.;
+        row[nx + 1] = 0.;
+      } else if (wall_mode == 1) {
+        row[0] = row[1];
+        row[nx + 1] = row[nx];
+      } else {
+        row[0] = TEMP_XM;
+        row[nx + 1] = TEMP_XP;
+      }
+    }
+  };
+  if (uy) {
+    if (int rc = fetch_f(t.uy[cur], v)) return rc;
+    centred(v, uy, 0);
+  }
+  if (p) {
+    if (int rc = fetch_d(t.p, v)) return rc;
+    centred(v, p, 1);
+  }
+  if (psi) {
+    if (int rc = fetch_d(t.psi, v)) return rc;
+    centred(v, psi, 1);
+  }
+  if (temp) {
+    if (int rc = fetch_f(t.t[cur], v)) return rc;
+    centred(v, temp, 2);
+  }
+  return SNS_OK;
+}
+
+}  // extern "C"

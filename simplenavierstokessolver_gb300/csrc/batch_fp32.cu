@@ -1,0 +1,429 @@
+// Batched FP32-stencil / FP64-Poisson form of the SMR-RK3 step (sm_103a).
+//
+// One launch per phase covers every resident case: blocks read a work item
+// (case, tile | column group | mode group) and the case's table entry.
+// Stencils, RK3 updates and velocity/temperature storage are FP32 with fused
+// multiply-adds; the pressure gradient, the divergence, the FFTs, the
+// tridiagonal solves, psi and p are FP64 (multiply-adds allowed: this form is
+// compared with the FP64 reference by error norms, not bits). The equations
+// are the reference's (src/temperature/update.c:11-87, src/fluid/
+// update_velocity.c:11-192, src/fluid/compute_potential.c:69-157,
+// src/fluid/correct_velocity.c:6-42, src/fluid/update_pressure.c:7-60) with
+// explicit diffusion in both directions.
+//
+// The per-mode tridiagonal systems use a partition method instead of the
+// serial Thomas sweep: a warp owns one line, lane k a segment of nx/32 rows;
+// each lane eliminates its segment's interior with precomputed factors, the
+// 32 interface unknowns form a tridiagonal system solved by parallel cyclic
+// reduction across lanes (precomputed multipliers), and the interiors are
+// recovered from the precomputed spike vectors. The critical path is
+// nx/32 + 5 steps instead of nx.
+#include <cstdint>
+
+#include "batch_internal.h"
+#include "fft_dev.cuh"
+
+namespace sns {
+namespace {
+
+__device__ __forceinline__ int wup(int y, int ny) { return y + 1 == ny ? 0 : y + 1; }
+__device__ __forceinline__ int wdn(int y, int ny) { return y == 0 ? ny - 1 : y - 1; }
+
+// ------------------------------------------------------------------ stencils
+__global__ void __launch_bounds__(kBTileX) k_b_stencil(const BCase *__restrict__ cases,
+                                                      const BTile *__restrict__ tiles, int rk) {
+  const BTile tl = tiles[blockIdx.x];
+  const BCase &C = cases[tl.c];
+  if (C.done) return;
+  const int nx = C.nx, ny = C.ny;
+  const int x = tl.x0 + threadIdx.x;
+  if (x >= nx) return;
+  const int y0 = tl.y0, y1 = min(y0 + kBTileY, ny);
+  const int pin = C.par ^ (rk & 1), pout = pin ^ 1;
+  const float *__restrict__ ux = C.ux[pin];
+  const float *__restrict__ uy = C.uy[pin];
+  const float *__restrict__ T = C.t[pin];
+  float *__restrict__ uxo = C.ux[pout];
+  float *__restrict__ uyo = C.uy[pout];
+  float *__restrict__ To = C.t[pout];
+  float *__restrict__ aux = C.aux;
+  float *__restrict__ auy = C.auy;
+  float *__restrict__ at = C.at;
+  const double *__restrict__ p = C.p;
+  const float adt = (float)C.adt[rk], bdt = (float)C.bdt[rk], gdt = (float)C.gdt[rk];
+  const bool hasb = rk > 0;
+  const bool with_t = C.with_t != 0, force = C.with_t && C.with_force;
+  const bool left = x == 0, right = x == nx - 1, has_ux = x >= 1;
+  const float rdy = C.rdy_f, kappa = C.kappa_f, nu = C.nu_f;
+  const float rxc_m = C.rdxc_f[x], rxc_p = C.rdxc_f[x + 1], rxf = C.rdxf_f[x];
+  const float rxf_m = has_ux ? C.rdxf_f[x - 1] : 0.f;
+  const float ccm = C.ccm_f[x], ccp = C.ccp_f[x], cfm = C.cfm_f[x], cfp = C.cfp_f[x];
+  const double rdxc_d = C.rdxc[x], rdy_d = C.rdy;
+
+  const int ym = wdn(y0, ny);
+  const size_t r0 = (size_t)y0 * nx + x, rm = (size_t)ym * nx + x;
+  float u0 = ux[r0], u1 = right ? 0.f : ux[r0 + 1];
+  float um0 = ux[rm], um1 = right ? 0.f : ux[rm + 1];
+  float v0 = uy[r0], vl = left ? 0.f : uy[r0 - 1];
+  const float vm = uy[rm];
+  float tc = T[r0];
+  const float tm = T[rm];
+  double pm = p[rm];
+  float gym_u = (u0 - um0) * rdy;
+  float pym_u = has_ux ? (0.5f * (cfm * vl + cfp * v0)) * gym_u : 0.f;
+  float gym_v = (v0 - vm) * rdy;
+  float pym_v = (0.5f * (0.5f * (vm + v0))) * gym_v;
+  float gym_t = (tc - tm) * rdy;
+  float pym_t = (0.5f * v0) * gym_t;
+
+  for (int y = y0; y < y1; ++y) {
+    const int yp = wup(y, ny);
+    const size_t r = (size_t)y * nx + x, rp = (size_t)yp * nx + x;
+    const float u0n = ux[rp];
+    const float u1n = right ? 0.f : ux[rp + 1];
+    const float v0n = uy[rp];
+    const float vln = left ? 0.f : uy[rp - 1];
+    const float vr = right ? 0.f : uy[r + 1];
+    const float tn = T[rp];
+    const double pc = p[r];
+    if (with_t) {  // src/temperature/update.c:32-85
+      const float tlv = left ? 0.5f : T[r - 1];
+      const float trv = right ? -0.5f : T[r + 1];
+      const float gxm = (tc - tlv) * rxc_m, gxp = (trv - tc) * rxc_p, gyp = (tn - tc) * rdy;
+      const float pyp = (0.5f * v0n) * gyp;
+      const float adv1 = -(ccm * u0 * gxm) - (ccp * u1 * gxp);
+      const float adv2 = -pym_t - pyp;
+      const float dif = kappa * ((gxp - gxm) * rxf + (gyp - gym_t) * rdy);
+      const float A = adv1 + adv2 + dif;
+      const float q = hasb ? fmaf(adt, A, bdt * at[r]) : adt * A;
+      at[r] = A;
+      To[r] = tc + q;
+      gym_t = gyp;
+      pym_t = pyp;
+    } else {
+      To[r] = tc;  // uncoupled temperature is carried along unchanged
+    }
+    if (has_ux) {  // src/fluid/update_velocity.c:136-203
+      const float ul = ux[r - 1];
+      const float gxm = (u0 - ul) * rxf_m, gxp = (u1 - u0) * rxf, gyp = (u0n - u0) * rdy;
+      const float vxm = 0.5f * (ul + u0), vxp = 0.5f * (u0 + u1);
+      const float adv1 = -(cfm * vxm * gxm) - (cfp * vxp * gxp);
+      const float pyp = (0.5f * (cfm * vln + cfp * v0n)) * gyp;
+      const float adv2 = -pym_u - pyp;
+      const float dif = nu * ((gxp - gxm) * rxc_m + (gyp - gym_u) * rdy);
+      const float pre = -(float)((pc - p[r - 1]) * rdxc_d);
+      float A = adv1 + adv2 + dif;
+      if (force) A += 0.5f * (T[r - 1] + tc);
+      float q = hasb ? fmaf(adt, A, bdt * aux[r]) : adt * A;
+      q = fmaf(gdt, pre, q);
+      aux[r] = A;
+      uxo[r] = u0 + q;
+      gym_u = gyp;
+      pym_u = pyp;
+    }
+    {  // src/fluid/update_velocity.c:230-291
+      const float gxm = (v0 - vl) * rxc_m, gxp = (vr - v0) * rxc_p, gyp = (v0n - v0) * rdy;
+      const float wxm = 0.5f * (um0 + u0), wxp = 0.5f * (um1 + u1);
+      const float adv1 = -(ccm * wxm * gxm) - (ccp * wxp * gxp);
+      const float pyp = (0.5f * (0.5f * (v0 + v0n))) * gyp;
+      const float adv2 = -pym_v - pyp;
+      const float dif = nu * ((gxp - gxm) * rxf + (gyp - gym_v) * rdy);
+      const float pre = -(float)((pc - pm) * rdy_d);
+      const float A = adv1 + adv2 + dif;
+      float q = hasb ? fmaf(adt, A, bdt * auy[r]) : adt * A;
+      q = fmaf(gdt, pre, q);
+      auy[r] = A;
+      uyo[r] = v0 + q;
+      gym_v = gyp;
+      pym_v = pyp;
+    }
+    um0 = u0;
+    um1 = u1;
+    u0 = u0n;
+    u1 = u1n;
+    vl = vln;
+    v0 = v0n;
+    pm = pc;
+    tc = tn;
+  }
+}
+
+// ------------------------------------------------------------------- Poisson
+// FP64 divergence of the FP32 predicted velocity (src/fluid/compute_potential.c:74-86)
+// and the forward real DFT along y of `fcols` columns.
+__global__ void __launch_bounds__(256) k_b_fwd(const BCase *__restrict__ cases, const BCols *__restrict__ cols,
+                                               int rk) {
+  extern __shared__ double2 zs[];
+  const BCols it = cols[blockIdx.x];
+  const BCase &C = cases[it.c];
+  if (C.done) return;
+  const int nx = C.nx, ny = C.ny, M = ny / 2, nc = C.fcols, x0 = it.x0;
+  const int pu = C.par ^ (rk & 1) ^ 1;
+  const float *__restrict__ ux = C.ux[pu];
+  const float *__restrict__ uy = C.uy[pu];
+  const double rgdt = C.rgdt[rk], rdy = C.rdy;
+  double *zd = reinterpret_cast<double *>(zs);
+  for (int e = threadIdx.x; e < nc * ny; e += blockDim.x) {
+    const int c = e % nc, y = e / nc, x = x0 + c;
+    double d = 0.0;
+    if (x < nx) {
+      const size_t r = (size_t)y * nx + x;
+      const float dux = (x == nx - 1 ? 0.f : ux[r + 1]) - ux[r];
+      const float duy = uy[(size_t)wup(y, ny) * nx + x] - uy[r];
+      d = rgdt * ((double)dux * C.rdxf[x] + (double)duy * rdy);
+    }
+    zd[2 * (c * M + fft::fft_slot(y >> 1, M, C.fft_nst, C.fft_first2)) + (y & 1)] = d;
+  }
+  __syncthreads();
+  const double2 *tw = reinterpret_cast<const double2 *>(C.tw);
+  fft::fft_stages<true>(zs, nc, M, ny, C.fft_nst, C.fft_first2, tw);
+  const int half = M / 2 + 1;
+  for (int e = threadIdx.x; e < nc * half; e += blockDim.x) {
+    const int c = e % nc, k = e / nc, x = x0 + c;
+    if (x < nx) fft::rfft_post(zs + c * M, C.spec + x, M, k, tw, (size_t)nx);
+  }
+}
+
+// inverse DFT and 1/jtot (src/fluid/compute_potential.c:146-157)
+__global__ void __launch_bounds__(256) k_b_bwd(const BCase *__restrict__ cases, const BCols *__restrict__ cols) {
+  extern __shared__ double2 zs[];
+  const BCols it = cols[blockIdx.x];
+  const BCase &C = cases[it.c];
+  if (C.done) return;
+  const int nx = C.nx, ny = C.ny, M = ny / 2, nc = C.fcols, x0 = it.x0;
+  const double2 *tw = reinterpret_cast<const double2 *>(C.tw);
+  const int half = M / 2 + 1;
+  for (int e = threadIdx.x; e < nc * half; e += blockDim.x) {
+    const int c = e % nc, k = e / nc, x = x0 + c;
+    double2 *zc = zs + c * M;
+    if (x >= nx) {
+      zc[fft::fft_slot(k, M, C.fft_nst, C.fft_first2)] = make_double2(0.0, 0.0);
+      if (k > 0) zc[fft::fft_slot(M - k, M, C.fft_nst, C.fft_first2)] = make_double2(0.0, 0.0);
+      continue;
+    }
+    fft::rfft_pre(C.spec + x, zc, M, k, tw, C.fft_nst, C.fft_first2, (size_t)nx);
+  }
+  __syncthreads();
+  fft::fft_stages<false>(zs, nc, M, ny, C.fft_nst, C.fft_first2, tw);
+  const double *zd = reinterpret_cast<const double *>(zs);
+  const double rny = 1.0 / ny;
+  for (int e = threadIdx.x; e < nc * ny; e += blockDim.x) {
+    const int c = e % nc, y = e / nc, x = x0 + c;
+    if (x < nx) C.psi[(size_t)y * nx + x] = zd[2 * (c * M + (y >> 1)) + (y & 1)] * rny;
+  }
+}
+
+// Partition-method solve of the mode lines J = j0 .. j0+3 (one warp each).
+// Per-mode factor block (doubles): inv[nx] up[nx] v[nx] w[nx] alpha[5][32]
+// beta[5][32] rD[32]; rows are indexed by x.
+__global__ void __launch_bounds__(32 * kBModesPerBlock) k_b_tri(const BCase *__restrict__ cases,
+                                                               const BModes *__restrict__ items) {
+  const BModes it = items[blockIdx.x];
+  const BCase &C = cases[it.c];
+  if (C.done) return;
+  const int lane = threadIdx.x & 31;
+  const int J = it.j0 + (threadIdx.x >> 5);
+  if (J >= C.nh) return;
+  const int n = C.nx, m = C.seg;
+  const int s = lane * m, e = s + m - 1;
+  double2 *line = C.spec + (size_t)J * n;
+  const double *f = C.pfac + (size_t)J * C.pstride;
+  const double *inv = f, *up = f + n, *vv = f + 2 * n, *ww = f + 3 * n;
+  const double *alpha = f + 4 * n, *beta = alpha + kPcrLevels * kSeg, *rD = beta + kPcrLevels * kSeg;
+  const double *lo = C.lo, *hi = C.hi;
+  // 1) interior rows s..e-1 with zero boundary values: forward and back substitution
+  double2 y = line[s];
+  y.x *= inv[s];
+  y.y *= inv[s];
+  line[s] = y;
+  for (int i = s + 1; i < e; ++i) {
+    double2 r = line[i];
+    const double a = lo[i], iv = inv[i];
+    r.x = iv * fma(-a, y.x, r.x);
+    r.y = iv * fma(-a, y.y, r.y);
+    line[i] = r;
+    y = r;
+  }
+  for (int i = e - 2; i >= s; --i) {
+    double2 r = line[i];
+    const double u = up[i];
+    r.x = fma(-u, y.x, r.x);
+    r.y = fma(-u, y.y, r.y);
+    line[i] = r;
+    y = r;
+  }
+  // y now holds the first interior value y_s; the last interior value y_{e-1}
+  const double2 ylast = line[e - 1];
+  // 2) reduced right-hand side of interface row e:
+  //    R = r_e - a_e y_{e-1} - c_e y'_{s'} (y'_{s'} from the next lane)
+  const double ynx = __shfl_down_sync(0xffffffffu, y.x, 1);
+  const double yny = __shfl_down_sync(0xffffffffu, y.y, 1);
+  const double2 re = line[e];
+  const double ae = lo[e], ce = lane < kSeg - 1 ? hi[e] : 0.0;
+  double Rx = re.x - ae * ylast.x - ce * (lane < kSeg - 1 ? ynx : 0.0);
+  double Ry = re.y - ae * ylast.y - ce * (lane < kSeg - 1 ? yny : 0.0);
+  if (J == 0 && lane == kSeg - 1) {  // singular mean mode: pin the last unknown to 0
+    Rx = 0.0;
+    Ry = 0.0;
+  }
+  // 3) parallel cyclic reduction over the 32 interface equations
+#pragma unroll
+  for (int lev = 0; lev < kPcrLevels; ++lev) {
+    const int d = 1 << lev;
+    const double mx = __shfl_up_sync(0xffffffffu, Rx, d), my = __shfl_up_sync(0xffffffffu, Ry, d);
+    const double px = __shfl_down_sync(0xffffffffu, Rx, d), py = __shfl_down_sync(0xffffffffu, Ry, d);
+    const double al = alpha[lev * kSeg + lane], be = beta[lev * kSeg + lane];
+    const double lmx = lane >= d ? mx : 0.0, lmy = lane >= d ? my : 0.0;
+    const double lpx = lane + d < kSeg ? px : 0.0, lpy = lane + d < kSeg ? py : 0.0;
+    Rx = fma(be, lpx, fma(al, lmx, Rx));
+    Ry = fma(be, lpy, fma(al, lmy, Ry));
+  }
+  const double xe_x = Rx * rD[lane], xe_y = Ry * rD[lane];
+  line[e] = make_double2(xe_x, xe_y);
+  // 4) interiors from the spikes: x_i = y_i + v_i x_{e(k-1)} + w_i x_{e(k)}
+  const double xl_x = __shfl_up_sync(0xffffffffu, xe_x, 1), xl_y = __shfl_up_sync(0xffffffffu, xe_y, 1);
+  const double lx_ = lane > 0 ? xl_x : 0.0, ly_ = lane > 0 ? xl_y : 0.0;
+  for (int i = s; i < e; ++i) {
+    double2 r = line[i];
+    r.x = fma(ww[i], xe_x, fma(vv[i], lx_, r.x));
+    r.y = fma(ww[i], xe_y, fma(vv[i], ly_, r.y));
+    line[i] = r;
+  }
+}
+
+// ---------------------------------------------------- correction and pressure
+__global__ void __launch_bounds__(kBTileX) k_b_corr(BCase *__restrict__ cases, const BTile *__restrict__ tiles,
+                                                   int rk) {
+  const BTile tl = tiles[blockIdx.x];
+  BCase &C = cases[tl.c];
+  if (C.done) return;
+  const int nx = C.nx, ny = C.ny;
+  const int x = tl.x0 + threadIdx.x;
+  const bool live = x < nx;
+  float mx = 0.f, my = 0.f;
+  if (live) {
+    const int y0 = tl.y0, y1 = min(y0 + kBTileY, ny);
+    const int pu = C.par ^ (rk & 1) ^ 1;
+    float *__restrict__ ux = C.ux[pu];
+    float *__restrict__ uy = C.uy[pu];
+    const double *__restrict__ psi = C.psi;
+    double *__restrict__ p = C.p;
+    const double gdt = C.gdt[rk], dxi = C.dxi[x], rdy = C.rdy;
+    const float rxc = C.rdxc_f[x], rdyf = C.rdy_f;
+    double sm = psi[(size_t)wdn(y0, ny) * nx + x];
+    for (int y = y0; y < y1; ++y) {
+      const size_t r = (size_t)y * nx + x;
+      const double sc = psi[r];
+      if (x >= 1) {  // src/fluid/correct_velocity.c:19-25
+        const float u = ux[r] - (float)((gdt * (sc - psi[r - 1])) * dxi);
+        ux[r] = u;
+        mx = fmaxf(mx, fabsf(u) * rxc);
+      }
+      const float v = uy[r] - (float)((gdt * (sc - sm)) * rdy);  // :31-37
+      uy[r] = v;
+      my = fmaxf(my, fabsf(v) * rdyf);
+      p[r] += sc;  // src/fluid/update_pressure.c:26-31
+      sm = sc;
+    }
+  }
+  if (rk == 2) {  // max |u|/dx for the next step's dt (src/param/decide_dt.c:35-50)
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+      my = fmaxf(my, __shfl_xor_sync(0xffffffffu, my, off));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomicMax(&C.umax[0], __float_as_uint(mx));
+      atomicMax(&C.umax[1], __float_as_uint(my));
+    }
+  }
+}
+
+// end of a step for every case: step/time bookkeeping, buffer swap, done flag,
+// dt of the next step (src/param/decide_dt.c:11-101, explicit scheme) and the
+// RK scalars derived from it
+struct RkCoefs {
+  double a[3], b[3];
+};
+
+__global__ void k_b_dt(BCase *cases, int ncases, RkCoefs rk) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncases) return;
+  BCase &C = cases[c];
+  if (C.done) return;
+  C.time += C.dt;
+  C.step += 1;
+  C.par ^= 1;
+  if (C.target_steps > 0 && C.step >= C.target_steps) C.done = 1;
+  const float ux_m = __uint_as_float(C.umax[0]), uy_m = __uint_as_float(C.umax[1]);
+  C.umax[0] = 0u;
+  C.umax[1] = 0u;
+  double dt_adv = 5.e-2;
+  if (ux_m > 0.f) dt_adv = fmin(dt_adv, 1.0 / (double)ux_m);
+  if (uy_m > 0.f) dt_adv = fmin(dt_adv, 1.0 / (double)uy_m);
+  dt_adv *= 0.7;
+  double dt = fmin(dt_adv, C.dt_dif);
+  if (C.fixed_dt > 0.0) dt = C.fixed_dt;
+  C.dt = dt;
+  for (int k = 0; k < 3; ++k) {
+    C.adt[k] = rk.a[k] * dt;
+    C.bdt[k] = rk.b[k] * dt;
+    C.gdt[k] = (rk.a[k] + rk.b[k]) * dt;
+    C.rgdt[k] = 1. / C.gdt[k];
+  }
+}
+
+}  // namespace
+
+// kernel attributes, set once outside any stream capture
+cudaError_t batch_kernels_init() {
+  cudaFuncSetAttribute(k_b_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+  cudaFuncSetAttribute(k_b_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+  return cudaGetLastError();
+}
+
+// the launch helpers below only enqueue: the graph replays are counted by sns_batch_step
+cudaError_t launch_batch_stencil(const BCase *cases, const BTile *tiles, int ntiles, int rk, cudaStream_t st) {
+  if (ntiles == 0) return cudaSuccess;
+  k_b_stencil<<<ntiles, kBTileX, 0, st>>>(cases, tiles, rk);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_fwd(const BCase *cases, const BCols *cols, int ncols, int rk, size_t smem, int threads,
+                             cudaStream_t st) {
+  if (ncols == 0) return cudaSuccess;
+  k_b_fwd<<<ncols, threads, smem, st>>>(cases, cols, rk);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_bwd(const BCase *cases, const BCols *cols, int ncols, size_t smem, int threads,
+                             cudaStream_t st) {
+  if (ncols == 0) return cudaSuccess;
+  k_b_bwd<<<ncols, threads, smem, st>>>(cases, cols);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_tri(const BCase *cases, const BModes *modes, int nmodes, cudaStream_t st) {
+  if (nmodes == 0) return cudaSuccess;
+  k_b_tri<<<nmodes, 32 * kBModesPerBlock, 0, st>>>(cases, modes);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_corr(const BCase *cases, const BTile *tiles, int ntiles, int rk, cudaStream_t st) {
+  if (ntiles == 0) return cudaSuccess;
+  k_b_corr<<<ntiles, kBTileX, 0, st>>>(const_cast<BCase *>(cases), tiles, rk);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_dt(BCase *cases, int ncases, const double *rk_a, const double *rk_b, cudaStream_t st) {
+  if (ncases == 0) return cudaSuccess;
+  RkCoefs rk;
+  for (int k = 0; k < 3; ++k) {
+    rk.a[k] = rk_a[k];
+    rk.b[k] = rk_b[k];
+  }
+  k_b_dt<<<(ncases + 127) / 128, 128, 0, st>>>(cases, ncases, rk);
+  return cudaGetLastError();
+}
+
+}  // namespace sns

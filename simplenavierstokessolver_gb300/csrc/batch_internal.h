@@ -1,0 +1,82 @@
+// Internal structures of the batched FP32-stencil / FP64-Poisson engine.
+//
+// Per-case device layout: FP32 fields ux, uy, T (two buffers each) and the RK
+// sources, FP64 p and psi, all dense ny x nx, x fastest, no halos (walls and
+// the periodic wrap are index logic, as in the plain path). The FP64
+// spectrum is mode-major here: mode J of column x at spec[J*nx + x], so a
+// warp solving one mode line reads contiguous segments.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace sns {
+
+constexpr int kSeg = 32;      // partition-method segments per line (one per lane)
+constexpr int kPcrLevels = 5; // log2(kSeg)
+
+struct BCase {
+  // ---- static
+  int nx, ny, nh;
+  int fft_nst, fft_first2, fcols;  // FFT stage layout, columns per FFT block
+  int with_t, with_force;
+  int seg;                         // rows per segment = nx / kSeg
+  double dy, rdy;
+  float rdy_f, kappa_f, nu_f;
+  double dt_dif;                   // explicit diffusive limit min(dt_dif_x, dt_dif_y)
+  double fixed_dt;
+  long long target_steps;
+  const float *rdxf_f, *rdxc_f;    // [nx], [nx+1]
+  const float *ccm_f, *ccp_f;      // DXC(i)/(2 DXF(i)), DXC(i+1)/(2 DXF(i))
+  const float *cfm_f, *cfp_f;      // DXF(i-1)/(2 DXC(i)), DXF(i)/(2 DXC(i))
+  const double *rdxf, *rdxc, *dxi; // FP64 metrics
+  const double *tw;                // [2*ny]
+  const double *lo, *hi;           // Poisson sub/super diagonals a_i, c_i (mode independent) [nx]
+  const double *pfac;              // per mode: inv[nx] up[nx] v[nx] w[nx] alpha[5*32] beta[5*32] rD[32]
+  size_t pstride;                  // doubles per mode in pfac
+  // ---- fields
+  float *ux[2], *uy[2], *t[2];
+  float *aux, *auy, *at;
+  double *p, *psi;
+  double2 *spec;
+  // ---- dynamic (device-owned)
+  int par;                         // buffer holding the current ux, uy, T
+  int done;
+  long long step;
+  double time, dt;
+  double adt[3], bdt[3], gdt[3], rgdt[3];
+  unsigned int umax[2];            // float bits of max |ux|/DXC and max |uy|/dy (next dt)
+};
+
+struct BTile {
+  int c, x0, y0;
+};
+struct BCols {
+  int c, x0;
+};
+struct BModes {
+  int c, j0;
+};
+
+constexpr int kBTileX = 64;
+constexpr int kBTileY = 8;
+constexpr int kBCorrY = 4;
+constexpr int kBModesPerBlock = 4;
+
+cudaError_t batch_kernels_init();
+cudaError_t launch_batch_stencil(const BCase *cases, const BTile *tiles, int ntiles, int rk, cudaStream_t st);
+cudaError_t launch_batch_fwd(const BCase *cases, const BCols *cols, int ncols, int rk, size_t smem, int threads,
+                             cudaStream_t st);
+cudaError_t launch_batch_tri(const BCase *cases, const BModes *modes, int nmodes, cudaStream_t st);
+cudaError_t launch_batch_bwd(const BCase *cases, const BCols *cols, int ncols, size_t smem, int threads,
+                             cudaStream_t st);
+cudaError_t launch_batch_corr(const BCase *cases, const BTile *tiles, int ntiles, int rk, cudaStream_t st);
+cudaError_t launch_batch_dt(BCase *cases, int ncases, const double *rk_a, const double *rk_b, cudaStream_t st);
+
+void count_launches(long long n);
+// sets the message returned by sns_last_error() on this thread
+void record_error(const char *msg);
+
+}  // namespace sns

@@ -90,11 +90,13 @@ __device__ __forceinline__ void fft_stages(double2 *z, int cols, int M, int N, i
 
 // split step of the forward real FFT for bin pair (k, M-k) of one column,
 // k in [0, M/2]: X[k] from the half-length complex spectrum Z (natural order)
-__device__ __forceinline__ void rfft_post(const double2 *zc, double2 *out, int M, int k, const double2 *tw) {
+// (bins of one column at out[J * os])
+__device__ __forceinline__ void rfft_post(const double2 *zc, double2 *out, int M, int k, const double2 *tw,
+                                          size_t os = 1) {
   if (k == 0) {
     const double2 z0 = zc[0];
     out[0] = make_double2(z0.x + z0.y, 0.0);
-    out[M] = make_double2(z0.x - z0.y, 0.0);
+    out[(size_t)M * os] = make_double2(z0.x - z0.y, 0.0);
   } else {
     const double2 A = zc[k], B = zc[M - k];
     const double sre = A.x + B.x, dim = A.y - B.y, dre = A.x - B.x, sim = A.y + B.y;
@@ -103,20 +105,21 @@ __device__ __forceinline__ void rfft_post(const double2 *zc, double2 *out, int M
     const double2 w = tw[k];
     const double wor = w.x * orr - w.y * oi;
     const double woi = w.x * oi + w.y * orr;
-    out[k] = make_double2(er + wor, ei + woi);
-    if (2 * k != M) out[M - k] = make_double2(er - wor, woi - ei);
+    out[(size_t)k * os] = make_double2(er + wor, ei + woi);
+    if (2 * k != M) out[(size_t)(M - k) * os] = make_double2(er - wor, woi - ei);
   }
 }
 
-// inverse split step for bin pair (k, M-k): Z slots (digit-reversed) from X;
+// inverse split step for bin pair (k, M-k): Z slots (digit-reversed) from X
+// (bins of one column at in[J * is]);
 // imaginary parts of X[0] and X[M] are ignored (FFTW c2r convention)
 __device__ __forceinline__ void rfft_pre(const double2 *in, double2 *zc, int M, int k, const double2 *tw, int nst,
-                                         int first2) {
+                                         int first2, size_t is = 1) {
   if (k == 0) {
-    const double x0r = in[0].x, xmr = in[M].x;
+    const double x0r = in[0].x, xmr = in[(size_t)M * is].x;
     zc[0] = make_double2(x0r + xmr, x0r - xmr);
   } else {
-    const double2 A = in[k], B = in[M - k];
+    const double2 A = in[(size_t)k * is], B = in[(size_t)(M - k) * is];
     const double er = A.x + B.x, ei = A.y - B.y, dr = A.x - B.x, di = A.y + B.y;
     const double2 w = tw[k];
     const double orr = dr * w.x + di * w.y;

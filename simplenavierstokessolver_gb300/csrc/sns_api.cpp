@@ -30,6 +30,8 @@ void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_rel
 
 static thread_local std::string g_error;
 
+void record_error(const char *msg) { g_error = msg; }
+
 static int fail(int code, const char *fmt, ...) {
   char buf[512];
   va_list ap;

@@ -1,0 +1,171 @@
+"""The batched FP32-stencil / FP64-Poisson form on the GPU.
+
+Accuracy is measured against the FP64 CPU oracle (bit-identical to the
+reference) run with the same dt and the explicit scheme, as relative L2 error
+per field over the interior; the tolerances below are the stated bars of this
+form. Batching must not change any case: a case computed alone and the same
+case computed in a mix of other cases (admitted or retired mid-run) agree
+bit for bit, because every case's arithmetic only reads its own data.
+"""
+import numpy as np
+import pytest
+
+from oracle.bindings import Config, OracleCase
+
+pytestmark = pytest.mark.gpu
+
+EXPLICIT_ONLY = [1.0, 1e30, 1e30, 1e30]  # cost table that always selects EXP(x)-EXP(y)
+FIELDS = ("ux", "uy", "p", "temp")
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    from simplenavierstokessolver_gb300.build import build
+
+    build()
+
+
+def interior(k, a):
+    return a[1:-1, 1:-1] if k != "ux" else a[1:-1, 1:-1]
+
+
+def rel_l2(a, b):
+    nb = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / (nb if nb > 0 else 1.0))
+
+
+def errors(got, ref):
+    return {k: rel_l2(interior(k, got[k]), interior(k, ref[k])) for k in FIELDS}
+
+
+def oracle_fixed_dt(desc, steps, dt):
+    from simplenavierstokessolver_gb300.batch import initial_temperature
+
+    cfg = Config(desc.itot, desc.jtot, ly=desc.ly, stretch=desc.stretch, Ra=desc.Ra, Pr=desc.Pr)
+    o = OracleCase(cfg, threads=4)
+    st = o.get_state()
+    o.set_state(st["ux"], st["uy"], st["p"], initial_temperature(desc))
+    o.set_dt(dt, 0, 0)
+    o.run(steps, decide=False)
+    return o
+
+
+@pytest.mark.parametrize("stretch", [1e9, 3], ids=["uniform", "stretched"])
+def test_single_case_matches_fp64_oracle(stretch):
+    from simplenavierstokessolver_gb300.batch import Batch, Desc
+
+    desc = Desc(64, 128, ly=2.0, stretch=stretch, Ra=1e6, Pr=1.0, seed=7, fixed_dt=0.01)
+    with Batch(256 << 20) as b:
+        s = b.add(desc)
+        b.step(60)
+        got = b.state(s)
+        st = b.status(s)
+    assert st["step"] == 60 and abs(st["time"] - 0.6) < 1e-12
+    o = oracle_fixed_dt(desc, 60, 0.01)
+    err = errors(got, o.get_state())
+    assert max(err.values()) < 1e-5, err
+
+
+def test_cfl_dt_tracks_the_oracle():
+    """dt from the device max-|u| reduction follows the reference's rule."""
+    from simplenavierstokessolver_gb300.batch import Batch, Desc, initial_temperature
+
+    desc = Desc(128, 256, ly=2.0, Ra=1e7, Pr=1.0, seed=3)
+    cfg = Config(128, 256, ly=2.0, Ra=1e7, Pr=1.0)
+    o = OracleCase(cfg, threads=4)
+    st0 = o.get_state()
+    o.set_state(st0["ux"], st0["uy"], st0["p"], initial_temperature(desc))
+    o.set_costs(EXPLICIT_ONLY)
+    with Batch(256 << 20) as b:
+        s = b.add(desc)
+        for n in (1, 20, 40):
+            b.step(n)
+            o.run(n)
+            st = b.status(s)
+            odt = o.get_dt()
+            assert st["step"] == odt["step"]
+            assert abs(st["time"] - odt["time"]) <= 1e-5 * odt["time"]
+        err = errors(b.state(s), o.get_state())
+    assert max(err.values()) < 1e-4, err
+
+
+def test_projection_is_solenoidal():
+    from simplenavierstokessolver_gb300.batch import Batch, Desc
+
+    desc = Desc(256, 512, Ra=1e8, Pr=1.0, seed=11)
+    with Batch(512 << 20) as b:
+        s = b.add(desc)
+        b.step(30)
+        got = b.state(s)
+    nx, ny = desc.itot, desc.jtot
+    dx, dy = 1.0 / nx, 2.0 / ny
+    ux, uy = got["ux"], got["uy"]
+    div = (ux[1:-1, 1:] - ux[1:-1, :-1]) / dx + (uy[2:, 1:-1] - uy[1:-1, 1:-1]) / dy
+    scale = max(np.abs(ux).max() / dx, np.abs(uy).max() / dy)
+    assert np.abs(div).max() < 1e-5 * scale  # FP32 velocity: round-off level
+
+
+def test_alone_and_in_the_mix_are_identical():
+    from simplenavierstokessolver_gb300.batch import Batch, Desc
+
+    descs = [Desc(64, 128, Ra=3e6, Pr=0.7, seed=1), Desc(128, 256, Ra=1e8, Pr=5.0, seed=2),
+             Desc(96, 64, ly=0.5, Ra=1e5, Pr=2.0, seed=3, stretch=4), Desc(256, 512, Ra=1e9, Pr=1.0, seed=4)]
+    alone = []
+    for d in descs:
+        with Batch(512 << 20) as b:
+            s = b.add(d)
+            b.step(25)
+            alone.append(b.state(s))
+    with Batch(1 << 30) as b:
+        slots = [b.add(d) for d in descs]
+        b.step(25)
+        mixed = [b.state(s) for s in slots]
+    for a, m in zip(alone, mixed):
+        for k in a:
+            assert np.array_equal(a[k], m[k]), k
+
+
+def test_admission_retirement_and_completion():
+    from simplenavierstokessolver_gb300 import _native as N
+    from simplenavierstokessolver_gb300.batch import Batch, Desc, case_bytes
+
+    small = Desc(64, 128, Ra=1e6, Pr=1.0, seed=21, steps=30)
+    other = Desc(128, 256, Ra=1e7, Pr=1.0, seed=22)
+    need = case_bytes(small) + case_bytes(other)
+    with Batch(need + case_bytes(small) // 2) as b:  # room for exactly these two
+        s1 = b.add(small)
+        b.step(10)
+        s2 = b.add(other)  # joins mid-run
+        assert b.try_add(Desc(64, 128, seed=23)) is None  # does not fit: rejected, nothing changes
+        b.step(40)  # small completes after its 30th step
+        st = b.status(s1)
+        assert st["done"] and st["step"] == 30
+        got_small = b.state(s1)
+        b.remove(s1)  # retire: memory returns to the arena
+        s3 = b.add(Desc(64, 128, Ra=1e6, Pr=1.0, seed=24))
+        b.step(5)
+        assert b.status(s2)["step"] == 45 and b.status(s3)["step"] == 5
+        got_other = b.state(s2)
+    with Batch(256 << 20) as b:
+        s = b.add(small)
+        b.step(35)
+        assert b.status(s)["step"] == 30
+        ref_small = b.state(s)
+    with Batch(256 << 20) as b:
+        s = b.add(other)
+        b.step(45)
+        ref_other = b.state(s)
+    for k in ref_small:
+        assert np.array_equal(got_small[k], ref_small[k]), k
+        assert np.array_equal(got_other[k], ref_other[k]), k
+    assert N.SNS_ERR_OOM == 4
+
+
+def test_unsupported_sizes_are_rejected():
+    from simplenavierstokessolver_gb300 import _native as N
+    from simplenavierstokessolver_gb300.batch import Batch, Desc
+
+    with Batch(64 << 20) as b:
+        for d in (Desc(48, 64), Desc(64, 96), Desc(64, 4)):
+            with pytest.raises(N.SnsError):
+                b.add(d)
