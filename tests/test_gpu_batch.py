@@ -50,18 +50,28 @@ def oracle_fixed_dt(desc, steps, dt):
     return o
 
 
+def explicit_dt(desc):
+    """the reference's first dt for this case with both directions explicit"""
+    o = OracleCase(Config(desc.itot, desc.jtot, ly=desc.ly, stretch=desc.stretch, Ra=desc.Ra, Pr=desc.Pr))
+    o.set_costs(EXPLICIT_ONLY)
+    o.decide_dt()
+    return o.get_dt()["dt"]
+
+
 @pytest.mark.parametrize("stretch", [1e9, 3], ids=["uniform", "stretched"])
 def test_single_case_matches_fp64_oracle(stretch):
     from simplenavierstokessolver_gb300.batch import Batch, Desc
 
-    desc = Desc(64, 128, ly=2.0, stretch=stretch, Ra=1e6, Pr=1.0, seed=7, fixed_dt=0.01)
+    desc = Desc(64, 128, ly=2.0, stretch=stretch, Ra=1e6, Pr=1.0, seed=7)
+    dt = explicit_dt(desc)
+    desc.fixed_dt = dt
     with Batch(256 << 20) as b:
         s = b.add(desc)
         b.step(60)
         got = b.state(s)
         st = b.status(s)
-    assert st["step"] == 60 and abs(st["time"] - 0.6) < 1e-12
-    o = oracle_fixed_dt(desc, 60, 0.01)
+    assert st["step"] == 60 and abs(st["time"] - 60 * dt) < 1e-12
+    o = oracle_fixed_dt(desc, 60, dt)
     err = errors(got, o.get_state())
     assert max(err.values()) < 1e-5, err
 
