@@ -34,6 +34,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 PEAKS_PATH = os.path.join(ROOT, "MEASURED_PEAKS.json")
+METRIC = "cell-steps/s plain FP64 vs batched FP32-stencil at stated L2 error; p50/p99"
 FALLBACK_HBM_GBS = 6800.0
 # FP64 instruction rate of this GPU (DADD = DMUL = DFMA issue rate), measured with
 # a pipe-saturating loop of independent FP64 ops on a GB300 (see the FP64 profile
@@ -209,7 +210,7 @@ def reference_arm(args, world, rank):
     total = sum(times)
     value = cfg.itot * cfg.jtot * args.steps / total
     line = {
-        "metric": "cell-steps/s (plain FP64 SMR-RK3 step)", "value": value, "unit": "cell-steps/s",
+        "metric": METRIC, "value": value, "unit": "cell-steps/s",
         "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (reference initial condition, srand(0))",
@@ -223,10 +224,133 @@ def reference_arm(args, world, rank):
 
 
 def workload_config(args):
-    return {"workload": f"rayleigh_benard_{args.nx}x{args.ny}_Ra{args.Ra:g}_Pr{args.Pr:g}_plain_fp64",
+    return {"workload": f"rayleigh_benard_{args.nx}x{args.ny}_Ra{args.Ra:g}_Pr{args.Pr:g}",
             "nx": args.nx, "ny": args.ny, "lx": 1.0, "ly": 2.0, "Ra": args.Ra, "Pr": args.Pr,
             "grid": "uniform", "scheme": "explicit x / explicit y (chosen by param_decide_dt)",
             "l2": "flushed between timed steps (256 MiB write)", "parallelism": "replicas only"}
+
+
+# ------------------------------------------------------ FP32-stencil / batched
+def fp32_single(args, torch):
+    """throughput of the FP32-stencil / FP64-Poisson form on the same case"""
+    from simplenavierstokessolver_gb300.batch import Batch, Desc
+
+    cells = args.nx * args.ny
+    with Batch(8 << 30) as b:
+        s = b.add(Desc(args.nx, args.ny, ly=2.0, Ra=args.Ra, Pr=args.Pr))
+        stream = torch.cuda.ExternalStream(b.stream())
+        flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+        b.step(args.warmup)
+        b.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        for a, e in ev:
+            a.record(stream)
+            b.step(1)
+            e.record(stream)
+            with torch.cuda.stream(stream):
+                flush.zero_()
+        b.synchronize()
+        ms = sum(a.elapsed_time(e) for a, e in ev)
+        del b, s
+    return {"value": cells * args.steps / (ms * 1e-3), "unit": "cell-steps/s", "ms_per_step": ms / args.steps,
+            "l2": "flushed between timed steps (256 MiB write)"}
+
+
+def fp32_accuracy(args):
+    """The FP32-stencil form against the bit-exact FP64 path (identical to the
+    reference) over args.acc_steps steps with the same dt sequence: the
+    batch's own CFL dt is replayed into the FP64 solver. Returns relative L2
+    per field (p modulo its mean) and both sets of Nusselt numbers."""
+    import numpy as np
+
+    from simplenavierstokessolver_gb300 import Case
+    from simplenavierstokessolver_gb300.batch import Batch, Desc
+
+    nsteps = args.acc_steps
+    desc = Desc(args.nx, args.ny, ly=2.0, Ra=args.Ra, Pr=args.Pr)
+    dts = []
+    with Batch(8 << 30) as b:
+        s = b.add(desc)
+        for _ in range(nsteps):
+            dts.append(b.status(s)["dt"])
+            b.step(1)
+        got = b.state(s)
+        diag32 = b.diagnostics(s)
+    with Case(args.nx, args.ny, ly=2.0, Ra=args.Ra, Pr=args.Pr) as c:
+        for dt in dts:
+            c.set_dt(dt, 0, 0)
+            c.integrate()
+        c.synchronize()
+        ref = c.get_state()
+        diag64 = c.diagnostics()
+    err = {}
+    for k in ("ux", "uy", "temp", "p"):
+        a, r = got[k][1:-1, 1:-1], ref[k][1:-1, 1:-1]
+        if k == "p":
+            a, r = a - a.mean(), r - r.mean()
+        err[k] = float(np.linalg.norm(a - r) / np.linalg.norm(r))
+    names = ["nu_wall", "nu_injection", "nu_kinetic_dissipation", "nu_thermal_dissipation"]
+    return {"steps": nsteps, "time": float(sum(dts)), "dt": "CFL dt of the FP32 run, replayed in the FP64 run",
+            "rel_l2": err, "nusselt_fp64": dict(zip(names, diag64[7:].tolist())),
+            "nusselt_fp32_stencil": dict(zip(names, diag32[7:].tolist())),
+            "divergence_max_fp32_stencil": float(diag32[0]), "divergence_max_fp64": float(diag64[0])}
+
+
+def ensemble_throughput(args, torch):
+    """64-case ensemble: batched FP32-stencil form (one graph launch per step
+    for all cases) against the plain FP64 path stepping the cases one by one"""
+    from simplenavierstokessolver_gb300 import Case
+    from simplenavierstokessolver_gb300.batch import Batch
+    from simplenavierstokessolver_gb300.workloads import ensemble
+
+    descs = ensemble(64)
+    cells = sum(d.itot * d.jtot for d in descs)
+    with Batch(8 << 30) as b:
+        for d in descs:
+            b.add(d)
+        stream = torch.cuda.ExternalStream(b.stream())
+        b.step(args.warmup)
+        b.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.step(args.ens_steps)
+        e1.record(stream)
+        b.synchronize()
+        ms_b = e0.elapsed_time(e1)
+    batched = cells * args.ens_steps / (ms_b * 1e-3)
+    plain_steps = max(2, args.ens_steps // 5)
+    total_s, plain_cells = 0.0, 0
+    for d in descs:
+        with Case(d.itot, d.jtot, ly=d.ly, Ra=d.Ra, Pr=d.Pr) as c:
+            c.run(2)
+            t0 = time.perf_counter()
+            c.run(plain_steps)
+            total_s += time.perf_counter() - t0
+            plain_cells += d.itot * d.jtot
+    plain = plain_cells * plain_steps / total_s
+    return {"cases": len(descs), "cells": cells, "batched_fp32_stencil": batched, "plain_fp64_one_by_one": plain,
+            "ratio": batched / plain, "unit": "cell-steps/s", "batched_steps": args.ens_steps,
+            "plain_steps_per_case": plain_steps,
+            "workload": "nx in {64,128,256}, ny=2nx, log10 Ra in [6,9], Pr in [0.7,7], SplitMix64 seeds 20261203+k"}
+
+
+def serving(args):
+    import numpy as np
+
+    from simplenavierstokessolver_gb300.batch import serve
+    from simplenavierstokessolver_gb300.workloads import serving_stream
+
+    descs, arrivals = serving_stream(args.serve_rate, args.serve_seconds)
+    r = serve(descs, arrivals, hbm_bytes=args.serve_hbm << 20, max_cases=256, chunk_steps=args.serve_chunk)
+    ttc = r["done"] - np.asarray(arrivals)
+    work = sum(d.itot * d.jtot * d.steps for d in descs)
+    return {"requests": len(descs), "rate_per_s": args.serve_rate, "arrival_window_s": args.serve_seconds,
+            "p50_s": float(np.percentile(ttc, 50)), "p99_s": float(np.percentile(ttc, 99)),
+            "mean_queue_wait_s": float(np.mean(r["admit"] - np.asarray(arrivals))),
+            "value": work / r["busy_s"], "unit": "cell-steps/s", "busy_s": r["busy_s"],
+            "hbm_arena_bytes": args.serve_hbm << 20, "chunk_steps": args.serve_chunk,
+            "workload": "Poisson arrivals; nx in {64,128,256,512}, ny=2nx, log10 Ra in [6,10], Pr in [0.7,7], "
+                        "steps in {200..2000}"}
 
 
 # ----------------------------------------------------------------- GPU arm
@@ -335,6 +459,14 @@ def gpu_arm(args, world, rank, local):
                    "+ sns_sync_to_host per step"}
     case.close()
 
+    extra = {}
+    if not args.plain_only:
+        extra["fp32_stencil"] = fp32_single(args, torch)
+        extra["fp32_stencil"]["vs_plain_fp64"] = extra["fp32_stencil"]["value"] / value
+        extra["fp32_stencil"]["accuracy_vs_fp64"] = fp32_accuracy(args)
+        extra["ensemble_64"] = ensemble_throughput(args, torch)
+        extra["serving"] = serving(args)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         from oracle.build import build as build_oracle
@@ -350,13 +482,14 @@ def gpu_arm(args, world, rank, local):
 
     if rank == 0:
         line = {
-            "metric": "cell-steps/s (plain FP64 SMR-RK3 step)", "value": value, "unit": "cell-steps/s",
+            "metric": METRIC, "value": value, "unit": "cell-steps/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (reference initial condition, srand(0))", "config": workload_config(args),
             "roofline": roofline, "fp64_roofline": fp64, "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(launches), "clocks": clk,
         }
+        line.update(extra)
         print(json.dumps(line))
     return 0
 
@@ -373,6 +506,13 @@ def main():
     ap.add_argument("--Pr", type=float, default=1.0)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--plain-only", action="store_true", help="skip the FP32-stencil, ensemble and serving parts")
+    ap.add_argument("--acc-steps", type=int, default=2000, help="steps of the FP32-vs-FP64 accuracy run")
+    ap.add_argument("--ens-steps", type=int, default=50)
+    ap.add_argument("--serve-rate", type=float, default=6.0)
+    ap.add_argument("--serve-seconds", type=float, default=12.0)
+    ap.add_argument("--serve-hbm", type=int, default=2048, help="serving arena in MiB")
+    ap.add_argument("--serve-chunk", type=int, default=10)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

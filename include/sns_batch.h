@@ -78,7 +78,28 @@ extern long long sns_batch_active_cells(const sns_batch *batch);
 /* the initial temperature a case of this description starts from, in the
  * reference's (jtot+2) x (itot+2) layout (for checking against other solvers) */
 extern int sns_batch_initial_temperature(const sns_case_desc *desc, double *temp);
+/* sns_diagnostics (include/sns_gpu.h) for one case of the batch: FP64
+ * compensated reductions over its FP32 fields. Waits. */
+extern int sns_batch_diagnostics(sns_batch *batch, int slot, double out[11]);
 /* errors of these calls are reported by sns_last_error() (include/sns_gpu.h) */
+
+/* Continuous batching in real time. Request r (description reqs[r], which
+ * must set steps > 0) arrives arrival_s[r] seconds after the call starts
+ * (non-decreasing). Arrived requests wait in FIFO order and are admitted
+ * into a batch with an hbm_bytes arena as soon as their footprint fits; all
+ * admitted cases advance together, chunk_steps steps per launch round, and
+ * each finished case is retired at the next round boundary, which returns
+ * its memory for the waiting requests. For each request: admit_s[r] and
+ * done_s[r] (seconds since the start; done_s - arrival_s is its
+ * time-to-completion). on_done, if not NULL, is called for each finished
+ * request before its retirement, with the batch and slot so that the caller
+ * can read its state. Returns SNS_OK or an error; a request larger than the
+ * whole arena is an SNS_ERR_OOM error. *busy_s receives the wall time from
+ * the first admission to the last completion. */
+typedef void (*sns_done_fn)(int request, sns_batch *batch, int slot, void *user);
+extern int sns_serve(const sns_case_desc *reqs, const double *arrival_s, int n, size_t hbm_bytes, int max_cases,
+                     int chunk_steps, double *admit_s, double *done_s, double *busy_s, sns_done_fn on_done,
+                     void *user);
 
 #ifdef __cplusplus
 }

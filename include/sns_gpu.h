@@ -203,6 +203,15 @@ extern int sns_integrate(const param_t *param, const parallel_t *parallel, fluid
 extern int sns_run(param_t *param, const parallel_t *parallel, fluid_t *fluid, temperature_t *temperature,
                    int nsteps);
 
+/* the reference's log quantities (src/logging.c:36-272) computed on the
+ * device in FP64 with compensated summation, without a host copy of the
+ * fields: out[0..1] divergence max and sum, [2..3] x and y momentum,
+ * [4..6] kinetic energy of ux and uy and thermal energy, [7..10] Nusselt
+ * number from the wall heat flux, the energy injection, the kinetic and the
+ * thermal dissipation. Blocks until done. */
+extern int sns_diagnostics(const param_t *param, const fluid_t *fluid, const temperature_t *temperature,
+                           double out[11]);
+
 /* per-kernel device time: with profiling enabled every kernel launched for
  * this solver is bracketed by CUDA events on its stream. sns_profile(f, 1)
  * resets the totals and starts, sns_profile(f, 0) stops. sns_profile_read

@@ -109,6 +109,7 @@ PROTOTYPES = {
     "sns_last_error": (c_char_p, []),
     "sns_kernel_launches": (c_longlong, []),
     "sns_abi_layout": (c_int, [POINTER(c_size_t), c_int]),
+    "sns_diagnostics": (c_int, [PP, PF, PT, _PD]),
     "sns_profile": (c_int, [PF, c_int]),
     "sns_profile_read": (c_int, [PF, POINTER(c_double), POINTER(c_longlong), c_int]),
     "sns_profile_kind_name": (c_char_p, [c_int]),
@@ -127,7 +128,12 @@ PROTOTYPES = {
     "sns_batch_cases": (c_int, [c_void_p, POINTER(c_int), c_int]),
     "sns_batch_active_cells": (c_longlong, [c_void_p]),
     "sns_batch_initial_temperature": (c_int, [PCD, _PD]),
+    "sns_batch_diagnostics": (c_int, [c_void_p, c_int, _PD]),
+    "sns_serve": (c_int, [PCD, _PD, c_int, c_size_t, c_int, c_int, _PD, _PD, _PD, c_void_p, c_void_p]),
 }
+
+# void (*sns_done_fn)(int request, sns_batch *batch, int slot, void *user)
+DONE_FN = ctypes.CFUNCTYPE(None, c_int, c_void_p, c_int, c_void_p)
 
 _lib = None
 

@@ -123,6 +123,9 @@ class Batch:
                                                ctypes.byref(done)), "sns_batch_case_status")
         return {"time": t.value, "dt": dt.value, "step": st.value, "done": bool(done.value)}
 
+    def diagnostics(self, slot: int) -> np.ndarray:
+        return diagnostics_of(self.h, slot)
+
     def state(self, slot: int):
         d = self.descs[slot]
         su, sc = (d.jtot + 2, d.itot + 1), (d.jtot + 2, d.itot + 2)
@@ -130,3 +133,39 @@ class Batch:
         N.check(self.lib.sns_batch_state(self.h, slot, _ptr(out["ux"]), _ptr(out["uy"]), _ptr(out["p"]),
                                          _ptr(out["psi"]), _ptr(out["temp"])), "sns_batch_state")
         return out
+
+
+def diagnostics_of(batch_handle, slot: int) -> np.ndarray:
+    out = np.zeros(11)
+    N.check(_lib().sns_batch_diagnostics(batch_handle, slot, _ptr(out)), "sns_batch_diagnostics")
+    return out
+
+
+def state_of(batch_handle, slot: int, desc: Desc):
+    su, sc = (desc.jtot + 2, desc.itot + 1), (desc.jtot + 2, desc.itot + 2)
+    out = {"ux": np.zeros(su), "uy": np.zeros(sc), "p": np.zeros(sc), "psi": np.zeros(sc), "temp": np.zeros(sc)}
+    N.check(_lib().sns_batch_state(batch_handle, slot, _ptr(out["ux"]), _ptr(out["uy"]), _ptr(out["p"]),
+                                   _ptr(out["psi"]), _ptr(out["temp"])), "sns_batch_state")
+    return out
+
+
+def serve(descs: list[Desc], arrivals: list[float], hbm_bytes: int, max_cases: int = 256, chunk_steps: int = 10,
+          keep_states: bool = False):
+    """Runs sns_serve (continuous batching in real time). Returns admission
+    and completion times (seconds from the start), the busy span and, with
+    keep_states, each request's final fields read just before retirement."""
+    n = len(descs)
+    arr = (N.CaseDesc * n)(*[d.c() for d in descs])
+    at = np.ascontiguousarray(arrivals, dtype=np.float64)
+    admit, done = np.zeros(n), np.zeros(n)
+    busy = c_double()
+    states = {}
+
+    def on_done(req, bh, slot, user):
+        states[req] = state_of(bh, slot, descs[req])
+
+    cb = N.DONE_FN(on_done) if keep_states else None
+    rc = _lib().sns_serve(arr, _ptr(at), n, hbm_bytes, max_cases, chunk_steps, _ptr(admit), _ptr(done),
+                          ctypes.byref(busy), ctypes.cast(cb, ctypes.c_void_p) if cb else None, None)
+    N.check(rc, "sns_serve")
+    return {"admit": admit, "done": done, "busy_s": busy.value, "states": states}

@@ -37,6 +37,7 @@ def cuda_home() -> str:
 UNITS = {
     "plain_fp64.cu": ["--fmad=false"],
     "batch_fp32.cu": [],
+    "diagnostics.cu": [],
     "sns_api.cpp": [],
     "batch_api.cpp": [],
 }

@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "batch_internal.h"
+#include "diag_internal.h"
 #include "host_common.h"
 #include "sns_batch.h"
 #include "sns_gpu.h"
@@ -49,7 +50,7 @@ static size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 // byte layout of one case inside its arena block
 struct CaseLayout {
   size_t rdxf_f, rdxc_f, ccm_f, ccp_f, cfm_f, cfp_f;
-  size_t rdxf, rdxc, dxi, tw, lo, hi, pfac;
+  size_t rdxf, rdxc, dxi, dxf, dxc, tw, lo, hi, pfac;
   size_t ux[2], uy[2], t[2], aux, auy, at, p, psi, spec;
   size_t total;
   size_t pstride;
@@ -74,6 +75,8 @@ static CaseLayout layout_for(int nx, int ny) {
   L.rdxf = take(sizeof(double) * nx);
   L.rdxc = take(sizeof(double) * (nx + 1));
   L.dxi = take(sizeof(double) * (nx + 1));
+  L.dxf = take(sizeof(double) * nx);
+  L.dxc = take(sizeof(double) * (nx + 1));
   L.tw = take(sizeof(double) * 2 * ny);
   L.lo = take(sizeof(double) * nx);
   L.hi = take(sizeof(double) * nx);
@@ -250,6 +253,8 @@ struct sns_batch {
   double rk_b[3] = {0. / 60., -17. / 60., -25. / 60.};
   double *staging = nullptr;  // pinned
   size_t staging_bytes = 0;
+  double *diag = nullptr;  // block partials of sns_batch_diagnostics
+  size_t diag_words = 0;
   std::mutex mu;
 };
 
@@ -406,6 +411,7 @@ int sns_batch_destroy(sns_batch *b) {
   cudaFree(b->d_cols);
   cudaFree(b->d_modes);
   if (b->staging) cudaFreeHost(b->staging);
+  cudaFree(b->diag);
   if (b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return SNS_OK;
@@ -506,6 +512,8 @@ int sns_batch_add(sns_batch *b, const sns_case_desc *d, const double *temp_init,
   chk(put(L.rdxf, rdxf.data(), sizeof(double) * nx));
   chk(put(L.rdxc, rdxc.data(), sizeof(double) * (nx + 1)));
   chk(put(L.dxi, dxi.data(), sizeof(double) * (nx + 1)));
+  chk(put(L.dxf, dxf.data(), sizeof(double) * nx));
+  chk(put(L.dxc, dxc.data(), sizeof(double) * (nx + 1)));
   chk(put(L.tw, tw.data(), sizeof(double) * tw.size()));
   chk(put(L.lo, lo.data(), sizeof(double) * nx));
   chk(put(L.hi, hi.data(), sizeof(double) * nx));
@@ -556,6 +564,8 @@ int sns_batch_add(sns_batch *b, const sns_case_desc *d, const double *temp_init,
   t.rdxf = reinterpret_cast<const double *>(base + L.rdxf);
   t.rdxc = reinterpret_cast<const double *>(base + L.rdxc);
   t.dxi = reinterpret_cast<const double *>(base + L.dxi);
+  t.dxf = reinterpret_cast<const double *>(base + L.dxf);
+  t.dxc = reinterpret_cast<const double *>(base + L.dxc);
   t.tw = reinterpret_cast<const double *>(base + L.tw);
   t.lo = reinterpret_cast<const double *>(base + L.lo);
   t.hi = reinterpret_cast<const double *>(base + L.hi);
@@ -757,3 +767,101 @@ int sns_batch_state(sns_batch *b, int slot, double *ux, double *uy, double *p, d
 }
 
 }  // extern "C"
+
+extern "C" int sns_batch_diagnostics(sns_batch *b, int slot, double out[11]) {
+  if (!b || slot < 0 || slot >= b->max_cases || !b->hc[slot].used || !out) return bfail(SNS_ERR_ARG, "bad slot");
+  std::lock_guard<std::mutex> lk(b->mu);
+  BCase t;
+  BCUDA(cudaStreamSynchronize(b->stream));
+  BCUDA(cudaMemcpy(&t, b->d_cases + slot, sizeof(BCase), cudaMemcpyDeviceToHost));
+  const size_t words = diag_partials_words(t.nx, t.ny);
+  if (b->diag_words < words) {
+    cudaFree(b->diag);
+    b->diag = nullptr;
+    BCUDA(cudaMalloc((void **)&b->diag, sizeof(double) * words));
+    b->diag_words = words;
+  }
+  const sns_case_desc &d = b->hc[slot].d;
+  const DiagArgs<float> a{t.nx, t.ny, t.dy, d.ly, sqrt(d.Pr) * sqrt(d.Ra), sqrt(d.Pr) / sqrt(d.Ra),
+                          1. / sqrt(d.Pr) / sqrt(d.Ra), t.dxf, t.dxc, t.ux[t.par], t.uy[t.par], t.t[t.par]};
+  int nb = 0;
+  BCUDA(launch_diag(a, b->diag, &nb, b->stream));
+  count_launches(1);
+  std::vector<double> h(words);
+  BCUDA(cudaMemcpyAsync(h.data(), b->diag, sizeof(double) * words, cudaMemcpyDeviceToHost, b->stream));
+  BCUDA(cudaStreamSynchronize(b->stream));
+  diag_finish(h.data(), nb, d.ly, out);
+  return SNS_OK;
+}
+
+// ---------------------------------------------------------------- serving
+#include <chrono>
+#include <deque>
+#include <thread>
+
+extern "C" int sns_serve(const sns_case_desc *reqs, const double *arrival_s, int n, size_t hbm_bytes, int max_cases,
+                         int chunk_steps, double *admit_s, double *done_s, double *busy_s, sns_done_fn on_done,
+                         void *user) {
+  if (!reqs || !arrival_s || n <= 0 || chunk_steps <= 0 || !admit_s || !done_s)
+    return bfail(SNS_ERR_ARG, "sns_serve: bad argument");
+  for (int r = 0; r < n; r++) {
+    if (int rc = check_desc(&reqs[r])) return rc;
+    if (reqs[r].steps <= 0) return bfail(SNS_ERR_ARG, "sns_serve: request %d has no step count", r);
+    if (r > 0 && arrival_s[r] < arrival_s[r - 1]) return bfail(SNS_ERR_ARG, "sns_serve: arrivals must not decrease");
+    if (layout_for(reqs[r].itot, reqs[r].jtot).total > hbm_bytes)
+      return bfail(SNS_ERR_OOM, "sns_serve: request %d is larger than the arena", r);
+  }
+  sns_batch *b = sns_batch_create(hbm_bytes, max_cases);
+  if (!b) return SNS_ERR_OOM;
+  using clock = std::chrono::steady_clock;
+  const auto t0 = clock::now();
+  auto now = [&]() { return std::chrono::duration<double>(clock::now() - t0).count(); };
+  std::deque<int> waiting;
+  std::vector<int> slot_req(max_cases, -1);
+  int next = 0, completed = 0, resident = 0;
+  double first_admit = -1.0, last_done = 0.0;
+  int rc = SNS_OK;
+  while (completed < n && rc == SNS_OK) {
+    double t = now();
+    while (next < n && arrival_s[next] <= t) waiting.push_back(next++);
+    while (!waiting.empty()) {  // FIFO admission while the head fits
+      const int r = waiting.front();
+      int slot = -1;
+      const int a = sns_batch_add(b, &reqs[r], nullptr, &slot);
+      if (a == SNS_ERR_OOM) break;
+      if (a != SNS_OK) {
+        rc = a;
+        break;
+      }
+      waiting.pop_front();
+      slot_req[slot] = r;
+      admit_s[r] = now();
+      if (first_admit < 0) first_admit = admit_s[r];
+      resident++;
+    }
+    if (rc != SNS_OK) break;
+    if (resident == 0) {
+      if (next < n) std::this_thread::sleep_for(std::chrono::duration<double>(std::max(0.0, arrival_s[next] - now())));
+      continue;
+    }
+    if ((rc = sns_batch_step(b, chunk_steps)) != SNS_OK) break;
+    if ((rc = sns_batch_synchronize(b)) != SNS_OK) break;
+    t = now();
+    for (int s = 0; s < max_cases; s++) {
+      const int r = slot_req[s];
+      if (r < 0) continue;
+      const CaseHost &h = b->hc[s];
+      if (h.steps_done < h.d.steps) continue;
+      done_s[r] = t;
+      last_done = t;
+      if (on_done) on_done(r, b, s, user);
+      if ((rc = sns_batch_remove(b, s)) != SNS_OK) break;
+      slot_req[s] = -1;
+      resident--;
+      completed++;
+    }
+  }
+  if (busy_s) *busy_s = first_admit >= 0 ? last_done - first_admit : 0.0;
+  sns_batch_destroy(b);
+  return rc;
+}

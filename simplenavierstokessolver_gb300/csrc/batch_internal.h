@@ -32,6 +32,7 @@ struct BCase {
   const float *ccm_f, *ccp_f;      // DXC(i)/(2 DXF(i)), DXC(i+1)/(2 DXF(i))
   const float *cfm_f, *cfp_f;      // DXF(i-1)/(2 DXC(i)), DXF(i)/(2 DXC(i))
   const double *rdxf, *rdxc, *dxi; // FP64 metrics
+  const double *dxf, *dxc;         // DXF(i), DXC(i) (diagnostics)
   const double *tw;                // [2*ny]
   const double *lo, *hi;           // Poisson sub/super diagonals a_i, c_i (mode independent) [nx]
   const double *pfac;              // per mode: inv[nx] up[nx] v[nx] w[nx] alpha[5*32] beta[5*32] rD[32]

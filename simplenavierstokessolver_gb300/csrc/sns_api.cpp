@@ -19,6 +19,7 @@
 #include <string>
 #include <vector>
 
+#include "diag_internal.h"
 #include "host_common.h"
 #include "sns_gpu.h"
 #include "sns_internal.h"
@@ -73,6 +74,7 @@ struct Context {
   // factors for the implicit solves: device buffer + host mirror
   double *fac = nullptr;
   size_t fac_words = 0;
+  double *diag = nullptr;  // block partials of sns_diagnostics
   // optional per-launch event timing (sns_profile)
   bool prof = false;
   std::vector<cudaEvent_t> prof_ev;  // two per slot
@@ -346,59 +348,60 @@ static void host_bc_temp(int nx, int ny, double *t) {
 }
 
 // -------------------------------------------------- dense <-> reference layout
-// dense interior (x fastest, ny rows) from/to a reference-layout array whose
-// rows have `width` entries and whose interior column x sits at offset `off`
+// The structures' host arrays are pinned, so one strided 2D DMA copy per
+// field moves the dense interior (x fastest, ny rows) to or from a
+// reference-layout array whose rows have `width` entries and whose interior
+// column x sits at offset `off`. Callers synchronise once after all copies.
 static int fetch(Context *c, const double *dev) {
   SNS_CUDA(cudaMemcpyAsync(c->staging, dev, sizeof(double) * (size_t)c->nx * c->ny, cudaMemcpyDeviceToHost,
                            c->stream));
-  SNS_CUDA(cudaStreamSynchronize(c->stream));
   return SNS_OK;
 }
 
 static int download(Context *c, const double *dev, double *host, int width, int off, int first_x) {
   const int nx = c->nx, ny = c->ny;
-  if (int rc = fetch(c, dev)) return rc;
-  for (int y = 0; y < ny; y++)
-    std::memcpy(host + (size_t)(y + 1) * width + off + first_x, c->staging + (size_t)y * nx + first_x,
-                sizeof(double) * (nx - first_x));
+  SNS_CUDA(cudaMemcpy2DAsync(host + width + off + first_x, sizeof(double) * width, dev + first_x,
+                             sizeof(double) * nx, sizeof(double) * (nx - first_x), ny, cudaMemcpyDeviceToHost,
+                             c->stream));
   return SNS_OK;
 }
 
+// ux (first_x = 1): the device keeps its wall column x = 0 at zero, it is never copied
 static int upload_field(Context *c, double *dev, const double *host, int width, int off, int first_x) {
   const int nx = c->nx, ny = c->ny;
-  SNS_CUDA(cudaStreamSynchronize(c->stream));
-  for (int y = 0; y < ny; y++) {
-    double *row = c->staging + (size_t)y * nx;
-    if (first_x > 0) std::memset(row, 0, sizeof(double) * first_x);
-    std::memcpy(row + first_x, host + (size_t)(y + 1) * width + off + first_x, sizeof(double) * (nx - first_x));
-  }
-  SNS_CUDA(cudaMemcpyAsync(dev, c->staging, sizeof(double) * (size_t)nx * ny, cudaMemcpyHostToDevice, c->stream));
-  SNS_CUDA(cudaStreamSynchronize(c->stream));
+  SNS_CUDA(cudaMemcpy2DAsync(dev + first_x, sizeof(double) * nx, host + width + off + first_x,
+                             sizeof(double) * width, sizeof(double) * (nx - first_x), ny, cudaMemcpyHostToDevice,
+                             c->stream));
   return SNS_OK;
 }
 
 // sources: srcux* rows of itot-1 entries for i = 2..itot, srcuy*/srctemp* rows of itot
 static int download_src(Context *c, const double *dev, double *host, int is_ux) {
   const int nx = c->nx, ny = c->ny;
-  SNS_CUDA(cudaMemcpyAsync(c->staging, dev, sizeof(double) * (size_t)nx * ny, cudaMemcpyDeviceToHost, c->stream));
-  SNS_CUDA(cudaStreamSynchronize(c->stream));
   const int w = is_ux ? nx - 1 : nx, x0 = is_ux ? 1 : 0;
-  for (int y = 0; y < ny; y++) std::memcpy(host + (size_t)y * w, c->staging + (size_t)y * nx + x0, sizeof(double) * w);
+  SNS_CUDA(cudaMemcpy2DAsync(host, sizeof(double) * w, dev + x0, sizeof(double) * nx, sizeof(double) * w, ny,
+                             cudaMemcpyDeviceToHost, c->stream));
   return SNS_OK;
 }
 
 static int upload_src(Context *c, double *dev, const double *host, int is_ux) {
   const int nx = c->nx, ny = c->ny;
-  SNS_CUDA(cudaStreamSynchronize(c->stream));
   const int w = is_ux ? nx - 1 : nx, x0 = is_ux ? 1 : 0;
-  for (int y = 0; y < ny; y++) {
-    double *row = c->staging + (size_t)y * nx;
-    if (x0) row[0] = 0.0;
-    std::memcpy(row + x0, host + (size_t)y * w, sizeof(double) * w);
-  }
-  SNS_CUDA(cudaMemcpyAsync(dev, c->staging, sizeof(double) * (size_t)nx * ny, cudaMemcpyHostToDevice, c->stream));
-  SNS_CUDA(cudaStreamSynchronize(c->stream));
+  SNS_CUDA(cudaMemcpy2DAsync(dev + x0, sizeof(double) * nx, host, sizeof(double) * w, sizeof(double) * w, ny,
+                             cudaMemcpyHostToDevice, c->stream));
   return SNS_OK;
+}
+
+// pinned, zeroed host array (nullptr on failure)
+static double *host_array(size_t n) {
+  void *p = nullptr;
+  if (cudaHostAlloc(&p, std::max<size_t>(n, 1) * sizeof(double), cudaHostAllocDefault) != cudaSuccess) return nullptr;
+  std::memset(p, 0, std::max<size_t>(n, 1) * sizeof(double));
+  return static_cast<double *>(p);
+}
+
+static void host_free(double *p) {
+  if (p) cudaFreeHost(p);
 }
 
 // -------------------------------------------------------------- RK scalars
@@ -822,16 +825,16 @@ fluid_t *fluid_init(const param_t *param, const parallel_t *parallel) {
   fe->magic = kFluidMagic;
   fe->ctx = c;
   fluid_t &h = fe->pub;
-  h.ux = static_cast<double *>(calloc(nu, sizeof(double)));
-  h.uy = static_cast<double *>(calloc(nc, sizeof(double)));
-  h.p = static_cast<double *>(calloc(nc, sizeof(double)));
-  h.psi = static_cast<double *>(calloc(nc, sizeof(double)));
-  h.srcuxa = static_cast<double *>(calloc(sx, sizeof(double)));
-  h.srcuxb = static_cast<double *>(calloc(sx, sizeof(double)));
-  h.srcuxg = static_cast<double *>(calloc(sx, sizeof(double)));
-  h.srcuya = static_cast<double *>(calloc(sc, sizeof(double)));
-  h.srcuyb = static_cast<double *>(calloc(sc, sizeof(double)));
-  h.srcuyg = static_cast<double *>(calloc(sc, sizeof(double)));
+  h.ux = host_array(nu);
+  h.uy = host_array(nc);
+  h.p = host_array(nc);
+  h.psi = host_array(nc);
+  h.srcuxa = host_array(sx);
+  h.srcuxb = host_array(sx);
+  h.srcuxg = host_array(sx);
+  h.srcuya = host_array(sc);
+  h.srcuyb = host_array(sc);
+  h.srcuyg = host_array(sc);
   Fields &f = fe->f;
   const size_t n = sc;
   int rc = SNS_OK;
@@ -861,7 +864,7 @@ int fluid_finalise(fluid_t *fluid) {
   FluidExt *fe = as_fluid(fluid);
   if (!fe) return fail(SNS_ERR_ARG, "fluid_finalise: not a fluid_t from fluid_init");
   fluid_t &h = fe->pub;
-  for (double *p : {h.ux, h.uy, h.p, h.psi, h.srcuxa, h.srcuxb, h.srcuxg, h.srcuya, h.srcuyb, h.srcuyg}) free(p);
+  for (double *p : {h.ux, h.uy, h.p, h.psi, h.srcuxa, h.srcuxb, h.srcuxg, h.srcuya, h.srcuyb, h.srcuyg}) host_free(p);
   Context *c = fe->ctx;
   if (c) {
     cudaStreamSynchronize(c->stream);
@@ -896,11 +899,11 @@ temperature_t *temperature_init(const param_t *param, const parallel_t *parallel
   te->cur = 0;
   te->snap = -2;
   temperature_t &h = te->pub;
-  h.temp = static_cast<double *>(calloc(nc, sizeof(double)));
-  h.tempforcex = static_cast<double *>(calloc(sx, sizeof(double)));
-  h.srctempa = static_cast<double *>(calloc(sc, sizeof(double)));
-  h.srctempb = static_cast<double *>(calloc(sc, sizeof(double)));
-  h.srctempg = static_cast<double *>(calloc(sc, sizeof(double)));
+  h.temp = host_array(nc);
+  h.tempforcex = host_array(sx);
+  h.srctempa = host_array(sc);
+  h.srctempb = host_array(sc);
+  h.srctempg = host_array(sc);
   // src/temperature/init.c:30-41: linear profile + rand() noise
   {
     const double factor = 0.1;
@@ -933,7 +936,7 @@ int temperature_finalise(temperature_t *temperature) {
   TempExt *te = as_temp(temperature);
   if (!te) return fail(SNS_ERR_ARG, "temperature_finalise: not a temperature_t from temperature_init");
   temperature_t &h = te->pub;
-  for (double *p : {h.temp, h.tempforcex, h.srctempa, h.srctempb, h.srctempg}) free(p);
+  for (double *p : {h.temp, h.tempforcex, h.srctempa, h.srctempb, h.srctempg}) host_free(p);
   Context *c = te->ctx;
   if (c) {
     cudaStreamSynchronize(c->stream);
@@ -1058,6 +1061,7 @@ int sns_sync_to_host(const param_t *param, fluid_t *fluid, temperature_t *temper
         (rc = download(c, fe->f.p, h.p, nx + 2, 1, 0)) || (rc = download(c, fe->f.psi, h.psi, nx + 2, 1, 0)) ||
         (rc = download_src(c, fe->f.aux, h.srcuxa, 1)) || (rc = download_src(c, fe->f.auy, h.srcuya, 0)))
       return rc;
+    SNS_CUDA(cudaStreamSynchronize(c->stream));
     host_bc_ux(nx, ny, h.ux);
     host_bc_uy(nx, ny, h.uy);
     host_bc_p(nx, ny, h.p);
@@ -1071,10 +1075,12 @@ int sns_sync_to_host(const param_t *param, fluid_t *fluid, temperature_t *temper
     int rc = SNS_OK;
     if ((rc = download(c, te->f.t[te->cur], h.temp, nx + 2, 1, 0)) || (rc = download_src(c, te->f.at, h.srctempa, 0)))
       return rc;
+    if (te->snap >= 0)
+      if (int rc2 = fetch(c, te->f.t[te->snap])) return rc2;
+    SNS_CUDA(cudaStreamSynchronize(c->stream));
     host_bc_temp(nx, ny, h.temp);
     if (te->snap >= 0) {
       // tempforcex (src/temperature/force.c:17-23) from the snapshot buffer
-      if (int rc2 = fetch(c, te->f.t[te->snap])) return rc2;
       for (int j = 1; j <= ny; j++)
         for (int i = 2; i <= nx; i++) {
           const double tm = c->staging[(size_t)(j - 1) * nx + (i - 2)], tp = c->staging[(size_t)(j - 1) * nx + (i - 1)];
@@ -1098,6 +1104,7 @@ int sns_sync_to_device(const param_t *param, fluid_t *fluid, temperature_t *temp
         (rc = upload_field(c, fe->f.p, h.p, nx + 2, 1, 0)) || (rc = upload_field(c, fe->f.psi, h.psi, nx + 2, 1, 0)) ||
         (rc = upload_src(c, fe->f.aux, h.srcuxa, 1)) || (rc = upload_src(c, fe->f.auy, h.srcuya, 0)))
       return rc;
+    SNS_CUDA(cudaStreamSynchronize(c->stream));
   }
   if (temperature) {
     TempExt *te = as_temp(temperature);
@@ -1109,7 +1116,30 @@ int sns_sync_to_device(const param_t *param, fluid_t *fluid, temperature_t *temp
     int rc = SNS_OK;
     if ((rc = upload_field(c, te->f.t[0], h.temp, nx + 2, 1, 0)) || (rc = upload_src(c, te->f.at, h.srctempa, 0)))
       return rc;
+    SNS_CUDA(cudaStreamSynchronize(c->stream));
   }
+  return SNS_OK;
+}
+
+int sns_diagnostics(const param_t *param, const fluid_t *fluid, const temperature_t *temperature, double out[11]) {
+  FluidExt *fe = as_fluid(fluid);
+  TempExt *te = as_temp(temperature);
+  if (!param || !fe || !te || !out) return fail(SNS_ERR_ARG, "sns_diagnostics: bad argument");
+  Context *c = fe->ctx;
+  const int nx = c->nx, ny = c->ny;
+  const size_t words = diag_partials_words(nx, ny);
+  if (!c->diag)
+    if (int rc = dev_alloc(c, &c->diag, words)) return rc;
+  const double Ra = param->Ra, Pr = param->Pr;
+  const DiagArgs<double> a{nx, ny, param->dy, param->ly, sqrt(Pr) * sqrt(Ra), sqrt(Pr) / sqrt(Ra),
+                           1. / sqrt(Pr) / sqrt(Ra), c->g.dxf, c->g.dxc, fe->f.ux, fe->f.uy, te->f.t[te->cur]};
+  int nb = 0;
+  SNS_CUDA(launch_diag(a, c->diag, &nb, c->stream));
+  count_launches(1);
+  std::vector<double> h(words);
+  SNS_CUDA(cudaMemcpyAsync(h.data(), c->diag, sizeof(double) * words, cudaMemcpyDeviceToHost, c->stream));
+  SNS_CUDA(cudaStreamSynchronize(c->stream));
+  diag_finish(h.data(), nb, param->ly, out);
   return SNS_OK;
 }
 

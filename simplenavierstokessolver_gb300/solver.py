@@ -208,6 +208,13 @@ class Case:
             self.p.time += self.p.dt
         self.synchronize()
 
+    def diagnostics(self) -> np.ndarray:
+        """the reference's 11 log quantities from the device state (sns_diagnostics)"""
+        out = np.zeros(11)
+        N.check(self.lib.sns_diagnostics(self.param, self.fluid, self.temperature,
+                                         out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))), "sns_diagnostics")
+        return out
+
     # ------------------------------------------------------- fused fast path
     def integrate(self):
         N.check(self.lib.sns_integrate(self.param, self.parallel, self.fluid, self.temperature), "sns_integrate")

@@ -167,6 +167,21 @@ def test_divergence_free_and_reference_diagnostics():
         assert abs(d_gpu[1]) < 1e-10
 
 
+def test_device_diagnostics_match_the_reference_logs():
+    """sns_diagnostics (device, compensated sums) against the oracle's
+    sequential sums of src/logging.c: equal to the latter's round-off"""
+    for cfg in (Config(64, 128, Ra=1e7, Pr=1.0), Config(48, 64, ly=1.0, Ra=1e6, Pr=0.7, stretch=3)):
+        o = OracleCase(cfg)
+        with gpu_case(cfg, [1, 2, 2, 3]) as c:
+            c.run(30)
+            o.run(30)
+            dg, dr = c.diagnostics(), o.diagnostics()
+        assert dg[0] == dr[0]  # the maximum is exact
+        scale = np.maximum(np.abs(dr), 1e-12)
+        assert np.all(np.abs(dg[2:] - dr[2:]) <= 1e-12 * scale), (dg, dr)
+        assert abs(dg[1] - dr[1]) < 1e-12
+
+
 def test_restart_through_host_arrays_continues_bitwise():
     """sync_to_host -> sync_to_device round trip (the restart path) changes nothing."""
     cfg = Config(32, 64, Ra=1e8, Pr=1.0)
