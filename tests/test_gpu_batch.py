@@ -189,3 +189,44 @@ def test_unsupported_sizes_are_rejected():
         for d in (Desc(48, 64), Desc(64, 96), Desc(64, 4)):
             with pytest.raises(N.SnsError):
                 b.add(d)
+
+
+def test_serving_results_equal_standalone_runs():
+    """Continuous batching: requests arriving while others run are admitted
+    when arena memory frees up; every request's final state equals the same
+    case run alone."""
+    from simplenavierstokessolver_gb300.batch import Batch, Desc, case_bytes, serve
+
+    descs = [Desc(64, 128, Ra=1e6 * (k + 1), Pr=1.0 + 0.3 * k, seed=100 + k, steps=20 + 7 * k) for k in range(5)]
+    descs.append(Desc(128, 256, Ra=1e8, Pr=0.8, seed=200, steps=25))
+    arrivals = [0.0, 0.0, 0.05, 0.1, 0.1, 0.15]
+    arena = case_bytes(descs[-1]) + case_bytes(descs[0])  # at most ~2 cases resident
+    r = serve(descs, arrivals, hbm_bytes=arena, max_cases=8, chunk_steps=5, keep_states=True)
+    assert len(r["states"]) == len(descs)
+    assert all(r["done"][k] >= r["admit"][k] >= arrivals[k] for k in range(len(descs)))
+    for k, d in enumerate(descs):
+        with Batch(case_bytes(d) + (1 << 20)) as b:
+            s = b.add(d)
+            b.step(d.steps + 3)  # finished cases stop at their step count
+            alone = b.state(s)
+        for f in alone:
+            assert np.array_equal(alone[f], r["states"][k][f]), (k, f)
+
+
+def test_batch_diagnostics_match_host_evaluation():
+    """sns_batch_diagnostics against the oracle's log quantities evaluated on
+    the batch's own (FP32) state"""
+    from simplenavierstokessolver_gb300.batch import Batch, Desc
+
+    d = Desc(64, 128, Ra=1e7, Pr=1.0, seed=9)
+    with Batch(256 << 20) as b:
+        s = b.add(d)
+        b.step(25)
+        dg = b.diagnostics(s)
+        st = b.state(s)
+    o = OracleCase(Config(64, 128, Ra=1e7, Pr=1.0))
+    o.set_state(st["ux"], st["uy"], st["p"], st["temp"])
+    dr = o.diagnostics()
+    scale = np.maximum(np.abs(dr), 1e-12)
+    assert np.all(np.abs(dg[1:] - dr[1:]) <= 1e-10 * scale + 1e-13), (dg, dr)
+    assert abs(dg[0] - dr[0]) <= 1e-12 * dr[0]
