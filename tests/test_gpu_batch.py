@@ -227,6 +227,6 @@ def test_batch_diagnostics_match_host_evaluation():
     o = OracleCase(Config(64, 128, Ra=1e7, Pr=1.0))
     o.set_state(st["ux"], st["uy"], st["p"], st["temp"])
     dr = o.diagnostics()
-    scale = np.maximum(np.abs(dr), 1e-12)
+    scale = np.maximum(np.abs(dr[1:]), 1e-12)
     assert np.all(np.abs(dg[1:] - dr[1:]) <= 1e-10 * scale + 1e-13), (dg, dr)
     assert abs(dg[0] - dr[0]) <= 1e-12 * dr[0]

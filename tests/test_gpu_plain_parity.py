@@ -177,7 +177,7 @@ def test_device_diagnostics_match_the_reference_logs():
             o.run(30)
             dg, dr = c.diagnostics(), o.diagnostics()
         assert dg[0] == dr[0]  # the maximum is exact
-        scale = np.maximum(np.abs(dr), 1e-12)
+        scale = np.maximum(np.abs(dr[2:]), 1e-12)
         assert np.all(np.abs(dg[2:] - dr[2:]) <= 1e-12 * scale), (dg, dr)
         assert abs(dg[1] - dr[1]) < 1e-12
 
