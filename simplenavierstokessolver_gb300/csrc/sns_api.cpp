@@ -66,6 +66,8 @@ struct Context {
   int refs = 0;
   int nx = 0, ny = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;  // temperature update overlapped with the Poisson solve
+  cudaEvent_t ev_fwd = nullptr, ev_temp = nullptr;
   DevGrid g{};
   std::vector<void *> allocs;
   std::vector<double> dxf, dxc;  // host copies of the reference arrays (0-based)
@@ -101,8 +103,9 @@ static void prof_collect(Context *c) {
 // when profiling is on; no work at all otherwise
 struct Prof {
   Context *c;
+  cudaStream_t st;
   long idx = -1;
-  Prof(Context *c_, int kind) : c(c_) {
+  Prof(Context *c_, int kind, cudaStream_t s_ = nullptr) : c(c_), st(s_ ? s_ : c_->stream) {
     if (!c->prof) return;
     if (c->prof_used >= 2048) prof_collect(c);
     if (2 * (c->prof_used + 1) > c->prof_ev.size()) {
@@ -118,10 +121,10 @@ struct Prof {
     }
     idx = (long)c->prof_used++;
     c->prof_kind[idx] = kind;
-    cudaEventRecord(c->prof_ev[2 * idx], c->stream);
+    cudaEventRecord(c->prof_ev[2 * idx], st);
   }
   ~Prof() {
-    if (idx >= 0) cudaEventRecord(c->prof_ev[2 * idx + 1], c->stream);
+    if (idx >= 0) cudaEventRecord(c->prof_ev[2 * idx + 1], st);
   }
 };
 
@@ -180,6 +183,9 @@ static void destroy_context(Context *c) {
   c->allocs.clear();
   if (c->staging) cudaFreeHost(c->staging);
   if (c->red_host) cudaFreeHost(c->red_host);
+  if (c->ev_fwd) cudaEventDestroy(c->ev_fwd);
+  if (c->ev_temp) cudaEventDestroy(c->ev_temp);
+  if (c->side) cudaStreamDestroy(c->side);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -190,6 +196,9 @@ static int build_context(Context *c, const param_t *param) {
   c->nx = nx;
   c->ny = ny;
   SNS_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  SNS_CUDA(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+  SNS_CUDA(cudaEventCreateWithFlags(&c->ev_fwd, cudaEventDisableTiming));
+  SNS_CUDA(cudaEventCreateWithFlags(&c->ev_temp, cudaEventDisableTiming));
   c->dxf.assign(param->dxf, param->dxf + nx);
   c->dxc.assign(param->dxc, param->dxc + nx + 1);
   DevGrid &g = c->g;
@@ -639,11 +648,13 @@ static int do_velocity_update(const param_t *param, int rk, FluidExt *fe, const 
   return SNS_OK;
 }
 
-static int poisson(Context *c, const StageScalars &s, Fields &f) {
-  {
-    Prof pf(c, K_POI_FWD);
-    SNS_CUDA(launch_poisson_fwd(c->g, s, f.ux, f.uy, f.spec, c->stream));
-  }
+static int poisson_forward(Context *c, const StageScalars &s, Fields &f) {
+  Prof pf(c, K_POI_FWD);
+  SNS_CUDA(launch_poisson_fwd(c->g, s, f.ux, f.uy, f.spec, c->stream));
+  return SNS_OK;
+}
+
+static int poisson_rest(Context *c, const StageScalars &s, Fields &f) {
   {
     Prof pf(c, K_POI_TRI);
     SNS_CUDA(launch_poisson_tri(c->g, f.spec, c->stream));
@@ -653,6 +664,11 @@ static int poisson(Context *c, const StageScalars &s, Fields &f) {
     SNS_CUDA(launch_poisson_bwd(c->g, s, f.spec, f.psi, c->stream));
   }
   return SNS_OK;
+}
+
+static int poisson(Context *c, const StageScalars &s, Fields &f) {
+  if (int rc = poisson_forward(c, s, f)) return rc;
+  return poisson_rest(c, s, f);
 }
 
 // dt from the reduction results (src/param/decide_dt.c:11-101)
@@ -1191,22 +1207,51 @@ void *sns_stream(const fluid_t *fluid) {
   return fe ? (void *)fe->ctx->stream : nullptr;
 }
 
+// One time step's substages (src/main.c:80-99) with fused kernels. With the
+// explicit scheme the temperature update of a substage, which reads only the
+// substage's starting T and u, runs on a side stream while the Poisson
+// tridiagonal sweep (a serial recurrence that occupies few SMs) runs on the
+// main stream; the velocity kernel has already taken its buoyancy from the
+// starting T, and the next substage waits for the new T. Same kernels, same
+// inputs, same bits as the sequential order.
 static int integrate_impl(const param_t *param, FluidExt *fe, TempExt *te, bool reduce_last) {
   Context *c = fe->ctx;
   Fields &f = fe->f;
   for (int rk = 0; rk < RKSTEPMAX; rk++) {
-    if (param->with_temperature && te) {
+    const bool with_t = param->with_temperature && te;
+    const bool overlap = with_t && !param->implicitx && !param->implicity;
+    const double *ux_k = f.ux, *uy_k = f.uy;  // the velocity this substage starts from
+    if (with_t) {
       te->snap = param->with_thermal_forcing ? te->cur : -1;
-      if (int rc = do_temp_update(param, rk, fe, te)) return rc;
+      if (!overlap)
+        if (int rc = do_temp_update(param, rk, fe, te)) return rc;
     }
     if (int rc = do_velocity_update(param, rk, fe, te)) return rc;
     const StageScalars s = stage_scalars(param, rk);
-    if (int rc = poisson(c, s, f)) return rc;
+    if (int rc = poisson_forward(c, s, f)) return rc;
+    if (overlap) {
+      int out = 0;
+      while (out == te->cur || out == te->snap) out++;
+      SNS_CUDA(cudaEventRecord(c->ev_fwd, c->stream));
+      SNS_CUDA(cudaStreamWaitEvent(c->side, c->ev_fwd, 0));
+      {
+        Prof pf(c, K_TEMP, c->side);
+        SNS_CUDA(launch_temp_update(c->g, s, 0, 0, te->f.t[te->cur], te->f.t[out], te->f.at, nullptr, ux_k, uy_k,
+                                    c->side));
+      }
+      SNS_CUDA(cudaEventRecord(c->ev_temp, c->side));
+      te->cur = out;
+    }
+    if (int rc = poisson_rest(c, s, f)) return rc;
     const bool red = reduce_last && rk == RKSTEPMAX - 1;
     if (red) SNS_CUDA(cudaMemsetAsync(f.colmax, 0, sizeof(unsigned long long) * (c->nx + 1), c->stream));
-    Prof pf(c, K_CORR_PRES);
-    SNS_CUDA(launch_correct_pressure(c->g, s, param->implicitx, param->implicity, f.psi, f.ux, f.uy, f.p,
-                                     red ? f.colmax : nullptr, red ? f.uymax : nullptr, c->stream));
+    {
+      Prof pf(c, K_CORR_PRES);
+      SNS_CUDA(launch_correct_pressure(c->g, s, param->implicitx, param->implicity, f.psi, f.ux, f.uy, f.p,
+                                       red ? f.colmax : nullptr, red ? f.uymax : nullptr, c->stream));
+    }
+    // the next substage reads the new T and overwrites the buffer of u_k
+    if (overlap) SNS_CUDA(cudaStreamWaitEvent(c->stream, c->ev_temp, 0));
   }
   return SNS_OK;
 }

@@ -177,8 +177,12 @@ def test_device_diagnostics_match_the_reference_logs():
             o.run(30)
             dg, dr = c.diagnostics(), o.diagnostics()
         assert dg[0] == dr[0]  # the maximum is exact
+        # the momenta (2, 3) are sums of signed terms that cancel to ~1e-20:
+        # their error is bounded by round-off of the summed magnitudes instead
+        atol = np.zeros(9)
+        atol[:2] = 1e-16
         scale = np.maximum(np.abs(dr[2:]), 1e-12)
-        assert np.all(np.abs(dg[2:] - dr[2:]) <= 1e-12 * scale), (dg, dr)
+        assert np.all(np.abs(dg[2:] - dr[2:]) <= 1e-12 * scale + atol), (dg, dr)
         assert abs(dg[1] - dr[1]) < 1e-12
 
 
