@@ -212,6 +212,23 @@ extern int sns_run(param_t *param, const parallel_t *parallel, fluid_t *fluid, t
 extern int sns_diagnostics(const param_t *param, const fluid_t *fluid, const temperature_t *temperature,
                            double out[11]);
 
+/* sns_diagnostics without any allocation; no counterpart in the reference.
+ * For callers that cannot allocate: a monitoring thread sampling a run in
+ * flight (cudaMalloc / cudaFree may synchronise the device and stall the
+ * solver) and a process whose HBM is committed to a batch arena. The block
+ * partials live in a fixed file-scope device array (4096 blocks, 672 KiB) and
+ * are summed on the device with the same compensated sums in the same order,
+ * so out[] equals sns_diagnostics's bit for bit. A grid needing more than
+ * 4096 partials, ceil((itot+1)/64) * ceil(jtot/16) > 4096 (1024 x 2048
+ * fits, 1024 x 4096 does not), returns SNS_ERR_UNSUPPORTED with a message. The first call on
+ * a device looks the scratch up (cudaGetSymbolAddress, with the case's device
+ * current); make it before any stream capture. Nothing in the scratch needs
+ * to start at zero. There is one scratch per device: calls that overlap on
+ * one device (several threads, several cases) race on it; serialise them.
+ * Blocks until done. */
+extern int sns_diagnostics_static(const param_t *param, const fluid_t *fluid, const temperature_t *temperature,
+                                  double out[11]);
+
 /* per-kernel device time: with profiling enabled every kernel launched for
  * this solver is bracketed by CUDA events on its stream. sns_profile(f, 1)
  * resets the totals and starts, sns_profile(f, 0) stops. sns_profile_read

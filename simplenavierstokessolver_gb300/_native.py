@@ -110,6 +110,7 @@ PROTOTYPES = {
     "sns_kernel_launches": (c_longlong, []),
     "sns_abi_layout": (c_int, [POINTER(c_size_t), c_int]),
     "sns_diagnostics": (c_int, [PP, PF, PT, _PD]),
+    "sns_diagnostics_static": (c_int, [PP, PF, PT, _PD]),
     "sns_profile": (c_int, [PF, c_int]),
     "sns_profile_read": (c_int, [PF, POINTER(c_double), POINTER(c_longlong), c_int]),
     "sns_profile_kind_name": (c_char_p, [c_int]),

@@ -30,4 +30,11 @@ size_t diag_partials_words(int nx, int ny);
 // Nu from wall flux, injection, kinetic dissipation, thermal dissipation
 void diag_finish(const double *partials, int nblocks, double ly, double out[11]);
 
+// allocation-free form: block partials in a fixed file-scope device array of
+// kDiagStaticBlocks blocks (672 KiB), the final sum on the device; grids with
+// more blocks (diag_blocks) are rejected. Blocks until done.
+constexpr int kDiagStaticBlocks = 4096;
+int diag_blocks(int nx, int ny);
+cudaError_t diag_static(const DiagArgs<double> &a, cudaStream_t st, double out[11]);
+
 }  // namespace sns

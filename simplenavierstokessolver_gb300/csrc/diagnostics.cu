@@ -10,6 +10,7 @@
 // round-off. Fields may be FP64 (plain path) or FP32 (batched form); FP32
 // values are widened exactly.
 #include <cstdint>
+#include <mutex>
 
 #include "diag_internal.h"
 
@@ -183,6 +184,106 @@ void diag_finish(const double *partials, int nblocks, double ly, double out[11])
   out[8] = r[5] / (lx * ly) + 1.;
   out[9] = r[6] / (lx * ly) + 1.;
   out[10] = r[8] / (lx * ly);
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant (sns_diagnostics_static in sns_api.cpp).
+//
+// Some callers cannot allocate: a monitoring thread that samples a run while
+// its kernels are in flight (cudaMalloc and cudaFree may synchronise the
+// device and stall the solver's stream, and the first call of the allocating
+// entry point makes a cudaMalloc), and a process whose device memory is
+// committed to a batch arena sized to the whole HBM (an allocation there
+// fails with out-of-memory). For them the block partials live in one
+// file-scope device array of fixed size, the final compensated sum runs on
+// the device, and the 11 results are copied straight into the caller's array:
+// no device or host memory is allocated.
+//
+// Scratch layout: kDiagStaticBlocks block partials of 2*kDiagSums+1 words,
+// then the 11 results. Nothing in it needs to start at zero: k_diag writes
+// every partial word of every block it launches and k_diag_finish reads only
+// those, then writes all 11 results. There is one scratch per device, so two
+// calls that overlap on one device (other host threads, other cases) race on
+// it and may return each other's or mixed results: serialise them.
+namespace {
+
+constexpr size_t kDiagStaticWords = (size_t)kDiagStaticBlocks * (2 * kDiagSums + 1);
+static __device__ __align__(256) double g_diag_scratch[kDiagStaticWords + 16];
+
+constexpr int kMaxDevices = 64;
+static double *g_scratch_ptr[kMaxDevices];
+static std::mutex g_scratch_mu;
+
+// the same compensated sums in the same order as diag_finish, one thread per
+// sum, so the results equal those of sns_diagnostics bit for bit
+__global__ void __launch_bounds__(32) k_diag_finish(const double *partials, int nblocks, double ly, double *out) {
+  __shared__ double r[kDiagSums + 1];
+  const int k = threadIdx.x;
+  if (k < kDiagSums) {
+    Neu m{0.0, 0.0};
+    for (int b = 0; b < nblocks; ++b) {
+      const double *p = partials + (size_t)b * (2 * kDiagSums + 1);
+      m.add(p[2 * k]);
+      m.add(p[2 * k + 1]);
+    }
+    r[k] = m.s + m.c;
+  } else if (k == kDiagSums) {
+    double divmax = 0.0;
+    for (int b = 0; b < nblocks; ++b) divmax = fmax(divmax, partials[(size_t)b * (2 * kDiagSums + 1) + 2 * kDiagSums]);
+    r[kDiagSums] = divmax;
+  }
+  __syncthreads();
+  if (k == 0) {
+    const double lx = 1.0;
+    out[0] = r[kDiagSums];
+    out[1] = r[7];
+    out[2] = r[0];
+    out[3] = r[1];
+    out[4] = r[2];
+    out[5] = r[3];
+    out[6] = r[4];
+    out[7] = r[9] / ly;
+    out[8] = r[5] / (lx * ly) + 1.;
+    out[9] = r[6] / (lx * ly) + 1.;
+    out[10] = r[8] / (lx * ly);
+  }
+}
+
+// set-up, once per device, with that device current: the scratch's address.
+// The first call on a device makes it (and may load the module); make that
+// first call before any stream capture.
+cudaError_t scratch_for_current_device(double **ptr) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_ptr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_diag_scratch);
+    if (e != cudaSuccess) return e;
+    g_scratch_ptr[dev] = static_cast<double *>(p);
+  }
+  *ptr = g_scratch_ptr[dev];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+int diag_blocks(int nx, int ny) { return ((nx + 1 + 63) / 64) * ((ny + kDiagRows - 1) / kDiagRows); }
+
+cudaError_t diag_static(const DiagArgs<double> &a, cudaStream_t st, double out[11]) {
+  if (diag_blocks(a.nx, a.ny) > kDiagStaticBlocks) return cudaErrorInvalidValue;
+  double *scratch = nullptr;
+  cudaError_t e = scratch_for_current_device(&scratch);
+  if (e != cudaSuccess) return e;
+  int nb = 0;
+  if ((e = launch_diag(a, scratch, &nb, st)) != cudaSuccess) return e;
+  double *res = scratch + kDiagStaticWords;
+  k_diag_finish<<<1, 32, 0, st>>>(scratch, nb, a.ly, res);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(out, res, 11 * sizeof(double), cudaMemcpyDeviceToHost, st)) != cudaSuccess) return e;
+  return cudaStreamSynchronize(st);
 }
 
 }  // namespace sns

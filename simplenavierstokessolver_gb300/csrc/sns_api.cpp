@@ -1159,6 +1159,32 @@ int sns_diagnostics(const param_t *param, const fluid_t *fluid, const temperatur
   return SNS_OK;
 }
 
+// sns_diagnostics without allocation, for callers that cannot allocate (a
+// monitoring thread sampling a run in flight, where cudaMalloc may
+// synchronise the device; a process whose HBM is committed to a batch arena).
+// The scratch is one file-scope device array in diagnostics.cu; calls that
+// overlap on one device race on it.
+int sns_diagnostics_static(const param_t *param, const fluid_t *fluid, const temperature_t *temperature,
+                           double out[11]) {
+  FluidExt *fe = as_fluid(fluid);
+  TempExt *te = as_temp(temperature);
+  if (!param || !fe || !te || !out) return fail(SNS_ERR_ARG, "sns_diagnostics_static: bad argument");
+  Context *c = fe->ctx;
+  const int nx = c->nx, ny = c->ny;
+  const int nb = diag_blocks(nx, ny);
+  if (nb > kDiagStaticBlocks)
+    return fail(SNS_ERR_UNSUPPORTED,
+                "sns_diagnostics_static: a %d x %d grid needs %d block partials, more than the %d of its static "
+                "scratch (at most (ceil((itot+1)/64) * ceil(jtot/16)) <= %d); use sns_diagnostics",
+                nx, ny, nb, kDiagStaticBlocks, kDiagStaticBlocks);
+  const double Ra = param->Ra, Pr = param->Pr;
+  const DiagArgs<double> a{nx, ny, param->dy, param->ly, sqrt(Pr) * sqrt(Ra), sqrt(Pr) / sqrt(Ra),
+                           1. / sqrt(Pr) / sqrt(Ra), c->g.dxf, c->g.dxc, fe->f.ux, fe->f.uy, te->f.t[te->cur]};
+  SNS_CUDA(diag_static(a, c->stream, out));
+  count_launches(2);
+  return SNS_OK;
+}
+
 static const char *kKindNames[K_NUM_KINDS] = {
     "temperature_update", "velocity_update", "poisson_forward_fft", "poisson_tridiagonal", "poisson_inverse_fft",
     "correct_and_pressure", "correct_velocity", "update_pressure", "max_velocity", "cn_solve_x", "cn_solve_y",
