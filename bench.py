@@ -56,6 +56,18 @@ KERNEL_MODEL = {
 }
 
 
+# DRAM bytes (read + write) per launch from one ncu capture of the default
+# workload (profiles/plain_fp64_512x1024_launches.md); keyed by kernel and size
+PROFILED_TRAFFIC = {
+    ("poisson_tridiagonal", 512, 1024): 8665344,
+    ("velocity_update", 512, 1024): 16838912,
+    ("poisson_forward_fft", 512, 1024): 8429056,
+    ("temperature_update", 512, 1024): 12647168,
+    ("poisson_inverse_fft", 512, 1024): 4314880,
+    ("correct_and_pressure", 512, 1024): 16792576,
+}
+
+
 def fft_ops_per_cell(ny: int, forward: bool) -> float:
     """FP64 instructions per real sample of one length-ny real FFT as the
     kernels perform it (radix-2 first stage if log2(ny/2) is odd, radix-4
@@ -426,7 +438,8 @@ def gpu_arm(args, world, rank, local):
     avg_s = kernels[dom]["avg_us"] * 1e-6
     achieved = bpc * cells / avg_s / 1e9 if bpc else None
     roofline = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak if achieved else None, "traffic": None,
+                "frac": achieved / peak if achieved else None,
+                "traffic": PROFILED_TRAFFIC.get((dom, args.nx, args.ny)),
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback",
                 "algorithmic_bytes_per_launch": bpc * cells if bpc else None,
                 "note": "FP64-pipe bound on GB300: see fp64_roofline"}

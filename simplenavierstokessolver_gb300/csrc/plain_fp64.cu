@@ -241,44 +241,114 @@ __global__ void __launch_bounds__(128) k_vel(const VelArgs a) {
   }
 }
 
+// ------------------------------------------------------- line recurrences
+// The recurrences below read each element once, in order, from memory that
+// only the same thread writes: the next chunk of kLineChunk elements (and
+// their factors, uniform across the warp) is loaded into registers while the
+// current chunk is eliminated, so the loads stay off the dependent chain.
+constexpr int kLineChunk = 8;
+
+__device__ __forceinline__ bool is_zero_bits(double v) { return (__double_as_longlong(v) << 1) == 0; }
+
+// forward elimination (src/linalg.c:14-23) over e = e0..e1-1 with element
+// stride s; prev is the eliminated value at e0-1. Returns the value at e1-1.
+__device__ __forceinline__ double line_forward(double *q, size_t s, const double *inv, const double *l, int e0, int e1,
+                                               double prev) {
+  double cq[kLineChunk], ci[kLineChunk], cl[kLineChunk];
+#pragma unroll
+  for (int k = 0; k < kLineChunk; ++k) {
+    const int e = e0 + k;
+    cq[k] = e < e1 ? q[(size_t)e * s] : 0.0;
+    ci[k] = e < e1 ? __ldg(inv + e) : 0.0;
+    cl[k] = e < e1 ? __ldg(l + e) : 0.0;
+  }
+#pragma unroll 1
+  for (int b = e0; b < e1; b += kLineChunk) {
+    double nq[kLineChunk], ni[kLineChunk], nl[kLineChunk];
+#pragma unroll
+    for (int k = 0; k < kLineChunk; ++k) {
+      const int e = b + kLineChunk + k;
+      nq[k] = e < e1 ? q[(size_t)e * s] : 0.0;
+      ni[k] = e < e1 ? __ldg(inv + e) : 0.0;
+      nl[k] = e < e1 ? __ldg(l + e) : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < kLineChunk; ++k) {
+      const int e = b + k;
+      if (e < e1) {
+        const double v = is_zero_bits(ci[k]) ? 0.0 : ci[k] * (cq[k] - cl[k] * prev);
+        q[(size_t)e * s] = v;
+        prev = v;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kLineChunk; ++k) {
+      cq[k] = nq[k];
+      ci[k] = ni[k];
+      cl[k] = nl[k];
+    }
+  }
+  return prev;
+}
+
+// back substitution (src/linalg.c:25-27) over e = hi down to lo; next is the
+// value at hi+1.
+__device__ __forceinline__ void line_backward(double *q, size_t s, const double *up, int hi, int lo, double next) {
+  double cq[kLineChunk], cu[kLineChunk];
+#pragma unroll
+  for (int k = 0; k < kLineChunk; ++k) {
+    const int e = hi - k;
+    cq[k] = e >= lo ? q[(size_t)e * s] : 0.0;
+    cu[k] = e >= lo ? __ldg(up + e) : 0.0;
+  }
+#pragma unroll 1
+  for (int b = hi; b >= lo; b -= kLineChunk) {
+    double nq[kLineChunk], nu[kLineChunk];
+#pragma unroll
+    for (int k = 0; k < kLineChunk; ++k) {
+      const int e = b - kLineChunk - k;
+      nq[k] = e >= lo ? q[(size_t)e * s] : 0.0;
+      nu[k] = e >= lo ? __ldg(up + e) : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < kLineChunk; ++k) {
+      const int e = b - k;
+      if (e >= lo) {
+        const double v = cq[k] - cu[k] * next;
+        q[(size_t)e * s] = v;
+        next = v;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kLineChunk; ++k) {
+      cq[k] = nq[k];
+      cu[k] = nu[k];
+    }
+  }
+}
+
 // ------------------------------------------------------- Crank-Nicolson solves
 // src/linalg.c:9-30 applied per row along x; factors are shared by all rows.
 // mode 0: rows x = 0..nx-1, first row divides by d0 (T: update.c:150-157, uy:
 //         update_velocity.c:509-516)
 // mode 1: ux rows x = 1..nx-1 of the (itot+1)-system whose rows 0 and itot are
 //         identity rows with zero right-hand side (update_velocity.c:249-253)
-__global__ void k_solve_x(int nx, int ny, LineFactors f, int mode, double *q) {
+__global__ void __launch_bounds__(32) k_solve_x(int nx, int ny, LineFactors f, int mode, double *q) {
   const int y = blockIdx.x * blockDim.x + threadIdx.x;
   if (y >= ny) return;
   double *row = q + (size_t)y * nx;
-  double prev;
-  int x0;
+  double prev = 0.0;
   if (mode == 0) {
     prev = row[0] / f.d0;
     row[0] = prev;
-    x0 = 1;
-  } else {
-    prev = 0.0;
-    x0 = 1;
   }
-  for (int x = x0; x < nx; ++x) {
-    const double inv = f.inv[x];
-    const double v = inv == 0.0 ? 0.0 : inv * (row[x] - f.l[x] * prev);
-    row[x] = v;
-    prev = v;
-  }
+  prev = line_forward(row, 1, f.inv, f.l, 1, nx, prev);
   // mode 1: the identity row itot+1 is zero, so row itot-1 is final already
-  const int xlo = mode == 0 ? 0 : 1;
-  double next = prev;
-  for (int x = nx - 2; x >= xlo; --x) {
-    const double v = row[x] - f.up[x] * next;
-    row[x] = v;
-    next = v;
-  }
+  line_backward(row, 1, f.up, nx - 2, mode == 0 ? 0 : 1, prev);
 }
 
 // src/linalg.c:52-108 applied per column along y (periodic), coalesced across x.
-__global__ void k_solve_y(int nx, int ny, PeriodicFactors f, int first_col, double *q) {
+__global__ void __launch_bounds__(32) k_solve_y(int nx, int ny, PeriodicFactors f, int first_col, double *q) {
   const int x = first_col + blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= nx) return;
   const int n = ny;
@@ -287,22 +357,26 @@ __global__ void k_solve_y(int nx, int ny, PeriodicFactors f, int first_col, doub
   const LineFactors &sub = f.sub;
   double prev = col[0] / sub.d0;
   col[0] = prev;
-  for (int y = 1; y < n - 1; ++y) {
-    const double inv = sub.inv[y];
-    const double v = inv == 0.0 ? 0.0 : inv * (col[y * s] - sub.l[y] * prev);
-    col[y * s] = v;
-    prev = v;
-  }
-  double next = prev;
-  for (int y = n - 3; y >= 0; --y) {
-    const double v = col[y * s] - sub.up[y] * next;
-    col[y * s] = v;
-    next = v;
-  }
+  prev = line_forward(col, s, sub.inv, sub.l, 1, n - 1, prev);
+  line_backward(col, s, sub.up, n - 3, 0, prev);
   const double q00 = col[0], q0l = col[(size_t)(n - 2) * s];
   const double last = (col[(size_t)(n - 1) * s] - f.u_last * q00 - f.l_last * q0l) / f.den;
   col[(size_t)(n - 1) * s] = last;
-  for (int y = 0; y <= n - 2; ++y) col[y * s] = col[y * s] + last * f.q1[y];
+#pragma unroll 1
+  for (int b = 0; b <= n - 2; b += kLineChunk) {
+    double cq[kLineChunk], c1[kLineChunk];
+#pragma unroll
+    for (int k = 0; k < kLineChunk; ++k) {
+      const int y = b + k;
+      cq[k] = y <= n - 2 ? col[(size_t)y * s] : 0.0;
+      c1[k] = y <= n - 2 ? __ldg(f.q1 + y) : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < kLineChunk; ++k) {
+      const int y = b + k;
+      if (y <= n - 2) col[(size_t)y * s] = cq[k] + last * c1[k];
+    }
+  }
 }
 
 __global__ void k_add_increment(int nx, int ny, int kind, const double *in, const double *q, double *out) {
@@ -671,14 +745,14 @@ cudaError_t launch_velocity_update(const DevGrid &g, const StageScalars &s, int 
 }
 
 cudaError_t launch_solve_x(const DevGrid &g, const LineFactors &f, int mode, double *q, cudaStream_t st) {
-  k_solve_x<<<(g.ny + 127) / 128, 128, 0, st>>>(g.nx, g.ny, f, mode, q);
+  k_solve_x<<<(g.ny + 31) / 32, 32, 0, st>>>(g.nx, g.ny, f, mode, q);
   count_launches(1);
   return cudaGetLastError();
 }
 
 cudaError_t launch_solve_y(const DevGrid &g, const PeriodicFactors &f, int first_col, double *q, cudaStream_t st) {
   const int cols = g.nx - first_col;
-  k_solve_y<<<(cols + 127) / 128, 128, 0, st>>>(g.nx, g.ny, f, first_col, q);
+  k_solve_y<<<(cols + 31) / 32, 32, 0, st>>>(g.nx, g.ny, f, first_col, q);
   count_launches(1);
   return cudaGetLastError();
 }
@@ -688,6 +762,39 @@ cudaError_t launch_add_increment(const DevGrid &g, int kind, const double *in, c
   const size_t n = (size_t)g.nx * g.ny;
   const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 16);
   k_add_increment<<<blocks, 256, 0, st>>>(g.nx, g.ny, kind, in, q, out);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+// --------------------------------------------------------- host transfers
+__global__ void __launch_bounds__(256) k_xfer(const XferList L) {
+  const XferField f = L.f[blockIdx.y];
+  const size_t total = (size_t)L.rows * f.width;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
+    const int y = (int)(k / f.width), x = (int)(k - (size_t)y * f.width);
+    f.dst[(size_t)y * f.dstride + x] = f.src[(size_t)y * f.sstride + x];
+  }
+}
+
+cudaError_t launch_xfer(const XferList &L, cudaStream_t st) {
+  if (L.n <= 0) return cudaSuccess;
+  k_xfer<<<dim3(2 * 152 / L.n + 1, L.n), 256, 0, st>>>(L);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+// TEMPFORCEX(i, j) = 0.5*TEMP(i-1, j) + 0.5*TEMP(i, j), i = 2..itot
+__global__ void __launch_bounds__(256) k_tempforce(int nx, int ny, const double *t, double *out) {
+  const size_t w = (size_t)nx - 1, total = w * ny;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
+    const size_t y = k / w, x = k - y * w;
+    out[k] = 0.5 * t[y * nx + x] + 0.5 * t[y * nx + x + 1];
+  }
+}
+
+cudaError_t launch_tempforce_to_host(const DevGrid &g, const double *t, double *host, cudaStream_t st) {
+  if (g.nx < 2) return cudaSuccess;
+  k_tempforce<<<2 * 152, 256, 0, st>>>(g.nx, g.ny, t, host);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -401,6 +401,33 @@ static int upload_src(Context *c, double *dev, const double *host, int is_ux) {
   return SNS_OK;
 }
 
+// The device alias of a pinned host array (nullptr when the array is not
+// pinned, e.g. a caller replaced the pointer: the copies then go through DMA).
+static double *dev_alias(const double *h) {
+  void *d = nullptr;
+  if (!h || cudaHostGetDevicePointer(&d, const_cast<double *>(h), 0) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return static_cast<double *>(d);
+}
+
+// one entry of a host -> device transfer list, as upload_field / upload_src lay it out
+static bool xfer_field(XferList &L, int nx, double *dev, const double *host, int width, int off, int first_x) {
+  const double *a = dev_alias(host);
+  if (!a || L.n >= kXferMax) return false;
+  L.f[L.n++] = XferField{a + width + off + first_x, dev + first_x, width, nx, nx - first_x};
+  return true;
+}
+
+static bool xfer_src(XferList &L, int nx, double *dev, const double *host, int is_ux) {
+  const double *a = dev_alias(host);
+  if (!a || L.n >= kXferMax) return false;
+  const int w = is_ux ? nx - 1 : nx, x0 = is_ux ? 1 : 0;
+  L.f[L.n++] = XferField{a, dev + x0, w, nx, w};
+  return true;
+}
+
 // pinned, zeroed host array (nullptr on failure)
 static double *host_array(size_t n) {
   void *p = nullptr;
@@ -1091,11 +1118,15 @@ int sns_sync_to_host(const param_t *param, fluid_t *fluid, temperature_t *temper
     int rc = SNS_OK;
     if ((rc = download(c, te->f.t[te->cur], h.temp, nx + 2, 1, 0)) || (rc = download_src(c, te->f.at, h.srctempa, 0)))
       return rc;
-    if (te->snap >= 0)
+    double *tf_alias = te->snap >= 0 ? dev_alias(h.tempforcex) : nullptr;
+    if (tf_alias) {
+      SNS_CUDA(launch_tempforce_to_host(c->g, te->f.t[te->snap], tf_alias, c->stream));
+    } else if (te->snap >= 0) {
       if (int rc2 = fetch(c, te->f.t[te->snap])) return rc2;
+    }
     SNS_CUDA(cudaStreamSynchronize(c->stream));
     host_bc_temp(nx, ny, h.temp);
-    if (te->snap >= 0) {
+    if (te->snap >= 0 && !tf_alias) {
       // tempforcex (src/temperature/force.c:17-23) from the snapshot buffer
       for (int j = 1; j <= ny; j++)
         for (int i = 2; i <= nx; i++) {
@@ -1107,33 +1138,52 @@ int sns_sync_to_host(const param_t *param, fluid_t *fluid, temperature_t *temper
   return SNS_OK;
 }
 
+// Host -> device: the pinned host arrays are read in place by one copy
+// kernel for all fields (strided 2D DMA of ~4 KB rows runs at less than half
+// the link rate); arrays that are not pinned go through 2D DMA copies.
 int sns_sync_to_device(const param_t *param, fluid_t *fluid, temperature_t *temperature) {
   if (!param) return fail(SNS_ERR_ARG, "sns_sync_to_device: NULL param");
   const int nx = param->itot;
-  if (fluid) {
-    FluidExt *fe = as_fluid(fluid);
-    if (!fe) return fail(SNS_ERR_ARG, "sns_sync_to_device: foreign fluid_t");
-    Context *c = fe->ctx;
-    fluid_t &h = fe->pub;
-    int rc = SNS_OK;
-    if ((rc = upload_field(c, fe->f.ux, h.ux, nx + 1, 0, 1)) || (rc = upload_field(c, fe->f.uy, h.uy, nx + 2, 1, 0)) ||
-        (rc = upload_field(c, fe->f.p, h.p, nx + 2, 1, 0)) || (rc = upload_field(c, fe->f.psi, h.psi, nx + 2, 1, 0)) ||
-        (rc = upload_src(c, fe->f.aux, h.srcuxa, 1)) || (rc = upload_src(c, fe->f.auy, h.srcuya, 0)))
-      return rc;
-    SNS_CUDA(cudaStreamSynchronize(c->stream));
+  FluidExt *fe = nullptr;
+  TempExt *te = nullptr;
+  if (fluid && !(fe = as_fluid(fluid))) return fail(SNS_ERR_ARG, "sns_sync_to_device: foreign fluid_t");
+  if (temperature && !(te = as_temp(temperature))) return fail(SNS_ERR_ARG, "sns_sync_to_device: foreign temperature_t");
+  if (fe && te && fe->ctx != te->ctx) return fail(SNS_ERR_ARG, "sns_sync_to_device: fluid and temperature of different cases");
+  Context *c = fe ? fe->ctx : te ? te->ctx : nullptr;
+  if (!c) return SNS_OK;
+  XferList L{};
+  L.rows = c->ny;
+  bool direct = true;
+  if (fe) {
+    const fluid_t &h = fe->pub;
+    direct = xfer_field(L, nx, fe->f.ux, h.ux, nx + 1, 0, 1) && xfer_field(L, nx, fe->f.uy, h.uy, nx + 2, 1, 0) &&
+             xfer_field(L, nx, fe->f.p, h.p, nx + 2, 1, 0) && xfer_field(L, nx, fe->f.psi, h.psi, nx + 2, 1, 0) &&
+             xfer_src(L, nx, fe->f.aux, h.srcuxa, 1) && xfer_src(L, nx, fe->f.auy, h.srcuya, 0);
   }
-  if (temperature) {
-    TempExt *te = as_temp(temperature);
-    if (!te) return fail(SNS_ERR_ARG, "sns_sync_to_device: foreign temperature_t");
-    Context *c = te->ctx;
-    temperature_t &h = te->pub;
+  if (te) {
     te->cur = 0;
     te->snap = -2;
-    int rc = SNS_OK;
-    if ((rc = upload_field(c, te->f.t[0], h.temp, nx + 2, 1, 0)) || (rc = upload_src(c, te->f.at, h.srctempa, 0)))
-      return rc;
-    SNS_CUDA(cudaStreamSynchronize(c->stream));
+    const temperature_t &h = te->pub;
+    direct = direct && xfer_field(L, nx, te->f.t[0], h.temp, nx + 2, 1, 0) && xfer_src(L, nx, te->f.at, h.srctempa, 0);
   }
+  if (direct) {
+    SNS_CUDA(launch_xfer(L, c->stream));
+  } else {
+    int rc = SNS_OK;
+    if (fe) {
+      const fluid_t &h = fe->pub;
+      if ((rc = upload_field(c, fe->f.ux, h.ux, nx + 1, 0, 1)) || (rc = upload_field(c, fe->f.uy, h.uy, nx + 2, 1, 0)) ||
+          (rc = upload_field(c, fe->f.p, h.p, nx + 2, 1, 0)) || (rc = upload_field(c, fe->f.psi, h.psi, nx + 2, 1, 0)) ||
+          (rc = upload_src(c, fe->f.aux, h.srcuxa, 1)) || (rc = upload_src(c, fe->f.auy, h.srcuya, 0)))
+        return rc;
+    }
+    if (te) {
+      const temperature_t &h = te->pub;
+      if ((rc = upload_field(c, te->f.t[0], h.temp, nx + 2, 1, 0)) || (rc = upload_src(c, te->f.at, h.srctempa, 0)))
+        return rc;
+    }
+  }
+  SNS_CUDA(cudaStreamSynchronize(c->stream));
   return SNS_OK;
 }
 

@@ -110,6 +110,23 @@ cudaError_t launch_solve_y(const DevGrid &g, const PeriodicFactors &f, int first
 // out = in + q on the interior (kind 0: T/uy all x; kind 1: ux x >= 1)
 cudaError_t launch_add_increment(const DevGrid &g, int kind, const double *in, const double *q, double *out,
                                  cudaStream_t st);
+// strided field copies in one launch (host arrays are pinned and read or
+// written in place through their device alias): row y of field k moves
+// width entries from src + y*sstride to dst + y*dstride
+struct XferField {
+  const double *src;
+  double *dst;
+  int sstride, dstride, width;
+};
+constexpr int kXferMax = 8;
+struct XferList {
+  XferField f[kXferMax];
+  int n, rows;
+};
+cudaError_t launch_xfer(const XferList &L, cudaStream_t st);
+// tempforcex (src/temperature/force.c:17-23) from dense T, written straight
+// into the (itot-1) x jtot host array through its device alias
+cudaError_t launch_tempforce_to_host(const DevGrid &g, const double *t, double *host, cudaStream_t st);
 cudaError_t launch_poisson_fwd(const DevGrid &g, const StageScalars &s, const double *ux, const double *uy,
                                double2 *spec, cudaStream_t st);
 cudaError_t launch_poisson_tri(const DevGrid &g, double2 *spec, cudaStream_t st);
