@@ -346,6 +346,56 @@ def ensemble_throughput(args, torch):
             "workload": "nx in {64,128,256}, ny=2nx, log10 Ra in [6,9], Pr in [0.7,7], SplitMix64 seeds 20261203+k"}
 
 
+def ensemble_accuracy(args):
+    """The 64-case ensemble in the batched FP32-stencil form against the FP64
+    path (bit-identical to the reference) over args.ens_acc_steps steps: each
+    case starts from its seeded initial temperature in both runs, and the
+    batch's CFL dt sequence is replayed into the FP64 run. Relative L2 per
+    field over the interior (p modulo its mean); max and median over cases."""
+    import numpy as np
+
+    from simplenavierstokessolver_gb300 import Case
+    from simplenavierstokessolver_gb300.batch import Batch, initial_temperature
+    from simplenavierstokessolver_gb300.workloads import ensemble
+
+    descs = ensemble(64)
+    n = args.ens_acc_steps
+    dts = [[] for _ in descs]
+    with Batch(8 << 30) as b:
+        slots = [b.add(d) for d in descs]
+        for _ in range(n):
+            for k, s in enumerate(slots):
+                dts[k].append(b.status(s)["dt"])
+            b.step(1)
+        got = [b.state(s) for s in slots]
+    fields = ("ux", "uy", "temp", "p")
+    errs = {f: [] for f in fields}
+    for k, d in enumerate(descs):
+        with Case(d.itot, d.jtot, ly=d.ly, Ra=d.Ra, Pr=d.Pr) as c:
+            st = c.get_state()
+            c.set_state(np.zeros_like(st["ux"]), np.zeros_like(st["uy"]), np.zeros_like(st["p"]),
+                        initial_temperature(d))
+            for dt in dts[k]:
+                c.set_dt(dt, 0, 0)
+                c.integrate()
+            ref = c.get_state()
+        for f in fields:
+            a, r = got[k][f][1:-1, 1:-1], ref[f][1:-1, 1:-1]
+            if f == "p":
+                a, r = a - a.mean(), r - r.mean()
+            nr = np.linalg.norm(r)
+            errs[f].append(float(np.linalg.norm(a - r) / nr) if nr > 0 else 0.0)
+    worst = int(np.argmax([max(errs[f][k] for f in fields) for k in range(len(descs))]))
+    wd = descs[worst]
+    return {"steps": n, "dt": "CFL dt of the FP32 run, replayed in the FP64 run",
+            "rel_l2_max": {f: max(errs[f]) for f in fields},
+            "rel_l2_median": {f: float(np.median(errs[f])) for f in fields},
+            "target": 1e-5,
+            "cases_within_target": int(sum(all(errs[f][k] <= 1e-5 for f in fields) for k in range(len(descs)))),
+            "worst_case": {"nx": wd.itot, "ny": wd.jtot, "Ra": wd.Ra, "Pr": wd.Pr,
+                           "rel_l2": {f: errs[f][worst] for f in fields}}}
+
+
 def serving(args):
     import numpy as np
 
@@ -478,6 +528,8 @@ def gpu_arm(args, world, rank, local):
         extra["fp32_stencil"]["vs_plain_fp64"] = extra["fp32_stencil"]["value"] / value
         extra["fp32_stencil"]["accuracy_vs_fp64"] = fp32_accuracy(args)
         extra["ensemble_64"] = ensemble_throughput(args, torch)
+        if args.ens_acc_steps > 0:
+            extra["ensemble_64"]["accuracy_vs_fp64"] = ensemble_accuracy(args)
         extra["serving"] = serving(args)
 
     cpu = None
@@ -522,6 +574,7 @@ def main():
     ap.add_argument("--plain-only", action="store_true", help="skip the FP32-stencil, ensemble and serving parts")
     ap.add_argument("--acc-steps", type=int, default=2000, help="steps of the FP32-vs-FP64 accuracy run")
     ap.add_argument("--ens-steps", type=int, default=50)
+    ap.add_argument("--ens-acc-steps", type=int, default=500, help="steps of the ensemble FP32-vs-FP64 accuracy run")
     ap.add_argument("--serve-rate", type=float, default=6.0)
     ap.add_argument("--serve-seconds", type=float, default=12.0)
     ap.add_argument("--serve-hbm", type=int, default=2048, help="serving arena in MiB")

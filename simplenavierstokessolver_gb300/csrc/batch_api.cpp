@@ -51,7 +51,7 @@ static size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 struct CaseLayout {
   size_t rdxf_f, rdxc_f, ccm_f, ccp_f, cfm_f, cfp_f;
   size_t rdxf, rdxc, dxi, dxf, dxc, tw, lo, hi, pfac;
-  size_t ux[2], uy[2], t[2], aux, auy, at, p, psi, spec;
+  size_t ux[2], uy[2], t[2], uxl[2], uyl[2], tl[2], aux, auy, at, p, psi, spec;
   size_t total;
   size_t pstride;
 };
@@ -86,6 +86,11 @@ static CaseLayout layout_for(int nx, int ny) {
     L.ux[k] = take(sizeof(float) * cells);
     L.uy[k] = take(sizeof(float) * cells);
     L.t[k] = take(sizeof(float) * cells);
+  }
+  for (int k = 0; k < 2; k++) {
+    L.uxl[k] = take(sizeof(float) * cells);
+    L.uyl[k] = take(sizeof(float) * cells);
+    L.tl[k] = take(sizeof(float) * cells);
   }
   L.aux = take(sizeof(float) * cells);
   L.auy = take(sizeof(float) * cells);
@@ -492,9 +497,14 @@ int sns_batch_add(sns_batch *b, const sns_case_desc *d, const double *temp_init,
   } else {
     initial_temperature(d, xc.data(), temp.data());
   }
-  std::vector<float> t_dense((size_t)nx * ny);
+  std::vector<float> t_dense((size_t)nx * ny), t_low((size_t)nx * ny);
   for (int j = 1; j <= ny; j++)
-    for (int i = 1; i <= nx; i++) t_dense[(size_t)(j - 1) * nx + (i - 1)] = (float)temp[(size_t)j * (nx + 2) + i];
+    for (int i = 1; i <= nx; i++) {
+      const double v = temp[(size_t)j * (nx + 2) + i];
+      const float hi = (float)v;
+      t_dense[(size_t)(j - 1) * nx + (i - 1)] = hi;
+      t_low[(size_t)(j - 1) * nx + (i - 1)] = (float)(v - (double)hi);
+    }
   auto put = [&](size_t o, const void *src, size_t bytes) {
     return cudaMemcpyAsync(base + o, src, bytes, cudaMemcpyHostToDevice, b->stream);
   };
@@ -523,6 +533,12 @@ int sns_batch_add(sns_batch *b, const sns_case_desc *d, const double *temp_init,
     chk(cudaMemsetAsync(base + L.uy[k], 0, sizeof(float) * cells, b->stream));
   }
   chk(put(L.t[0], t_dense.data(), sizeof(float) * cells));
+  chk(put(L.tl[0], t_low.data(), sizeof(float) * cells));
+  chk(cudaMemsetAsync(base + L.tl[1], 0, sizeof(float) * cells, b->stream));
+  for (int k = 0; k < 2; k++) {
+    chk(cudaMemsetAsync(base + L.uxl[k], 0, sizeof(float) * cells, b->stream));
+    chk(cudaMemsetAsync(base + L.uyl[k], 0, sizeof(float) * cells, b->stream));
+  }
   chk(cudaMemsetAsync(base + L.t[1], 0, sizeof(float) * cells, b->stream));
   for (size_t o : {L.aux, L.auy, L.at}) chk(cudaMemsetAsync(base + o, 0, sizeof(float) * cells, b->stream));
   chk(cudaMemsetAsync(base + L.p, 0, sizeof(double) * cells, b->stream));
@@ -575,6 +591,11 @@ int sns_batch_add(sns_batch *b, const sns_case_desc *d, const double *temp_init,
     t.ux[k] = reinterpret_cast<float *>(base + L.ux[k]);
     t.uy[k] = reinterpret_cast<float *>(base + L.uy[k]);
     t.t[k] = reinterpret_cast<float *>(base + L.t[k]);
+  }
+  for (int k = 0; k < 2; k++) {
+    t.uxl[k] = reinterpret_cast<float *>(base + L.uxl[k]);
+    t.uyl[k] = reinterpret_cast<float *>(base + L.uyl[k]);
+    t.tl[k] = reinterpret_cast<float *>(base + L.tl[k]);
   }
   t.aux = reinterpret_cast<float *>(base + L.aux);
   t.auy = reinterpret_cast<float *>(base + L.auy);
@@ -700,11 +721,14 @@ int sns_batch_state(sns_batch *b, int slot, double *ux, double *uy, double *p, d
     b->staging_bytes = sizeof(double) * cells;
   }
   const int cur = t.par;
-  auto fetch_f = [&](const float *src, std::vector<double> &dst) -> int {
+  // compensated FP32 storage: value = hi + lo, exact in double
+  auto fetch_f = [&](const float *src, const float *low, std::vector<double> &dst) -> int {
     BCUDA(cudaMemcpy(b->staging, src, sizeof(float) * cells, cudaMemcpyDeviceToHost));
+    BCUDA(cudaMemcpy(reinterpret_cast<float *>(b->staging) + cells, low, sizeof(float) * cells,
+                     cudaMemcpyDeviceToHost));
     const float *f = reinterpret_cast<const float *>(b->staging);
     dst.resize(cells);
-    for (size_t k = 0; k < cells; k++) dst[k] = f[k];
+    for (size_t k = 0; k < cells; k++) dst[k] = (double)f[k] + (double)f[cells + k];
     return SNS_OK;
   };
   auto fetch_d = [&](const double *src, std::vector<double> &dst) -> int {
@@ -714,7 +738,7 @@ int sns_batch_state(sns_batch *b, int slot, double *ux, double *uy, double *p, d
   };
   std::vector<double> v;
   if (ux) {
-    if (int rc = fetch_f(t.ux[cur], v)) return rc;
+    if (int rc = fetch_f(t.ux[cur], t.uxl[cur], v)) return rc;
     std::memset(ux, 0, sizeof(double) * (size_t)(nx + 1) * (ny + 2));
     for (int j = 1; j <= ny; j++)
       for (int i = 2; i <= nx; i++) ux[(size_t)j * (nx + 1) + (i - 1)] = v[(size_t)(j - 1) * nx + (i - 1)];
@@ -748,7 +772,7 @@ int sns_batch_state(sns_batch *b, int slot, double *ux, double *uy, double *p, d
     }
   };
   if (uy) {
-    if (int rc = fetch_f(t.uy[cur], v)) return rc;
+    if (int rc = fetch_f(t.uy[cur], t.uyl[cur], v)) return rc;
     centred(v, uy, 0);
   }
   if (p) {
@@ -760,7 +784,7 @@ int sns_batch_state(sns_batch *b, int slot, double *ux, double *uy, double *p, d
     centred(v, psi, 1);
   }
   if (temp) {
-    if (int rc = fetch_f(t.t[cur], v)) return rc;
+    if (int rc = fetch_f(t.t[cur], t.tl[cur], v)) return rc;
     centred(v, temp, 2);
   }
   return SNS_OK;
@@ -782,8 +806,21 @@ extern "C" int sns_batch_diagnostics(sns_batch *b, int slot, double out[11]) {
     b->diag_words = words;
   }
   const sns_case_desc &d = b->hc[slot].d;
-  const DiagArgs<float> a{t.nx, t.ny, t.dy, d.ly, sqrt(d.Pr) * sqrt(d.Ra), sqrt(d.Pr) / sqrt(d.Ra),
-                          1. / sqrt(d.Pr) / sqrt(d.Ra), t.dxf, t.dxc, t.ux[t.par], t.uy[t.par], t.t[t.par]};
+  const DiagArgs<float> a{t.nx,
+                          t.ny,
+                          t.dy,
+                          d.ly,
+                          sqrt(d.Pr) * sqrt(d.Ra),
+                          sqrt(d.Pr) / sqrt(d.Ra),
+                          1. / sqrt(d.Pr) / sqrt(d.Ra),
+                          t.dxf,
+                          t.dxc,
+                          t.ux[t.par],
+                          t.uy[t.par],
+                          t.t[t.par],
+                          t.uxl[t.par],
+                          t.uyl[t.par],
+                          t.tl[t.par]};
   int nb = 0;
   BCUDA(launch_diag(a, b->diag, &nb, b->stream));
   count_launches(1);

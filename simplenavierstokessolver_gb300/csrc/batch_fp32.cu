@@ -2,8 +2,10 @@
 //
 // One launch per phase covers every resident case: blocks read a work item
 // (case, tile | column group | mode group) and the case's table entry.
-// Stencils, RK3 updates and velocity/temperature storage are FP32 with fused
-// multiply-adds; the pressure gradient, the divergence, the FFTs, the
+// Stencils and RK3 updates are FP32 with fused multiply-adds; velocity and
+// temperature are stored as compensated FP32 pairs (hi + lo, about 48
+// significant bits) so that the per-substage rounding of the stored state
+// does not accumulate, while every stencil reads the hi words only; the pressure gradient, the divergence, the FFTs, the
 // tridiagonal solves, psi and p are FP64 (multiply-adds allowed: this form is
 // compared with the FP64 reference by error norms, not bits). The equations
 // are the reference's (src/temperature/update.c:11-87, src/fluid/
@@ -27,25 +29,55 @@ namespace sns {
 namespace {
 
 __device__ __forceinline__ int wup(int y, int ny) { return y + 1 == ny ? 0 : y + 1; }
+
+// (hi + lo) + q in compensated FP32: the rounding error of hi + q (Knuth's
+// TwoSum) joins the low word, then the pair is renormalised (Fast2Sum).
+// Additions only, so no contraction can change the result.
+__device__ __forceinline__ void acc2(float hi, float lo, float q, float &ho, float &lw) {
+  const float s = hi + q;
+  const float bp = s - hi;
+  const float e = (hi - (s - bp)) + (q - bp);
+  const float l = lo + e;
+  const float h2 = s + l;
+  lw = l - (h2 - s);
+  ho = h2;
+}
 __device__ __forceinline__ int wdn(int y, int ny) { return y == 0 ? ny - 1 : y - 1; }
 
 // ------------------------------------------------------------------ stencils
+// A compensated value (hi + lo). Differences of neighbours use both words, so
+// gradients and Laplacians are accurate to FP32 rounding of the difference
+// itself rather than of the values; products and interpolations use hi.
+struct F2 {
+  float h, l;
+};
+__device__ __forceinline__ F2 ld2(const float *__restrict__ h, const float *__restrict__ l, size_t i) {
+  return F2{h[i], l[i]};
+}
+__device__ __forceinline__ float dif(F2 a, F2 b) { return (a.h - b.h) + (a.l - b.l); }
+
 __global__ void __launch_bounds__(kBTileX) k_b_stencil(const BCase *__restrict__ cases,
                                                       const BTile *__restrict__ tiles, int rk) {
-  const BTile tl = tiles[blockIdx.x];
-  const BCase &C = cases[tl.c];
+  const BTile tile = tiles[blockIdx.x];
+  const BCase &C = cases[tile.c];
   if (C.done) return;
   const int nx = C.nx, ny = C.ny;
-  const int x = tl.x0 + threadIdx.x;
+  const int x = tile.x0 + threadIdx.x;
   if (x >= nx) return;
-  const int y0 = tl.y0, y1 = min(y0 + kBTileY, ny);
+  const int y0 = tile.y0, y1 = min(y0 + kBTileY, ny);
   const int pin = C.par ^ (rk & 1), pout = pin ^ 1;
   const float *__restrict__ ux = C.ux[pin];
   const float *__restrict__ uy = C.uy[pin];
   const float *__restrict__ T = C.t[pin];
+  const float *__restrict__ uxl = C.uxl[pin];
+  const float *__restrict__ uyl = C.uyl[pin];
+  const float *__restrict__ Tl = C.tl[pin];
   float *__restrict__ uxo = C.ux[pout];
   float *__restrict__ uyo = C.uy[pout];
   float *__restrict__ To = C.t[pout];
+  float *__restrict__ uxlo = C.uxl[pout];
+  float *__restrict__ uylo = C.uyl[pout];
+  float *__restrict__ Tlo = C.tl[pout];
   float *__restrict__ aux = C.aux;
   float *__restrict__ auy = C.auy;
   float *__restrict__ at = C.at;
@@ -59,81 +91,83 @@ __global__ void __launch_bounds__(kBTileX) k_b_stencil(const BCase *__restrict__
   const float rxf_m = has_ux ? C.rdxf_f[x - 1] : 0.f;
   const float ccm = C.ccm_f[x], ccp = C.ccp_f[x], cfm = C.cfm_f[x], cfp = C.cfp_f[x];
   const double rdxc_d = C.rdxc[x], rdy_d = C.rdy;
+  const F2 Z{0.f, 0.f};
 
   const int ym = wdn(y0, ny);
   const size_t r0 = (size_t)y0 * nx + x, rm = (size_t)ym * nx + x;
-  float u0 = ux[r0], u1 = right ? 0.f : ux[r0 + 1];
-  float um0 = ux[rm], um1 = right ? 0.f : ux[rm + 1];
-  float v0 = uy[r0], vl = left ? 0.f : uy[r0 - 1];
-  const float vm = uy[rm];
-  float tc = T[r0];
-  const float tm = T[rm];
+  F2 u0 = ld2(ux, uxl, r0), u1 = right ? Z : ld2(ux, uxl, r0 + 1);
+  F2 um0 = ld2(ux, uxl, rm), um1 = right ? Z : ld2(ux, uxl, rm + 1);
+  F2 v0 = ld2(uy, uyl, r0), vl = left ? Z : ld2(uy, uyl, r0 - 1);
+  const F2 vm = ld2(uy, uyl, rm);
+  F2 tc = ld2(T, Tl, r0);
+  const F2 tm = ld2(T, Tl, rm);
   double pm = p[rm];
-  float gym_u = (u0 - um0) * rdy;
-  float pym_u = has_ux ? (0.5f * (cfm * vl + cfp * v0)) * gym_u : 0.f;
-  float gym_v = (v0 - vm) * rdy;
-  float pym_v = (0.5f * (0.5f * (vm + v0))) * gym_v;
-  float gym_t = (tc - tm) * rdy;
-  float pym_t = (0.5f * v0) * gym_t;
+  float gym_u = dif(u0, um0) * rdy;
+  float pym_u = has_ux ? (0.5f * (cfm * vl.h + cfp * v0.h)) * gym_u : 0.f;
+  float gym_v = dif(v0, vm) * rdy;
+  float pym_v = (0.5f * (0.5f * (vm.h + v0.h))) * gym_v;
+  float gym_t = dif(tc, tm) * rdy;
+  float pym_t = (0.5f * v0.h) * gym_t;
 
   for (int y = y0; y < y1; ++y) {
     const int yp = wup(y, ny);
     const size_t r = (size_t)y * nx + x, rp = (size_t)yp * nx + x;
-    const float u0n = ux[rp];
-    const float u1n = right ? 0.f : ux[rp + 1];
-    const float v0n = uy[rp];
-    const float vln = left ? 0.f : uy[rp - 1];
-    const float vr = right ? 0.f : uy[r + 1];
-    const float tn = T[rp];
+    const F2 u0n = ld2(ux, uxl, rp);
+    const F2 u1n = right ? Z : ld2(ux, uxl, rp + 1);
+    const F2 v0n = ld2(uy, uyl, rp);
+    const F2 vln = left ? Z : ld2(uy, uyl, rp - 1);
+    const F2 vr = right ? Z : ld2(uy, uyl, r + 1);
+    const F2 tn = ld2(T, Tl, rp);
+    const F2 tlv = left ? F2{0.5f, 0.f} : ld2(T, Tl, r - 1);  // T(0, j) = +0.5 (include/temperature.h)
     const double pc = p[r];
     if (with_t) {  // src/temperature/update.c:32-85
-      const float tlv = left ? 0.5f : T[r - 1];
-      const float trv = right ? -0.5f : T[r + 1];
-      const float gxm = (tc - tlv) * rxc_m, gxp = (trv - tc) * rxc_p, gyp = (tn - tc) * rdy;
-      const float pyp = (0.5f * v0n) * gyp;
-      const float adv1 = -(ccm * u0 * gxm) - (ccp * u1 * gxp);
+      const F2 trv = right ? F2{-0.5f, 0.f} : ld2(T, Tl, r + 1);
+      const float gxm = dif(tc, tlv) * rxc_m, gxp = dif(trv, tc) * rxc_p, gyp = dif(tn, tc) * rdy;
+      const float pyp = (0.5f * v0n.h) * gyp;
+      const float adv1 = -(ccm * u0.h * gxm) - (ccp * u1.h * gxp);
       const float adv2 = -pym_t - pyp;
-      const float dif = kappa * ((gxp - gxm) * rxf + (gyp - gym_t) * rdy);
-      const float A = adv1 + adv2 + dif;
+      const float dfs = kappa * ((gxp - gxm) * rxf + (gyp - gym_t) * rdy);
+      const float A = adv1 + adv2 + dfs;
       const float q = hasb ? fmaf(adt, A, bdt * at[r]) : adt * A;
       at[r] = A;
-      To[r] = tc + q;
+      acc2(tc.h, tc.l, q, To[r], Tlo[r]);
       gym_t = gyp;
       pym_t = pyp;
     } else {
-      To[r] = tc;  // uncoupled temperature is carried along unchanged
+      To[r] = tc.h;  // uncoupled temperature is carried along unchanged
+      Tlo[r] = tc.l;
     }
     if (has_ux) {  // src/fluid/update_velocity.c:136-203
-      const float ul = ux[r - 1];
-      const float gxm = (u0 - ul) * rxf_m, gxp = (u1 - u0) * rxf, gyp = (u0n - u0) * rdy;
-      const float vxm = 0.5f * (ul + u0), vxp = 0.5f * (u0 + u1);
+      const F2 ul = ld2(ux, uxl, r - 1);
+      const float gxm = dif(u0, ul) * rxf_m, gxp = dif(u1, u0) * rxf, gyp = dif(u0n, u0) * rdy;
+      const float vxm = 0.5f * (ul.h + u0.h), vxp = 0.5f * (u0.h + u1.h);
       const float adv1 = -(cfm * vxm * gxm) - (cfp * vxp * gxp);
-      const float pyp = (0.5f * (cfm * vln + cfp * v0n)) * gyp;
+      const float pyp = (0.5f * (cfm * vln.h + cfp * v0n.h)) * gyp;
       const float adv2 = -pym_u - pyp;
-      const float dif = nu * ((gxp - gxm) * rxc_m + (gyp - gym_u) * rdy);
+      const float dfs = nu * ((gxp - gxm) * rxc_m + (gyp - gym_u) * rdy);
       const float pre = -(float)((pc - p[r - 1]) * rdxc_d);
-      float A = adv1 + adv2 + dif;
-      if (force) A += 0.5f * (T[r - 1] + tc);
+      float A = adv1 + adv2 + dfs;
+      if (force) A += 0.5f * ((tlv.h + tc.h) + (tlv.l + tc.l));
       float q = hasb ? fmaf(adt, A, bdt * aux[r]) : adt * A;
       q = fmaf(gdt, pre, q);
       aux[r] = A;
-      uxo[r] = u0 + q;
+      acc2(u0.h, u0.l, q, uxo[r], uxlo[r]);
       gym_u = gyp;
       pym_u = pyp;
     }
     {  // src/fluid/update_velocity.c:230-291
-      const float gxm = (v0 - vl) * rxc_m, gxp = (vr - v0) * rxc_p, gyp = (v0n - v0) * rdy;
-      const float wxm = 0.5f * (um0 + u0), wxp = 0.5f * (um1 + u1);
+      const float gxm = dif(v0, vl) * rxc_m, gxp = dif(vr, v0) * rxc_p, gyp = dif(v0n, v0) * rdy;
+      const float wxm = 0.5f * (um0.h + u0.h), wxp = 0.5f * (um1.h + u1.h);
       const float adv1 = -(ccm * wxm * gxm) - (ccp * wxp * gxp);
-      const float pyp = (0.5f * (0.5f * (v0 + v0n))) * gyp;
+      const float pyp = (0.5f * (0.5f * (v0.h + v0n.h))) * gyp;
       const float adv2 = -pym_v - pyp;
-      const float dif = nu * ((gxp - gxm) * rxf + (gyp - gym_v) * rdy);
+      const float dfs = nu * ((gxp - gxm) * rxf + (gyp - gym_v) * rdy);
       const float pre = -(float)((pc - pm) * rdy_d);
-      const float A = adv1 + adv2 + dif;
+      const float A = adv1 + adv2 + dfs;
       float q = hasb ? fmaf(adt, A, bdt * auy[r]) : adt * A;
       q = fmaf(gdt, pre, q);
       auy[r] = A;
-      uyo[r] = v0 + q;
+      acc2(v0.h, v0.l, q, uyo[r], uylo[r]);
       gym_v = gyp;
       pym_v = pyp;
     }
@@ -161,6 +195,8 @@ __global__ void __launch_bounds__(256) k_b_fwd(const BCase *__restrict__ cases, 
   const int pu = C.par ^ (rk & 1) ^ 1;
   const float *__restrict__ ux = C.ux[pu];
   const float *__restrict__ uy = C.uy[pu];
+  const float *__restrict__ uxl = C.uxl[pu];
+  const float *__restrict__ uyl = C.uyl[pu];
   const double rgdt = C.rgdt[rk], rdy = C.rdy;
   double *zd = reinterpret_cast<double *>(zs);
   for (int e = threadIdx.x; e < nc * ny; e += blockDim.x) {
@@ -168,8 +204,9 @@ __global__ void __launch_bounds__(256) k_b_fwd(const BCase *__restrict__ cases, 
     double d = 0.0;
     if (x < nx) {
       const size_t r = (size_t)y * nx + x;
-      const float dux = (x == nx - 1 ? 0.f : ux[r + 1]) - ux[r];
-      const float duy = uy[(size_t)wup(y, ny) * nx + x] - uy[r];
+      const size_t ry = (size_t)wup(y, ny) * nx + x;
+      const float dux = x == nx - 1 ? -(ux[r] + uxl[r]) : (ux[r + 1] - ux[r]) + (uxl[r + 1] - uxl[r]);
+      const float duy = (uy[ry] - uy[r]) + (uyl[ry] - uyl[r]);
       d = rgdt * ((double)dux * C.rdxf[x] + (double)duy * rdy);
     }
     zd[2 * (c * M + fft::fft_slot(y >> 1, M, C.fft_nst, C.fft_first2)) + (y & 1)] = d;
@@ -306,6 +343,8 @@ __global__ void __launch_bounds__(kBTileX) k_b_corr(BCase *__restrict__ cases, c
     const int pu = C.par ^ (rk & 1) ^ 1;
     float *__restrict__ ux = C.ux[pu];
     float *__restrict__ uy = C.uy[pu];
+    float *__restrict__ uxl = C.uxl[pu];
+    float *__restrict__ uyl = C.uyl[pu];
     const double *__restrict__ psi = C.psi;
     double *__restrict__ p = C.p;
     const double gdt = C.gdt[rk], dxi = C.dxi[x], rdy = C.rdy;
@@ -315,12 +354,16 @@ __global__ void __launch_bounds__(kBTileX) k_b_corr(BCase *__restrict__ cases, c
       const size_t r = (size_t)y * nx + x;
       const double sc = psi[r];
       if (x >= 1) {  // src/fluid/correct_velocity.c:19-25
-        const float u = ux[r] - (float)((gdt * (sc - psi[r - 1])) * dxi);
+        float u, ul;
+        acc2(ux[r], uxl[r], -(float)((gdt * (sc - psi[r - 1])) * dxi), u, ul);
         ux[r] = u;
+        uxl[r] = ul;
         mx = fmaxf(mx, fabsf(u) * rxc);
       }
-      const float v = uy[r] - (float)((gdt * (sc - sm)) * rdy);  // :31-37
+      float v, vlo;
+      acc2(uy[r], uyl[r], -(float)((gdt * (sc - sm)) * rdy), v, vlo);  // :31-37
       uy[r] = v;
+      uyl[r] = vlo;
       my = fmaxf(my, fabsf(v) * rdyf);
       p[r] += sc;  // src/fluid/update_pressure.c:26-31
       sm = sc;

@@ -39,6 +39,9 @@ struct BCase {
   size_t pstride;                  // doubles per mode in pfac
   // ---- fields
   float *ux[2], *uy[2], *t[2];
+  // low words of the compensated storage: value = hi (ux/uy/t above) + lo,
+  // double-buffered like the high words
+  float *uxl[2], *uyl[2], *tl[2];
   float *aux, *auy, *at;
   double *p, *psi;
   double2 *spec;

@@ -21,6 +21,8 @@ struct DiagArgs {
   double kappa;       // 1./sqrt(Pr)/sqrt(Ra)
   const double *dxf, *dxc;
   const F *ux, *uy, *t;
+  // low words of compensated FP32 storage (value = hi + lo), or nullptr
+  const float *uxl = nullptr, *uyl = nullptr, *tl = nullptr;
 };
 
 template <typename F>

@@ -38,14 +38,17 @@ __global__ void __launch_bounds__(64) k_diag(DiagArgs<F> a, double *partials) {
   if (x <= nx) {
     const double dy = a.dy, q = a.sqrt_pr_ra, nu = a.nu, kap = a.kappa;
     const bool cell = x < nx;  // cell centre i = x+1 <= nx
+    auto LD = [](const F *hi, const float *lo, size_t k) -> double {
+      return lo ? (double)hi[k] + (double)lo[k] : (double)hi[k];
+    };
     auto UX = [&](int xi, int y) -> double {  // ux at i = xi+1; walls i = 1 and nx+1 are zero
-      return (xi <= 0 || xi >= nx) ? 0.0 : (double)a.ux[(size_t)y * nx + xi];
+      return (xi <= 0 || xi >= nx) ? 0.0 : LD(a.ux, a.uxl, (size_t)y * nx + xi);
     };
     auto UY = [&](int xi, int y) -> double {  // uy at i = xi+1, zero at i = 0 and nx+1
-      return (xi < 0 || xi >= nx) ? 0.0 : (double)a.uy[(size_t)y * nx + xi];
+      return (xi < 0 || xi >= nx) ? 0.0 : LD(a.uy, a.uyl, (size_t)y * nx + xi);
     };
     auto TT = [&](int xi, int y) -> double {
-      return xi < 0 ? 0.5 : xi >= nx ? -0.5 : (double)a.t[(size_t)y * nx + xi];
+      return xi < 0 ? 0.5 : xi >= nx ? -0.5 : LD(a.t, a.tl, (size_t)y * nx + xi);
     };
     const double dxc = a.dxc[x];                 // DXC(i), i = x+1 <= nx+1
     const double dxf = cell ? a.dxf[x] : 1.0;    // DXF(i)
