@@ -229,6 +229,35 @@ extern int sns_diagnostics(const param_t *param, const fluid_t *fluid, const tem
 extern int sns_diagnostics_static(const param_t *param, const fluid_t *fluid, const temperature_t *temperature,
                                   double out[11]);
 
+/* Checkpoint of the device state in the reference's save layout
+ * (src/save.c:13-68, src/fileio.c:226-345, src/simple_npyio.c:1222):
+ * dirname/{step,itot,jtot,time,lx,ly,Ra,Pr,xf,xc,yf,yc,ux,uy,p[,temp]}.npy,
+ * byte for byte the files the reference's save() writes for the same state
+ * (it writes into output/save/step%010d). dirname is created if needed.
+ * Asynchronous: ux, uy, p and T are copied on the device in stream order,
+ * the copy to pinned host memory runs on a separate stream and a host thread
+ * writes the files; the call returns after enqueuing the device copy, so
+ * the solver may keep stepping. One checkpoint per solver is in flight; a
+ * second call waits for the first. */
+extern int sns_checkpoint(const param_t *param, const fluid_t *fluid, const temperature_t *temperature,
+                          const char *dirname);
+/* waits for the last checkpoint of this solver; its status and message */
+extern int sns_checkpoint_wait(const fluid_t *fluid);
+/* Restart from a directory written by the reference's save() or by
+ * sns_checkpoint (src/param/init.c:245-247, src/fluid/init.c:53-81,
+ * src/temperature/init.c:51): step and time into param, rows 1..jtot of ux,
+ * uy, p and temp into the host arrays, the boundary rules, zeroed explicit
+ * sources, then sns_sync_to_device. Shapes and dtypes are checked
+ * (SNS_ERR_ARG with the file's name otherwise). */
+extern int sns_restart(param_t *param, fluid_t *fluid, temperature_t *temperature, const char *dirname);
+/* Host-only NPY helpers with the reference's file format (no device needed):
+ * dtype is the reference's descriptor text, "'float64'" or "'int32'"; the
+ * reader also accepts numpy's '<f8' / '<i4' and checks ndim and shape. */
+extern int sns_npy_write(const char *path, const char *dtype, int ndim, const size_t *shape, const void *data,
+                         size_t nbytes);
+extern int sns_npy_read(const char *path, const char *dtype, int ndim, const size_t *shape, void *data,
+                        size_t nbytes);
+
 /* per-kernel device time: with profiling enabled every kernel launched for
  * this solver is bracketed by CUDA events on its stream. sns_profile(f, 1)
  * resets the totals and starts, sns_profile(f, 0) stops. sns_profile_read

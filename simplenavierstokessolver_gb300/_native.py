@@ -111,6 +111,11 @@ PROTOTYPES = {
     "sns_abi_layout": (c_int, [POINTER(c_size_t), c_int]),
     "sns_diagnostics": (c_int, [PP, PF, PT, _PD]),
     "sns_diagnostics_static": (c_int, [PP, PF, PT, _PD]),
+    "sns_checkpoint": (c_int, [PP, PF, PT, ctypes.c_char_p]),
+    "sns_checkpoint_wait": (c_int, [PF]),
+    "sns_restart": (c_int, [PP, PF, PT, ctypes.c_char_p]),
+    "sns_npy_write": (c_int, [c_char_p, c_char_p, c_int, POINTER(c_size_t), c_void_p, c_size_t]),
+    "sns_npy_read": (c_int, [c_char_p, c_char_p, c_int, POINTER(c_size_t), c_void_p, c_size_t]),
     "sns_profile": (c_int, [PF, c_int]),
     "sns_profile_read": (c_int, [PF, POINTER(c_double), POINTER(c_longlong), c_int]),
     "sns_profile_kind_name": (c_char_p, [c_int]),

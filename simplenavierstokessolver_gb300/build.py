@@ -40,6 +40,7 @@ UNITS = {
     "diagnostics.cu": [],
     "sns_api.cpp": [],
     "batch_api.cpp": [],
+    "npy.cpp": [],
 }
 
 

@@ -17,10 +17,12 @@
 #include <atomic>
 #include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "diag_internal.h"
 #include "host_common.h"
+#include "npy.h"
 #include "sns_gpu.h"
 #include "sns_internal.h"
 
@@ -77,6 +79,16 @@ struct Context {
   double *fac = nullptr;
   size_t fac_words = 0;
   double *diag = nullptr;  // block partials of sns_diagnostics
+  // asynchronous checkpoint (sns_checkpoint): a device snapshot of ux, uy, p
+  // and T taken on the solver's stream, its copy to pinned memory on ck_stream,
+  // and a host thread that writes the files
+  double *ck_dev = nullptr;
+  double *ck_host = nullptr;
+  cudaStream_t ck_stream = nullptr;
+  cudaEvent_t ck_snap = nullptr, ck_done = nullptr;
+  std::thread ck_thread;
+  int ck_status = SNS_OK;
+  std::string ck_error;
   // optional per-launch event timing (sns_profile)
   bool prof = false;
   std::vector<cudaEvent_t> prof_ev;  // two per slot
@@ -176,7 +188,12 @@ static int upload(Context *c, const T **dst, const std::vector<T> &src) {
 }
 
 static void destroy_context(Context *c) {
+  if (c->ck_thread.joinable()) c->ck_thread.join();
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->ck_host) cudaFreeHost(c->ck_host);
+  if (c->ck_snap) cudaEventDestroy(c->ck_snap);
+  if (c->ck_done) cudaEventDestroy(c->ck_done);
+  if (c->ck_stream) cudaStreamDestroy(c->ck_stream);
   for (cudaEvent_t e : c->prof_ev) cudaEventDestroy(e);
   c->prof_ev.clear();
   for (void *p : c->allocs) cudaFree(p);
@@ -1207,6 +1224,213 @@ int sns_diagnostics(const param_t *param, const fluid_t *fluid, const temperatur
   SNS_CUDA(cudaStreamSynchronize(c->stream));
   diag_finish(h.data(), nb, param->ly, out);
   return SNS_OK;
+}
+
+// ------------------------------------------------------------ checkpoints
+// The reference's save layout (src/save.c:13-68, src/fileio.c:226-345): one
+// NPY file per quantity; 2D fields hold rows j = 1..jtot of the reference
+// arrays, wall and halo columns included.
+struct CheckpointJob {
+  std::string dir;
+  int step, itot, jtot, with_t, device;
+  double time, lx, ly, Ra, Pr;
+  std::vector<double> xf, xc, yf, yc;
+};
+
+static int write_checkpoint(const CheckpointJob &J, const double *snap, std::string *err) {
+  const int nx = J.itot, ny = J.jtot;
+  const size_t cells = (size_t)nx * ny;
+  if (make_dirs(J.dir.c_str(), err)) return 1;
+  auto path = [&](const char *name) { return J.dir + "/" + name + ".npy"; };
+  int rc = 0;
+  auto w0 = [&](const char *name, const char *dtype, const void *v, size_t n) {
+    if (!rc) rc = npy_write(path(name).c_str(), dtype, 0, nullptr, v, n, err);
+  };
+  auto w1 = [&](const char *name, const std::vector<double> &v) {
+    const size_t shape[1] = {v.size()};
+    if (!rc) rc = npy_write(path(name).c_str(), "'float64'", 1, shape, v.data(), sizeof(double) * v.size(), err);
+  };
+  w0("step", "'int32'", &J.step, sizeof(int));
+  w0("itot", "'int32'", &J.itot, sizeof(int));
+  w0("jtot", "'int32'", &J.jtot, sizeof(int));
+  w0("time", "'float64'", &J.time, sizeof(double));
+  w0("lx", "'float64'", &J.lx, sizeof(double));
+  w0("ly", "'float64'", &J.ly, sizeof(double));
+  w0("Ra", "'float64'", &J.Ra, sizeof(double));
+  w0("Pr", "'float64'", &J.Pr, sizeof(double));
+  w1("xf", J.xf);
+  w1("xc", J.xc);
+  w1("yf", J.yf);
+  w1("yc", J.yc);
+  // field rows: walls / halo columns by the boundary rules the reference
+  // applied after each update (src/fluid/boundary_conditions.c:6-55,
+  // src/temperature/boundary_conditions.c:6-21)
+  auto field = [&](const char *name, const double *d, int kind) {
+    if (rc) return;
+    const int w = kind == 0 ? nx + 1 : nx + 2;
+    std::vector<double> rows((size_t)ny * w);
+    for (int j = 0; j < ny; j++) {
+      double *r = rows.data() + (size_t)j * w;
+      const double *src = d + (size_t)j * nx;
+      if (kind == 0) {  // ux, i = 1..nx+1: dense x = 0..nx-1 is i = 1..nx (x = 0 the wall)
+        std::memcpy(r, src, sizeof(double) * nx);
+        r[nx] = 0.;
+        r[0] = 0.;
+      } else {
+        std::memcpy(r + 1, src, sizeof(double) * nx);
+        if (kind == 1) {  // uy: no-slip walls
+          r[0] = 0.;
+          r[nx + 1] = 0.;
+        } else if (kind == 2) {  // p: Neumann
+          r[0] = r[1];
+          r[nx + 1] = r[nx];
+        } else {  // temperature: fixed wall values
+          r[0] = TEMP_XM;
+          r[nx + 1] = TEMP_XP;
+        }
+      }
+    }
+    const size_t shape[2] = {(size_t)ny, (size_t)w};
+    rc = npy_write(path(name).c_str(), "'float64'", 2, shape, rows.data(), sizeof(double) * rows.size(), err);
+  };
+  field("ux", snap, 0);
+  field("uy", snap + cells, 1);
+  field("p", snap + 2 * cells, 2);
+  if (J.with_t) field("temp", snap + 3 * cells, 3);
+  return rc;
+}
+
+int sns_checkpoint(const param_t *param, const fluid_t *fluid, const temperature_t *temperature, const char *dirname) {
+  FluidExt *fe = as_fluid(fluid);
+  TempExt *te = temperature ? as_temp(temperature) : nullptr;
+  if (!param || !fe || !dirname || (temperature && !te)) return fail(SNS_ERR_ARG, "sns_checkpoint: bad argument");
+  Context *c = fe->ctx;
+  if (c->ck_thread.joinable()) c->ck_thread.join();  // one checkpoint in flight per solver
+  const int nx = c->nx, ny = c->ny;
+  const size_t cells = (size_t)nx * ny;
+  if (!c->ck_dev) {
+    if (int rc = dev_alloc(c, &c->ck_dev, 4 * cells)) return rc;
+    SNS_CUDA(cudaMallocHost(&c->ck_host, sizeof(double) * 4 * cells));
+    SNS_CUDA(cudaStreamCreateWithFlags(&c->ck_stream, cudaStreamNonBlocking));
+    SNS_CUDA(cudaEventCreateWithFlags(&c->ck_snap, cudaEventDisableTiming));
+    SNS_CUDA(cudaEventCreateWithFlags(&c->ck_done, cudaEventDisableTiming));
+  }
+  const bool with_t = param->with_temperature && te;
+  // snapshot on the solver's stream: later launches may overwrite the fields
+  SNS_CUDA(cudaMemcpyAsync(c->ck_dev, fe->f.ux, sizeof(double) * cells, cudaMemcpyDeviceToDevice, c->stream));
+  SNS_CUDA(cudaMemcpyAsync(c->ck_dev + cells, fe->f.uy, sizeof(double) * cells, cudaMemcpyDeviceToDevice, c->stream));
+  SNS_CUDA(cudaMemcpyAsync(c->ck_dev + 2 * cells, fe->f.p, sizeof(double) * cells, cudaMemcpyDeviceToDevice, c->stream));
+  if (with_t)
+    SNS_CUDA(cudaMemcpyAsync(c->ck_dev + 3 * cells, te->f.t[te->cur], sizeof(double) * cells,
+                             cudaMemcpyDeviceToDevice, c->stream));
+  SNS_CUDA(cudaEventRecord(c->ck_snap, c->stream));
+  SNS_CUDA(cudaStreamWaitEvent(c->ck_stream, c->ck_snap, 0));
+  SNS_CUDA(cudaMemcpyAsync(c->ck_host, c->ck_dev, sizeof(double) * (with_t ? 4 : 3) * cells, cudaMemcpyDeviceToHost,
+                           c->ck_stream));
+  SNS_CUDA(cudaEventRecord(c->ck_done, c->ck_stream));
+  CheckpointJob J;
+  J.dir = dirname;
+  J.step = param->step;
+  J.itot = param->itot;
+  J.jtot = param->jtot;
+  J.with_t = with_t ? 1 : 0;
+  J.time = param->time;
+  J.lx = param->lx;
+  J.ly = param->ly;
+  J.Ra = param->Ra;
+  J.Pr = param->Pr;
+  J.xf.assign(param->xf, param->xf + nx + 1);
+  J.xc.assign(param->xc, param->xc + nx + 2);
+  J.yf.assign(param->yf, param->yf + ny + 1);
+  J.yc.assign(param->yc, param->yc + ny);
+  SNS_CUDA(cudaGetDevice(&J.device));
+  c->ck_status = SNS_OK;
+  c->ck_error.clear();
+  try {
+    c->ck_thread = std::thread([c, J]() {
+      std::string err;
+      cudaError_t e = cudaSetDevice(J.device);
+      if (e == cudaSuccess) e = cudaEventSynchronize(c->ck_done);
+      if (e != cudaSuccess) {
+        c->ck_status = SNS_ERR_CUDA;
+        c->ck_error = std::string("checkpoint copy: ") + cudaGetErrorString(e);
+        return;
+      }
+      if (write_checkpoint(J, c->ck_host, &err)) {
+        c->ck_status = SNS_ERR_ARG;
+        c->ck_error = err;
+      }
+    });
+  } catch (...) {
+    return fail(SNS_ERR_STATE, "sns_checkpoint: cannot start the writer thread");
+  }
+  return SNS_OK;
+}
+
+int sns_npy_write(const char *path, const char *dtype, int ndim, const size_t *shape, const void *data,
+                  size_t nbytes) {
+  if (!path || !dtype || ndim < 0 || (ndim > 0 && !shape) || (nbytes && !data))
+    return fail(SNS_ERR_ARG, "sns_npy_write: bad argument");
+  std::string err;
+  if (npy_write(path, dtype, ndim, shape, data, nbytes, &err)) return fail(SNS_ERR_ARG, "%s", err.c_str());
+  return SNS_OK;
+}
+
+int sns_npy_read(const char *path, const char *dtype, int ndim, const size_t *shape, void *data, size_t nbytes) {
+  if (!path || !dtype || ndim < 0 || (ndim > 0 && !shape) || (nbytes && !data))
+    return fail(SNS_ERR_ARG, "sns_npy_read: bad argument");
+  std::string err;
+  if (npy_read(path, dtype, ndim, shape, data, nbytes, &err)) return fail(SNS_ERR_ARG, "%s", err.c_str());
+  return SNS_OK;
+}
+
+int sns_checkpoint_wait(const fluid_t *fluid) {
+  FluidExt *fe = as_fluid(fluid);
+  if (!fe) return fail(SNS_ERR_ARG, "sns_checkpoint_wait: bad argument");
+  Context *c = fe->ctx;
+  if (c->ck_thread.joinable()) c->ck_thread.join();
+  if (c->ck_status != SNS_OK) return fail(c->ck_status, "sns_checkpoint: %s", c->ck_error.c_str());
+  return SNS_OK;
+}
+
+int sns_restart(param_t *param, fluid_t *fluid, temperature_t *temperature, const char *dirname) {
+  FluidExt *fe = as_fluid(fluid);
+  TempExt *te = temperature ? as_temp(temperature) : nullptr;
+  if (!param || !fe || !dirname || (temperature && !te)) return fail(SNS_ERR_ARG, "sns_restart: bad argument");
+  const int nx = param->itot, ny = param->jtot;
+  const std::string dir(dirname);
+  std::string err;
+  int step = 0;
+  double time = 0.;
+  // src/param/init.c:245-247
+  if (npy_read((dir + "/step.npy").c_str(), "'int32'", 0, nullptr, &step, sizeof(int), &err) ||
+      npy_read((dir + "/time.npy").c_str(), "'float64'", 0, nullptr, &time, sizeof(double), &err))
+    return fail(SNS_ERR_ARG, "sns_restart: %s", err.c_str());
+  // src/fluid/init.c:53-81, src/temperature/init.c:51: rows 1..jtot, then the boundary rules
+  fluid_t &h = fe->pub;
+  const size_t su[2] = {(size_t)ny, (size_t)nx + 1}, sc[2] = {(size_t)ny, (size_t)nx + 2};
+  if (npy_read((dir + "/ux.npy").c_str(), "'float64'", 2, su, h.ux + (nx + 1), sizeof(double) * su[0] * su[1], &err) ||
+      npy_read((dir + "/uy.npy").c_str(), "'float64'", 2, sc, h.uy + (nx + 2), sizeof(double) * sc[0] * sc[1], &err) ||
+      npy_read((dir + "/p.npy").c_str(), "'float64'", 2, sc, h.p + (nx + 2), sizeof(double) * sc[0] * sc[1], &err))
+    return fail(SNS_ERR_ARG, "sns_restart: %s", err.c_str());
+  host_bc_ux(nx, ny, h.ux);
+  host_bc_uy(nx, ny, h.uy);
+  host_bc_p(nx, ny, h.p);
+  std::memset(h.psi, 0, sizeof(double) * sc[1] * (ny + 2));
+  // a restarted reference run starts from zeroed (calloc'd) source arrays
+  std::memset(h.srcuxa, 0, sizeof(double) * (size_t)(nx - 1) * ny);
+  std::memset(h.srcuya, 0, sizeof(double) * (size_t)nx * ny);
+  if (te && param->with_temperature) {
+    temperature_t &t = te->pub;
+    if (npy_read((dir + "/temp.npy").c_str(), "'float64'", 2, sc, t.temp + (nx + 2), sizeof(double) * sc[0] * sc[1],
+                 &err))
+      return fail(SNS_ERR_ARG, "sns_restart: %s", err.c_str());
+    host_bc_temp(nx, ny, t.temp);
+    std::memset(t.srctempa, 0, sizeof(double) * (size_t)nx * ny);
+  }
+  param->step = step;
+  param->time = time;
+  return sns_sync_to_device(param, fluid, te ? temperature : nullptr);
 }
 
 // sns_diagnostics without allocation, for callers that cannot allocate (a

@@ -215,6 +215,17 @@ class Case:
                                          out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))), "sns_diagnostics")
         return out
 
+    # ------------------------------------------------------ checkpoints
+    def checkpoint(self, dirname: str):
+        """asynchronous: the files appear after checkpoint_wait()"""
+        N.check(self.lib.sns_checkpoint(self.param, self.fluid, self.temperature, dirname.encode()), "sns_checkpoint")
+
+    def checkpoint_wait(self):
+        N.check(self.lib.sns_checkpoint_wait(self.fluid), "sns_checkpoint_wait")
+
+    def restart(self, dirname: str):
+        N.check(self.lib.sns_restart(self.param, self.fluid, self.temperature, dirname.encode()), "sns_restart")
+
     # ------------------------------------------------------- fused fast path
     def integrate(self):
         N.check(self.lib.sns_integrate(self.param, self.parallel, self.fluid, self.temperature), "sns_integrate")
@@ -231,3 +242,24 @@ class Case:
 
 def kernel_launches() -> int:
     return int(N.lib().sns_kernel_launches())
+
+
+def save_dirname(step: int, root: str = "output/save") -> str:
+    """the directory the reference's save() uses for a step (src/save.c:40-50)"""
+    return f"{root}/step{step:010d}"
+
+
+def npy_write(path: str, array: np.ndarray):
+    """an NPY file in the reference's format (float64 or int32, C order)"""
+    a = np.asarray(array, order="C")
+    dtype = {np.dtype(np.float64): b"'float64'", np.dtype(np.int32): b"'int32'"}[a.dtype]
+    shape = (ctypes.c_size_t * max(a.ndim, 1))(*a.shape)
+    N.check(N.lib().sns_npy_write(path.encode(), dtype, a.ndim, shape, a.ctypes.data, a.nbytes), "sns_npy_write")
+
+
+def npy_read(path: str, shape, dtype=np.float64) -> np.ndarray:
+    a = np.empty(shape, dtype=dtype)
+    d = {np.dtype(np.float64): b"'float64'", np.dtype(np.int32): b"'int32'"}[a.dtype]
+    s = (ctypes.c_size_t * max(a.ndim, 1))(*a.shape)
+    N.check(N.lib().sns_npy_read(path.encode(), d, a.ndim, s, a.ctypes.data, a.nbytes), "sns_npy_read")
+    return a

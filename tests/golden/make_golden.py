@@ -10,6 +10,9 @@ precision.
 
 Usage:  python tests/golden/make_golden.py      (from the repository root)
 
+Also copies the NPY files the reference's save() writes after a run
+(``save_<case>/``), the byte-level reference for checkpoints.
+
 The fixtures are consumed by tests/test_oracle_pinning.py (the C restatement
 against them, on the CPU) and tests/test_gpu_plain_parity.py (the CUDA path
 against them, on the GPU).
@@ -60,7 +63,32 @@ def seeded_fields(cfg: Config, seed: int):
     return ux, uy, p, t
 
 
+# checkpoint fixtures: the reference's own save() output after `steps` steps
+SAVE_CASES = {"rb_uniform_32x64": 25}
+
+
+def save_fixtures():
+    import glob
+    import shutil
+
+    for name, steps in SAVE_CASES.items():
+        cfg, costs, _, _ = CASES[name]
+        out = os.path.join(OUT, f"save_{name}")
+        shutil.rmtree(out, ignore_errors=True)
+        os.makedirs(out)
+        with RefCase(cfg) as ref, tempfile.TemporaryDirectory() as d:
+            ref.set_costs(costs)
+            ref.run(steps)
+            if ref.save(d) != 0:
+                raise RuntimeError("reference save failed")
+            (step_dir,) = glob.glob(os.path.join(d, "output", "save", "step*"))
+            for f in sorted(os.listdir(step_dir)):
+                shutil.copy(os.path.join(step_dir, f), out)
+        print("save", name, sorted(os.listdir(out)))
+
+
 def main():
+    save_fixtures()
     manifest = {}
     for seed, (name, (cfg, costs, steps, seeded)) in enumerate(sorted(CASES.items())):
         with RefCase(cfg) as ref:
