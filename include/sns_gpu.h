@@ -229,6 +229,30 @@ extern int sns_diagnostics(const param_t *param, const fluid_t *fluid, const tem
 extern int sns_diagnostics_static(const param_t *param, const fluid_t *fluid, const temperature_t *temperature,
                                   double out[11]);
 
+/* statistics_t (include/statistics.h:8-13): the number of samples and host
+ * arrays in the reference's layouts (include/arrays/statistics.h: ux1/ux2
+ * (jtot+2) x (itot+1), uy1/uy2/temp1/temp2 (jtot+2) x (itot+2)). The running
+ * sums live on the device; the host arrays are filled by statistics_output
+ * and sns_statistics_output_to. */
+typedef struct statistics_t_ {
+  int num;
+  double *ux1, *ux2;
+  double *uy1, *uy2;
+  double *temp1, *temp2;
+} statistics_t;
+
+/* include/statistics.h:15-19 (src/statistics/{init,finalise,collect,output}.c):
+ * collect adds u and u^2 of the current device state on the solver's stream
+ * (asynchronous); output writes NPY files to output/stat/step%010d relative to
+ * the working directory, as the reference does, byte for byte. */
+extern statistics_t *statistics_init(const param_t *param, const parallel_t *parallel);
+extern int statistics_finalise(statistics_t *statistics);
+extern int statistics_collect(param_t *param, const parallel_t *parallel, const fluid_t *fluid,
+                              const temperature_t *temperature, statistics_t *statistics);
+extern int statistics_output(const param_t *param, const parallel_t *parallel, const statistics_t *statistics);
+/* statistics_output into a given directory (created if needed) */
+extern int sns_statistics_output_to(const param_t *param, const statistics_t *statistics, const char *dirname);
+
 /* Checkpoint of the device state in the reference's save layout
  * (src/save.c:13-68, src/fileio.c:226-345, src/simple_npyio.c:1222):
  * dirname/{step,itot,jtot,time,lx,ly,Ra,Pr,xf,xc,yf,yc,ux,uy,p[,temp]}.npy,

@@ -216,6 +216,7 @@ class RefCase(_Case):
             lib.ref_get_grid.argtypes = [_P] * 5
             lib.ref_logging.argtypes = [ctypes.c_char_p]
             lib.ref_save.argtypes = [ctypes.c_char_p]
+            lib.ref_stats_run.argtypes = [_I, ctypes.c_char_p]
             cls._lib = lib
         return cls._lib
 
@@ -273,6 +274,12 @@ class RefCase(_Case):
     def logging(self, directory: str):
         os.makedirs(os.path.join(directory, "output", "log"), exist_ok=True)
         return self.lib().ref_logging(directory.encode())
+
+    def stats_run(self, nsteps: int, directory: str):
+        """nsteps steps collecting statistics after each, then the reference's
+        statistics_output under directory/output/stat"""
+        os.makedirs(os.path.join(directory, "output", "stat"), exist_ok=True)
+        return self.lib().ref_stats_run(nsteps, directory.encode())
 
     def save(self, directory: str):
         os.makedirs(os.path.join(directory, "output", "save"), exist_ok=True)

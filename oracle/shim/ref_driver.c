@@ -26,6 +26,7 @@
 #include "temperature.h"
 #include "logging.h"
 #include "save.h"
+#include "statistics.h"
 
 static param_t *g_param;
 static parallel_t *g_parallel;
@@ -191,6 +192,26 @@ int ref_logging(const char *dir) {
 }
 
 /* the reference's snapshot writer (src/save.c:52-68) under <dir>/output/save */
+/* nsteps steps with statistics_collect after each (src/main.c:46-50), then
+ * statistics_output (it writes output/stat/step%010d under dir) */
+int ref_stats_run(int nsteps, const char *dir) {
+  statistics_t *st = statistics_init(g_param, g_parallel);
+  for (int s = 0; s < nsteps; s++) {
+    ref_run(1, 1);
+    statistics_collect(g_param, g_parallel, g_fluid, g_temperature, st);
+  }
+  char cwd[4096];
+  int rc = 0;
+  if (!getcwd(cwd, sizeof cwd)) rc = 1;
+  if (!rc && chdir(dir) != 0) rc = 2;
+  if (!rc) {
+    statistics_output(g_param, g_parallel, st);
+    if (chdir(cwd) != 0) rc = 3;
+  }
+  statistics_finalise(st);
+  return rc;
+}
+
 int ref_save(const char *dir) {
   char cwd[4096];
   if (!getcwd(cwd, sizeof cwd)) return 1;

@@ -76,7 +76,13 @@ class CaseDesc(ctypes.Structure):
                 ("steps", c_longlong), ("seed", ctypes.c_ulonglong), ("fixed_dt", c_double)]
 
 
+class Statistics(ctypes.Structure):
+    _fields_ = [("num", c_int), ("ux1", _PD), ("ux2", _PD), ("uy1", _PD), ("uy2", _PD), ("temp1", _PD),
+                ("temp2", _PD)]
+
+
 PP, PL, PF, PT = POINTER(Param), POINTER(Parallel), POINTER(Fluid), POINTER(Temperature)
+PS = POINTER(Statistics)
 PCD = POINTER(CaseDesc)
 
 # name -> (restype, argtypes)
@@ -111,6 +117,11 @@ PROTOTYPES = {
     "sns_abi_layout": (c_int, [POINTER(c_size_t), c_int]),
     "sns_diagnostics": (c_int, [PP, PF, PT, _PD]),
     "sns_diagnostics_static": (c_int, [PP, PF, PT, _PD]),
+    "statistics_init": (PS, [PP, PL]),
+    "statistics_finalise": (c_int, [PS]),
+    "statistics_collect": (c_int, [PP, PL, PF, PT, PS]),
+    "statistics_output": (c_int, [PP, PL, PS]),
+    "sns_statistics_output_to": (c_int, [PP, PS, c_char_p]),
     "sns_checkpoint": (c_int, [PP, PF, PT, ctypes.c_char_p]),
     "sns_checkpoint_wait": (c_int, [PF]),
     "sns_restart": (c_int, [PP, PF, PT, ctypes.c_char_p]),

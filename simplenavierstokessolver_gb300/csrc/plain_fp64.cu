@@ -766,6 +766,43 @@ cudaError_t launch_add_increment(const DevGrid &g, int kind, const double *in, c
   return cudaGetLastError();
 }
 
+// ------------------------------------------------------------- statistics
+// UX1 += pow(UX, 1.), UX2 += pow(UX, 2.) etc. per point and sample
+// (src/statistics/collect.c:19-24, 38-43, 57-62); pow(v, 1.) is v and
+// pow(v, 2.) the correctly rounded square, v * v.
+__global__ void __launch_bounds__(256) k_stats(int nx, int ny, const double *ux, const double *uy, const double *t,
+                                               double *s) {
+  const size_t wu = (size_t)nx + 1, wc = (size_t)nx + 2;
+  const size_t nu = wu * ny, nc = wc * ny;
+  double *ux1 = s, *ux2 = s + nu, *uy1 = s + 2 * nu, *uy2 = uy1 + nc, *t1 = uy2 + nc, *t2 = t1 + nc;
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < nc; k += (size_t)gridDim.x * blockDim.x) {
+    const int y = (int)(k / wc), i = (int)(k - (size_t)y * wc);  // i = 0..nx+1
+    const size_t d = (size_t)y * nx + (i - 1);
+    const bool wall = i == 0 || i == nx + 1;
+    const double v = wall ? 0.0 : uy[d];
+    uy1[k] += v;
+    uy2[k] += v * v;
+    if (t) {
+      const double tv = i == 0 ? kTempXm : i == nx + 1 ? kTempXp : t[d];
+      t1[k] += tv;
+      t2[k] += tv * tv;
+    }
+    if (i >= 1) {  // ux at i = 1..nx+1; dense x = i-1 holds the wall i = 1 as zero
+      const size_t ku = (size_t)y * wu + (i - 1);
+      const double u = i == nx + 1 ? 0.0 : ux[d];
+      ux1[ku] += u;
+      ux2[ku] += u * u;
+    }
+  }
+}
+
+cudaError_t launch_stats(const DevGrid &g, const double *ux, const double *uy, const double *t, double *s,
+                         cudaStream_t st) {
+  k_stats<<<2 * 152, 256, 0, st>>>(g.nx, g.ny, ux, uy, t, s);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 // --------------------------------------------------------- host transfers
 __global__ void __launch_bounds__(256) k_xfer(const XferList L) {
   const XferField f = L.f[blockIdx.y];

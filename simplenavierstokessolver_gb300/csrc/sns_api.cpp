@@ -16,6 +16,7 @@
 #include <algorithm>
 #include <atomic>
 #include <mutex>
+#include <new>
 #include <string>
 #include <thread>
 #include <vector>
@@ -1431,6 +1432,159 @@ int sns_restart(param_t *param, fluid_t *fluid, temperature_t *temperature, cons
   param->step = step;
   param->time = time;
   return sns_sync_to_device(param, fluid, te ? temperature : nullptr);
+}
+
+// ------------------------------------------------------------- statistics
+constexpr uint64_t kStatsMagic = 0x534e535354415453ull;  // "SNSSTATS"
+
+struct StatsExt {
+  statistics_t pub;  // first member: statistics_t* and StatsExt* coincide
+  uint64_t magic;
+  int nx, ny, with_t;
+  Context *ctx;           // the solver whose stream the sums are taken on (first collect)
+  double *dev = nullptr;  // ux1, ux2 [ny][nx+1]; uy1, uy2, temp1, temp2 [ny][nx+2]
+};
+
+static StatsExt *as_stats(const statistics_t *s) {
+  StatsExt *e = reinterpret_cast<StatsExt *>(const_cast<statistics_t *>(s));
+  return (e && e->magic == kStatsMagic) ? e : nullptr;
+}
+
+statistics_t *statistics_init(const param_t *param, const parallel_t *parallel) {
+  if (!param || !parallel) {
+    fail(SNS_ERR_ARG, "statistics_init: bad argument");
+    return nullptr;
+  }
+  const int nx = param->itot, ny = param->jtot;
+  StatsExt *e = new (std::nothrow) StatsExt();
+  if (!e) {
+    fail(SNS_ERR_OOM, "statistics_init: out of host memory");
+    return nullptr;
+  }
+  e->magic = kStatsMagic;
+  e->nx = nx;
+  e->ny = ny;
+  e->with_t = param->with_temperature ? 1 : 0;
+  const size_t nu = (size_t)(nx + 1) * (ny + 2), nc = (size_t)(nx + 2) * (ny + 2);
+  statistics_t &h = e->pub;
+  h.num = 0;
+  h.ux1 = static_cast<double *>(calloc(nu, sizeof(double)));
+  h.ux2 = static_cast<double *>(calloc(nu, sizeof(double)));
+  h.uy1 = static_cast<double *>(calloc(nc, sizeof(double)));
+  h.uy2 = static_cast<double *>(calloc(nc, sizeof(double)));
+  h.temp1 = static_cast<double *>(calloc(nc, sizeof(double)));
+  h.temp2 = static_cast<double *>(calloc(nc, sizeof(double)));
+  if (!h.ux1 || !h.ux2 || !h.uy1 || !h.uy2 || !h.temp1 || !h.temp2) {
+    statistics_finalise(&h);
+    fail(SNS_ERR_OOM, "statistics_init: out of host memory");
+    return nullptr;
+  }
+  return &h;
+}
+
+int statistics_finalise(statistics_t *statistics) {
+  StatsExt *e = as_stats(statistics);
+  if (!e) return fail(SNS_ERR_ARG, "statistics_finalise: not a statistics_t from statistics_init");
+  if (e->dev) {
+    if (e->ctx && e->ctx->stream) cudaStreamSynchronize(e->ctx->stream);
+    cudaFree(e->dev);
+  }
+  for (double *p : {e->pub.ux1, e->pub.ux2, e->pub.uy1, e->pub.uy2, e->pub.temp1, e->pub.temp2}) free(p);
+  e->magic = 0;
+  delete e;
+  return SNS_OK;
+}
+
+int statistics_collect(param_t *param, const parallel_t *parallel, const fluid_t *fluid,
+                       const temperature_t *temperature, statistics_t *statistics) {
+  StatsExt *e = as_stats(statistics);
+  FluidExt *fe = as_fluid(fluid);
+  TempExt *te = temperature ? as_temp(temperature) : nullptr;
+  if (!param || !parallel || !e || !fe || (temperature && !te))
+    return fail(SNS_ERR_ARG, "statistics_collect: bad argument");
+  Context *c = fe->ctx;
+  if (e->nx != c->nx || e->ny != c->ny) return fail(SNS_ERR_ARG, "statistics_collect: grid size mismatch");
+  if (e->ctx && e->ctx != c) return fail(SNS_ERR_ARG, "statistics_collect: statistics of another solver");
+  const size_t nx = c->nx, ny = c->ny, words = 2 * (nx + 1) * ny + 4 * (nx + 2) * ny;
+  if (!e->dev) {
+    e->ctx = c;
+    void *p = nullptr;
+    cudaError_t err = cudaMalloc(&p, sizeof(double) * words);
+    if (err != cudaSuccess) return fail(SNS_ERR_OOM, "statistics_collect: cudaMalloc: %s", cudaGetErrorString(err));
+    e->dev = static_cast<double *>(p);
+    SNS_CUDA(cudaMemsetAsync(e->dev, 0, sizeof(double) * words, c->stream));
+  }
+  SNS_CUDA(launch_stats(c->g, fe->f.ux, fe->f.uy, te ? te->f.t[te->cur] : nullptr, e->dev, c->stream));
+  e->pub.num += 1;
+  return SNS_OK;
+}
+
+int sns_statistics_output_to(const param_t *param, const statistics_t *statistics, const char *dirname) {
+  StatsExt *e = as_stats(statistics);
+  if (!param || !e || !dirname) return fail(SNS_ERR_ARG, "sns_statistics_output_to: bad argument");
+  const int nx = e->nx, ny = e->ny;
+  const size_t wu = (size_t)nx + 1, wc = (size_t)nx + 2;
+  statistics_t &h = e->pub;
+  if (e->dev) {  // rows j = 1..jtot of the host arrays
+    Context *c = e->ctx;
+    const size_t nu = wu * ny, nc = wc * ny;
+    const double *d = e->dev;
+    SNS_CUDA(cudaMemcpyAsync(h.ux1 + wu, d, sizeof(double) * nu, cudaMemcpyDeviceToHost, c->stream));
+    SNS_CUDA(cudaMemcpyAsync(h.ux2 + wu, d + nu, sizeof(double) * nu, cudaMemcpyDeviceToHost, c->stream));
+    SNS_CUDA(cudaMemcpyAsync(h.uy1 + wc, d + 2 * nu, sizeof(double) * nc, cudaMemcpyDeviceToHost, c->stream));
+    SNS_CUDA(cudaMemcpyAsync(h.uy2 + wc, d + 2 * nu + nc, sizeof(double) * nc, cudaMemcpyDeviceToHost, c->stream));
+    SNS_CUDA(cudaMemcpyAsync(h.temp1 + wc, d + 2 * nu + 2 * nc, sizeof(double) * nc, cudaMemcpyDeviceToHost,
+                             c->stream));
+    SNS_CUDA(cudaMemcpyAsync(h.temp2 + wc, d + 2 * nu + 3 * nc, sizeof(double) * nc, cudaMemcpyDeviceToHost,
+                             c->stream));
+    SNS_CUDA(cudaStreamSynchronize(c->stream));
+  }
+  // src/statistics/output.c:9-63
+  std::string err, dir(dirname);
+  if (make_dirs(dirname, &err)) return fail(SNS_ERR_ARG, "sns_statistics_output_to: %s", err.c_str());
+  auto path = [&](const char *n) { return dir + "/" + n + ".npy"; };
+  int rc = 0;
+  auto w0 = [&](const char *n, const char *dt, const void *v, size_t b) {
+    if (!rc) rc = npy_write(path(n).c_str(), dt, 0, nullptr, v, b, &err);
+  };
+  auto w1 = [&](const char *n, const double *v, size_t len) {
+    const size_t shape[1] = {len};
+    if (!rc) rc = npy_write(path(n).c_str(), "'float64'", 1, shape, v, sizeof(double) * len, &err);
+  };
+  auto w2 = [&](const char *n, const double *v, size_t w) {
+    const size_t shape[2] = {(size_t)ny, w};
+    if (!rc) rc = npy_write(path(n).c_str(), "'float64'", 2, shape, v + w, sizeof(double) * w * ny, &err);
+  };
+  w0("num", "'int32'", &h.num, sizeof(int));
+  w0("step", "'int32'", &param->step, sizeof(int));
+  w0("itot", "'int32'", &param->itot, sizeof(int));
+  w0("jtot", "'int32'", &param->jtot, sizeof(int));
+  w0("time", "'float64'", &param->time, sizeof(double));
+  w0("lx", "'float64'", &param->lx, sizeof(double));
+  w0("ly", "'float64'", &param->ly, sizeof(double));
+  w0("Ra", "'float64'", &param->Ra, sizeof(double));
+  w0("Pr", "'float64'", &param->Pr, sizeof(double));
+  w1("xf", param->xf, (size_t)nx + 1);
+  w1("xc", param->xc, (size_t)nx + 2);
+  w1("yf", param->yf, (size_t)ny + 1);
+  w1("yc", param->yc, (size_t)ny);
+  w2("ux1", h.ux1, wu);
+  w2("uy1", h.uy1, wc);
+  w2("ux2", h.ux2, wu);
+  w2("uy2", h.uy2, wc);
+  if (param->with_temperature) {
+    w2("temp1", h.temp1, wc);
+    w2("temp2", h.temp2, wc);
+  }
+  if (rc) return fail(SNS_ERR_ARG, "sns_statistics_output_to: %s", err.c_str());
+  return SNS_OK;
+}
+
+int statistics_output(const param_t *param, const parallel_t *parallel, const statistics_t *statistics) {
+  if (!param || !parallel) return fail(SNS_ERR_ARG, "statistics_output: bad argument");
+  char dir[64];
+  snprintf(dir, sizeof dir, "output/stat/step%010d", param->step);  // src/statistics/output.c:41-51
+  return sns_statistics_output_to(param, statistics, dir);
 }
 
 // sns_diagnostics without allocation, for callers that cannot allocate (a

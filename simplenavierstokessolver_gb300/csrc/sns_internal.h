@@ -127,6 +127,11 @@ cudaError_t launch_xfer(const XferList &L, cudaStream_t st);
 // tempforcex (src/temperature/force.c:17-23) from dense T, written straight
 // into the (itot-1) x jtot host array through its device alias
 cudaError_t launch_tempforce_to_host(const DevGrid &g, const double *t, double *host, cudaStream_t st);
+// running sums of src/statistics/collect.c:10-63 over rows j = 1..jtot of the
+// reference-width arrays (walls included): s = ux1, ux2 [ny][nx+1], then
+// uy1, uy2, temp1, temp2 [ny][nx+2]; t may be null (no temperature sums)
+cudaError_t launch_stats(const DevGrid &g, const double *ux, const double *uy, const double *t, double *s,
+                         cudaStream_t st);
 cudaError_t launch_poisson_fwd(const DevGrid &g, const StageScalars &s, const double *ux, const double *uy,
                                double2 *spec, cudaStream_t st);
 cudaError_t launch_poisson_tri(const DevGrid &g, double2 *spec, cudaStream_t st);

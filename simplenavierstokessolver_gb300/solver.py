@@ -263,3 +263,40 @@ def npy_read(path: str, shape, dtype=np.float64) -> np.ndarray:
     s = (ctypes.c_size_t * max(a.ndim, 1))(*a.shape)
     N.check(N.lib().sns_npy_read(path.encode(), d, a.ndim, s, a.ctypes.data, a.nbytes), "sns_npy_read")
     return a
+
+
+class Statistics:
+    """statistics_t of the reference (include/statistics.h) over a Case:
+    running sums of u and u^2 on the device (statistics_collect), written as
+    the reference's statistics_output files."""
+
+    def __init__(self, case: Case):
+        self.case = case
+        self.lib = case.lib
+        self.s = self.lib.statistics_init(case.param, case.parallel)
+        if not self.s:
+            raise N.SnsError(N.SNS_ERR_ARG, "statistics_init")
+
+    def collect(self):
+        c = self.case
+        N.check(self.lib.statistics_collect(c.param, c.parallel, c.fluid, c.temperature, self.s),
+                "statistics_collect")
+
+    @property
+    def num(self) -> int:
+        return self.s.contents.num
+
+    def output_to(self, dirname: str):
+        N.check(self.lib.sns_statistics_output_to(self.case.param, self.s, dirname.encode()),
+                "sns_statistics_output_to")
+
+    def close(self):
+        if getattr(self, "s", None):
+            self.lib.statistics_finalise(self.s)
+            self.s = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -11,7 +11,9 @@ precision.
 Usage:  python tests/golden/make_golden.py      (from the repository root)
 
 Also copies the NPY files the reference's save() writes after a run
-(``save_<case>/``), the byte-level reference for checkpoints.
+(``save_<case>/``) and those its statistics_output() writes after collecting
+every step (``stat_<case>/``): the byte-level references for checkpoints and
+statistics.
 
 The fixtures are consumed by tests/test_oracle_pinning.py (the C restatement
 against them, on the CPU) and tests/test_gpu_plain_parity.py (the CUDA path
@@ -85,6 +87,19 @@ def save_fixtures():
             for f in sorted(os.listdir(step_dir)):
                 shutil.copy(os.path.join(step_dir, f), out)
         print("save", name, sorted(os.listdir(out)))
+        # statistics collected after every step (src/statistics/collect.c) and
+        # written by statistics_output (src/statistics/output.c)
+        out = os.path.join(OUT, f"stat_{name}")
+        shutil.rmtree(out, ignore_errors=True)
+        os.makedirs(out)
+        with RefCase(cfg) as ref, tempfile.TemporaryDirectory() as d:
+            ref.set_costs(costs)
+            if ref.stats_run(steps, d) != 0:
+                raise RuntimeError("reference statistics failed")
+            (step_dir,) = glob.glob(os.path.join(d, "output", "stat", "step*"))
+            for f in sorted(os.listdir(step_dir)):
+                shutil.copy(os.path.join(step_dir, f), out)
+        print("stat", name, sorted(os.listdir(out)))
 
 
 def main():

@@ -77,3 +77,19 @@ def test_restart_rejects_mismatched_files(tmp_path):
             c.restart(GOLD)
         with pytest.raises(N.SnsError, match="cannot open"):
             c.restart(str(tmp_path / "nothing"))
+
+
+def test_statistics_equal_the_reference_output(tmp_path):
+    """statistics collected after every step of the golden case, written
+    like statistics_output: byte for byte the reference's own files
+    (tests/golden/stat_rb_uniform_32x64)."""
+    from simplenavierstokessolver_gb300.solver import Statistics
+
+    c, steps = golden_case()
+    with c, Statistics(c) as st:
+        for _ in range(steps):
+            c.run(1)
+            st.collect()
+        assert st.num == steps
+        st.output_to(str(tmp_path / "stat"))
+    same_files(tmp_path / "stat", os.path.join(HERE, "golden", "stat_rb_uniform_32x64"))
