@@ -229,6 +229,22 @@ extern int sns_diagnostics(const param_t *param, const fluid_t *fluid, const tem
 extern int sns_diagnostics_static(const param_t *param, const fluid_t *fluid, const temperature_t *temperature,
                                   double out[11]);
 
+/* param_estimate_cost (include/param.h, src/param/estimate_cost.c:44-74)
+ * with a deterministic cost model instead of wall-clock emulation: fills
+ * expimp_wtimes[implicity][implicitx] with the predicted seconds of one RK
+ * substage for this grid on the current device (its SM count and clock), so
+ * param_decide_dt picks the same treatment in every run. */
+extern int param_estimate_cost(param_t *param, const parallel_t *parallel);
+/* the same model for a given device description, host only:
+ * out[2*implicity + implicitx] in seconds per substage */
+extern int sns_cost_model(int itot, int jtot, int sm_count, double clock_ghz, int with_temperature, double out[4]);
+/* the reference's wall-clock estimate (emulate(), src/param/estimate_cost.c:
+ * 11-42) measured with CUDA events on this device: out[2*implicity +
+ * implicitx] in seconds per substage over `reps` substages. Like the
+ * reference it creates fresh fields through fluid_init/temperature_init,
+ * which draw from rand(). param's dt and treatment are restored. */
+extern int sns_measure_cost(param_t *param, const parallel_t *parallel, int reps, double out[4]);
+
 /* statistics_t (include/statistics.h:8-13): the number of samples and host
  * arrays in the reference's layouts (include/arrays/statistics.h: ux1/ux2
  * (jtot+2) x (itot+1), uy1/uy2/temp1/temp2 (jtot+2) x (itot+2)). The running

@@ -117,6 +117,9 @@ PROTOTYPES = {
     "sns_abi_layout": (c_int, [POINTER(c_size_t), c_int]),
     "sns_diagnostics": (c_int, [PP, PF, PT, _PD]),
     "sns_diagnostics_static": (c_int, [PP, PF, PT, _PD]),
+    "param_estimate_cost": (c_int, [PP, PL]),
+    "sns_cost_model": (c_int, [c_int, c_int, c_int, c_double, c_int, _PD]),
+    "sns_measure_cost": (c_int, [PP, PL, c_int, _PD]),
     "statistics_init": (PS, [PP, PL]),
     "statistics_finalise": (c_int, [PS]),
     "statistics_collect": (c_int, [PP, PL, PF, PT, PS]),

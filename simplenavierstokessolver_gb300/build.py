@@ -41,6 +41,7 @@ UNITS = {
     "sns_api.cpp": [],
     "batch_api.cpp": [],
     "npy.cpp": [],
+    "cost_model.cpp": [],
 }
 
 

@@ -1101,6 +1101,83 @@ int fluid_update_pressure(const param_t *param, const parallel_t *parallel, cons
   return SNS_OK;
 }
 
+// ------------------------------------------------------------ cost model
+int sns_cost_model(int itot, int jtot, int sm_count, double clock_ghz, int with_temperature, double out[4]) {
+  if (itot < 2 || jtot < 2 || sm_count < 1 || !(clock_ghz > 0.0) || !out)
+    return fail(SNS_ERR_ARG, "sns_cost_model: bad argument");
+  double w[2][2];
+  cost_model(itot, jtot, sm_count, clock_ghz * 1e9, with_temperature != 0, w);
+  for (int k = 0; k < 4; k++) out[k] = w[k / 2][k % 2];
+  return SNS_OK;
+}
+
+// src/param/estimate_cost.c:44-74 with the deterministic model in place of
+// wall-clock emulation: expimp_wtimes[implicity][implicitx] in seconds per
+// substage for the current device
+int param_estimate_cost(param_t *param, const parallel_t *parallel) {
+  if (!param || !parallel) return fail(SNS_ERR_ARG, "param_estimate_cost: bad argument");
+  int dev = 0, sms = 0, khz = 0;
+  SNS_CUDA(cudaGetDevice(&dev));
+  SNS_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  SNS_CUDA(cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, dev));
+  cost_model(param->itot, param->jtot, sms, khz * 1e3, param->with_temperature, param->expimp_wtimes);
+  return SNS_OK;
+}
+
+// the reference's emulate() (src/param/estimate_cost.c:11-42) timed with CUDA
+// events: per treatment, fresh fields from fluid_init / temperature_init
+// (which draw rand() like the reference's), dt = 1e-8, `reps` substages rk = 0
+// through the reference-named calls after one warm-up; seconds per substage
+int sns_measure_cost(param_t *param, const parallel_t *parallel, int reps, double out[4]) {
+  if (!param || !parallel || reps < 1 || !out) return fail(SNS_ERR_ARG, "sns_measure_cost: bad argument");
+  const double dt0 = param->dt;
+  const int ix0 = param->implicitx, iy0 = param->implicity;
+  int rc = SNS_OK;
+  for (int k = 0; k < 4 && rc == SNS_OK; k++) {
+    param->dt = 1.e-8;
+    param->implicitx = k % 2;
+    param->implicity = k / 2;
+    fluid_t *fl = fluid_init(param, parallel);
+    temperature_t *tm = fl ? temperature_init(param, parallel) : nullptr;
+    if (!fl || !tm) {
+      if (fl) fluid_finalise(fl);
+      rc = SNS_ERR_OOM;
+      break;
+    }
+    Context *c = as_fluid(fl)->ctx;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    auto substage = [&]() -> int {
+      int r = SNS_OK;
+      if (param->with_temperature) {
+        if ((r = temperature_compute_force(param, parallel, tm)) || (r = temperature_update_temp(param, parallel, 0, fl, tm)))
+          return r;
+      }
+      if ((r = fluid_update_velocity(param, parallel, 0, fl, tm)) || (r = fluid_compute_potential(param, parallel, 0, fl)) ||
+          (r = fluid_correct_velocity(param, parallel, 0, fl)) || (r = fluid_update_pressure(param, parallel, 0, fl)))
+        return r;
+      return SNS_OK;
+    };
+    float ms = 0.f;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) rc = SNS_ERR_CUDA;
+    if (rc == SNS_OK) rc = substage();
+    if (rc == SNS_OK && cudaEventRecord(e0, c->stream) != cudaSuccess) rc = SNS_ERR_CUDA;
+    for (int r = 0; r < reps && rc == SNS_OK; r++) rc = substage();
+    if (rc == SNS_OK && (cudaEventRecord(e1, c->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                         cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+      rc = SNS_ERR_CUDA;
+    out[k] = 1e-3 * ms / reps;
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    temperature_finalise(tm);
+    fluid_finalise(fl);
+  }
+  param->dt = dt0;
+  param->implicitx = ix0;
+  param->implicity = iy0;
+  if (rc != SNS_OK) return fail(rc, "sns_measure_cost: %s", sns_last_error());
+  return SNS_OK;
+}
+
 int param_decide_dt(param_t *param, const parallel_t *parallel, const fluid_t *fluid) {
   FluidExt *fe = as_fluid(fluid);
   if (!param || !parallel || !fe) return fail(SNS_ERR_ARG, "param_decide_dt: bad argument");

@@ -156,5 +156,7 @@ enum KernelKind {
 
 // counts kernel launches (process-wide)
 void count_launches(long long n);
+// predicted seconds per RK substage, out[implicity][implicitx] (cost_model.cpp)
+void cost_model(int nx, int ny, int sms, double clock_hz, bool with_t, double out[2][2]);
 
 }  // namespace sns

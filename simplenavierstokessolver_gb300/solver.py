@@ -183,6 +183,19 @@ class Case:
             N.check(self.lib.temperature_update_boundaries_temp(self.param, self.parallel, t.temp),
                     "temperature_update_boundaries_temp")
 
+    def estimate_cost(self):
+        """param_estimate_cost: the deterministic model fills expimp_wtimes"""
+        N.check(self.lib.param_estimate_cost(self.param, self.parallel), "param_estimate_cost")
+        p = self.p
+        return [p.expimp_wtimes[y][x] for y in range(2) for x in range(2)]
+
+    def measure_cost(self, reps: int = 20):
+        """seconds per substage of EXP/IMP combinations, CUDA-event timed
+        (index 2*implicity + implicitx)"""
+        out = (ctypes.c_double * 4)()
+        N.check(self.lib.sns_measure_cost(self.param, self.parallel, reps, out), "sns_measure_cost")
+        return list(out)
+
     def param_decide_dt(self):
         N.check(self.lib.param_decide_dt(self.param, self.parallel, self.fluid), "param_decide_dt")
 
@@ -300,3 +313,10 @@ class Statistics:
 
     def __exit__(self, *exc):
         self.close()
+
+
+def cost_model(itot: int, jtot: int, sm_count: int = 152, clock_ghz: float = 2.07, with_temperature: bool = True):
+    """predicted seconds per substage, index 2*implicity + implicitx (host only)"""
+    out = (ctypes.c_double * 4)()
+    N.check(N.lib().sns_cost_model(itot, jtot, sm_count, clock_ghz, int(with_temperature), out), "sns_cost_model")
+    return list(out)
