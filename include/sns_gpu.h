@@ -298,6 +298,15 @@ extern int sns_npy_write(const char *path, const char *dtype, int ndim, const si
 extern int sns_npy_read(const char *path, const char *dtype, int ndim, const size_t *shape, void *data,
                         size_t nbytes);
 
+/* The Poisson solve (and, with the explicit scheme, the temperature update of
+ * the fused step) runs as one cooperative launch by default: the serial
+ * tridiagonal sweeps on a few SMs, the DFTs and the temperature update on
+ * the others, pipelined column by column; identical results to the
+ * three-kernel form. on = 0 selects the three-kernel form for this solver
+ * (for comparisons); sizes the device cannot hold cooperatively fall back
+ * by themselves. */
+extern int sns_set_fused(const fluid_t *fluid, int on);
+
 /* per-kernel device time: with profiling enabled every kernel launched for
  * this solver is bracketed by CUDA events on its stream. sns_profile(f, 1)
  * resets the totals and starts, sns_profile(f, 0) stops. sns_profile_read

@@ -118,6 +118,7 @@ PROTOTYPES = {
     "sns_diagnostics": (c_int, [PP, PF, PT, _PD]),
     "sns_diagnostics_static": (c_int, [PP, PF, PT, _PD]),
     "param_estimate_cost": (c_int, [PP, PL]),
+    "sns_set_fused": (c_int, [PF, c_int]),
     "sns_cost_model": (c_int, [c_int, c_int, c_int, c_double, c_int, _PD]),
     "sns_measure_cost": (c_int, [PP, PL, c_int, _PD]),
     "statistics_init": (PS, [PP, PL]),

@@ -113,13 +113,22 @@ __device__ __forceinline__ void rfft_post(const double2 *zc, double2 *out, int M
 // inverse split step for bin pair (k, M-k): Z slots (digit-reversed) from X
 // (bins of one column at in[J * is]);
 // imaginary parts of X[0] and X[M] are ignored (FFTW c2r convention)
+// CG: load the input through L2 only (data written by other blocks of the running kernel)
+template <bool CG = false>
 __device__ __forceinline__ void rfft_pre(const double2 *in, double2 *zc, int M, int k, const double2 *tw, int nst,
                                          int first2, size_t is = 1) {
+  auto ld = [](const double2 *p) -> double2 {
+    if constexpr (CG) {
+      return __ldcg(p);
+    } else {
+      return *p;
+    }
+  };
   if (k == 0) {
-    const double x0r = in[0].x, xmr = in[(size_t)M * is].x;
+    const double x0r = ld(in).x, xmr = ld(in + (size_t)M * is).x;
     zc[0] = make_double2(x0r + xmr, x0r - xmr);
   } else {
-    const double2 A = in[(size_t)k * is], B = in[(size_t)(M - k) * is];
+    const double2 A = ld(in + (size_t)k * is), B = ld(in + (size_t)(M - k) * is);
     const double er = A.x + B.x, ei = A.y - B.y, dr = A.x - B.x, di = A.y + B.y;
     const double2 w = tw[k];
     const double orr = dr * w.x + di * w.y;

@@ -12,6 +12,7 @@
 // row to row by each thread, RHS-independent Thomas factors are precomputed,
 // and the implicit-source terms (exactly zero in the explicit scheme) are not
 // evaluated.
+#include <algorithm>
 #include <cfloat>
 #include <cstdint>
 
@@ -46,12 +47,10 @@ struct TempArgs {
 };
 
 // src/temperature/update.c:11-87 (sources) and :114-122, :221-226 (RK3 update)
+// for column x, rows y0 .. y0+kRows-1
 template <int IMPX, int IMPY, bool RCP>
-__global__ void __launch_bounds__(128) k_temp(const TempArgs a) {
+__device__ __forceinline__ void temp_column(const TempArgs &a, int x, int y0) {
   const int nx = a.g.nx, ny = a.g.ny;
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= nx) return;
-  const int y0 = blockIdx.y * kRows;
   const int y1 = min(y0 + kRows, ny);
   const double *T = a.t_in;
   const double dcm = a.g.dxc[x], dcp = a.g.dxc[x + 1], df = a.g.dxf[x];
@@ -98,6 +97,13 @@ __global__ void __launch_bounds__(128) k_temp(const TempArgs a) {
     gym = gyp;
     pym = pyp;
   }
+}
+
+template <int IMPX, int IMPY, bool RCP>
+__global__ void __launch_bounds__(128) k_temp(const TempArgs a) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= a.g.nx) return;
+  temp_column<IMPX, IMPY, RCP>(a, x, blockIdx.y * kRows);
 }
 
 // ------------------------------------------------------------------ velocity
@@ -403,11 +409,10 @@ using fft::fft_stages;
 
 // src/fluid/compute_potential.c:69-92: right-hand side (div u*)/(gamma dt)
 // and its real DFT along y (forward, FFTW conventions).
+// columns x0 .. x0+cols-1 by the whole block, z: cols * ny/2 complex in shared memory
 template <bool RCP>
-__global__ void __launch_bounds__(256) k_poisson_fwd(const PoissonArgs a) {
-  extern __shared__ double2 z[];
+__device__ __forceinline__ void poisson_fwd_cols(const PoissonArgs &a, int x0, double2 *z) {
   const int nx = a.g.nx, ny = a.g.ny, M = ny / 2, C = a.cols;
-  const int x0 = blockIdx.x * C;
   double *zd = reinterpret_cast<double *>(z);
   const double dy = a.g.dy, rdy = a.g.rdy;
   for (int e = threadIdx.x; e < C * ny; e += blockDim.x) {
@@ -432,6 +437,12 @@ __global__ void __launch_bounds__(256) k_poisson_fwd(const PoissonArgs a) {
     if (x >= nx) continue;
     fft::rfft_post(z + c * M, a.spec + (size_t)x * a.g.jpitch, M, k, tw);
   }
+}
+
+template <bool RCP>
+__global__ void __launch_bounds__(256) k_poisson_fwd(const PoissonArgs a) {
+  extern __shared__ double2 z[];
+  poisson_fwd_cols<RCP>(a, blockIdx.x * a.cols, z);
 }
 
 // Thomas sweeps of the Poisson modes. On this GPU an FP64 warp instruction
@@ -549,10 +560,10 @@ __global__ void __launch_bounds__(32) k_poisson_tri(const DevGrid g, double2 *sp
 
 // src/fluid/compute_potential.c:146-157: inverse real DFT along y and the
 // 1/jtot normalisation, psi on the interior (halo and walls implied).
-__global__ void __launch_bounds__(256) k_poisson_bwd(const PoissonArgs a) {
-  extern __shared__ double2 z[];
+// CG: read the spectrum through L2 (written by other blocks of the same launch)
+template <bool CG>
+__device__ __forceinline__ void poisson_bwd_cols(const PoissonArgs &a, int x0, double2 *z) {
   const int nx = a.g.nx, ny = a.g.ny, M = ny / 2, C = a.cols;
-  const int x0 = blockIdx.x * C;
   const double2 *tw = reinterpret_cast<const double2 *>(a.g.tw);
   const int half = M / 2 + 1;
   for (int e = threadIdx.x; e < C * half; e += blockDim.x) {
@@ -563,7 +574,7 @@ __global__ void __launch_bounds__(256) k_poisson_bwd(const PoissonArgs a) {
       if (k > 0) zc[fft_slot(M - k, M, a.g.fft_nst, a.g.fft_first2)] = make_double2(0.0, 0.0);
       continue;
     }
-    fft::rfft_pre(a.spec + (size_t)x * a.g.jpitch, zc, M, k, tw, a.g.fft_nst, a.g.fft_first2);
+    fft::rfft_pre<CG>(a.spec + (size_t)x * a.g.jpitch, zc, M, k, tw, a.g.fft_nst, a.g.fft_first2);
   }
   __syncthreads();
   fft_stages<false>(z, C, M, ny, a.g.fft_nst, a.g.fft_first2, tw);
@@ -572,6 +583,241 @@ __global__ void __launch_bounds__(256) k_poisson_bwd(const PoissonArgs a) {
     const int c = e % C, y = e / C, x = x0 + c;
     if (x >= nx) continue;
     a.psi[(size_t)y * nx + x] = zd[2 * (c * M + (y >> 1)) + (y & 1)] * a.s.rny;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_poisson_bwd(const PoissonArgs a) {
+  extern __shared__ double2 z[];
+  poisson_bwd_cols<false>(a, blockIdx.x * a.cols, z);
+}
+
+// ------------------------------------------- fused Poisson (+ temperature)
+// One cooperative launch per substage, one block per SM. The serial Thomas
+// sweeps (latency bound, 2 x ceil(nh/32) warps) run on the first blocks, one
+// warp per SM sub-partition; every other block is a worker that computes
+// forward DFT column groups in ascending x, then (optionally) the explicit
+// temperature update, then inverse DFT column groups in descending x. The
+// sweep of a mode line consumes spectrum rows as the workers publish them,
+// and a worker inverts a column group as soon as every sweep warp has passed
+// it on the way back, so the DFTs and the temperature update hide behind the
+// sweep. Arithmetic and its order are those of the three separate kernels,
+// so the results are identical.
+//
+// Synchronisation: fwd_done[g] = epoch when group g's spectrum rows are
+// written (release: block barrier, fence, store); a sweep warp reads flags
+// with relaxed loads and issues one fence before reading the rows it
+// verified (acquire). bwd_cnt[s] counts the sweep warps that finished span s
+// (span = kFusedSpan x elements), cumulative over launches, so a worker waits
+// for epoch * lines. Spectrum reads of data written in this launch go
+// through L2 (__ldcg). Every wait polls at most kFusedSpin times; a wait that
+// gives up sets *err and its warp or block stops, so the launch always ends.
+constexpr int kFusedThreads = 512;
+// sweep warps per block, one per SM sub-partition. Dependent FP64 chains run
+// ~20% slower with four warps on one SM than with one, but every SM given to
+// the sweeps is taken from the DFT workers, whose FP64 throughput bounds the
+// launch as much as the sweeps do: measured on GB300, four per block is the
+// fastest at 512 x 1024 (within 1%), 1024 x 2048 and 2048 x 4096.
+constexpr int kFusedTriWarps = 4;
+constexpr int kFusedSpan = 64;
+constexpr unsigned kFusedSpin = 1u << 22;
+constexpr size_t kFusedMinSmem = 116 * 1024;  // above half an SM's shared memory: one block per SM
+
+struct FusedArgs {
+  PoissonArgs p;
+  TempArgs t;                      // explicit temperature update, when with_temp
+  int with_temp;
+  unsigned *fwd_done;              // [groups]
+  unsigned long long *bwd_cnt;     // [spans]
+  unsigned *err;                   // 1: a sweep wait gave up, 2: a worker wait gave up
+  unsigned epoch;
+  int tri_blocks, tri_warps, lines, groups;
+};
+
+__device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed_u32(unsigned *p, unsigned v) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// one component of 32 modes (lines[lg]); false when a wait gave up
+__device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
+  const DevGrid &g = a.p.g;
+  const int lane = threadIdx.x & 31, nx = g.nx, C = a.p.cols;
+  const int J0 = (lg >> 1) * 32, J = J0 + lane;
+  const bool act = J < g.nh;
+  const int Jc = act ? J : J0;
+  const size_t jp = (size_t)g.jpitch, vs = 2 * jp;
+  double *col = reinterpret_cast<double *>(a.p.spec + Jc) + (lg & 1);
+  const double *inv = g.pinv + Jc, *up = g.pup + Jc;
+  int vg = 0;  // groups 0 .. vg-1 are verified complete
+  // make rows up to x readable: the lanes read the next 64
+  // completion flags (two each, relaxed), the leading run of complete groups
+  // is taken (polling while x's group is not among them), and one fence then
+  // orders the row reads after them
+  auto need = [&](int x) -> bool {
+    const int gx = x / C;
+    if (gx < vg) return true;
+    unsigned spin = 0;
+    while (vg <= gx) {
+      const int g0 = vg + lane, g1 = vg + 32 + lane;
+      const bool ok0 = g0 >= a.groups || ld_relaxed_u32(a.fwd_done + g0) == a.epoch;
+      const bool ok1 = g1 >= a.groups || ld_relaxed_u32(a.fwd_done + g1) == a.epoch;
+      const unsigned n0 = __ballot_sync(0xffffffffu, !ok0), n1 = __ballot_sync(0xffffffffu, !ok1);
+      const int run = n0 ? __ffs(n0) - 1 : (n1 ? 32 + __ffs(n1) - 1 : 64);
+      vg = min(vg + run, a.groups);
+      if (vg <= gx) {
+        if (++spin >= kFusedSpin) return false;
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    return true;
+  };
+  // ---- forward elimination (src/linalg.c:33-45)
+  if (!need(0)) return false;
+  double prev = __ldcg(col) / g.pd0[Jc];
+  if (act) col[0] = prev;
+  double cq[kLineChunk], ci[kLineChunk];
+  if (nx > 1 && !need(min(kLineChunk, nx - 1))) return false;
+#pragma unroll
+  for (int k = 0; k < kLineChunk; ++k) {
+    const int e = 1 + k;
+    cq[k] = e < nx ? __ldcg(col + (size_t)e * vs) : 0.0;
+    ci[k] = e < nx ? __ldg(inv + (size_t)e * jp) : 0.0;
+  }
+#pragma unroll 1
+  for (int b = 1; b < nx; b += kLineChunk) {
+    double nq[kLineChunk], ni[kLineChunk];
+    const int nb = b + kLineChunk;
+    if (nb < nx && !need(min(nb + kLineChunk - 1, nx - 1))) return false;
+#pragma unroll
+    for (int k = 0; k < kLineChunk; ++k) {
+      const int e = nb + k;
+      nq[k] = e < nx ? __ldcg(col + (size_t)e * vs) : 0.0;
+      ni[k] = e < nx ? __ldg(inv + (size_t)e * jp) : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < kLineChunk; ++k) {
+      const int x = b + k;
+      if (x < nx) {
+        const double iv = ci[k];
+        // |pivot| < DBL_EPSILON rows carry 1/pivot = +0: the reference sets them to 0
+        const double v = __double_as_longlong(iv) == 0 ? 0.0 : iv * (cq[k] - pl[x] * prev);
+        if (act) col[(size_t)x * vs] = v;
+        prev = v;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kLineChunk; ++k) {
+      cq[k] = nq[k];
+      ci[k] = ni[k];
+    }
+  }
+  // ---- back substitution (src/linalg.c:46-48), x = nx-2 .. 0; span s is
+  // final once x passes its lowest element
+  auto signal = [&](int s) {
+    __threadfence();
+    __syncwarp();
+    if (lane == 0) atomicAdd(a.bwd_cnt + s, 1ull);
+  };
+  const int top = (nx - 1) / kFusedSpan;
+  if (top * kFusedSpan > nx - 2) signal(top);  // a top span holding only x = nx-1
+  double next = prev;
+  double cu[kLineChunk];
+  const int hi = nx - 2;
+#pragma unroll
+  for (int k = 0; k < kLineChunk; ++k) {
+    const int e = hi - k;
+    cq[k] = e >= 0 ? __ldcg(col + (size_t)e * vs) : 0.0;
+    cu[k] = e >= 0 ? __ldg(up + (size_t)e * jp) : 0.0;
+  }
+#pragma unroll 1
+  for (int b = hi; b >= 0; b -= kLineChunk) {
+    double nq[kLineChunk], nu[kLineChunk];
+#pragma unroll
+    for (int k = 0; k < kLineChunk; ++k) {
+      const int e = b - kLineChunk - k;
+      nq[k] = e >= 0 ? __ldcg(col + (size_t)e * vs) : 0.0;
+      nu[k] = e >= 0 ? __ldg(up + (size_t)e * jp) : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < kLineChunk; ++k) {
+      const int x = b - k;
+      if (x >= 0) {
+        const double v = cq[k] - cu[k] * next;
+        if (act) col[(size_t)x * vs] = v;
+        next = v;
+        if (x % kFusedSpan == 0) signal(x / kFusedSpan);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kLineChunk; ++k) {
+      cq[k] = nq[k];
+      cu[k] = nu[k];
+    }
+  }
+  return true;
+}
+
+template <bool RCP>
+__global__ void __launch_bounds__(kFusedThreads, 1) k_poisson_fused(const FusedArgs a) {
+  extern __shared__ double2 fz[];
+  const DevGrid &g = a.p.g;
+  const int nx = g.nx, C = a.p.cols;
+  if ((int)blockIdx.x < a.tri_blocks) {
+    double *pl = reinterpret_cast<double *>(fz);
+    for (int x = threadIdx.x; x < nx; x += blockDim.x) pl[x] = g.pl[x];
+    __syncthreads();
+    const int w = threadIdx.x >> 5;
+    const int lg = blockIdx.x * a.tri_warps + w;
+    if (w >= a.tri_warps || lg >= a.lines) return;
+    if (!fused_sweep(a, pl, lg) && (threadIdx.x & 31) == 0) atomicOr(a.err, 1u);
+    return;
+  }
+  __shared__ int s_ok;
+  const int wk = blockIdx.x - a.tri_blocks, W = gridDim.x - a.tri_blocks;
+  // forward DFT column groups, ascending x
+  for (int gi = wk; gi < a.groups; gi += W) {
+    poisson_fwd_cols<RCP>(a.p, gi * C, fz);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      st_relaxed_u32(a.fwd_done + gi, a.epoch);
+    }
+  }
+  // explicit temperature update, while the sweeps run
+  if (a.with_temp) {
+    const int xb = (nx + kFusedThreads - 1) / kFusedThreads, yb = (g.ny + kRows - 1) / kRows;
+    for (int u = wk; u < xb * yb; u += W) {
+      const int x = (u % xb) * kFusedThreads + threadIdx.x;
+      if (x < nx) temp_column<0, 0, RCP>(a.t, x, (u / xb) * kRows);
+    }
+  }
+  // inverse DFT column groups, descending x, once every sweep warp passed them
+  const unsigned long long target = (unsigned long long)a.epoch * (unsigned long long)a.lines;
+  for (int k = wk; k < a.groups; k += W) {
+    const int gi = a.groups - 1 - k;
+    if (threadIdx.x == 0) {
+      const int s = gi * C / kFusedSpan;
+      unsigned spin = 0;
+      unsigned long long v;
+      while ((v = ld_relaxed_u64(a.bwd_cnt + s)) < target && ++spin < kFusedSpin) __nanosleep(128);
+      s_ok = v >= target;
+      if (!s_ok) atomicOr(a.err, 2u);
+      __threadfence();
+    }
+    __syncthreads();
+    if (!s_ok) return;
+    poisson_bwd_cols<true>(a.p, gi * C, fz);
+    __syncthreads();
   }
 }
 
@@ -876,6 +1122,66 @@ cudaError_t launch_poisson_tri(const DevGrid &g, double2 *spec, cudaStream_t st)
   k_poisson_tri<<<dim3((g.nh + 31) / 32, 2), 32, smem, st>>>(g, spec);
   count_launches(1);
   return cudaGetLastError();
+}
+
+static int fused_cols(const DevGrid &g) {
+  return (g.nx > 1024 && (size_t)2 * g.ny * sizeof(double) <= 160 * 1024) ? 2 : 1;
+}
+
+void fused_layout(const DevGrid &g, int *groups, int *spans) {
+  const int C = fused_cols(g);
+  *groups = (g.nx + C - 1) / C;
+  *spans = (g.nx + kFusedSpan - 1) / kFusedSpan;
+}
+
+cudaError_t launch_poisson_fused(const DevGrid &g, const StageScalars &s, const double *ux, const double *uy,
+                                 double2 *spec, double *psi, const double *t_in, double *t_out, double *at,
+                                 const double *ux_k, const double *uy_k, FusedState &fs, cudaStream_t st) {
+  int dev = 0, sms = 0, coop = 0;
+  cudaError_t e;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev)) != cudaSuccess) return e;
+  const int C = fused_cols(g);
+  const int lines = 2 * ((g.nh + 31) / 32);
+  const int tri_warps = kFusedTriWarps;
+  const int tri_blocks = (lines + tri_warps - 1) / tri_warps;
+  const size_t smem = std::max({sizeof(double) * (size_t)g.nx, (size_t)C * g.ny * sizeof(double), kFusedMinSmem});
+  if (!coop || g.nx > kTriMaxNx || smem > 200 * 1024 || sms - tri_blocks < 8) return cudaErrorNotSupported;
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_poisson_fused<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_poisson_fused<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    attr = true;
+  }
+  int per_sm = 0;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, g.rcp ? (const void *)k_poisson_fused<true>
+                                                                        : (const void *)k_poisson_fused<false>,
+                                                         kFusedThreads, smem)) != cudaSuccess)
+    return e;
+  if (per_sm < 1) return cudaErrorNotSupported;
+  FusedArgs a{};
+  a.p = PoissonArgs{g, s, ux, uy, spec, psi, C};
+  a.t = TempArgs{g, s, t_in, t_out, at, nullptr, ux_k, uy_k};
+  a.with_temp = t_out != nullptr;
+  a.fwd_done = fs.fwd_done;
+  a.bwd_cnt = fs.bwd_cnt;
+  a.err = fs.err;
+  a.epoch = ++fs.epoch;
+  a.tri_blocks = tri_blocks;
+  a.tri_warps = tri_warps;
+  a.lines = lines;
+  int spans = 0;
+  fused_layout(g, &a.groups, &spans);
+  void *args[] = {&a};
+  e = cudaLaunchCooperativeKernel(g.rcp ? (const void *)k_poisson_fused<true> : (const void *)k_poisson_fused<false>,
+                                  dim3(sms), dim3(kFusedThreads), args, smem, st);
+  if (e != cudaSuccess) {
+    --fs.epoch;
+    return e;
+  }
+  count_launches(1);
+  return cudaSuccess;
 }
 
 cudaError_t launch_poisson_bwd(const DevGrid &g, const StageScalars &s, const double2 *spec, double *psi,

@@ -80,6 +80,12 @@ struct Context {
   double *fac = nullptr;
   size_t fac_words = 0;
   double *diag = nullptr;  // block partials of sns_diagnostics
+  // fused Poisson (+ temperature) launches: flag words, on unless disabled
+  // or unsupported for this size
+  bool fused = true;
+  bool fused_ready = false;
+  FusedState fz;
+  unsigned *fz_err_host = nullptr;  // pinned
   // asynchronous checkpoint (sns_checkpoint): a device snapshot of ux, uy, p
   // and T taken on the solver's stream, its copy to pinned memory on ck_stream,
   // and a host thread that writes the files
@@ -201,6 +207,7 @@ static void destroy_context(Context *c) {
   c->allocs.clear();
   if (c->staging) cudaFreeHost(c->staging);
   if (c->red_host) cudaFreeHost(c->red_host);
+  if (c->fz_err_host) cudaFreeHost(c->fz_err_host);
   if (c->ev_fwd) cudaEventDestroy(c->ev_fwd);
   if (c->ev_temp) cudaEventDestroy(c->ev_temp);
   if (c->side) cudaStreamDestroy(c->side);
@@ -711,9 +718,71 @@ static int poisson_rest(Context *c, const StageScalars &s, Fields &f) {
   return SNS_OK;
 }
 
-static int poisson(Context *c, const StageScalars &s, Fields &f) {
+// flag words of the fused launch, allocated and zeroed on first use
+static int fused_prepare(Context *c) {
+  if (c->fused_ready) return SNS_OK;
+  int groups = 0, spans = 0;
+  fused_layout(c->g, &groups, &spans);
+  if (int rc = dev_alloc(c, &c->fz.fwd_done, (size_t)groups)) return rc;
+  if (int rc = dev_alloc(c, &c->fz.bwd_cnt, (size_t)spans)) return rc;
+  if (int rc = dev_alloc(c, &c->fz.err, (size_t)1)) return rc;
+  SNS_CUDA(cudaMemsetAsync(c->fz.fwd_done, 0, sizeof(unsigned) * groups, c->stream));
+  SNS_CUDA(cudaMemsetAsync(c->fz.bwd_cnt, 0, sizeof(unsigned long long) * spans, c->stream));
+  SNS_CUDA(cudaMemsetAsync(c->fz.err, 0, sizeof(unsigned), c->stream));
+  if (!c->fz_err_host) SNS_CUDA(cudaMallocHost(&c->fz_err_host, sizeof(unsigned)));
+  *c->fz_err_host = 0;
+  c->fz.epoch = 0;
+  c->fused_ready = true;
+  return SNS_OK;
+}
+
+// after a stream synchronisation: a fused launch whose wait gave up leaves
+// its results undefined; report it, reset the flags and stop fusing
+static int fused_check(Context *c) {
+  if (!c->fused_ready || !c->fz_err_host || *c->fz_err_host == 0) return SNS_OK;
+  const unsigned code = *c->fz_err_host;
+  *c->fz_err_host = 0;
+  c->fused = false;
+  c->fused_ready = false;
+  return fail(SNS_ERR_STATE, "fused Poisson launch: a %s wait gave up (code %u); results of that step are invalid",
+              (code & 1) ? "sweep" : "worker", code);
+}
+
+static int fused_enqueue_err(Context *c) {
+  if (c->fused_ready)
+    SNS_CUDA(cudaMemcpyAsync(c->fz_err_host, c->fz.err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+  return SNS_OK;
+}
+
+// the Poisson solve as one fused launch when possible (temperature update
+// folded in when t_out is given), else as three kernels; *fused_out tells
+// which ran
+static int poisson_any(Context *c, const StageScalars &s, Fields &f, const double *t_in, double *t_out, double *at,
+                       const double *ux_k, const double *uy_k, bool *fused_out) {
+  *fused_out = false;
+  if (c->fused) {
+    if (int rc = fused_prepare(c)) return rc;
+    cudaError_t e;
+    {
+      Prof pf(c, K_POI_FUSED);
+      e = launch_poisson_fused(c->g, s, f.ux, f.uy, f.spec, f.psi, t_in, t_out, at, ux_k, uy_k, c->fz, c->stream);
+    }
+    if (e == cudaSuccess) {
+      *fused_out = true;
+      return SNS_OK;
+    }
+    if (e != cudaErrorNotSupported && e != cudaErrorCooperativeLaunchTooLarge)
+      return fail(SNS_ERR_CUDA, "fused Poisson launch: %s", cudaGetErrorString(e));
+    cudaGetLastError();
+    c->fused = false;  // this size cannot run fused here: three kernels from now on
+  }
   if (int rc = poisson_forward(c, s, f)) return rc;
   return poisson_rest(c, s, f);
+}
+
+static int poisson(Context *c, const StageScalars &s, Fields &f) {
+  bool fused = false;
+  return poisson_any(c, s, f, nullptr, nullptr, nullptr, nullptr, nullptr, &fused);
 }
 
 // dt from the reduction results (src/param/decide_dt.c:11-101)
@@ -778,8 +847,9 @@ static int reduce_to_host(Context *c, Fields &f, bool launch) {
   }
   SNS_CUDA(cudaMemcpyAsync(c->red_host, f.colmax, sizeof(unsigned long long) * (c->nx + 1), cudaMemcpyDeviceToHost,
                            c->stream));
+  if (int rc = fused_enqueue_err(c)) return rc;
   SNS_CUDA(cudaStreamSynchronize(c->stream));
-  return SNS_OK;
+  return fused_check(c);
 }
 
 }  // namespace sns
@@ -1693,7 +1763,7 @@ int sns_diagnostics_static(const param_t *param, const fluid_t *fluid, const tem
 static const char *kKindNames[K_NUM_KINDS] = {
     "temperature_update", "velocity_update", "poisson_forward_fft", "poisson_tridiagonal", "poisson_inverse_fft",
     "correct_and_pressure", "correct_velocity", "update_pressure", "max_velocity", "cn_solve_x", "cn_solve_y",
-    "add_increment"};
+    "add_increment", "poisson_fused"};
 
 int sns_profile(const fluid_t *fluid, int enable) {
   FluidExt *fe = as_fluid(fluid);
@@ -1729,7 +1799,15 @@ const char *sns_profile_kind_name(int kind) {
 int sns_synchronize(const fluid_t *fluid) {
   FluidExt *fe = as_fluid(fluid);
   if (!fe) return fail(SNS_ERR_ARG, "sns_synchronize: bad fluid");
+  if (int rc = fused_enqueue_err(fe->ctx)) return rc;
   SNS_CUDA(cudaStreamSynchronize(fe->ctx->stream));
+  return fused_check(fe->ctx);
+}
+
+int sns_set_fused(const fluid_t *fluid, int on) {
+  FluidExt *fe = as_fluid(fluid);
+  if (!fe) return fail(SNS_ERR_ARG, "sns_set_fused: bad fluid");
+  fe->ctx->fused = on != 0;
   return SNS_OK;
 }
 
@@ -1745,6 +1823,14 @@ void *sns_stream(const fluid_t *fluid) {
 // main stream; the velocity kernel has already taken its buoyancy from the
 // starting T, and the next substage waits for the new T. Same kernels, same
 // inputs, same bits as the sequential order.
+// One time step's substages (src/main.c:80-99) with fused kernels. With the
+// explicit scheme the temperature update of a substage, which reads only the
+// substage's starting T and u, runs inside the fused Poisson launch on the
+// SMs that the latency-bound tridiagonal sweeps leave free (or, when the
+// Poisson solve runs as three kernels, on a side stream during the sweep);
+// the velocity kernel has already taken its buoyancy from the starting T, and
+// the next substage reads the new T. Same kernels' arithmetic, same inputs,
+// same bits as the sequential order.
 static int integrate_impl(const param_t *param, FluidExt *fe, TempExt *te, bool reduce_last) {
   Context *c = fe->ctx;
   Fields &f = fe->f;
@@ -1759,21 +1845,31 @@ static int integrate_impl(const param_t *param, FluidExt *fe, TempExt *te, bool 
     }
     if (int rc = do_velocity_update(param, rk, fe, te)) return rc;
     const StageScalars s = stage_scalars(param, rk);
-    if (int rc = poisson_forward(c, s, f)) return rc;
-    if (overlap) {
-      int out = 0;
+    int out = 0;
+    if (overlap)
       while (out == te->cur || out == te->snap) out++;
-      SNS_CUDA(cudaEventRecord(c->ev_fwd, c->stream));
-      SNS_CUDA(cudaStreamWaitEvent(c->side, c->ev_fwd, 0));
-      {
-        Prof pf(c, K_TEMP, c->side);
-        SNS_CUDA(launch_temp_update(c->g, s, 0, 0, te->f.t[te->cur], te->f.t[out], te->f.at, nullptr, ux_k, uy_k,
-                                    c->side));
-      }
-      SNS_CUDA(cudaEventRecord(c->ev_temp, c->side));
-      te->cur = out;
+    bool fused = false;
+    if (overlap && c->fused) {
+      if (int rc = poisson_any(c, s, f, te->f.t[te->cur], te->f.t[out], te->f.at, ux_k, uy_k, &fused)) return rc;
+      if (fused) te->cur = out;
     }
-    if (int rc = poisson_rest(c, s, f)) return rc;
+    if (!fused) {
+      if (overlap) {
+        if (int rc = poisson_forward(c, s, f)) return rc;
+        SNS_CUDA(cudaEventRecord(c->ev_fwd, c->stream));
+        SNS_CUDA(cudaStreamWaitEvent(c->side, c->ev_fwd, 0));
+        {
+          Prof pf(c, K_TEMP, c->side);
+          SNS_CUDA(launch_temp_update(c->g, s, 0, 0, te->f.t[te->cur], te->f.t[out], te->f.at, nullptr, ux_k, uy_k,
+                                      c->side));
+        }
+        SNS_CUDA(cudaEventRecord(c->ev_temp, c->side));
+        te->cur = out;
+        if (int rc = poisson_rest(c, s, f)) return rc;
+      } else {
+        if (int rc = poisson_any(c, s, f, nullptr, nullptr, nullptr, nullptr, nullptr, &fused)) return rc;
+      }
+    }
     const bool red = reduce_last && rk == RKSTEPMAX - 1;
     if (red) SNS_CUDA(cudaMemsetAsync(f.colmax, 0, sizeof(unsigned long long) * (c->nx + 1), c->stream));
     {
@@ -1782,7 +1878,7 @@ static int integrate_impl(const param_t *param, FluidExt *fe, TempExt *te, bool 
                                        red ? f.colmax : nullptr, red ? f.uymax : nullptr, c->stream));
     }
     // the next substage reads the new T and overwrites the buffer of u_k
-    if (overlap) SNS_CUDA(cudaStreamWaitEvent(c->stream, c->ev_temp, 0));
+    if (overlap && !fused) SNS_CUDA(cudaStreamWaitEvent(c->stream, c->ev_temp, 0));
   }
   return SNS_OK;
 }

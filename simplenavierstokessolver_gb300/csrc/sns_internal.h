@@ -132,6 +132,20 @@ cudaError_t launch_tempforce_to_host(const DevGrid &g, const double *t, double *
 // uy1, uy2, temp1, temp2 [ny][nx+2]; t may be null (no temperature sums)
 cudaError_t launch_stats(const DevGrid &g, const double *ux, const double *uy, const double *t, double *s,
                          cudaStream_t st);
+// fused Poisson solve (+ explicit temperature update): device flag words,
+// sized by fused_layout, zeroed once; epoch advances by one per launch
+struct FusedState {
+  unsigned *fwd_done = nullptr;          // [groups]
+  unsigned long long *bwd_cnt = nullptr; // [spans]
+  unsigned *err = nullptr;               // [1]
+  unsigned epoch = 0;
+};
+void fused_layout(const DevGrid &g, int *groups, int *spans);
+// cudaErrorNotSupported when the device cannot hold the cooperative grid for
+// this size; t_out == nullptr: no temperature update in the launch
+cudaError_t launch_poisson_fused(const DevGrid &g, const StageScalars &s, const double *ux, const double *uy,
+                                 double2 *spec, double *psi, const double *t_in, double *t_out, double *at,
+                                 const double *ux_k, const double *uy_k, FusedState &fs, cudaStream_t st);
 cudaError_t launch_poisson_fwd(const DevGrid &g, const StageScalars &s, const double *ux, const double *uy,
                                double2 *spec, cudaStream_t st);
 cudaError_t launch_poisson_tri(const DevGrid &g, double2 *spec, cudaStream_t st);
@@ -151,7 +165,7 @@ cudaError_t launch_umax(const DevGrid &g, const double *ux, const double *uy, un
 // kernel kinds for the optional per-launch event timing (sns_profile_*)
 enum KernelKind {
   K_TEMP = 0, K_VEL, K_POI_FWD, K_POI_TRI, K_POI_BWD, K_CORR_PRES, K_CORR, K_PRES, K_UMAX, K_SOLVE_X, K_SOLVE_Y,
-  K_ADD_INC, K_NUM_KINDS
+  K_ADD_INC, K_POI_FUSED, K_NUM_KINDS
 };
 
 // counts kernel launches (process-wide)

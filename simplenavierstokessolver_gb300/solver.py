@@ -246,6 +246,10 @@ class Case:
     def run(self, nsteps: int):
         N.check(self.lib.sns_run(self.param, self.parallel, self.fluid, self.temperature, nsteps), "sns_run")
 
+    def set_fused(self, on: bool):
+        """one cooperative launch per Poisson solve (default) or three kernels"""
+        N.check(self.lib.sns_set_fused(self.fluid, int(on)), "sns_set_fused")
+
     def synchronize(self):
         N.check(self.lib.sns_synchronize(self.fluid), "sns_synchronize")
 
