@@ -58,11 +58,14 @@ KERNEL_MODEL = {
 }
 
 
-# DRAM bytes (read + write) per launch from one ncu capture of the default
-# workload (profiles/plain_fp64_512x1024_launches.md); keyed by kernel and size
+# DRAM bytes (read + write) per launch from ncu captures of the default
+# workload (profiles/plain_fp64_fused_512x1024_ncu.md for the fused launch and
+# the velocity update, the three-kernel form's from an earlier capture of the
+# same size); keyed by kernel and size
 PROFILED_TRAFFIC = {
+    ("poisson_fused", 512, 1024): 29669376 + 8960,  # profiles/plain_fp64_fused_512x1024_ncu.md
     ("poisson_tridiagonal", 512, 1024): 8665344,
-    ("velocity_update", 512, 1024): 16838912,
+    ("velocity_update", 512, 1024): 25227776,
     ("poisson_forward_fft", 512, 1024): 8429056,
     ("temperature_update", 512, 1024): 12647168,
     ("poisson_inverse_fft", 512, 1024): 4314880,
