@@ -315,7 +315,9 @@ def fp32_accuracy(args):
 
 def ensemble_throughput(args, torch):
     """64-case ensemble: batched FP32-stencil form (one graph launch per step
-    for all cases) against the plain FP64 path stepping the cases one by one"""
+    for all cases, launch shapes picked by sns_batch_autotune; the default
+    shapes' rate beside it) against the plain FP64 path stepping the cases
+    one by one"""
     from simplenavierstokessolver_gb300 import Case
     from simplenavierstokessolver_gb300.batch import Batch
     from simplenavierstokessolver_gb300.workloads import ensemble
@@ -329,12 +331,20 @@ def ensemble_throughput(args, torch):
         b.step(args.warmup)
         b.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        b.step(args.ens_steps)
-        e1.record(stream)
-        b.synchronize()
-        ms_b = e0.elapsed_time(e1)
+
+        def timed():
+            e0.record(stream)
+            b.step(args.ens_steps)
+            e1.record(stream)
+            b.synchronize()
+            return e0.elapsed_time(e1)
+
+        default_shapes = b.tuning()
+        ms_default = timed()
+        tuned_shapes, _ = b.autotune(steps=5)
+        ms_b = timed()
     batched = cells * args.ens_steps / (ms_b * 1e-3)
+    batched_default = cells * args.ens_steps / (ms_default * 1e-3)
     plain_steps = max(2, args.ens_steps // 5)
     total_s, plain_cells = 0.0, 0
     for d in descs:
@@ -345,7 +355,9 @@ def ensemble_throughput(args, torch):
             total_s += time.perf_counter() - t0
             plain_cells += d.itot * d.jtot
     plain = plain_cells * plain_steps / total_s
-    return {"cases": len(descs), "cells": cells, "batched_fp32_stencil": batched, "plain_fp64_one_by_one": plain,
+    return {"cases": len(descs), "cells": cells, "batched_fp32_stencil": batched,
+            "batched_default_shapes": batched_default, "default_shapes": default_shapes,
+            "autotuned_shapes": tuned_shapes, "plain_fp64_one_by_one": plain,
             "ratio": batched / plain, "unit": "cell-steps/s", "batched_steps": args.ens_steps,
             "plain_steps_per_case": plain_steps,
             "workload": "nx in {64,128,256}, ny=2nx, log10 Ra in [6,9], Pr in [0.7,7], SplitMix64 seeds 20261203+k"}

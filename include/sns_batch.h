@@ -46,6 +46,15 @@ typedef struct sns_case_desc {
   double fixed_dt;           /* > 0: use this dt every step instead of the CFL decision */
 } sns_case_desc;
 
+/* Launch shapes of the step's kernels. The defaults (64, 8, 4, 0) are set at
+ * creation; sns_batch_autotune measures alternatives on the resident cases. */
+typedef struct sns_batch_tuning {
+  int tile_x;          /* stencil / correction block width: 32, 64 or 128 columns */
+  int tile_rows;       /* rows each stencil / correction thread marches: 1 .. 64 */
+  int modes_per_block; /* tridiagonal mode lines (warps) per block: 2, 4 or 8 */
+  int fcols_shift;     /* DFT columns per block: the per-case default times 2^shift, -3 .. 3 */
+} sns_batch_tuning;
+
 /* a batch with a device arena of hbm_bytes and room for max_cases cases */
 extern sns_batch *sns_batch_create(size_t hbm_bytes, int max_cases);
 extern int sns_batch_destroy(sns_batch *batch);
@@ -100,6 +109,20 @@ typedef void (*sns_done_fn)(int request, sns_batch *batch, int slot, void *user)
 extern int sns_serve(const sns_case_desc *reqs, const double *arrival_s, int n, size_t hbm_bytes, int max_cases,
                      int chunk_steps, double *admit_s, double *done_s, double *busy_s, sns_done_fn on_done,
                      void *user);
+
+/* current launch shapes */
+extern int sns_batch_get_tuning(const sns_batch *batch, sns_batch_tuning *tuning);
+/* fixed launch shapes (SNS_ERR_ARG outside the ranges above); results do not
+ * depend on them: every shape computes the same arithmetic per point */
+extern int sns_batch_set_tuning(sns_batch *batch, const sns_batch_tuning *tuning);
+/* Autotuner: a coordinate search over tile_rows {4, 8, 16}, tile_x {32, 64,
+ * 128}, fcols_shift {-1, 0, 1} and modes_per_block {2, 4, 8}, each candidate
+ * timed with CUDA events over `steps` graph replays of the resident cases.
+ * The cases' device state is copied aside (arena up to its high-water mark
+ * and the case table: SNS_ERR_OOM if that much memory is not free) and put
+ * back after every candidate, so tuning leaves every case where it was. The
+ * fastest shapes are kept; chosen and ms_per_step (optional) report them. */
+extern int sns_batch_autotune(sns_batch *batch, int steps, sns_batch_tuning *chosen, double *ms_per_step);
 
 #ifdef __cplusplus
 }

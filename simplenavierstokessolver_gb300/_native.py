@@ -76,6 +76,12 @@ class CaseDesc(ctypes.Structure):
                 ("steps", c_longlong), ("seed", ctypes.c_ulonglong), ("fixed_dt", c_double)]
 
 
+class Tuning(ctypes.Structure):
+    """sns_batch_tuning (include/sns_batch.h)."""
+
+    _fields_ = [("tile_x", c_int), ("tile_rows", c_int), ("modes_per_block", c_int), ("fcols_shift", c_int)]
+
+
 class Statistics(ctypes.Structure):
     _fields_ = [("num", c_int), ("ux1", _PD), ("ux2", _PD), ("uy1", _PD), ("uy2", _PD), ("temp1", _PD),
                 ("temp2", _PD)]
@@ -150,6 +156,9 @@ PROTOTYPES = {
     "sns_batch_active_cells": (c_longlong, [c_void_p]),
     "sns_batch_initial_temperature": (c_int, [PCD, _PD]),
     "sns_batch_diagnostics": (c_int, [c_void_p, c_int, _PD]),
+    "sns_batch_get_tuning": (c_int, [c_void_p, POINTER(Tuning)]),
+    "sns_batch_set_tuning": (c_int, [c_void_p, POINTER(Tuning)]),
+    "sns_batch_autotune": (c_int, [c_void_p, c_int, POINTER(Tuning), _PD]),
     "sns_serve": (c_int, [PCD, _PD, c_int, c_size_t, c_int, c_int, _PD, _PD, _PD, c_void_p, c_void_p]),
 }
 

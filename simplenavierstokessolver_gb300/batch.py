@@ -123,6 +123,22 @@ class Batch:
                                                ctypes.byref(done)), "sns_batch_case_status")
         return {"time": t.value, "dt": dt.value, "step": st.value, "done": bool(done.value)}
 
+    def tuning(self) -> dict:
+        t = N.Tuning()
+        N.check(self.lib.sns_batch_get_tuning(self.h, ctypes.byref(t)), "sns_batch_get_tuning")
+        return {f: getattr(t, f) for f, _ in N.Tuning._fields_}
+
+    def set_tuning(self, **kw):
+        t = N.Tuning(**{**self.tuning(), **kw})
+        N.check(self.lib.sns_batch_set_tuning(self.h, ctypes.byref(t)), "sns_batch_set_tuning")
+
+    def autotune(self, steps: int = 5):
+        """pick launch shapes by timing candidates on the resident cases
+        (their state is left unchanged); returns the shapes and ms per step"""
+        t, ms = N.Tuning(), ctypes.c_double()
+        N.check(self.lib.sns_batch_autotune(self.h, steps, ctypes.byref(t), ctypes.byref(ms)), "sns_batch_autotune")
+        return {f: getattr(t, f) for f, _ in N.Tuning._fields_}, ms.value
+
     def diagnostics(self, slot: int) -> np.ndarray:
         return diagnostics_of(self.h, slot)
 

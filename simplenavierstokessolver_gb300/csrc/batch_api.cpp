@@ -260,6 +260,7 @@ struct sns_batch {
   size_t staging_bytes = 0;
   double *diag = nullptr;  // block partials of sns_batch_diagnostics
   size_t diag_words = 0;
+  sns_batch_tuning tune{kBTileX, kBTileY, kBModesPerBlock, 0};
   std::mutex mu;
 };
 
@@ -305,23 +306,41 @@ static int ensure_device_list(T **ptr, size_t *cap, size_t need) {
 }
 
 // work lists for the current case set and the graph of one step
+// DFT columns per block for a case under the current tuning: the admission
+// default scaled by 2^fcols_shift, within [1, 16], nx and 160 KiB of shared memory
+static int tuned_fcols(const sns_batch *b, const CaseHost &h) {
+  int fc = h.fcols;
+  if (b->tune.fcols_shift > 0) fc <<= b->tune.fcols_shift;
+  if (b->tune.fcols_shift < 0) fc >>= -b->tune.fcols_shift;
+  fc = std::max(1, std::min(fc, 16));
+  while (fc > 1 && (fc > h.d.itot || sizeof(double) * (size_t)fc * h.d.jtot > 160 * 1024)) fc >>= 1;
+  return fc;
+}
+
 static int rebuild(sns_batch *b) {
   std::vector<BTile> tiles;
   std::vector<BCols> cols;
   std::vector<BModes> modes;
   size_t smem = 0;
   int threads = 64;
+  const int tx = b->tune.tile_x, ty = b->tune.tile_rows, mpb = b->tune.modes_per_block;
   for (int c = 0; c < b->max_cases; c++) {
     const CaseHost &h = b->hc[c];
     if (!h.used) continue;
     if (h.d.steps > 0 && h.steps_done >= h.d.steps) continue;
     const int nx = h.d.itot, ny = h.d.jtot, nh = ny / 2 + 1;
-    for (int y0 = 0; y0 < ny; y0 += kBTileY)
-      for (int x0 = 0; x0 < nx; x0 += kBTileX) tiles.push_back({c, x0, y0});
-    for (int x0 = 0; x0 < nx; x0 += h.fcols) cols.push_back({c, x0});
-    for (int j0 = 0; j0 < nh; j0 += kBModesPerBlock) modes.push_back({c, j0});
-    smem = std::max(smem, sizeof(double) * (size_t)h.fcols * ny);
-    threads = std::max(threads, std::min(256, (h.fcols * (ny / 2) / 4 + 31) / 32 * 32));
+    const int fc = tuned_fcols(b, h);
+    if (b->table[c].fcols != fc) {  // the kernels read a case's column count from its table entry
+      b->table[c].fcols = fc;
+      BCUDA(cudaMemcpyAsync(reinterpret_cast<char *>(b->d_cases + c) + offsetof(BCase, fcols), &b->table[c].fcols,
+                            sizeof(int), cudaMemcpyHostToDevice, b->stream));
+    }
+    for (int y0 = 0; y0 < ny; y0 += ty)
+      for (int x0 = 0; x0 < nx; x0 += tx) tiles.push_back({c, x0, y0});
+    for (int x0 = 0; x0 < nx; x0 += fc) cols.push_back({c, x0});
+    for (int j0 = 0; j0 < nh; j0 += mpb) modes.push_back({c, j0});
+    smem = std::max(smem, sizeof(double) * (size_t)fc * ny);
+    threads = std::max(threads, std::min(256, (fc * (ny / 2) / 4 + 31) / 32 * 32));
   }
   if (int rc = ensure_device_list(&b->d_tiles, &b->cap_tiles, std::max<size_t>(tiles.size(), 1))) return rc;
   if (int rc = ensure_device_list(&b->d_cols, &b->cap_cols, std::max<size_t>(cols.size(), 1))) return rc;
@@ -351,15 +370,15 @@ static int rebuild(sns_batch *b) {
   BCUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   cudaError_t err = cudaSuccess;
   for (int rk = 0; rk < 3 && err == cudaSuccess; rk++) {
-    if ((err = launch_batch_stencil(b->d_cases, b->d_tiles, b->ntiles, rk, b->stream)) != cudaSuccess) break;
+    if ((err = launch_batch_stencil(b->d_cases, b->d_tiles, b->ntiles, rk, tx, ty, b->stream)) != cudaSuccess) break;
     if ((err = launch_batch_fwd(b->d_cases, b->d_cols, b->ncols, rk, b->fft_smem, b->fft_threads, b->stream)) !=
         cudaSuccess)
       break;
-    if ((err = launch_batch_tri(b->d_cases, b->d_modes, b->nmodes, b->stream)) != cudaSuccess) break;
+    if ((err = launch_batch_tri(b->d_cases, b->d_modes, b->nmodes, mpb, b->stream)) != cudaSuccess) break;
     if ((err = launch_batch_bwd(b->d_cases, b->d_cols, b->ncols, b->fft_smem, b->fft_threads, b->stream)) !=
         cudaSuccess)
       break;
-    if ((err = launch_batch_corr(b->d_cases, b->d_tiles, b->ntiles, rk, b->stream)) != cudaSuccess) break;
+    if ((err = launch_batch_corr(b->d_cases, b->d_tiles, b->ntiles, rk, tx, ty, b->stream)) != cudaSuccess) break;
   }
   if (err == cudaSuccess) err = launch_batch_dt(b->d_cases, b->max_cases, b->rk_a, b->rk_b, b->stream);
   cudaGraph_t g = nullptr;
@@ -666,6 +685,117 @@ int sns_batch_step(sns_batch *b, int nsteps) {
     }
     if (finished_one) b->dirty = true;  // drop finished cases from the work lists
   }
+  return SNS_OK;
+}
+
+static bool valid_tuning(const sns_batch_tuning &t) {
+  return (t.tile_x == 32 || t.tile_x == 64 || t.tile_x == 128) && (t.tile_rows >= 1 && t.tile_rows <= 64) &&
+         (t.modes_per_block == 2 || t.modes_per_block == 4 || t.modes_per_block == 8) && t.fcols_shift >= -3 &&
+         t.fcols_shift <= 3;
+}
+
+int sns_batch_get_tuning(const sns_batch *b, sns_batch_tuning *t) {
+  if (!b || !t) return bfail(SNS_ERR_ARG, "sns_batch_get_tuning: bad argument");
+  *t = b->tune;
+  return SNS_OK;
+}
+
+int sns_batch_set_tuning(sns_batch *b, const sns_batch_tuning *t) {
+  if (!b || !t || !valid_tuning(*t)) return bfail(SNS_ERR_ARG, "sns_batch_set_tuning: bad tuning");
+  std::lock_guard<std::mutex> lk(b->mu);
+  b->tune = *t;
+  b->dirty = true;
+  return SNS_OK;
+}
+
+// Coordinate search over the launch shapes on the resident cases. Their
+// device state (the arena up to its high-water mark and the case table) is
+// copied aside first and put back before every candidate and at the end, so
+// tuning leaves every case exactly where it was.
+int sns_batch_autotune(sns_batch *b, int steps, sns_batch_tuning *chosen, double *ms_per_step) {
+  if (!b || steps < 1) return bfail(SNS_ERR_ARG, "sns_batch_autotune: bad argument");
+  std::lock_guard<std::mutex> lk(b->mu);
+  size_t high = 0;
+  bool any = false;
+  for (const CaseHost &h : b->hc)
+    if (h.used) {
+      high = std::max(high, h.off + h.bytes);
+      any = any || !(h.d.steps > 0 && h.steps_done >= h.d.steps);
+    }
+  if (!any) return bfail(SNS_ERR_STATE, "sns_batch_autotune: no active case to tune on");
+  char *save = nullptr;
+  BCase *save_table = nullptr;
+  if (cudaMalloc((void **)&save, std::max<size_t>(high, 1)) != cudaSuccess ||
+      cudaMalloc((void **)&save_table, sizeof(BCase) * b->max_cases) != cudaSuccess) {
+    cudaGetLastError();
+    if (save) cudaFree(save);
+    return bfail(SNS_ERR_OOM, "sns_batch_autotune: %zu bytes for the state snapshot are not available", high);
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = SNS_OK;
+  auto cuda = [&](cudaError_t e, const char *what) {
+    if (rc == SNS_OK && e != cudaSuccess) rc = bfail(SNS_ERR_CUDA, "sns_batch_autotune: %s: %s", what, cudaGetErrorString(e));
+    return rc == SNS_OK;
+  };
+  std::vector<int> fc0(b->max_cases);
+  for (int c = 0; c < b->max_cases; c++) fc0[c] = b->table[c].fcols;
+  auto restore = [&]() {
+    for (int c = 0; c < b->max_cases; c++) b->table[c].fcols = fc0[c];  // as in the restored device table
+    cuda(cudaMemcpyAsync(b->arena, save, high, cudaMemcpyDeviceToDevice, b->stream), "restore");
+    cuda(cudaMemcpyAsync(b->d_cases, save_table, sizeof(BCase) * b->max_cases, cudaMemcpyDeviceToDevice, b->stream),
+         "restore");
+  };
+  cuda(cudaEventCreate(&e0), "event");
+  cuda(cudaEventCreate(&e1), "event");
+  cuda(cudaMemcpyAsync(save, b->arena, high, cudaMemcpyDeviceToDevice, b->stream), "snapshot");
+  cuda(cudaMemcpyAsync(save_table, b->d_cases, sizeof(BCase) * b->max_cases, cudaMemcpyDeviceToDevice, b->stream),
+       "snapshot");
+  const sns_batch_tuning start = b->tune;
+  auto measure = [&](const sns_batch_tuning &t) -> double {
+    b->tune = t;
+    if (rc != SNS_OK || rebuild(b) != SNS_OK) {
+      if (rc == SNS_OK) rc = SNS_ERR_CUDA;
+      return 1e30;
+    }
+    float ms = 0.f;
+    cuda(cudaGraphLaunch(b->exec, b->stream), "warm-up");  // table's fcols may have changed: one untimed step
+    cuda(cudaEventRecord(e0, b->stream), "event");
+    for (int s = 0; s < steps; s++) cuda(cudaGraphLaunch(b->exec, b->stream), "step");
+    cuda(cudaEventRecord(e1, b->stream), "event");
+    cuda(cudaEventSynchronize(e1), "sync");
+    cuda(cudaEventElapsedTime(&ms, e0, e1), "timing");
+    restore();
+    return rc == SNS_OK ? ms / steps : 1e30;
+  };
+  sns_batch_tuning best = start;
+  double best_ms = measure(best);
+  const int rows[] = {4, 8, 16}, widths[] = {32, 64, 128}, shifts[] = {-1, 0, 1}, mpbs[] = {2, 4, 8};
+  for (int dim = 0; dim < 4 && rc == SNS_OK; dim++) {
+    for (int k = 0; k < 3 && rc == SNS_OK; k++) {
+      sns_batch_tuning t = best;
+      if (dim == 0) t.tile_rows = rows[k];
+      if (dim == 1) t.tile_x = widths[k];
+      if (dim == 2) t.fcols_shift = shifts[k];
+      if (dim == 3) t.modes_per_block = mpbs[k];
+      if (std::memcmp(&t, &best, sizeof t) == 0) continue;
+      const double ms = measure(t);
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = t;
+      }
+    }
+  }
+  b->tune = rc == SNS_OK ? best : start;
+  b->dirty = true;
+  cudaStreamSynchronize(b->stream);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(save);
+  cudaFree(save_table);
+  if (rc != SNS_OK) return rc;
+  if (int r = rebuild(b)) return r;
+  if (chosen) *chosen = best;
+  if (ms_per_step) *ms_per_step = best_ms;
   return SNS_OK;
 }
 

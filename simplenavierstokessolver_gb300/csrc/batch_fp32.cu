@@ -56,15 +56,15 @@ __device__ __forceinline__ F2 ld2(const float *__restrict__ h, const float *__re
 }
 __device__ __forceinline__ float dif(F2 a, F2 b) { return (a.h - b.h) + (a.l - b.l); }
 
-__global__ void __launch_bounds__(kBTileX) k_b_stencil(const BCase *__restrict__ cases,
-                                                      const BTile *__restrict__ tiles, int rk) {
+__global__ void __launch_bounds__(kBTileXMax) k_b_stencil(const BCase *__restrict__ cases,
+                                                         const BTile *__restrict__ tiles, int rk, int rows) {
   const BTile tile = tiles[blockIdx.x];
   const BCase &C = cases[tile.c];
   if (C.done) return;
   const int nx = C.nx, ny = C.ny;
   const int x = tile.x0 + threadIdx.x;
   if (x >= nx) return;
-  const int y0 = tile.y0, y1 = min(y0 + kBTileY, ny);
+  const int y0 = tile.y0, y1 = min(y0 + rows, ny);
   const int pin = C.par ^ (rk & 1), pout = pin ^ 1;
   const float *__restrict__ ux = C.ux[pin];
   const float *__restrict__ uy = C.uy[pin];
@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(256) k_b_bwd(const BCase *__restrict__ cases, 
 // Partition-method solve of the mode lines J = j0 .. j0+3 (one warp each).
 // Per-mode factor block (doubles): inv[nx] up[nx] v[nx] w[nx] alpha[5][32]
 // beta[5][32] rD[32]; rows are indexed by x.
-__global__ void __launch_bounds__(32 * kBModesPerBlock) k_b_tri(const BCase *__restrict__ cases,
+__global__ void __launch_bounds__(32 * kBModesPerBlockMax) k_b_tri(const BCase *__restrict__ cases,
                                                                const BModes *__restrict__ items) {
   const BModes it = items[blockIdx.x];
   const BCase &C = cases[it.c];
@@ -329,8 +329,8 @@ __global__ void __launch_bounds__(32 * kBModesPerBlock) k_b_tri(const BCase *__r
 }
 
 // ---------------------------------------------------- correction and pressure
-__global__ void __launch_bounds__(kBTileX) k_b_corr(BCase *__restrict__ cases, const BTile *__restrict__ tiles,
-                                                   int rk) {
+__global__ void __launch_bounds__(kBTileXMax) k_b_corr(BCase *__restrict__ cases, const BTile *__restrict__ tiles,
+                                                      int rk, int rows) {
   const BTile tl = tiles[blockIdx.x];
   BCase &C = cases[tl.c];
   if (C.done) return;
@@ -339,7 +339,7 @@ __global__ void __launch_bounds__(kBTileX) k_b_corr(BCase *__restrict__ cases, c
   const bool live = x < nx;
   float mx = 0.f, my = 0.f;
   if (live) {
-    const int y0 = tl.y0, y1 = min(y0 + kBTileY, ny);
+    const int y0 = tl.y0, y1 = min(y0 + rows, ny);
     const int pu = C.par ^ (rk & 1) ^ 1;
     float *__restrict__ ux = C.ux[pu];
     float *__restrict__ uy = C.uy[pu];
@@ -426,9 +426,10 @@ cudaError_t batch_kernels_init() {
 }
 
 // the launch helpers below only enqueue: the graph replays are counted by sns_batch_step
-cudaError_t launch_batch_stencil(const BCase *cases, const BTile *tiles, int ntiles, int rk, cudaStream_t st) {
+cudaError_t launch_batch_stencil(const BCase *cases, const BTile *tiles, int ntiles, int rk, int tile_x, int rows,
+                                 cudaStream_t st) {
   if (ntiles == 0) return cudaSuccess;
-  k_b_stencil<<<ntiles, kBTileX, 0, st>>>(cases, tiles, rk);
+  k_b_stencil<<<ntiles, tile_x, 0, st>>>(cases, tiles, rk, rows);
   return cudaGetLastError();
 }
 
@@ -446,15 +447,17 @@ cudaError_t launch_batch_bwd(const BCase *cases, const BCols *cols, int ncols, s
   return cudaGetLastError();
 }
 
-cudaError_t launch_batch_tri(const BCase *cases, const BModes *modes, int nmodes, cudaStream_t st) {
+cudaError_t launch_batch_tri(const BCase *cases, const BModes *modes, int nmodes, int modes_per_block,
+                             cudaStream_t st) {
   if (nmodes == 0) return cudaSuccess;
-  k_b_tri<<<nmodes, 32 * kBModesPerBlock, 0, st>>>(cases, modes);
+  k_b_tri<<<nmodes, 32 * modes_per_block, 0, st>>>(cases, modes);
   return cudaGetLastError();
 }
 
-cudaError_t launch_batch_corr(const BCase *cases, const BTile *tiles, int ntiles, int rk, cudaStream_t st) {
+cudaError_t launch_batch_corr(const BCase *cases, const BTile *tiles, int ntiles, int rk, int tile_x, int rows,
+                              cudaStream_t st) {
   if (ntiles == 0) return cudaSuccess;
-  k_b_corr<<<ntiles, kBTileX, 0, st>>>(const_cast<BCase *>(cases), tiles, rk);
+  k_b_corr<<<ntiles, tile_x, 0, st>>>(const_cast<BCase *>(cases), tiles, rk, rows);
   return cudaGetLastError();
 }
 

@@ -64,19 +64,24 @@ struct BModes {
   int c, j0;
 };
 
-constexpr int kBTileX = 64;
-constexpr int kBTileY = 8;
+constexpr int kBTileX = 64;   // default stencil/correction block width (tunable: 32, 64, 128)
+constexpr int kBTileXMax = 128;
+constexpr int kBTileY = 8;    // default rows per stencil/correction thread (tunable: 4, 8, 16)
 constexpr int kBCorrY = 4;
-constexpr int kBModesPerBlock = 4;
+constexpr int kBModesPerBlock = 4;     // default tridiagonal warps per block (tunable: 2, 4, 8)
+constexpr int kBModesPerBlockMax = 8;
 
 cudaError_t batch_kernels_init();
-cudaError_t launch_batch_stencil(const BCase *cases, const BTile *tiles, int ntiles, int rk, cudaStream_t st);
+cudaError_t launch_batch_stencil(const BCase *cases, const BTile *tiles, int ntiles, int rk, int tile_x, int rows,
+                                 cudaStream_t st);
 cudaError_t launch_batch_fwd(const BCase *cases, const BCols *cols, int ncols, int rk, size_t smem, int threads,
                              cudaStream_t st);
-cudaError_t launch_batch_tri(const BCase *cases, const BModes *modes, int nmodes, cudaStream_t st);
+cudaError_t launch_batch_tri(const BCase *cases, const BModes *modes, int nmodes, int modes_per_block,
+                             cudaStream_t st);
 cudaError_t launch_batch_bwd(const BCase *cases, const BCols *cols, int ncols, size_t smem, int threads,
                              cudaStream_t st);
-cudaError_t launch_batch_corr(const BCase *cases, const BTile *tiles, int ntiles, int rk, cudaStream_t st);
+cudaError_t launch_batch_corr(const BCase *cases, const BTile *tiles, int ntiles, int rk, int tile_x, int rows,
+                              cudaStream_t st);
 cudaError_t launch_batch_dt(BCase *cases, int ncases, const double *rk_a, const double *rk_b, cudaStream_t st);
 
 void count_launches(long long n);

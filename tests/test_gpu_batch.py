@@ -230,3 +230,43 @@ def test_batch_diagnostics_match_host_evaluation():
     scale = np.maximum(np.abs(dr[1:]), 1e-12)
     assert np.all(np.abs(dg[1:] - dr[1:]) <= 1e-10 * scale + 1e-13), (dg, dr)
     assert abs(dg[0] - dr[0]) <= 1e-12 * dr[0]
+
+
+def test_tuning_changes_speed_not_results():
+    """every launch shape computes the same arithmetic per point: results are
+    identical; the autotuner leaves the cases' state untouched"""
+    from simplenavierstokessolver_gb300.batch import Batch, Desc
+
+    descs = [Desc(64, 128, Ra=3e6, Pr=0.7, seed=1), Desc(128, 256, Ra=1e8, Pr=5.0, seed=2),
+             Desc(96, 64, ly=0.5, Ra=1e5, Pr=2.0, seed=3, stretch=4)]
+    shapes = [dict(tile_x=64, tile_rows=8, modes_per_block=4, fcols_shift=0),
+              dict(tile_x=32, tile_rows=16, modes_per_block=8, fcols_shift=1),
+              dict(tile_x=128, tile_rows=4, modes_per_block=2, fcols_shift=-1)]
+    results = []
+    for shape in shapes:
+        with Batch(1 << 30) as b:
+            slots = [b.add(d) for d in descs]
+            b.set_tuning(**shape)
+            b.step(12)
+            results.append([b.state(s) for s in slots])
+    for other in results[1:]:
+        for a, m in zip(results[0], other):
+            for k in a:
+                assert np.array_equal(a[k], m[k]), k
+    with Batch(1 << 30) as b:
+        slots = [b.add(d) for d in descs]
+        b.step(5)
+        before = [b.state(s) for s in slots]
+        st_before = [b.status(s) for s in slots]
+        chosen, ms = b.autotune(steps=3)
+        assert ms > 0 and chosen["tile_x"] in (32, 64, 128)
+        after = [b.state(s) for s in slots]
+        assert [b.status(s) for s in slots] == st_before
+        for a, m in zip(before, after):
+            for k in a:
+                assert np.array_equal(a[k], m[k]), k
+        b.step(7)  # continuing with the tuned shapes gives the untuned run's results
+        tuned = [b.state(s) for s in slots]
+    for a, m in zip(results[0], tuned):
+        for k in a:
+            assert np.array_equal(a[k], m[k]), k
