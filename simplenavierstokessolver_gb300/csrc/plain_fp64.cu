@@ -339,10 +339,12 @@ __device__ __forceinline__ void line_backward(double *q, size_t s, const double 
 //         update_velocity.c:509-516)
 // mode 1: ux rows x = 1..nx-1 of the (itot+1)-system whose rows 0 and itot are
 //         identity rows with zero right-hand side (update_velocity.c:249-253)
-__global__ void __launch_bounds__(32) k_solve_x(int nx, int ny, LineFactors f, int mode, double *q) {
+__global__ void __launch_bounds__(32) k_solve_x(int nx, int ny, const SolveXSet set) {
   const int y = blockIdx.x * blockDim.x + threadIdx.x;
   if (y >= ny) return;
-  double *row = q + (size_t)y * nx;
+  const LineFactors &f = set.f[blockIdx.y];
+  const int mode = set.mode[blockIdx.y];
+  double *row = set.q[blockIdx.y] + (size_t)y * nx;
   double prev = 0.0;
   if (mode == 0) {
     prev = row[0] / f.d0;
@@ -354,11 +356,12 @@ __global__ void __launch_bounds__(32) k_solve_x(int nx, int ny, LineFactors f, i
 }
 
 // src/linalg.c:52-108 applied per column along y (periodic), coalesced across x.
-__global__ void __launch_bounds__(32) k_solve_y(int nx, int ny, PeriodicFactors f, int first_col, double *q) {
-  const int x = first_col + blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(32) k_solve_y(int nx, int ny, const SolveYSet set) {
+  const int x = set.first_col[blockIdx.y] + blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= nx) return;
+  const PeriodicFactors &f = set.f[blockIdx.y];
   const int n = ny;
-  double *col = q + x;
+  double *col = set.q[blockIdx.y] + x;
   const size_t s = (size_t)nx;
   const LineFactors &sub = f.sub;
   double prev = col[0] / sub.d0;
@@ -990,17 +993,36 @@ cudaError_t launch_velocity_update(const DevGrid &g, const StageScalars &s, int 
   return cudaGetLastError();
 }
 
-cudaError_t launch_solve_x(const DevGrid &g, const LineFactors &f, int mode, double *q, cudaStream_t st) {
-  k_solve_x<<<(g.ny + 31) / 32, 32, 0, st>>>(g.nx, g.ny, f, mode, q);
+cudaError_t launch_solve_x_set(const DevGrid &g, const SolveXSet &set, cudaStream_t st) {
+  if (set.n < 1 || set.n > 3) return cudaErrorInvalidValue;
+  k_solve_x<<<dim3((g.ny + 31) / 32, set.n), 32, 0, st>>>(g.nx, g.ny, set);
   count_launches(1);
   return cudaGetLastError();
 }
 
-cudaError_t launch_solve_y(const DevGrid &g, const PeriodicFactors &f, int first_col, double *q, cudaStream_t st) {
-  const int cols = g.nx - first_col;
-  k_solve_y<<<(cols + 31) / 32, 32, 0, st>>>(g.nx, g.ny, f, first_col, q);
+cudaError_t launch_solve_y_set(const DevGrid &g, const SolveYSet &set, cudaStream_t st) {
+  if (set.n < 1 || set.n > 3) return cudaErrorInvalidValue;
+  k_solve_y<<<dim3((g.nx + 31) / 32, set.n), 32, 0, st>>>(g.nx, g.ny, set);
   count_launches(1);
   return cudaGetLastError();
+}
+
+cudaError_t launch_solve_x(const DevGrid &g, const LineFactors &f, int mode, double *q, cudaStream_t st) {
+  SolveXSet set{};
+  set.f[0] = f;
+  set.mode[0] = mode;
+  set.q[0] = q;
+  set.n = 1;
+  return launch_solve_x_set(g, set, st);
+}
+
+cudaError_t launch_solve_y(const DevGrid &g, const PeriodicFactors &f, int first_col, double *q, cudaStream_t st) {
+  SolveYSet set{};
+  set.f[0] = f;
+  set.first_col[0] = first_col;
+  set.q[0] = q;
+  set.n = 1;
+  return launch_solve_y_set(g, set, st);
 }
 
 cudaError_t launch_add_increment(const DevGrid &g, int kind, const double *in, const double *q, double *out,

@@ -596,8 +596,14 @@ static int push_factors(Context *c, const HostFactors &hf, size_t off, LineFacto
   return SNS_OK;
 }
 
+// factor layout: one x system at 0 and one y system at 4(nx+1) for the
+// reference-named calls; three x systems (stride 3(nx+2)) and two y systems
+// (stride 4 ny) after 9(nx+2) for the merged sweeps of the fused step
+static size_t xset_off(const Context *c, int k) { return (size_t)k * 3 * (c->nx + 2); }
+static size_t yset_off(const Context *c, int k) { return 9 * (size_t)(c->nx + 2) + (size_t)k * 4 * c->ny; }
+
 static int ensure_factor_buffer(Context *c) {
-  const size_t need = 4 * (size_t)(c->nx + 1) + 5 * (size_t)c->ny + 16;
+  const size_t need = std::max(4 * (size_t)(c->nx + 1) + 5 * (size_t)c->ny, yset_off(c, 2)) + 16;
   if (c->fac_words >= need) return SNS_OK;
   if (int rc = dev_alloc(c, &c->fac, need)) return rc;
   c->fac_words = need;
@@ -695,6 +701,91 @@ static int do_velocity_update(const param_t *param, int rk, FluidExt *fe, const 
     SNS_CUDA(launch_add_increment(c->g, 1, f.ux, f.qx, f.ux_alt, c->stream));
     SNS_CUDA(launch_add_increment(c->g, 0, f.uy, f.qy, f.uy_alt, c->stream));
   }
+  std::swap(f.ux, f.ux_alt);
+  std::swap(f.uy, f.uy_alt);
+  return SNS_OK;
+}
+
+// The implicit-scheme substage updates of the fused step: temperature and
+// velocity sources first, then the Crank-Nicolson sweeps of the three fields
+// side by side (one launch per direction), then the increments. Each field
+// goes through exactly the operations of do_temp_update / do_velocity_update
+// on the same inputs (the velocity sources read the starting T, which the
+// temperature increment does not touch); only independent launches merge.
+static int implicit_updates(const param_t *param, int rk, FluidExt *fe, TempExt *te) {
+  Context *c = fe->ctx;
+  Fields &f = fe->f;
+  const int impx = param->implicitx, impy = param->implicity;
+  const bool with_t = param->with_temperature && te;
+  const StageScalars s = stage_scalars(param, rk);
+  if (int rc = ensure_implicit_buffers(fe)) return rc;
+  int out = 0;
+  if (with_t) {
+    if (!te->f.qt)
+      if (int rc = dev_alloc(c, &te->f.qt, (size_t)c->nx * c->ny)) return rc;
+    while (out == te->cur || out == te->snap) out++;
+    Prof pf(c, K_TEMP);
+    SNS_CUDA(launch_temp_update(c->g, s, impx, impy, te->f.t[te->cur], te->f.t[out], te->f.at, te->f.qt, f.ux, f.uy,
+                                c->stream));
+  }
+  const double *tf = (te && te->snap >= 0) ? te->f.t[te->snap] : nullptr;
+  {
+    Prof pf(c, K_VEL);
+    SNS_CUDA(launch_velocity_update(c->g, s, impx, impy, f.ux, f.uy, f.p, tf, f.ux_alt, f.uy_alt, f.aux, f.auy, f.qx,
+                                    f.qy, c->stream));
+  }
+  // fields: temperature (if coupled), ux, uy
+  const int kinds[3] = {0, 1, 2};
+  double *qs[3] = {with_t ? te->f.qt : nullptr, f.qx, f.qy};
+  if (impx) {
+    SolveXSet set{};
+    for (int k = with_t ? 0 : 1; k < 3; k++) {
+      HostFactors hf;
+      x_system(param, rk, kinds[k], hf);
+      if (int rc = push_factors(c, hf, xset_off(c, k), set.f[set.n])) return rc;
+      set.mode[set.n] = kinds[k] == 1 ? 1 : 0;
+      set.q[set.n] = qs[k];
+      set.n++;
+    }
+    Prof pf(c, K_SOLVE_X);
+    SNS_CUDA(launch_solve_x_set(c->g, set, c->stream));
+  }
+  if (impy) {
+    SolveYSet set{};
+    for (int sys = with_t ? 0 : 1; sys < 2; sys++) {  // y systems: temperature, velocity
+      HostFactors sub;
+      std::vector<double> q1;
+      PeriodicFactors pf{};
+      y_system(param, rk, sys == 0 ? 1 : 0, sub, q1, pf.l_last, pf.u_last, pf.den);
+      const size_t off = yset_off(c, sys);
+      if (int rc = push_factors(c, sub, off, pf.sub)) return rc;
+      const size_t qoff = off + 3 * sub.l.size();
+      SNS_CUDA(cudaMemcpyAsync(c->fac + qoff, q1.data(), q1.size() * sizeof(double), cudaMemcpyHostToDevice,
+                               c->stream));
+      pf.q1 = c->fac + qoff;
+      if (sys == 0) {
+        set.f[set.n] = pf;
+        set.first_col[set.n] = 0;
+        set.q[set.n++] = te->f.qt;
+      } else {
+        set.f[set.n] = pf;
+        set.first_col[set.n] = 1;  // ux
+        set.q[set.n++] = f.qx;
+        set.f[set.n] = pf;
+        set.first_col[set.n] = 0;  // uy
+        set.q[set.n++] = f.qy;
+      }
+    }
+    Prof pr(c, K_SOLVE_Y);
+    SNS_CUDA(launch_solve_y_set(c->g, set, c->stream));
+  }
+  {
+    Prof pf(c, K_ADD_INC);
+    if (with_t) SNS_CUDA(launch_add_increment(c->g, 0, te->f.t[te->cur], te->f.qt, te->f.t[out], c->stream));
+    SNS_CUDA(launch_add_increment(c->g, 1, f.ux, f.qx, f.ux_alt, c->stream));
+    SNS_CUDA(launch_add_increment(c->g, 0, f.uy, f.qy, f.uy_alt, c->stream));
+  }
+  if (with_t) te->cur = out;
   std::swap(f.ux, f.ux_alt);
   std::swap(f.uy, f.uy_alt);
   return SNS_OK;
@@ -1838,12 +1929,13 @@ static int integrate_impl(const param_t *param, FluidExt *fe, TempExt *te, bool 
     const bool with_t = param->with_temperature && te;
     const bool overlap = with_t && !param->implicitx && !param->implicity;
     const double *ux_k = f.ux, *uy_k = f.uy;  // the velocity this substage starts from
-    if (with_t) {
-      te->snap = param->with_thermal_forcing ? te->cur : -1;
-      if (!overlap)
-        if (int rc = do_temp_update(param, rk, fe, te)) return rc;
+    const bool implicit = param->implicitx || param->implicity;
+    if (with_t) te->snap = param->with_thermal_forcing ? te->cur : -1;
+    if (implicit) {
+      if (int rc = implicit_updates(param, rk, fe, te)) return rc;
+    } else {
+      if (int rc = do_velocity_update(param, rk, fe, te)) return rc;
     }
-    if (int rc = do_velocity_update(param, rk, fe, te)) return rc;
     const StageScalars s = stage_scalars(param, rk);
     int out = 0;
     if (overlap)

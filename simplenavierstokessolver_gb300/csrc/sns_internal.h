@@ -107,6 +107,22 @@ cudaError_t launch_velocity_update(const DevGrid &g, const StageScalars &s, int 
 // (mode 0: first row divides by d0 (T, uy); mode 1: ux rows 2..nx with a zero row before)
 cudaError_t launch_solve_x(const DevGrid &g, const LineFactors &f, int mode, double *q, cudaStream_t st);
 cudaError_t launch_solve_y(const DevGrid &g, const PeriodicFactors &f, int first_col, double *q, cudaStream_t st);
+// up to three independent fields (temperature, ux, uy) in one launch: their
+// serial sweeps run side by side
+struct SolveXSet {
+  LineFactors f[3];
+  int mode[3];
+  double *q[3];
+  int n;
+};
+struct SolveYSet {
+  PeriodicFactors f[3];
+  int first_col[3];
+  double *q[3];
+  int n;
+};
+cudaError_t launch_solve_x_set(const DevGrid &g, const SolveXSet &s, cudaStream_t st);
+cudaError_t launch_solve_y_set(const DevGrid &g, const SolveYSet &s, cudaStream_t st);
 // out = in + q on the interior (kind 0: T/uy all x; kind 1: ux x >= 1)
 cudaError_t launch_add_increment(const DevGrid &g, int kind, const double *in, const double *q, double *out,
                                  cudaStream_t st);
