@@ -273,6 +273,55 @@ def fp32_single(args, torch):
             "l2": "flushed between timed steps (256 MiB write)"}
 
 
+def large_instance(args, torch, nx=2048, ny=4096, Ra=1e10, steps=10):
+    """the 2048 x 4096, Ra 1e10 instance: plain FP64 (sns_run, treatment by
+    param_decide_dt with the fixed cost table) and the FP32-stencil form, per
+    step with CUDA events after warm-up; the plain path's per-kernel times"""
+    import ctypes
+
+    from simplenavierstokessolver_gb300 import Case
+    from simplenavierstokessolver_gb300.batch import Batch, Desc
+
+    cells = nx * ny
+    out = {"workload": f"rayleigh_benard_{nx}x{ny}_Ra{Ra:.0e}_Pr1", "steps": steps}
+    with Case(nx, ny, ly=2.0, Ra=Ra, Pr=1.0) as c:
+        lib = c.lib
+        stream = torch.cuda.ExternalStream(c.stream())
+        c.run(3)
+        c.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        c.run(steps)
+        e1.record(stream)
+        c.synchronize()
+        ms = e0.elapsed_time(e1)
+        d = c.get_dt()
+        lib.sns_profile(c.fluid, 1)
+        c.run(2)
+        c.synchronize()
+        kms = (ctypes.c_double * 32)()
+        kcnt = (ctypes.c_longlong * 32)()
+        n = lib.sns_profile_read(c.fluid, kms, kcnt, 32)
+        lib.sns_profile(c.fluid, 0)
+        kernels = {lib.sns_profile_kind_name(k).decode(): round(1e3 * kms[k] / kcnt[k], 1) for k in range(n) if kcnt[k]}
+    out["plain_fp64"] = {"value": cells * steps / (ms * 1e-3), "ms_per_step": ms / steps,
+                         "scheme": f"implicit x {d['implicitx']}, implicit y {d['implicity']}",
+                         "kernel_avg_us": kernels}
+    with Batch(16 << 30) as b:
+        b.add(Desc(nx, ny, ly=2.0, Ra=Ra, Pr=1.0))
+        stream = torch.cuda.ExternalStream(b.stream())
+        b.step(3)
+        b.synchronize()
+        e0.record(stream)
+        b.step(steps)
+        e1.record(stream)
+        b.synchronize()
+        ms = e0.elapsed_time(e1)
+    out["fp32_stencil"] = {"value": cells * steps / (ms * 1e-3), "ms_per_step": ms / steps,
+                           "scheme": "explicit x / explicit y (batched form)"}
+    return out
+
+
 def fp32_accuracy(args):
     """The FP32-stencil form against the bit-exact FP64 path (identical to the
     reference) over args.acc_steps steps with the same dt sequence: the
@@ -355,9 +404,33 @@ def ensemble_throughput(args, torch):
             total_s += time.perf_counter() - t0
             plain_cells += d.itot * d.jtot
     plain = plain_cells * plain_steps / total_s
+    # the plain path at its best on many small cases: every case on its own
+    # stream with its first CFL dt kept fixed (no per-step host decision), the
+    # Poisson solve as three kernels (the fused launch takes the whole GPU),
+    # steps issued round-robin so that the cases' kernels overlap
+    cases = [Case(d.itot, d.jtot, ly=d.ly, Ra=d.Ra, Pr=d.Pr) for d in descs]
+    try:
+        for c in cases:
+            c.set_fused(False)
+            c.param_decide_dt()
+            c.integrate()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(plain_steps):
+            for c in cases:
+                c.integrate()
+        for c in cases:
+            c.synchronize()
+        conc_s = time.perf_counter() - t0
+    finally:
+        for c in cases:
+            c.close()
+    plain_concurrent = cells * plain_steps / conc_s
     return {"cases": len(descs), "cells": cells, "batched_fp32_stencil": batched,
             "batched_default_shapes": batched_default, "default_shapes": default_shapes,
             "autotuned_shapes": tuned_shapes, "plain_fp64_one_by_one": plain,
+            "plain_fp64_concurrent_streams": plain_concurrent,
+            "ratio_vs_concurrent": batched / plain_concurrent,
             "ratio": batched / plain, "unit": "cell-steps/s", "batched_steps": args.ens_steps,
             "plain_steps_per_case": plain_steps,
             "workload": "nx in {64,128,256}, ny=2nx, log10 Ra in [6,9], Pr in [0.7,7], SplitMix64 seeds 20261203+k"}
@@ -534,6 +607,15 @@ def gpu_arm(args, world, rank, local):
         ach = opc * cells / avg_s / 1e9
         fp64 = {"kernel": dom, "achieved": ach, "peak": MEASURED_FP64_GOPS, "unit": "Gop/s (FP64 instructions)",
                 "frac": ach / MEASURED_FP64_GOPS, "ops_per_cell": opc}
+    # the whole explicit step against the FP64 issue rate: FP64 operations per
+    # cell-step from the kernels' counts (3 substages of temperature, velocity,
+    # forward DFT, sweep, inverse DFT and correction)
+    ops_step = 3 * (KERNEL_MODEL["temperature_update"][1] + KERNEL_MODEL["velocity_update"][1] +
+                    fft_ops_per_cell(args.ny, True) + KERNEL_MODEL["poisson_tridiagonal"][1] +
+                    fft_ops_per_cell(args.ny, False) + KERNEL_MODEL["correct_and_pressure"][1])
+    step_fp64 = {"ops_per_cell_step": ops_step, "achieved": value * ops_step / 1e9, "peak": MEASURED_FP64_GOPS,
+                 "unit": "Gop/s (FP64 instructions)", "frac": value * ops_step / 1e9 / MEASURED_FP64_GOPS,
+                 "peak_source": "measured on GB300 (profiles/fp64_pipe_gb300.md)"}
 
     # ---- end to end through the C ABI with host buffers
     # each step: host arrays -> device (sns_sync_to_device), one time step
@@ -575,6 +657,8 @@ def gpu_arm(args, world, rank, local):
         if args.ens_acc_steps > 0:
             extra["ensemble_64"]["accuracy_vs_fp64"] = ensemble_accuracy(args)
         extra["serving"] = serving(args)
+        if args.large_steps > 0:
+            extra["large_instance"] = large_instance(args, torch, steps=args.large_steps)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -595,7 +679,7 @@ def gpu_arm(args, world, rank, local):
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (reference initial condition, srand(0))", "config": workload_config(args),
-            "roofline": roofline, "fp64_roofline": fp64, "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e,
+            "roofline": roofline, "fp64_roofline": fp64, "step_fp64_roofline": step_fp64, "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(launches), "clocks": clk,
         }
         line.update(extra)
@@ -619,6 +703,7 @@ def main():
     ap.add_argument("--acc-steps", type=int, default=2000, help="steps of the FP32-vs-FP64 accuracy run")
     ap.add_argument("--ens-steps", type=int, default=50)
     ap.add_argument("--ens-acc-steps", type=int, default=500, help="steps of the ensemble FP32-vs-FP64 accuracy run")
+    ap.add_argument("--large-steps", type=int, default=10, help="timed steps of the 2048x4096 Ra=1e10 instance")
     ap.add_argument("--serve-rate", type=float, default=6.0)
     ap.add_argument("--serve-seconds", type=float, default=12.0)
     ap.add_argument("--serve-hbm", type=int, default=2048, help="serving arena in MiB")
