@@ -216,3 +216,17 @@ def test_fused_poisson_equals_three_kernels(nx, ny, costs):
             states.append(c.get_state())
     for k in states[0]:
         assert np.array_equal(states[0][k], states[1][k]), k
+
+
+@pytest.mark.parametrize("nx,ny", [(2, 2), (3, 4), (5, 8), (7, 16), (33, 64), (100, 32), (1030, 16)],
+                         ids=lambda v: str(v))
+def test_small_and_odd_grids(nx, ny):
+    """edge sizes: the smallest grids, odd itot, itot not a multiple of the
+    warp or of the column groups, jtot = 2 (a one-point complex DFT)"""
+    cfg = Config(nx, ny, ly=2.0, Ra=1e4, Pr=1.0)
+    o = OracleCase(cfg)
+    with gpu_case(cfg, [1, 2, 2, 3]) as c:
+        c.run(5)
+        o.run(5)
+        assert c.get_dt() == o.get_dt()
+        assert_bitwise(c.get_state(), o.get_state(), FIELDS, f"{nx}x{ny}")
