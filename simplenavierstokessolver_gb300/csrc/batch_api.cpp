@@ -323,7 +323,14 @@ static int rebuild(sns_batch *b) {
   std::vector<BModes> modes;
   size_t smem = 0;
   int threads = 64;
-  const int tx = b->tune.tile_x, ty = b->tune.tile_rows, mpb = b->tune.modes_per_block;
+  const int tx = b->tune.tile_x, ty = b->tune.tile_rows;
+  // the tridiagonal launch stages each warp's line in shared memory: fewer
+  // warps per block when the longest line would not fit
+  int nmax = 32;
+  for (const CaseHost &h : b->hc)
+    if (h.used && !(h.d.steps > 0 && h.steps_done >= h.d.steps)) nmax = std::max(nmax, h.d.itot);
+  int mpb = b->tune.modes_per_block;
+  while (mpb > 1 && batch_tri_smem(nmax, mpb) > 200 * 1024) mpb /= 2;
   for (int c = 0; c < b->max_cases; c++) {
     const CaseHost &h = b->hc[c];
     if (!h.used) continue;
@@ -374,7 +381,7 @@ static int rebuild(sns_batch *b) {
     if ((err = launch_batch_fwd(b->d_cases, b->d_cols, b->ncols, rk, b->fft_smem, b->fft_threads, b->stream)) !=
         cudaSuccess)
       break;
-    if ((err = launch_batch_tri(b->d_cases, b->d_modes, b->nmodes, mpb, b->stream)) != cudaSuccess) break;
+    if ((err = launch_batch_tri(b->d_cases, b->d_modes, b->nmodes, mpb, nmax, b->stream)) != cudaSuccess) break;
     if ((err = launch_batch_bwd(b->d_cases, b->d_cols, b->ncols, b->fft_smem, b->fft_threads, b->stream)) !=
         cudaSuccess)
       break;
@@ -802,6 +809,9 @@ int sns_batch_autotune(sns_batch *b, int steps, sns_batch_tuning *chosen, double
 int sns_batch_synchronize(sns_batch *b) {
   if (!b) return bfail(SNS_ERR_ARG, "NULL batch");
   BCUDA(cudaStreamSynchronize(b->stream));
+  if (unsigned e = batch_error_take())
+    return bfail(SNS_ERR_STATE, "batched tridiagonal solve: a bulk-copy wait gave up (code %u); results are invalid",
+                 e);
   return SNS_OK;
 }
 

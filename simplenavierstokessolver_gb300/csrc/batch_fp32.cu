@@ -250,21 +250,69 @@ __global__ void __launch_bounds__(256) k_b_bwd(const BCase *__restrict__ cases, 
   }
 }
 
-// Partition-method solve of the mode lines J = j0 .. j0+3 (one warp each).
+// Partition-method solve of the mode lines J = j0 .. j0+w-1 (one warp each).
 // Per-mode factor block (doubles): inv[nx] up[nx] v[nx] w[nx] alpha[5][32]
-// beta[5][32] rD[32]; rows are indexed by x.
+// beta[5][32] rD[32]; rows are indexed by x. Each warp first moves its mode
+// line (16 nx bytes) and factor block into shared memory with two bulk
+// asynchronous copies (the TMA engine, completion on an mbarrier), solves
+// there, and writes the line back with coalesced stores: the per-lane
+// segment sweeps then read shared memory instead of scattered global lines.
+__device__ unsigned g_tri_err;  // nonzero: a bulk-copy wait gave up (read and cleared by the host)
+
+constexpr unsigned kTriWaitSpins = 1u << 22;
+
+__device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
+  for (unsigned k = 0; k < kTriWaitSpins; ++k) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
+}
+
 __global__ void __launch_bounds__(32 * kBModesPerBlockMax) k_b_tri(const BCase *__restrict__ cases,
-                                                               const BModes *__restrict__ items) {
+                                                               const BModes *__restrict__ items, int nmax) {
+  extern __shared__ __align__(128) unsigned char tri_sm[];
   const BModes it = items[blockIdx.x];
   const BCase &C = cases[it.c];
   if (C.done) return;
-  const int lane = threadIdx.x & 31;
-  const int J = it.j0 + (threadIdx.x >> 5);
-  if (J >= C.nh) return;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int J = it.j0 + w;
+  if (J >= C.nh) return;  // the whole warp
   const int n = C.nx, m = C.seg;
   const int s = lane * m, e = s + m - 1;
-  double2 *line = C.spec + (size_t)J * n;
-  const double *f = C.pfac + (size_t)J * C.pstride;
+  double2 *gline = C.spec + (size_t)J * n;
+  const size_t per_warp = 48 * (size_t)nmax + 8 * (2 * kPcrLevels * kSeg + kSeg);
+  double2 *line = reinterpret_cast<double2 *>(tri_sm + 128 + (size_t)w * per_warp);
+  double *f = reinterpret_cast<double *>(line + nmax);
+  unsigned long long *bar = reinterpret_cast<unsigned long long *>(tri_sm) + w;
+  const unsigned line_bytes = 16u * (unsigned)n, fac_bytes = 8u * (unsigned)C.pstride;
+  if (lane == 0) {
+    const unsigned b = smem_addr(bar);
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(line_bytes + fac_bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(line)),
+                 "l"(__cvta_generic_to_global(gline)), "r"(line_bytes), "r"(b)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(f)),
+                 "l"(__cvta_generic_to_global(C.pfac + (size_t)J * C.pstride)), "r"(fac_bytes), "r"(b)
+                 : "memory");
+  }
+  __syncwarp();
+  if (!mbar_wait(smem_addr(bar), 0)) {
+    if (lane == 0) atomicOr(&g_tri_err, 1u);
+    return;  // this line is left unsolved; the host reports the error
+  }
   const double *inv = f, *up = f + n, *vv = f + 2 * n, *ww = f + 3 * n;
   const double *alpha = f + 4 * n, *beta = alpha + kPcrLevels * kSeg, *rD = beta + kPcrLevels * kSeg;
   const double *lo = C.lo, *hi = C.hi;
@@ -326,6 +374,8 @@ __global__ void __launch_bounds__(32 * kBModesPerBlockMax) k_b_tri(const BCase *
     r.y = fma(ww[i], xe_y, fma(vv[i], ly_, r.y));
     line[i] = r;
   }
+  __syncwarp();
+  for (int i = lane; i < n; i += 32) gline[i] = line[i];
 }
 
 // ---------------------------------------------------- correction and pressure
@@ -422,6 +472,7 @@ __global__ void k_b_dt(BCase *cases, int ncases, RkCoefs rk) {
 cudaError_t batch_kernels_init() {
   cudaFuncSetAttribute(k_b_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
   cudaFuncSetAttribute(k_b_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+  cudaFuncSetAttribute(k_b_tri, cudaFuncAttributeMaxDynamicSharedMemorySize, 210 * 1024);
   return cudaGetLastError();
 }
 
@@ -447,11 +498,22 @@ cudaError_t launch_batch_bwd(const BCase *cases, const BCols *cols, int ncols, s
   return cudaGetLastError();
 }
 
-cudaError_t launch_batch_tri(const BCase *cases, const BModes *modes, int nmodes, int modes_per_block,
+size_t batch_tri_smem(int nmax, int modes_per_block) {
+  return 128 + (size_t)modes_per_block * (48 * (size_t)nmax + 8 * (2 * kPcrLevels * kSeg + kSeg));
+}
+
+cudaError_t launch_batch_tri(const BCase *cases, const BModes *modes, int nmodes, int modes_per_block, int nmax,
                              cudaStream_t st) {
   if (nmodes == 0) return cudaSuccess;
-  k_b_tri<<<nmodes, 32 * modes_per_block, 0, st>>>(cases, modes);
+  k_b_tri<<<nmodes, 32 * modes_per_block, batch_tri_smem(nmax, modes_per_block), st>>>(cases, modes, nmax);
   return cudaGetLastError();
+}
+
+unsigned batch_error_take() {
+  unsigned v = 0, z = 0;
+  if (cudaMemcpyFromSymbol(&v, g_tri_err, sizeof v) != cudaSuccess) return 0xffffffffu;
+  if (v) cudaMemcpyToSymbol(g_tri_err, &z, sizeof z);
+  return v;
 }
 
 cudaError_t launch_batch_corr(const BCase *cases, const BTile *tiles, int ntiles, int rk, int tile_x, int rows,

@@ -76,8 +76,12 @@ cudaError_t launch_batch_stencil(const BCase *cases, const BTile *tiles, int nti
                                  cudaStream_t st);
 cudaError_t launch_batch_fwd(const BCase *cases, const BCols *cols, int ncols, int rk, size_t smem, int threads,
                              cudaStream_t st);
-cudaError_t launch_batch_tri(const BCase *cases, const BModes *modes, int nmodes, int modes_per_block,
+// shared memory of the tridiagonal launch for lines up to nmax long
+size_t batch_tri_smem(int nmax, int modes_per_block);
+cudaError_t launch_batch_tri(const BCase *cases, const BModes *modes, int nmodes, int modes_per_block, int nmax,
                              cudaStream_t st);
+// the tridiagonal kernels' error word (a bulk-copy wait gave up), cleared on read
+unsigned batch_error_take();
 cudaError_t launch_batch_bwd(const BCase *cases, const BCols *cols, int ncols, size_t smem, int threads,
                              cudaStream_t st);
 cudaError_t launch_batch_corr(const BCase *cases, const BTile *tiles, int ntiles, int rk, int tile_x, int rows,
