@@ -9,7 +9,7 @@
  * signatures; each comment names the reference interface it replaces.
  *
  * Ownership and residency. fluid_init / temperature_init allocate the host
- * arrays of the structure (reference layouts, include/arrays/*.h) and a device
+ * arrays of the structure (reference layouts, include/arrays/ headers) and a device
  * mirror that holds the authoritative state from then on. The hot-path calls
  * only enqueue GPU work on the solver's CUDA stream; the host arrays are
  * refreshed by sns_sync_to_host (call it before logging/saving/statistics)
