@@ -110,6 +110,17 @@ extern int sns_serve(const sns_case_desc *reqs, const double *arrival_s, int n, 
                      int chunk_steps, double *admit_s, double *done_s, double *busy_s, sns_done_fn on_done,
                      void *user);
 
+/* A case's state in the reference's save layout (src/save.c:13-68): the
+ * files sns_checkpoint (sns_gpu.h) writes for the plain path, with velocity
+ * and temperature widened from their compensated FP32 pairs. Blocks. */
+extern int sns_batch_checkpoint(sns_batch *batch, int slot, const char *dirname);
+/* Admits a case from a directory in that layout (written by the reference's
+ * save(), sns_checkpoint or sns_batch_checkpoint): step, time, ux, uy, p and
+ * temp; the explicit sources start at zero as in a restarted reference run,
+ * the first dt follows from the restored velocity. desc->steps is the step
+ * index at which the case completes (it counts from the restored step). */
+extern int sns_batch_add_restart(sns_batch *batch, const sns_case_desc *desc, const char *dirname, int *slot);
+
 /* current launch shapes */
 extern int sns_batch_get_tuning(const sns_batch *batch, sns_batch_tuning *tuning);
 /* fixed launch shapes (SNS_ERR_ARG outside the ranges above); results do not

@@ -157,6 +157,8 @@ PROTOTYPES = {
     "sns_batch_initial_temperature": (c_int, [PCD, _PD]),
     "sns_batch_diagnostics": (c_int, [c_void_p, c_int, _PD]),
     "sns_batch_get_tuning": (c_int, [c_void_p, POINTER(Tuning)]),
+    "sns_batch_checkpoint": (c_int, [c_void_p, c_int, c_char_p]),
+    "sns_batch_add_restart": (c_int, [c_void_p, PCD, c_char_p, POINTER(c_int)]),
     "sns_batch_set_tuning": (c_int, [c_void_p, POINTER(Tuning)]),
     "sns_batch_autotune": (c_int, [c_void_p, c_int, POINTER(Tuning), _PD]),
     "sns_serve": (c_int, [PCD, _PD, c_int, c_size_t, c_int, c_int, _PD, _PD, _PD, c_void_p, c_void_p]),

@@ -91,6 +91,19 @@ class Batch:
         self.descs[slot.value] = desc
         return slot.value
 
+    def add_restart(self, desc: Desc, dirname: str) -> int:
+        """admit a case from a directory in the reference's save layout"""
+        d = desc.c()
+        slot = c_int(-1)
+        N.check(self.lib.sns_batch_add_restart(self.h, ctypes.byref(d), dirname.encode(), ctypes.byref(slot)),
+                "sns_batch_add_restart")
+        self.descs[slot.value] = desc
+        return slot.value
+
+    def checkpoint(self, slot: int, dirname: str):
+        """the case's state in the reference's save layout"""
+        N.check(self.lib.sns_batch_checkpoint(self.h, slot, dirname.encode()), "sns_batch_checkpoint")
+
     def try_add(self, desc: Desc) -> int | None:
         d = desc.c()
         slot = c_int(-1)

@@ -23,6 +23,7 @@
 #include "batch_internal.h"
 #include "diag_internal.h"
 #include "host_common.h"
+#include "npy.h"
 #include "sns_batch.h"
 #include "sns_gpu.h"
 
@@ -468,10 +469,18 @@ int sns_batch_initial_temperature(const sns_case_desc *desc, double *temp) {
   return SNS_OK;
 }
 
-int sns_batch_add(sns_batch *b, const sns_case_desc *d, const double *temp_init, int *slot_out) {
-  if (!b) return bfail(SNS_ERR_ARG, "NULL batch");
-  if (int rc = check_desc(d)) return rc;
-  std::lock_guard<std::mutex> lk(b->mu);
+}  // extern "C"
+
+// a full starting state in the reference's layouts (restart): ux
+// (jtot+2) x (itot+1), uy, p, temp (jtot+2) x (itot+2), rows 1..jtot used
+struct StartState {
+  const double *ux, *uy, *p, *temp;
+  long long step;
+  double time;
+};
+
+static int admit(sns_batch *b, const sns_case_desc *d, const double *temp_init, const StartState *st,
+                 int *slot_out) {
   int slot = -1;
   for (int c = 0; c < b->max_cases; c++)
     if (!b->hc[c].used) {
@@ -518,6 +527,7 @@ int sns_batch_add(sns_batch *b, const sns_case_desc *d, const double *temp_init,
                  pfac.data() + L.pstride * J);
   const std::vector<double> tw = twiddle_table(ny);
   std::vector<double> temp((size_t)(nx + 2) * (ny + 2));
+  if (st) temp_init = st->temp;
   if (temp_init) {
     std::memcpy(temp.data(), temp_init, sizeof(double) * temp.size());
   } else {
@@ -558,16 +568,51 @@ int sns_batch_add(sns_batch *b, const sns_case_desc *d, const double *temp_init,
     chk(cudaMemsetAsync(base + L.ux[k], 0, sizeof(float) * cells, b->stream));
     chk(cudaMemsetAsync(base + L.uy[k], 0, sizeof(float) * cells, b->stream));
   }
+  // restart: velocity as compensated pairs, pressure as is; and the first dt
+  // from its maximum exactly as the correction kernel and k_b_dt form it
+  std::vector<float> ux_h, ux_l, uy_h, uy_l;
+  std::vector<double> p_d;
+  float ux_max = 0.f, uy_max = 0.f;
+  if (st) {
+    ux_h.assign(cells, 0.f);
+    ux_l.assign(cells, 0.f);
+    uy_h.assign(cells, 0.f);
+    uy_l.assign(cells, 0.f);
+    p_d.assign(cells, 0.0);
+    for (int j = 1; j <= ny; j++)
+      for (int x = 0; x < nx; x++) {
+        const size_t k = (size_t)(j - 1) * nx + x;
+        if (x >= 1) {  // ux at i = x+1 (x = 0 is the wall i = 1, kept zero)
+          const double v = st->ux[(size_t)j * (nx + 1) + x];
+          ux_h[k] = (float)v;
+          ux_l[k] = (float)(v - (double)ux_h[k]);
+          ux_max = std::fmax(ux_max, std::fabs(ux_h[k]) * rdxc_f[x]);
+        }
+        const double w = st->uy[(size_t)j * (nx + 2) + x + 1];
+        uy_h[k] = (float)w;
+        uy_l[k] = (float)(w - (double)uy_h[k]);
+        uy_max = std::fmax(uy_max, std::fabs(uy_h[k]) * (float)(1.0 / dy));
+        p_d[k] = st->p[(size_t)j * (nx + 2) + x + 1];
+      }
+    chk(put(L.ux[0], ux_h.data(), sizeof(float) * cells));
+    chk(put(L.uxl[0], ux_l.data(), sizeof(float) * cells));
+    chk(put(L.uy[0], uy_h.data(), sizeof(float) * cells));
+    chk(put(L.uyl[0], uy_l.data(), sizeof(float) * cells));
+  }
   chk(put(L.t[0], t_dense.data(), sizeof(float) * cells));
   chk(put(L.tl[0], t_low.data(), sizeof(float) * cells));
   chk(cudaMemsetAsync(base + L.tl[1], 0, sizeof(float) * cells, b->stream));
-  for (int k = 0; k < 2; k++) {
+  for (int k = st ? 1 : 0; k < 2; k++) {
     chk(cudaMemsetAsync(base + L.uxl[k], 0, sizeof(float) * cells, b->stream));
     chk(cudaMemsetAsync(base + L.uyl[k], 0, sizeof(float) * cells, b->stream));
   }
   chk(cudaMemsetAsync(base + L.t[1], 0, sizeof(float) * cells, b->stream));
   for (size_t o : {L.aux, L.auy, L.at}) chk(cudaMemsetAsync(base + o, 0, sizeof(float) * cells, b->stream));
-  chk(cudaMemsetAsync(base + L.p, 0, sizeof(double) * cells, b->stream));
+  if (st) {
+    chk(put(L.p, p_d.data(), sizeof(double) * cells));
+  } else {
+    chk(cudaMemsetAsync(base + L.p, 0, sizeof(double) * cells, b->stream));
+  }
   chk(cudaMemsetAsync(base + L.psi, 0, sizeof(double) * cells, b->stream));
   chk(cudaMemsetAsync(base + L.spec, 0, sizeof(double2) * (size_t)nh * nx, b->stream));
   // ---- table entry
@@ -631,10 +676,16 @@ int sns_batch_add(sns_batch *b, const sns_case_desc *d, const double *temp_init,
   t.spec = reinterpret_cast<double2 *>(base + L.spec);
   t.par = 0;
   t.done = 0;
-  t.step = 0;
-  t.time = 0.0;
-  // first dt from u = 0: advective limit 0.7 * 0.05 (src/param/decide_dt.c:42)
-  t.dt = d->fixed_dt > 0 ? d->fixed_dt : fmin(5.e-2 * 0.7, t.dt_dif);
+  t.step = st ? st->step : 0;
+  t.time = st ? st->time : 0.0;
+  if (t.target_steps > 0 && t.step >= t.target_steps) t.done = 1;
+  // first dt: from u = 0 the advective limit 0.7 * 0.05 (src/param/decide_dt.c:42);
+  // on restart the rule of k_b_dt on the restored velocity
+  double dt_adv = 5.e-2;
+  if (ux_max > 0.f) dt_adv = fmin(dt_adv, 1.0 / (double)ux_max);
+  if (uy_max > 0.f) dt_adv = fmin(dt_adv, 1.0 / (double)uy_max);
+  dt_adv *= 0.7;
+  t.dt = d->fixed_dt > 0 ? d->fixed_dt : fmin(dt_adv, t.dt_dif);
   for (int k = 0; k < 3; k++) {
     t.adt[k] = b->rk_a[k] * t.dt;
     t.bdt[k] = b->rk_b[k] * t.dt;
@@ -653,11 +704,51 @@ int sns_batch_add(sns_batch *b, const sns_case_desc *d, const double *temp_init,
   h.d = *d;
   h.off = off;
   h.bytes = L.total;
-  h.steps_done = 0;
+  h.steps_done = t.step;
   h.fcols = fc;
   b->dirty = true;
   if (slot_out) *slot_out = slot;
   return SNS_OK;
+}
+
+extern "C" {
+
+int sns_batch_add(sns_batch *b, const sns_case_desc *d, const double *temp_init, int *slot_out) {
+  if (!b) return bfail(SNS_ERR_ARG, "NULL batch");
+  if (int rc = check_desc(d)) return rc;
+  std::lock_guard<std::mutex> lk(b->mu);
+  return admit(b, d, temp_init, nullptr, slot_out);
+}
+
+// restart of a case from the reference's save layout (src/param/init.c:245-247,
+// src/fluid/init.c:53-81, src/temperature/init.c:51)
+int sns_batch_add_restart(sns_batch *b, const sns_case_desc *d, const char *dirname, int *slot_out) {
+  if (!b || !dirname) return bfail(SNS_ERR_ARG, "sns_batch_add_restart: bad argument");
+  if (int rc = check_desc(d)) return rc;
+  const int nx = d->itot, ny = d->jtot;
+  std::vector<double> ux((size_t)(nx + 1) * (ny + 2), 0.0), uy((size_t)(nx + 2) * (ny + 2), 0.0),
+      p(uy.size(), 0.0), temp(uy.size(), 0.0);
+  const std::string dir(dirname);
+  std::string err;
+  int step = 0;
+  double time = 0.0;
+  const size_t su[2] = {(size_t)ny, (size_t)nx + 1}, sc[2] = {(size_t)ny, (size_t)nx + 2};
+  if (npy_read((dir + "/step.npy").c_str(), "'int32'", 0, nullptr, &step, sizeof(int), &err) ||
+      npy_read((dir + "/time.npy").c_str(), "'float64'", 0, nullptr, &time, sizeof(double), &err) ||
+      npy_read((dir + "/ux.npy").c_str(), "'float64'", 2, su, ux.data() + (nx + 1), sizeof(double) * su[0] * su[1],
+               &err) ||
+      npy_read((dir + "/uy.npy").c_str(), "'float64'", 2, sc, uy.data() + (nx + 2), sizeof(double) * sc[0] * sc[1],
+               &err) ||
+      npy_read((dir + "/p.npy").c_str(), "'float64'", 2, sc, p.data() + (nx + 2), sizeof(double) * sc[0] * sc[1],
+               &err))
+    return bfail(SNS_ERR_ARG, "sns_batch_add_restart: %s", err.c_str());
+  if (d->with_temperature &&
+      npy_read((dir + "/temp.npy").c_str(), "'float64'", 2, sc, temp.data() + (nx + 2), sizeof(double) * sc[0] * sc[1],
+               &err))
+    return bfail(SNS_ERR_ARG, "sns_batch_add_restart: %s", err.c_str());
+  const StartState st{ux.data(), uy.data(), p.data(), temp.data(), step, time};
+  std::lock_guard<std::mutex> lk(b->mu);
+  return admit(b, d, nullptr, &st, slot_out);
 }
 
 int sns_batch_remove(sns_batch *b, int slot) {
@@ -932,7 +1023,62 @@ int sns_batch_state(sns_batch *b, int slot, double *ux, double *uy, double *p, d
 
 }  // extern "C"
 
-extern "C" int sns_batch_diagnostics(sns_batch *b, int slot, double out[11]) {
+extern "C" // a case's state in the reference's save layout (src/save.c:13-68): the same
+// files sns_checkpoint writes for the plain path; velocity and temperature
+// are the compensated FP32 pairs widened exactly (hi + lo)
+extern "C" int sns_batch_checkpoint(sns_batch *b, int slot, const char *dirname) {
+  if (!b || slot < 0 || slot >= b->max_cases || !b->hc[slot].used || !dirname)
+    return bfail(SNS_ERR_ARG, "sns_batch_checkpoint: bad argument");
+  const sns_case_desc d = b->hc[slot].d;
+  const int nx = d.itot, ny = d.jtot;
+  std::vector<double> ux((size_t)(nx + 1) * (ny + 2)), uy((size_t)(nx + 2) * (ny + 2)), p(uy.size()), psi(uy.size()),
+      temp(uy.size());
+  if (int rc = sns_batch_state(b, slot, ux.data(), uy.data(), p.data(), psi.data(), temp.data())) return rc;
+  double time = 0.0, dt = 0.0;
+  long long step = 0;
+  int done = 0;
+  if (int rc = sns_batch_case_status(b, slot, &time, &dt, &step, &done)) return rc;
+  std::vector<double> xf(nx + 1), xc(nx + 2), dxf(nx), dxc(nx + 1), yf(ny + 1), yc(ny);
+  double dy;
+  make_grid(nx, ny, 1.0, d.ly, d.stretch, xf.data(), xc.data(), dxf.data(), dxc.data(), yf.data(), yc.data(), &dy);
+  std::string err, dir(dirname);
+  if (make_dirs(dirname, &err)) return bfail(SNS_ERR_ARG, "sns_batch_checkpoint: %s", err.c_str());
+  auto path = [&](const char *n) { return dir + "/" + n + ".npy"; };
+  int rc = 0;
+  const int istep = (int)step, itot = nx, jtot = ny;
+  const double lx = 1.0;
+  auto w0 = [&](const char *n, const char *dtype, const void *v, size_t bytes) {
+    if (!rc) rc = npy_write(path(n).c_str(), dtype, 0, nullptr, v, bytes, &err);
+  };
+  auto w1 = [&](const char *n, const std::vector<double> &v) {
+    const size_t shape[1] = {v.size()};
+    if (!rc) rc = npy_write(path(n).c_str(), "'float64'", 1, shape, v.data(), sizeof(double) * v.size(), &err);
+  };
+  auto w2 = [&](const char *n, const std::vector<double> &v, size_t w) {
+    const size_t shape[2] = {(size_t)ny, w};
+    if (!rc) rc = npy_write(path(n).c_str(), "'float64'", 2, shape, v.data() + w, sizeof(double) * w * ny, &err);
+  };
+  w0("step", "'int32'", &istep, sizeof(int));
+  w0("itot", "'int32'", &itot, sizeof(int));
+  w0("jtot", "'int32'", &jtot, sizeof(int));
+  w0("time", "'float64'", &time, sizeof(double));
+  w0("lx", "'float64'", &lx, sizeof(double));
+  w0("ly", "'float64'", &d.ly, sizeof(double));
+  w0("Ra", "'float64'", &d.Ra, sizeof(double));
+  w0("Pr", "'float64'", &d.Pr, sizeof(double));
+  w1("xf", xf);
+  w1("xc", xc);
+  w1("yf", yf);
+  w1("yc", yc);
+  w2("ux", ux, (size_t)nx + 1);
+  w2("uy", uy, (size_t)nx + 2);
+  w2("p", p, (size_t)nx + 2);
+  if (d.with_temperature) w2("temp", temp, (size_t)nx + 2);
+  if (rc) return bfail(SNS_ERR_ARG, "sns_batch_checkpoint: %s", err.c_str());
+  return SNS_OK;
+}
+
+int sns_batch_diagnostics(sns_batch *b, int slot, double out[11]) {
   if (!b || slot < 0 || slot >= b->max_cases || !b->hc[slot].used || !out) return bfail(SNS_ERR_ARG, "bad slot");
   std::lock_guard<std::mutex> lk(b->mu);
   BCase t;

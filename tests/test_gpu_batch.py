@@ -270,3 +270,51 @@ def test_tuning_changes_speed_not_results():
     for a, m in zip(results[0], tuned):
         for k in a:
             assert np.array_equal(a[k], m[k]), k
+
+
+def test_checkpoint_and_restart_continue_bit_for_bit(tmp_path):
+    """serving snapshot and resume: a case checkpointed after 15 steps and
+    admitted from the files into another batch continues exactly as the
+    uninterrupted case; the files read back as the reference's save layout"""
+    from simplenavierstokessolver_gb300.batch import Batch, Desc
+
+    d = Desc(128, 256, Ra=1e8, Pr=1.0, seed=5)
+    with Batch(512 << 20) as b:
+        s = b.add(d)
+        b.step(15)
+        b.checkpoint(s, str(tmp_path / "ck"))
+        b.step(10)
+        straight = b.state(s)
+        st_straight = b.status(s)
+    assert int(np.load(tmp_path / "ck" / "step.npy")) == 15
+    assert np.load(tmp_path / "ck" / "ux.npy").shape == (256, 129)
+    with Batch(512 << 20) as b:
+        s = b.add_restart(d, str(tmp_path / "ck"))
+        assert b.status(s)["step"] == 15
+        b.step(10)
+        resumed = b.state(s)
+        st_resumed = b.status(s)
+    assert st_resumed["step"] == st_straight["step"] and st_resumed["time"] == st_straight["time"]
+    for k in ("ux", "uy", "p", "temp"):
+        assert np.array_equal(straight[k], resumed[k]), k
+
+
+def test_restart_from_a_plain_checkpoint(tmp_path):
+    """a plain-path checkpoint (the reference's save layout, byte-identical to
+    its save() files) admits into a batch: the FP64 state is held exactly up
+    to the compensated pairs' ~48 significant bits"""
+    from simplenavierstokessolver_gb300.batch import Batch, Desc
+    from simplenavierstokessolver_gb300.solver import Case
+
+    with Case(64, 128, Ra=1e7, Pr=1.0) as c:
+        c.run(20)
+        c.checkpoint(str(tmp_path / "plain"))
+        c.checkpoint_wait()
+        ref = c.get_state()
+    with Batch(256 << 20) as b:
+        s = b.add_restart(Desc(64, 128, Ra=1e7, Pr=1.0), str(tmp_path / "plain"))
+        got = b.state(s)
+        assert b.status(s)["step"] == 20
+    for k in ("ux", "uy", "temp"):  # FP64 values held as compensated FP32 pairs: ~2^-48 relative
+        assert np.abs(got[k] - ref[k])[1:-1, 1:-1].max() <= 1e-13 * max(np.abs(ref[k]).max(), 1.0), k
+    assert np.array_equal(got["p"][1:-1, 1:-1], ref["p"][1:-1, 1:-1])
