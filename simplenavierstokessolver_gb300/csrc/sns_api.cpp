@@ -846,9 +846,9 @@ static int fused_enqueue_err(Context *c) {
 }
 
 // the Poisson solve as one fused launch when possible (temperature update
-// folded in when t_out is given), else as three kernels; *fused_out tells
-// which ran
-static int poisson_any(Context *c, const StageScalars &s, Fields &f, const double *t_in, double *t_out, double *at,
+// folded in when t_out is given); *fused_out tells whether it ran. When it
+// did not, nothing was launched and the caller runs the separate kernels.
+static int try_fused(Context *c, const StageScalars &s, Fields &f, const double *t_in, double *t_out, double *at,
                        const double *ux_k, const double *uy_k, bool *fused_out) {
   *fused_out = false;
   if (c->fused) {
@@ -867,13 +867,15 @@ static int poisson_any(Context *c, const StageScalars &s, Fields &f, const doubl
     cudaGetLastError();
     c->fused = false;  // this size cannot run fused here: three kernels from now on
   }
-  if (int rc = poisson_forward(c, s, f)) return rc;
-  return poisson_rest(c, s, f);
+  return SNS_OK;
 }
 
 static int poisson(Context *c, const StageScalars &s, Fields &f) {
   bool fused = false;
-  return poisson_any(c, s, f, nullptr, nullptr, nullptr, nullptr, nullptr, &fused);
+  if (int rc = try_fused(c, s, f, nullptr, nullptr, nullptr, nullptr, nullptr, &fused)) return rc;
+  if (fused) return SNS_OK;
+  if (int rc = poisson_forward(c, s, f)) return rc;
+  return poisson_rest(c, s, f);
 }
 
 // dt from the reduction results (src/param/decide_dt.c:11-101)
@@ -1942,7 +1944,7 @@ static int integrate_impl(const param_t *param, FluidExt *fe, TempExt *te, bool 
       while (out == te->cur || out == te->snap) out++;
     bool fused = false;
     if (overlap && c->fused) {
-      if (int rc = poisson_any(c, s, f, te->f.t[te->cur], te->f.t[out], te->f.at, ux_k, uy_k, &fused)) return rc;
+      if (int rc = try_fused(c, s, f, te->f.t[te->cur], te->f.t[out], te->f.at, ux_k, uy_k, &fused)) return rc;
       if (fused) te->cur = out;
     }
     if (!fused) {
@@ -1959,7 +1961,7 @@ static int integrate_impl(const param_t *param, FluidExt *fe, TempExt *te, bool 
         te->cur = out;
         if (int rc = poisson_rest(c, s, f)) return rc;
       } else {
-        if (int rc = poisson_any(c, s, f, nullptr, nullptr, nullptr, nullptr, nullptr, &fused)) return rc;
+        if (int rc = poisson(c, s, f)) return rc;
       }
     }
     const bool red = reduce_last && rk == RKSTEPMAX - 1;
