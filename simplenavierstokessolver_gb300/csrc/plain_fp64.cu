@@ -618,9 +618,11 @@ constexpr int kFusedThreads = 512;
 // sweep warps per block, one per SM sub-partition. Dependent FP64 chains run
 // ~20% slower with four warps on one SM than with one, but every SM given to
 // the sweeps is taken from the DFT workers, whose FP64 throughput bounds the
-// launch as much as the sweeps do: measured on GB300, four per block is the
-// fastest at 512 x 1024 (within 1%), 1024 x 2048 and 2048 x 4096.
+// launch as much as the sweeps do. Measured on GB300: two per block is the
+// fastest while at least kFusedMinWorkers workers remain (512 x 1024: 177 us
+// against 183 us with four), four per block beyond (1024 x 2048, 2048 x 4096).
 constexpr int kFusedTriWarps = 4;
+constexpr int kFusedMinWorkers = 130;
 constexpr int kFusedSpan = 64;
 constexpr unsigned kFusedSpin = 1u << 22;
 constexpr size_t kFusedMinSmem = 116 * 1024;  // above half an SM's shared memory: one block per SM
@@ -1166,7 +1168,8 @@ cudaError_t launch_poisson_fused(const DevGrid &g, const StageScalars &s, const 
   if ((e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev)) != cudaSuccess) return e;
   const int C = fused_cols(g);
   const int lines = 2 * ((g.nh + 31) / 32);
-  const int tri_warps = kFusedTriWarps;
+  // two sweep warps per block when that still leaves kFusedMinWorkers workers
+  const int tri_warps = sms - (lines + 1) / 2 >= kFusedMinWorkers ? 2 : kFusedTriWarps;
   const int tri_blocks = (lines + tri_warps - 1) / tri_warps;
   const size_t smem = std::max({sizeof(double) * (size_t)g.nx, (size_t)C * g.ny * sizeof(double), kFusedMinSmem});
   if (!coop || g.nx > kTriMaxNx || smem > 200 * 1024 || sms - tri_blocks < 8) return cudaErrorNotSupported;
