@@ -189,6 +189,14 @@ extern int sns_parallel_destroy(parallel_t *parallel);
 extern int sns_sync_to_host(const param_t *param, fluid_t *fluid, temperature_t *temperature);
 /* host arrays -> device (interior values are taken; halos are implied) */
 extern int sns_sync_to_device(const param_t *param, fluid_t *fluid, temperature_t *temperature);
+/* the same two copies restricted to ux, uy, p and temp, the whole input and
+ * output of a time step taken with sns_integrate / sns_run (psi is written
+ * before it is read, the first substage multiplies the previous sources by
+ * zero and the buoyancy is recomputed from temp): psi, srcuxa, srcuya,
+ * srctempa and tempforcex stay as they are on the side being written. Not
+ * for use between the reference-named calls of one step. */
+extern int sns_sync_state_to_host(const param_t *param, fluid_t *fluid, temperature_t *temperature);
+extern int sns_sync_state_to_device(const param_t *param, fluid_t *fluid, temperature_t *temperature);
 /* waits for all GPU work queued for this fluid's solver */
 extern int sns_synchronize(const fluid_t *fluid);
 /* the CUDA stream (cudaStream_t) the solver enqueues on */

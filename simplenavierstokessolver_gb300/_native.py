@@ -114,6 +114,8 @@ PROTOTYPES = {
     "sns_parallel_destroy": (c_int, [PL]),
     "sns_sync_to_host": (c_int, [PP, PF, PT]),
     "sns_sync_to_device": (c_int, [PP, PF, PT]),
+    "sns_sync_state_to_host": (c_int, [PP, PF, PT]),
+    "sns_sync_state_to_device": (c_int, [PP, PF, PT]),
     "sns_synchronize": (c_int, [PF]),
     "sns_stream": (c_void_p, [PF]),
     "sns_integrate": (c_int, [PP, PL, PF, PT]),

@@ -1349,42 +1349,53 @@ int param_decide_dt(param_t *param, const parallel_t *parallel, const fluid_t *f
   return SNS_OK;
 }
 
-int sns_sync_to_host(const param_t *param, fluid_t *fluid, temperature_t *temperature) {
-  if (!param) return fail(SNS_ERR_ARG, "sns_sync_to_host: NULL param");
+// Device -> host. state_only: ux, uy, p and temp alone, the whole input and
+// output of a time step (psi is rewritten before it is read, the explicit
+// sources of the last substage are multiplied by zero at the first one, and
+// tempforcex is recomputed from temp); the other host arrays keep what they
+// held.
+static int sync_to_host_impl(const param_t *param, fluid_t *fluid, temperature_t *temperature, bool state_only,
+                             const char *fn) {
+  if (!param) return fail(SNS_ERR_ARG, "%s: NULL param", fn);
   const int nx = param->itot, ny = param->jtot;
   if (fluid) {
     FluidExt *fe = as_fluid(fluid);
-    if (!fe) return fail(SNS_ERR_ARG, "sns_sync_to_host: foreign fluid_t");
+    if (!fe) return fail(SNS_ERR_ARG, "%s: foreign fluid_t", fn);
     Context *c = fe->ctx;
     fluid_t &h = fe->pub;
     int rc = SNS_OK;
     if ((rc = download(c, fe->f.ux, h.ux, nx + 1, 0, 1)) || (rc = download(c, fe->f.uy, h.uy, nx + 2, 1, 0)) ||
-        (rc = download(c, fe->f.p, h.p, nx + 2, 1, 0)) || (rc = download(c, fe->f.psi, h.psi, nx + 2, 1, 0)) ||
-        (rc = download_src(c, fe->f.aux, h.srcuxa, 1)) || (rc = download_src(c, fe->f.auy, h.srcuya, 0)))
+        (rc = download(c, fe->f.p, h.p, nx + 2, 1, 0)))
+      return rc;
+    if (!state_only &&
+        ((rc = download(c, fe->f.psi, h.psi, nx + 2, 1, 0)) || (rc = download_src(c, fe->f.aux, h.srcuxa, 1)) ||
+         (rc = download_src(c, fe->f.auy, h.srcuya, 0))))
       return rc;
     SNS_CUDA(cudaStreamSynchronize(c->stream));
     host_bc_ux(nx, ny, h.ux);
     host_bc_uy(nx, ny, h.uy);
     host_bc_p(nx, ny, h.p);
-    host_bc_p(nx, ny, h.psi);
+    if (!state_only) host_bc_p(nx, ny, h.psi);
   }
   if (temperature) {
     TempExt *te = as_temp(temperature);
-    if (!te) return fail(SNS_ERR_ARG, "sns_sync_to_host: foreign temperature_t");
+    if (!te) return fail(SNS_ERR_ARG, "%s: foreign temperature_t", fn);
     Context *c = te->ctx;
     temperature_t &h = te->pub;
     int rc = SNS_OK;
-    if ((rc = download(c, te->f.t[te->cur], h.temp, nx + 2, 1, 0)) || (rc = download_src(c, te->f.at, h.srctempa, 0)))
+    if ((rc = download(c, te->f.t[te->cur], h.temp, nx + 2, 1, 0)) ||
+        (!state_only && (rc = download_src(c, te->f.at, h.srctempa, 0))))
       return rc;
-    double *tf_alias = te->snap >= 0 ? dev_alias(h.tempforcex) : nullptr;
+    const int snap = state_only ? -1 : te->snap;
+    double *tf_alias = snap >= 0 ? dev_alias(h.tempforcex) : nullptr;
     if (tf_alias) {
-      SNS_CUDA(launch_tempforce_to_host(c->g, te->f.t[te->snap], tf_alias, c->stream));
-    } else if (te->snap >= 0) {
-      if (int rc2 = fetch(c, te->f.t[te->snap])) return rc2;
+      SNS_CUDA(launch_tempforce_to_host(c->g, te->f.t[snap], tf_alias, c->stream));
+    } else if (snap >= 0) {
+      if (int rc2 = fetch(c, te->f.t[snap])) return rc2;
     }
     SNS_CUDA(cudaStreamSynchronize(c->stream));
     host_bc_temp(nx, ny, h.temp);
-    if (te->snap >= 0 && !tf_alias) {
+    if (snap >= 0 && !tf_alias) {
       // tempforcex (src/temperature/force.c:17-23) from the snapshot buffer
       for (int j = 1; j <= ny; j++)
         for (int i = 2; i <= nx; i++) {
@@ -1396,17 +1407,28 @@ int sns_sync_to_host(const param_t *param, fluid_t *fluid, temperature_t *temper
   return SNS_OK;
 }
 
+int sns_sync_to_host(const param_t *param, fluid_t *fluid, temperature_t *temperature) {
+  return sync_to_host_impl(param, fluid, temperature, false, "sns_sync_to_host");
+}
+
+int sns_sync_state_to_host(const param_t *param, fluid_t *fluid, temperature_t *temperature) {
+  return sync_to_host_impl(param, fluid, temperature, true, "sns_sync_state_to_host");
+}
+
 // Host -> device: the pinned host arrays are read in place by one copy
 // kernel for all fields (strided 2D DMA of ~4 KB rows runs at less than half
 // the link rate); arrays that are not pinned go through 2D DMA copies.
-int sns_sync_to_device(const param_t *param, fluid_t *fluid, temperature_t *temperature) {
-  if (!param) return fail(SNS_ERR_ARG, "sns_sync_to_device: NULL param");
+// state_only: ux, uy, p and temp alone; the device keeps its psi and sources
+// and the buoyancy is recomputed from the uploaded temp.
+static int sync_to_device_impl(const param_t *param, fluid_t *fluid, temperature_t *temperature, bool state_only,
+                               const char *fn) {
+  if (!param) return fail(SNS_ERR_ARG, "%s: NULL param", fn);
   const int nx = param->itot;
   FluidExt *fe = nullptr;
   TempExt *te = nullptr;
-  if (fluid && !(fe = as_fluid(fluid))) return fail(SNS_ERR_ARG, "sns_sync_to_device: foreign fluid_t");
-  if (temperature && !(te = as_temp(temperature))) return fail(SNS_ERR_ARG, "sns_sync_to_device: foreign temperature_t");
-  if (fe && te && fe->ctx != te->ctx) return fail(SNS_ERR_ARG, "sns_sync_to_device: fluid and temperature of different cases");
+  if (fluid && !(fe = as_fluid(fluid))) return fail(SNS_ERR_ARG, "%s: foreign fluid_t", fn);
+  if (temperature && !(te = as_temp(temperature))) return fail(SNS_ERR_ARG, "%s: foreign temperature_t", fn);
+  if (fe && te && fe->ctx != te->ctx) return fail(SNS_ERR_ARG, "%s: fluid and temperature of different cases", fn);
   Context *c = fe ? fe->ctx : te ? te->ctx : nullptr;
   if (!c) return SNS_OK;
   XferList L{};
@@ -1415,14 +1437,17 @@ int sns_sync_to_device(const param_t *param, fluid_t *fluid, temperature_t *temp
   if (fe) {
     const fluid_t &h = fe->pub;
     direct = xfer_field(L, nx, fe->f.ux, h.ux, nx + 1, 0, 1) && xfer_field(L, nx, fe->f.uy, h.uy, nx + 2, 1, 0) &&
-             xfer_field(L, nx, fe->f.p, h.p, nx + 2, 1, 0) && xfer_field(L, nx, fe->f.psi, h.psi, nx + 2, 1, 0) &&
-             xfer_src(L, nx, fe->f.aux, h.srcuxa, 1) && xfer_src(L, nx, fe->f.auy, h.srcuya, 0);
+             xfer_field(L, nx, fe->f.p, h.p, nx + 2, 1, 0);
+    if (!state_only)
+      direct = direct && xfer_field(L, nx, fe->f.psi, h.psi, nx + 2, 1, 0) &&
+               xfer_src(L, nx, fe->f.aux, h.srcuxa, 1) && xfer_src(L, nx, fe->f.auy, h.srcuya, 0);
   }
   if (te) {
     te->cur = 0;
     te->snap = -2;
     const temperature_t &h = te->pub;
-    direct = direct && xfer_field(L, nx, te->f.t[0], h.temp, nx + 2, 1, 0) && xfer_src(L, nx, te->f.at, h.srctempa, 0);
+    direct = direct && xfer_field(L, nx, te->f.t[0], h.temp, nx + 2, 1, 0) &&
+             (state_only || xfer_src(L, nx, te->f.at, h.srctempa, 0));
   }
   if (direct) {
     SNS_CUDA(launch_xfer(L, c->stream));
@@ -1431,18 +1456,30 @@ int sns_sync_to_device(const param_t *param, fluid_t *fluid, temperature_t *temp
     if (fe) {
       const fluid_t &h = fe->pub;
       if ((rc = upload_field(c, fe->f.ux, h.ux, nx + 1, 0, 1)) || (rc = upload_field(c, fe->f.uy, h.uy, nx + 2, 1, 0)) ||
-          (rc = upload_field(c, fe->f.p, h.p, nx + 2, 1, 0)) || (rc = upload_field(c, fe->f.psi, h.psi, nx + 2, 1, 0)) ||
-          (rc = upload_src(c, fe->f.aux, h.srcuxa, 1)) || (rc = upload_src(c, fe->f.auy, h.srcuya, 0)))
+          (rc = upload_field(c, fe->f.p, h.p, nx + 2, 1, 0)))
+        return rc;
+      if (!state_only &&
+          ((rc = upload_field(c, fe->f.psi, h.psi, nx + 2, 1, 0)) || (rc = upload_src(c, fe->f.aux, h.srcuxa, 1)) ||
+           (rc = upload_src(c, fe->f.auy, h.srcuya, 0))))
         return rc;
     }
     if (te) {
       const temperature_t &h = te->pub;
-      if ((rc = upload_field(c, te->f.t[0], h.temp, nx + 2, 1, 0)) || (rc = upload_src(c, te->f.at, h.srctempa, 0)))
+      if ((rc = upload_field(c, te->f.t[0], h.temp, nx + 2, 1, 0)) ||
+          (!state_only && (rc = upload_src(c, te->f.at, h.srctempa, 0))))
         return rc;
     }
   }
   SNS_CUDA(cudaStreamSynchronize(c->stream));
   return SNS_OK;
+}
+
+int sns_sync_to_device(const param_t *param, fluid_t *fluid, temperature_t *temperature) {
+  return sync_to_device_impl(param, fluid, temperature, false, "sns_sync_to_device");
+}
+
+int sns_sync_state_to_device(const param_t *param, fluid_t *fluid, temperature_t *temperature) {
+  return sync_to_device_impl(param, fluid, temperature, true, "sns_sync_state_to_device");
 }
 
 int sns_diagnostics(const param_t *param, const fluid_t *fluid, const temperature_t *temperature, double out[11]) {

@@ -130,6 +130,14 @@ class Case:
     def sync_to_device(self):
         N.check(self.lib.sns_sync_to_device(self.param, self.fluid, self.temperature), "sns_sync_to_device")
 
+    def sync_state_to_host(self):
+        """ux, uy, p and temp alone (the whole-step state)"""
+        N.check(self.lib.sns_sync_state_to_host(self.param, self.fluid, self.temperature), "sns_sync_state_to_host")
+
+    def sync_state_to_device(self):
+        N.check(self.lib.sns_sync_state_to_device(self.param, self.fluid, self.temperature),
+                "sns_sync_state_to_device")
+
     def get_state(self):
         self.sync_to_host()
         h = self.host_arrays()

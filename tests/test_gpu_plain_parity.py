@@ -200,6 +200,42 @@ def test_restart_through_host_arrays_continues_bitwise():
         assert_bitwise(c.get_state(), o.get_state(), ("ux", "uy", "p", "temp"), "after restart")
 
 
+@pytest.mark.parametrize("costs", [[1, 2, 2, 3], [4, 3, 2, 1]], ids=["exp_exp", "imp_imp"])
+def test_state_only_syncs_around_whole_steps_are_bitwise(costs):
+    """sns_sync_state_to_host / _to_device move ux, uy, p and temp alone. The
+    state saved after 3 steps and put back after 2 more (the device keeps the
+    later psi and sources) continues exactly like the oracle's uninterrupted
+    run, and the synced host state equals what the full sync gives."""
+    cfg = Config(48, 64, ly=1.5, Ra=1e7, Pr=0.8, stretch=3)
+    o = OracleCase(cfg)
+    o.set_costs(costs)
+    keys = ("ux", "uy", "p", "temp")
+    with gpu_case(cfg, costs) as c:
+        h = c.host_arrays()
+        c.run(3)
+        c.sync_state_to_host()
+        saved = {k: h[k].copy() for k in keys}
+        clock = c.get_dt()
+        h["psi"][...] = np.nan  # not touched by the state-only copies
+        c.run(2)
+        c.sync_state_to_host()
+        assert np.isnan(h["psi"]).all()
+        assert not np.array_equal(h["ux"], saved["ux"])
+        for k in keys:
+            h[k][...] = saved[k]
+        c.sync_state_to_device()
+        c.set_time(clock["time"], clock["step"])
+        c.run(4)
+        c.sync_state_to_host()
+        state = {k: h[k].copy() for k in keys}
+        o.run(7)
+        full = c.get_state()
+        assert c.get_dt() == o.get_dt()
+        assert_bitwise(full, o.get_state(), FIELDS, "after a state-only restore")
+        for k in keys:
+            assert np.array_equal(state[k], full[k]), k
+
+
 @pytest.mark.parametrize("nx,ny,costs", [(64, 128, [1, 2, 2, 3]), (2048, 256, [1, 2, 2, 3]),
                                           (96, 64, [4, 3, 2, 1])], ids=["64x128", "2048x256", "impimp_96x64"])
 def test_fused_poisson_equals_three_kernels(nx, ny, costs):
