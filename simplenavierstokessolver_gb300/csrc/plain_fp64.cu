@@ -106,6 +106,42 @@ __global__ void __launch_bounds__(128) k_temp(const TempArgs a) {
   temp_column<IMPX, IMPY, RCP>(a, x, blockIdx.y * kRows);
 }
 
+// ------------------------------------------------- exact power-of-two products
+// x * 2^e is exact when x and the product are normal numbers, or x is zero,
+// and then equals x with its exponent field moved by e. GB300 issues FP64
+// instructions at a small fraction of its integer rate, so on grids whose
+// spacings are powers of two (DevGrid::p2: the reciprocal spacings and the
+// advective coefficients are then powers of two too) the velocity kernel
+// takes those products, and the 1/2 of every interpolation, in the integer
+// unit. An operand other than zero whose exponent field lies outside
+// [1 + kP2Margin, 0x7fe - kP2Margin] (magnitude below 2^-958 or from 2^958 up,
+// subnormals, infinities, NaN), where the moved field could leave the normal
+// range, clears the row's flag and the row is recomputed with FP64 products.
+constexpr unsigned kP2Margin = 64;  // largest |e| taken this way (checked on the host)
+constexpr unsigned kP2Lo = (1u + kP2Margin) << 20;
+constexpr unsigned kP2Span = (0x7feu - 2u * kP2Margin) << 20;
+
+// c == 2^e: e in the position of the exponent field of the high word
+__device__ __forceinline__ int p2_field(double c) { return (((__double2hiint(c) >> 20) & 0x7ff) - 1023) * (1 << 20); }
+
+template <bool FAST>
+struct Mul {
+  bool ok = true;
+  // x * c where c == 2^e and E == p2_field(c)
+  __device__ __forceinline__ double by(double x, double c, int E) {
+    if constexpr (FAST) {
+      const int hi = __double2hiint(x), lo = __double2loint(x);
+      const unsigned m = (unsigned)hi & 0x7fffffffu;
+      const bool zero = (m | (unsigned)lo) == 0u;
+      ok &= zero | (m - kP2Lo < kP2Span);
+      return __hiloint2double(zero ? hi : hi + E, lo);
+    } else {
+      return x * c;
+    }
+  }
+  __device__ __forceinline__ double half(double x) { return by(x, 0.5, -(1 << 20)); }
+};
+
 // ------------------------------------------------------------------ velocity
 struct VelArgs {
   DevGrid g;
@@ -114,9 +150,128 @@ struct VelArgs {
   double *ux_out, *uy_out, *aux, *auy, *qx, *qy;
 };
 
+// metrics of column x: ux at i = x+1 (DXF(i-1), DXF(i), DXC(i)), uy at
+// i = x+1 (DXC(i), DXC(i+1), DXF(i)), with the exponents of the power-of-two
+// factors when they are taken in the integer unit
+struct VelCol {
+  double uf_m, uf_p, uc_c, ruf_m, ruf_p, ruc_c, fm, fp;
+  double vc_m, vc_p, vf_c, rvc_m, rvc_p, rvf_c, cm, cp;
+  int e_ruf_m, e_ruf_p, e_ruc_c, e_fm, e_fp, e_rvc_m, e_rvc_p, e_rvf_c, e_cm, e_cp, e_rdy;
+};
+
+// one row: the values carried from the row below, and this row's loads
+struct VelIn {
+  double u0, u1, um0, um1, v0, vl, pm;  // ux(x+1..x+2, y), ux(.., y-1), uy(x+1, y), uy(x, y), p(x+1, y-1)
+  double gym_u, pym_u, gym_v, pym_v;    // y-face terms between rows y-1 and y
+  double u0n, u1n, v0n, vln, vr, pc, ul, pl, tfl, tfr, aux, auy;
+};
+
+struct VelOut {
+  double ux, ax, qx, uy, ay, qy;
+  double gym_u, pym_u, gym_v, pym_v;
+};
+
 // src/fluid/update_velocity.c:11-104 (ux sources), :106-192 (uy sources),
-// :219-230 / :371-381 (RK3 increments) and :436-441 / :580-585 (update).
-template <int IMPX, int IMPY, bool RCP>
+// :219-230 / :371-381 (RK3 increments) and :436-441 / :580-585 (update), for
+// one row of column x. Returns false when a FAST product was out of range.
+template <int IMPX, int IMPY, bool RCP, bool FAST>
+__device__ __forceinline__ bool vel_row(const VelArgs &a, const VelCol &k, const VelIn &in, bool has_ux,
+                                        VelOut &o) {
+  Mul<FAST> m;
+  const double dy = a.g.dy, rdy = a.g.rdy, nu = a.s.nu;
+  // difference / spacing
+  auto D = [&](double v, double d, double rd, int E) {
+    if constexpr (FAST) {
+      return m.by(v, rd, E);
+    } else {
+      return dv<RCP>(v, d, rd);
+    }
+  };
+  // coefficient * value
+  auto C = [&](double c, double v, int E) {
+    if constexpr (FAST) {
+      return m.by(v, c, E);
+    } else {
+      return c * v;
+    }
+  };
+  o.gym_u = in.gym_u;
+  o.pym_u = in.pym_u;
+  // ---- ux(i, j), i = x+1 >= 2
+  if (has_ux) {
+    const double gxm = D(in.u0 - in.ul, k.uf_m, k.ruf_m, k.e_ruf_m);
+    const double gxp = D(in.u1 - in.u0, k.uf_p, k.ruf_p, k.e_ruf_p);
+    const double gyp = D(in.u0n - in.u0, dy, rdy, k.e_rdy);
+    const double vxm = m.half(in.ul) + m.half(in.u0);
+    const double vxp = m.half(in.u0) + m.half(in.u1);
+    const double adv1 = -(C(k.fm, vxm, k.e_fm) * gxm) - (C(k.fp, vxp, k.e_fp) * gxp);
+    const double pyp = m.half(C(k.fm, in.vln, k.e_fm) + C(k.fp, in.v0n, k.e_fp)) * gyp;
+    const double adv2 = -in.pym_u - pyp;
+    const double dif1 = D(nu * (gxp - gxm), k.uc_c, k.ruc_c, k.e_ruc_c);
+    const double dif2 = D(nu * (gyp - in.gym_u), dy, rdy, k.e_rdy);
+    const double pre = -D(in.pc - in.pl, k.uc_c, k.ruc_c, k.e_ruc_c);
+    double A = adv1 + adv2;
+    if (!IMPX) A = A + dif1;
+    if (!IMPY) A = A + dif2;
+    if (a.tf) A = A + (m.half(in.tfl) + m.half(in.tfr));
+    double G;
+    if (IMPX && IMPY) {
+      G = (dif1 + dif2) + pre;
+    } else if (IMPX) {
+      G = dif1 + pre;
+    } else if (IMPY) {
+      G = dif2 + pre;
+    } else {
+      G = pre;
+    }
+    double q = a.s.adt * A;
+    if (a.s.has_b) q = q + a.s.bdt * in.aux;
+    q = q + a.s.gdt * G;
+    o.ax = A;
+    o.qx = q;
+    o.ux = in.u0 + q;
+    o.gym_u = gyp;
+    o.pym_u = pyp;
+  }
+  // ---- uy(i, j), i = x+1 >= 1
+  {
+    const double gxm = D(in.v0 - in.vl, k.vc_m, k.rvc_m, k.e_rvc_m);
+    const double gxp = D(in.vr - in.v0, k.vc_p, k.rvc_p, k.e_rvc_p);
+    const double gyp = D(in.v0n - in.v0, dy, rdy, k.e_rdy);
+    const double wxm = m.half(in.um0) + m.half(in.u0);
+    const double wxp = m.half(in.um1) + m.half(in.u1);
+    const double adv1 = -(C(k.cm, wxm, k.e_cm) * gxm) - (C(k.cp, wxp, k.e_cp) * gxp);
+    const double pyp = m.half(m.half(in.v0) + m.half(in.v0n)) * gyp;
+    const double adv2 = -in.pym_v - pyp;
+    const double dif1 = D(nu * (gxp - gxm), k.vf_c, k.rvf_c, k.e_rvf_c);
+    const double dif2 = D(nu * (gyp - in.gym_v), dy, rdy, k.e_rdy);
+    const double pre = -D(in.pc - in.pm, dy, rdy, k.e_rdy);
+    double A = adv1 + adv2;
+    if (!IMPX) A = A + dif1;
+    if (!IMPY) A = A + dif2;
+    double G;
+    if (IMPX && IMPY) {
+      G = (dif1 + dif2) + pre;
+    } else if (IMPX) {
+      G = dif1 + pre;
+    } else if (IMPY) {
+      G = dif2 + pre;
+    } else {
+      G = pre;
+    }
+    double q = a.s.adt * A;
+    if (a.s.has_b) q = q + a.s.bdt * in.auy;
+    q = q + a.s.gdt * G;
+    o.ay = A;
+    o.qy = q;
+    o.uy = in.v0 + q;
+    o.gym_v = gyp;
+    o.pym_v = pyp;
+  }
+  return m.ok;
+}
+
+template <int IMPX, int IMPY, bool RCP, bool FAST>
 __global__ void __launch_bounds__(128) k_vel(const VelArgs a) {
   const int nx = a.g.nx, ny = a.g.ny;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -125,125 +280,111 @@ __global__ void __launch_bounds__(128) k_vel(const VelArgs a) {
   const int y1 = min(y0 + kRows, ny);
   const bool left = x == 0, right = x == nx - 1;
   const bool has_ux = x >= 1;  // ux is updated for i = 2..itot
-  const double dy = a.g.dy, rdy = a.g.rdy, nu = a.s.nu;
-  // ux at i = x+1: DXF(i-1), DXF(i), DXC(i); uy at i = x+1: DXC(i), DXC(i+1), DXF(i)
-  const double uf_m = has_ux ? a.g.dxf[x - 1] : 1.0, uf_p = a.g.dxf[x], uc_c = a.g.dxc[x];
-  const double ruf_m = has_ux ? a.g.rdxf[x - 1] : 1.0, ruf_p = a.g.rdxf[x], ruc_c = a.g.rdxc[x];
-  const double fm = a.g.c_fm[x], fp = a.g.c_fp[x];
-  const double vc_m = a.g.dxc[x], vc_p = a.g.dxc[x + 1], vf_c = a.g.dxf[x];
-  const double rvc_m = a.g.rdxc[x], rvc_p = a.g.rdxc[x + 1], rvf_c = a.g.rdxf[x];
-  const double cm = a.g.c_cm[x], cp = a.g.c_cp[x];
+  const double dy = a.g.dy, rdy = a.g.rdy;
+  VelCol k;
+  k.uf_m = has_ux ? a.g.dxf[x - 1] : 1.0;
+  k.uf_p = a.g.dxf[x];
+  k.uc_c = a.g.dxc[x];
+  k.ruf_m = has_ux ? a.g.rdxf[x - 1] : 1.0;
+  k.ruf_p = a.g.rdxf[x];
+  k.ruc_c = a.g.rdxc[x];
+  k.fm = a.g.c_fm[x];
+  k.fp = a.g.c_fp[x];
+  k.vc_m = a.g.dxc[x];
+  k.vc_p = a.g.dxc[x + 1];
+  k.vf_c = a.g.dxf[x];
+  k.rvc_m = a.g.rdxc[x];
+  k.rvc_p = a.g.rdxc[x + 1];
+  k.rvf_c = a.g.rdxf[x];
+  k.cm = a.g.c_cm[x];
+  k.cp = a.g.c_cp[x];
+  if constexpr (FAST) {
+    k.e_ruf_m = p2_field(k.ruf_m);
+    k.e_ruf_p = p2_field(k.ruf_p);
+    k.e_ruc_c = p2_field(k.ruc_c);
+    k.e_fm = p2_field(k.fm);
+    k.e_fp = p2_field(k.fp);
+    k.e_rvc_m = p2_field(k.rvc_m);
+    k.e_rvc_p = p2_field(k.rvc_p);
+    k.e_rvf_c = p2_field(k.rvf_c);
+    k.e_cm = p2_field(k.cm);
+    k.e_cp = p2_field(k.cp);
+    k.e_rdy = p2_field(rdy);
+  } else {
+    k.e_ruf_m = k.e_ruf_p = k.e_ruc_c = k.e_fm = k.e_fp = k.e_rvc_m = k.e_rvc_p = k.e_rvf_c = k.e_cm = k.e_cp =
+        k.e_rdy = 0;
+  }
   const double *ux = a.ux, *uy = a.uy, *p = a.p;
 
+  VelIn in;
   const int ym = wrap_dn(y0, ny);
   const size_t r0 = (size_t)y0 * nx + x, rm = (size_t)ym * nx + x;
-  double u0 = ux[r0], u1 = right ? 0.0 : ux[r0 + 1];
-  double um0 = ux[rm], um1 = right ? 0.0 : ux[rm + 1];
-  double v0 = uy[r0];
-  double vl = left ? 0.0 : uy[r0 - 1];
-  double pm = p[rm];
+  in.u0 = ux[r0];
+  in.u1 = right ? 0.0 : ux[r0 + 1];
+  in.um0 = ux[rm];
+  in.um1 = right ? 0.0 : ux[rm + 1];
+  in.v0 = uy[r0];
+  in.vl = left ? 0.0 : uy[r0 - 1];
+  in.pm = p[rm];
   // y-faces between rows y0-1 and y0
-  double gym_u = dv<RCP>(u0 - um0, dy, rdy);
-  double pym_u = 0.0;
-  if (has_ux) pym_u = (0.5 * (fm * vl + fp * v0)) * gym_u;
+  in.gym_u = dv<RCP>(in.u0 - in.um0, dy, rdy);
+  in.pym_u = 0.0;
+  if (has_ux) in.pym_u = (0.5 * (k.fm * in.vl + k.fp * in.v0)) * in.gym_u;
   const double vm = uy[rm];
-  double gym_v = dv<RCP>(v0 - vm, dy, rdy);
-  double pym_v = (0.5 * (0.5 * vm + 0.5 * v0)) * gym_v;
+  in.gym_v = dv<RCP>(in.v0 - vm, dy, rdy);
+  in.pym_v = (0.5 * (0.5 * vm + 0.5 * in.v0)) * in.gym_v;
+  in.ul = in.pl = in.tfl = in.tfr = in.aux = in.auy = 0.0;
 
   for (int y = y0; y < y1; ++y) {
     const int yp = wrap_up(y, ny);
     const size_t r = (size_t)y * nx + x, rp = (size_t)yp * nx + x;
-    const double u0n = ux[rp];
-    const double u1n = right ? 0.0 : ux[rp + 1];
-    const double v0n = uy[rp];
-    const double vln = left ? 0.0 : uy[rp - 1];
-    const double vr = right ? 0.0 : uy[r + 1];
-    const double pc = p[r];
-    // ---- ux(i, j), i = x+1 >= 2
+    in.u0n = ux[rp];
+    in.u1n = right ? 0.0 : ux[rp + 1];
+    in.v0n = uy[rp];
+    in.vln = left ? 0.0 : uy[rp - 1];
+    in.vr = right ? 0.0 : uy[r + 1];
+    in.pc = p[r];
     if (has_ux) {
-      const double ul = ux[r - 1];
-      const double gxm = dv<RCP>(u0 - ul, uf_m, ruf_m);
-      const double gxp = dv<RCP>(u1 - u0, uf_p, ruf_p);
-      const double gyp = dv<RCP>(u0n - u0, dy, rdy);
-      const double vxm = 0.5 * ul + 0.5 * u0;
-      const double vxp = 0.5 * u0 + 0.5 * u1;
-      const double adv1 = -((fm * vxm) * gxm) - ((fp * vxp) * gxp);
-      const double pyp = (0.5 * (fm * vln + fp * v0n)) * gyp;
-      const double adv2 = -pym_u - pyp;
-      const double dif1 = dv<RCP>(nu * (gxp - gxm), uc_c, ruc_c);
-      const double dif2 = dv<RCP>(nu * (gyp - gym_u), dy, rdy);
-      const double pre = -dv<RCP>(pc - p[r - 1], uc_c, ruc_c);
-      double A = adv1 + adv2;
-      if (!IMPX) A = A + dif1;
-      if (!IMPY) A = A + dif2;
-      if (a.tf) A = A + (0.5 * a.tf[r - 1] + 0.5 * a.tf[r]);
-      double G;
-      if (IMPX && IMPY) {
-        G = (dif1 + dif2) + pre;
-      } else if (IMPX) {
-        G = dif1 + pre;
-      } else if (IMPY) {
-        G = dif2 + pre;
-      } else {
-        G = pre;
+      in.ul = ux[r - 1];
+      in.pl = p[r - 1];
+      if (a.tf) {
+        in.tfl = a.tf[r - 1];
+        in.tfr = a.tf[r];
       }
-      double q = a.s.adt * A;
-      if (a.s.has_b) q = q + a.s.bdt * a.aux[r];
-      q = q + a.s.gdt * G;
-      a.aux[r] = A;
-      if (IMPX || IMPY) {
-        a.qx[r] = q;
-      } else {
-        a.ux_out[r] = u0 + q;
-      }
-      gym_u = gyp;
-      pym_u = pyp;
+      if (a.s.has_b) in.aux = a.aux[r];
     }
-    // ---- uy(i, j), i = x+1 >= 1
-    {
-      const double gxm = dv<RCP>(v0 - vl, vc_m, rvc_m);
-      const double gxp = dv<RCP>(vr - v0, vc_p, rvc_p);
-      const double gyp = dv<RCP>(v0n - v0, dy, rdy);
-      const double wxm = 0.5 * um0 + 0.5 * u0;
-      const double wxp = 0.5 * um1 + 0.5 * u1;
-      const double adv1 = -((cm * wxm) * gxm) - ((cp * wxp) * gxp);
-      const double pyp = (0.5 * (0.5 * v0 + 0.5 * v0n)) * gyp;
-      const double adv2 = -pym_v - pyp;
-      const double dif1 = dv<RCP>(nu * (gxp - gxm), vf_c, rvf_c);
-      const double dif2 = dv<RCP>(nu * (gyp - gym_v), dy, rdy);
-      const double pre = -dv<RCP>(pc - pm, dy, rdy);
-      double A = adv1 + adv2;
-      if (!IMPX) A = A + dif1;
-      if (!IMPY) A = A + dif2;
-      double G;
-      if (IMPX && IMPY) {
-        G = (dif1 + dif2) + pre;
-      } else if (IMPX) {
-        G = dif1 + pre;
-      } else if (IMPY) {
-        G = dif2 + pre;
-      } else {
-        G = pre;
-      }
-      double q = a.s.adt * A;
-      if (a.s.has_b) q = q + a.s.bdt * a.auy[r];
-      q = q + a.s.gdt * G;
-      a.auy[r] = A;
-      if (IMPX || IMPY) {
-        a.qy[r] = q;
-      } else {
-        a.uy_out[r] = v0 + q;
-      }
-      gym_v = gyp;
-      pym_v = pyp;
+    if (a.s.has_b) in.auy = a.auy[r];
+    VelOut o;
+    if constexpr (FAST) {
+      if (!vel_row<IMPX, IMPY, RCP, true>(a, k, in, has_ux, o)) vel_row<IMPX, IMPY, RCP, false>(a, k, in, has_ux, o);
+    } else {
+      vel_row<IMPX, IMPY, RCP, false>(a, k, in, has_ux, o);
     }
-    um0 = u0;
-    um1 = u1;
-    u0 = u0n;
-    u1 = u1n;
-    v0 = v0n;
-    vl = vln;
-    pm = pc;
+    if (has_ux) {
+      a.aux[r] = o.ax;
+      if (IMPX || IMPY) {
+        a.qx[r] = o.qx;
+      } else {
+        a.ux_out[r] = o.ux;
+      }
+    }
+    a.auy[r] = o.ay;
+    if (IMPX || IMPY) {
+      a.qy[r] = o.qy;
+    } else {
+      a.uy_out[r] = o.uy;
+    }
+    in.gym_u = o.gym_u;
+    in.pym_u = o.pym_u;
+    in.gym_v = o.gym_v;
+    in.pym_v = o.pym_v;
+    in.um0 = in.u0;
+    in.um1 = in.u1;
+    in.u0 = in.u0n;
+    in.u1 = in.u1n;
+    in.v0 = in.v0n;
+    in.vl = in.vln;
+    in.pm = in.pc;
   }
 }
 
@@ -978,17 +1119,22 @@ cudaError_t launch_velocity_update(const DevGrid &g, const StageScalars &s, int 
                                    double *qx, double *qy, cudaStream_t st) {
   const VelArgs a{g, s, ux, uy, p, tforce, ux_out, uy_out, aux, auy, qx, qy};
   const dim3 grid = march_grid(g), block(kBlockX);
-#define SNS_V(X, Y, R) k_vel<X, Y, R><<<grid, block, 0, st>>>(a)
-  if (g.rcp) {
-    if (impx && impy) SNS_V(1, 1, true);
-    else if (impx) SNS_V(1, 0, true);
-    else if (impy) SNS_V(0, 1, true);
-    else SNS_V(0, 0, true);
+#define SNS_V(X, Y, R, F) k_vel<X, Y, R, F><<<grid, block, 0, st>>>(a)
+  if (g.p2) {
+    if (impx && impy) SNS_V(1, 1, true, true);
+    else if (impx) SNS_V(1, 0, true, true);
+    else if (impy) SNS_V(0, 1, true, true);
+    else SNS_V(0, 0, true, true);
+  } else if (g.rcp) {
+    if (impx && impy) SNS_V(1, 1, true, false);
+    else if (impx) SNS_V(1, 0, true, false);
+    else if (impy) SNS_V(0, 1, true, false);
+    else SNS_V(0, 0, true, false);
   } else {
-    if (impx && impy) SNS_V(1, 1, false);
-    else if (impx) SNS_V(1, 0, false);
-    else if (impy) SNS_V(0, 1, false);
-    else SNS_V(0, 0, false);
+    if (impx && impy) SNS_V(1, 1, false, false);
+    else if (impx) SNS_V(1, 0, false, false);
+    else if (impy) SNS_V(0, 1, false, false);
+    else SNS_V(0, 0, false, false);
   }
 #undef SNS_V
   count_launches(1);

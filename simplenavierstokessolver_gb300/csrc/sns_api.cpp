@@ -255,6 +255,18 @@ static int build_context(Context *c, const param_t *param) {
     rdxc[i - 1] = 1.0 / DXC(i);
     dxi[i - 1] = 1. / DXC(i);  // src/fluid/correct_velocity.c:13
   }
+  {
+    // the velocity kernel's power-of-two products in integer arithmetic
+    auto p2 = [](double v) {
+      int e;
+      return is_pow2_double(v) && (std::frexp(v, &e), std::abs(e - 1) <= 64);
+    };
+    bool ok = rcp && p2(g.rdy);
+    for (int i = 0; i < nx; i++) ok = ok && p2(rdxf[i]) && p2(ccm[i]) && p2(ccp[i]);
+    for (int i = 0; i <= nx; i++) ok = ok && p2(rdxc[i]);
+    for (int i = 1; i < nx; i++) ok = ok && p2(cfm[i]) && p2(cfp[i]);
+    g.p2 = ok;
+  }
   int rc = SNS_OK;
   if ((rc = upload(c, &g.dxf, c->dxf)) || (rc = upload(c, &g.dxc, c->dxc)) || (rc = upload(c, &g.rdxf, rdxf)) ||
       (rc = upload(c, &g.rdxc, rdxc)) || (rc = upload(c, &g.dxi, dxi)) || (rc = upload(c, &g.c_cm, ccm)) ||

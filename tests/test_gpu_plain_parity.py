@@ -127,6 +127,54 @@ def test_each_hot_path_call_matches(costs, stretch):
             assert_bitwise(c.get_state(), o.get_state(), ("p",), f"fluid_update_pressure rk={rk}")
 
 
+@pytest.mark.parametrize("implicit", [0, 1], ids=["exp_exp", "imp_imp"])
+def test_velocity_update_with_extreme_magnitudes(implicit):
+    """On a uniform power-of-two grid the velocity kernel forms its products by
+    powers of two in integer arithmetic and recomputes a row with FP64
+    products when an operand is a subnormal, infinite or beyond 2^+-958.
+    Seeded fields with exact zeros, subnormals, tiny and huge normals must
+    still match the oracle bit for bit."""
+    cfg = Config(64, 32, ly=0.5, Ra=2e5, Pr=0.8)
+    rng = np.random.default_rng(5)
+    su, sc = (cfg.jtot + 2, cfg.itot + 1), (cfg.jtot + 2, cfg.itot + 2)
+
+    def sprinkle(a, huge=False):
+        pick = rng.uniform(size=a.shape)
+        sign = np.where(rng.uniform(size=a.shape) < 0.5, -1.0, 1.0)
+        a[pick < 0.05] = 0.0
+        a[(pick >= 0.05) & (pick < 0.07)] = (sign * 5e-320)[(pick >= 0.05) & (pick < 0.07)]
+        a[(pick >= 0.07) & (pick < 0.09)] = (sign * 3e-295)[(pick >= 0.07) & (pick < 0.09)]
+        a[(pick >= 0.09) & (pick < 0.10)] = (sign * 1e150)[(pick >= 0.09) & (pick < 0.10)]
+        if huge:
+            a[(pick >= 0.10) & (pick < 0.11)] = (sign * 1e290)[(pick >= 0.10) & (pick < 0.11)]
+        return a
+
+    state = (sprinkle(0.2 * rng.uniform(-1, 1, su)), sprinkle(0.2 * rng.uniform(-1, 1, sc)),
+             sprinkle(0.05 * rng.uniform(-1, 1, sc), huge=True), sprinkle(rng.uniform(-0.5, 0.5, sc)))
+    src = {"srcuxa": sprinkle(rng.uniform(-1, 1, (cfg.jtot, cfg.itot - 1))),
+           "srcuya": sprinkle(rng.uniform(-1, 1, (cfg.jtot, cfg.itot))),
+           "srctempa": rng.uniform(-1, 1, (cfg.jtot, cfg.itot))}
+    o = OracleCase(cfg)
+    o.set_state(*state)
+    o.set_sources(src["srcuxa"], src["srcuya"], src["srctempa"])
+    with gpu_case(cfg, [1, 2, 2, 3]) as c:
+        c.set_state(*state, sources=src)
+        o.call("update_boundaries")
+        # a fixed dt: the huge velocities would make the chosen one vanishingly small
+        for x in (c, o):
+            x.set_dt(1e-3, implicit, implicit)
+        for rk in range(2):
+            c.temperature_compute_force()
+            c.temperature_update_temp(rk)
+            o.call("temperature_force_and_update", rk)
+            c.fluid_update_velocity(rk)
+            o.call("fluid_update_velocity", rk)
+            # the huge seeds overflow by the second substage: NaN where the oracle has NaN
+            for got, want in ((c.get_state(), o.get_state()), (c.get_sources(), o.get_sources())):
+                for k in set(got) & {"ux", "uy", "srcuxa", "srcuya"}:
+                    assert np.array_equal(got[k], want[k], equal_nan=True), f"{k} after rk={rk}"
+
+
 def test_rayleigh_benard_128x256_long_run_is_bitwise():
     """The 128x256, Ra=1e8, Pr=1 Rayleigh-Benard case from the reference's own
     initial condition (srand(0)), 300 steps of the fused path."""
