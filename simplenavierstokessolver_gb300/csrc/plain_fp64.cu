@@ -1005,7 +1005,7 @@ __global__ void __launch_bounds__(128) k_corr(const CorrArgs a) {
   unsigned long long mx = 0ull, my = 0ull;
   if (live) {
     const int y0 = blockIdx.y * kCorrRows;
-    const int y1 = min(y0 + kCorrRows, ny);
+    int y1 = min(y0 + kCorrRows, ny);
     const double gdt = a.s.gdt, dy = a.g.dy, rdy = a.g.rdy;
     const double dxi = a.g.dxi[x];
     const double dcm = a.g.dxc[x], dcp = a.g.dxc[x + 1], df = a.g.dxf[x];
@@ -1013,6 +1013,40 @@ __global__ void __launch_bounds__(128) k_corr(const CorrArgs a) {
     const bool left = x == 0, right = x == nx - 1;
     const double *psi = a.psi;
     double sm = psi[(size_t)wrap_dn(y0, ny) * nx + x];
+    if constexpr (!IMPX && !IMPY && CORR && PRES) {
+      if (y1 - y0 == kCorrRows) {
+        // every operand of the rows loaded before the first store (the
+        // stores could alias later loads for the compiler): one memory round
+        // trip per thread instead of kCorrRows
+        double ps[kCorrRows], pw[kCorrRows], u[kCorrRows], v[kCorrRows], pp[kCorrRows];
+#pragma unroll
+        for (int k = 0; k < kCorrRows; ++k) {
+          const size_t r = (size_t)(y0 + k) * nx + x;
+          ps[k] = psi[r];
+          pw[k] = left ? 0.0 : psi[r - 1];
+          u[k] = left ? 0.0 : a.ux[r];
+          v[k] = a.uy[r];
+          pp[k] = a.p[r];
+        }
+#pragma unroll
+        for (int k = 0; k < kCorrRows; ++k) {
+          const size_t r = (size_t)(y0 + k) * nx + x;
+          const double sc = ps[k];
+          const double sl = left ? sc : pw[k];  // Neumann psi(0) = psi(1)
+          if (!left) {
+            const double un = u[k] - ((gdt * (sc - sl)) * dxi);
+            a.ux[r] = un;
+            mx = max(mx, abs_bits(un));
+          }
+          const double vn = v[k] - dv<RCP>(gdt * (sc - sm), dy, rdy);
+          a.uy[r] = vn;
+          my = max(my, abs_bits(vn));
+          a.p[r] = pp[k] + sc;
+          sm = sc;
+        }
+        y1 = y0;  // done: skip the row loop below
+      }
+    }
     for (int y = y0; y < y1; ++y) {
       const size_t r = (size_t)y * nx + x;
       const double sc = psi[r];
