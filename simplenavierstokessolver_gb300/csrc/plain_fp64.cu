@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cfloat>
 #include <cstdint>
+#include <type_traits>
 
 #include "fft_dev.cuh"
 #include "sns_internal.h"
@@ -37,83 +38,14 @@ __device__ __forceinline__ int wrap_dn(int y, int ny) { return y == 0 ? ny - 1 :
 constexpr int kRows = 8;     // rows marched by one thread in the stencil kernels
 constexpr int kBlockX = 64;  // columns per block: ~6-7 blocks per SM at 512 x 1024 for load balance
 
-// ---------------------------------------------------------------- temperature
-struct TempArgs {
-  DevGrid g;
-  StageScalars s;
-  const double *t_in;
-  double *t_out, *at, *qt;
-  const double *ux, *uy;
-};
-
-// src/temperature/update.c:11-87 (sources) and :114-122, :221-226 (RK3 update)
-// for column x, rows y0 .. y0+kRows-1
-template <int IMPX, int IMPY, bool RCP>
-__device__ __forceinline__ void temp_column(const TempArgs &a, int x, int y0) {
-  const int nx = a.g.nx, ny = a.g.ny;
-  const int y1 = min(y0 + kRows, ny);
-  const double *T = a.t_in;
-  const double dcm = a.g.dxc[x], dcp = a.g.dxc[x + 1], df = a.g.dxf[x];
-  const double rcm = a.g.rdxc[x], rcp = a.g.rdxc[x + 1], rf = a.g.rdxf[x];
-  const double cm = a.g.c_cm[x], cp = a.g.c_cp[x];
-  const double dy = a.g.dy, rdy = a.g.rdy, kappa = a.s.kappa;
-  const bool left = x == 0, right = x == nx - 1;
-  double tc = T[(size_t)y0 * nx + x];
-  // y-face between rows y0-1 and y0 (periodic halo, src/temperature/boundary_conditions.c:13-14)
-  double gym = dv<RCP>(tc - T[(size_t)wrap_dn(y0, ny) * nx + x], dy, rdy);
-  double pym = (0.5 * a.uy[(size_t)y0 * nx + x]) * gym;
-  for (int y = y0; y < y1; ++y) {
-    const int yp = wrap_up(y, ny);
-    const size_t r = (size_t)y * nx + x;
-    const double tp = T[(size_t)yp * nx + x];
-    const double tl = left ? kTempXm : T[r - 1];
-    const double tr = right ? kTempXp : T[r + 1];
-    const double gxm = dv<RCP>(tc - tl, dcm, rcm);
-    const double gxp = dv<RCP>(tr - tc, dcp, rcp);
-    const double gyp = dv<RCP>(tp - tc, dy, rdy);
-    const double pyp = (0.5 * a.uy[(size_t)yp * nx + x]) * gyp;
-    const double uxm = a.ux[r];
-    const double uxp = right ? 0.0 : a.ux[r + 1];
-    const double adv1 = -((cm * uxm) * gxm) - ((cp * uxp) * gxp);
-    const double adv2 = -pym - pyp;
-    const double dif1 = dv<RCP>(kappa * (gxp - gxm), df, rf);
-    const double dif2 = dv<RCP>(kappa * (gyp - gym), dy, rdy);
-    double A = adv1 + adv2;
-    if (!IMPX) A = A + dif1;
-    if (!IMPY) A = A + dif2;
-    double q = a.s.adt * A;
-    if (a.s.has_b) q = q + a.s.bdt * a.at[r];
-    if (IMPX || IMPY) {
-      const double G = (IMPX && IMPY) ? dif1 + dif2 : (IMPX ? dif1 : dif2);
-      q = q + a.s.gdt * G;
-    }
-    a.at[r] = A;
-    if (IMPX || IMPY) {
-      a.qt[r] = q;
-    } else {
-      a.t_out[r] = tc + q;
-    }
-    tc = tp;
-    gym = gyp;
-    pym = pyp;
-  }
-}
-
-template <int IMPX, int IMPY, bool RCP>
-__global__ void __launch_bounds__(128) k_temp(const TempArgs a) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= a.g.nx) return;
-  temp_column<IMPX, IMPY, RCP>(a, x, blockIdx.y * kRows);
-}
-
 // ------------------------------------------------- exact power-of-two products
 // x * 2^e is exact when x and the product are normal numbers, or x is zero,
 // and then equals x with its exponent field moved by e. GB300 issues FP64
 // instructions at a small fraction of its integer rate, so on grids whose
 // spacings are powers of two (DevGrid::p2: the reciprocal spacings and the
-// advective coefficients are then powers of two too) the velocity kernel
-// takes those products, and the 1/2 of every interpolation, in the integer
-// unit. An operand other than zero whose exponent field lies outside
+// advective coefficients are then powers of two too) the velocity,
+// temperature and correction kernels take those products, and the 1/2 of
+// every interpolation, in the integer unit. An operand other than zero whose exponent field lies outside
 // [1 + kP2Margin, 0x7fe - kP2Margin] (magnitude below 2^-958 or from 2^958 up,
 // subnormals, infinities, NaN), where the moved field could leave the normal
 // range, clears the row's flag and the row is recomputed with FP64 products.
@@ -141,6 +73,132 @@ struct Mul {
   }
   __device__ __forceinline__ double half(double x) { return by(x, 0.5, -(1 << 20)); }
 };
+
+// ---------------------------------------------------------------- temperature
+struct TempArgs {
+  DevGrid g;
+  StageScalars s;
+  const double *t_in;
+  double *t_out, *at, *qt;
+  const double *ux, *uy;
+};
+
+// one row of the temperature update: tc = T(x, y), gym, pym the y-face
+// terms between rows y-1 and y; tp, tl, tr, uyp, uxm, uxp this row's loads
+struct TempRow {
+  double A, q, gyp, pyp;
+};
+
+template <int IMPX, int IMPY, bool RCP, bool FAST>
+__device__ __forceinline__ bool temp_row(const TempArgs &a, double tc, double gym, double pym, double tp, double tl,
+                                         double tr, double uyp, double uxm, double uxp, double atr, double dcm,
+                                         double dcp, double df, double rcm, double rcp, double rf, double cm,
+                                         double cp, const int *e, TempRow &o) {
+  Mul<FAST> m;
+  const double dy = a.g.dy, rdy = a.g.rdy, kappa = a.s.kappa;
+  auto D = [&](double v, double d, double rd, int E) {
+    if constexpr (FAST) {
+      return m.by(v, rd, E);
+    } else {
+      return dv<RCP>(v, d, rd);
+    }
+  };
+  auto Cf = [&](double c, double v, int E) {
+    if constexpr (FAST) {
+      return m.by(v, c, E);
+    } else {
+      return c * v;
+    }
+  };
+  // e: exponents of rcm, rcp, rdy, rf, cm, cp
+  const double gxm = D(tc - tl, dcm, rcm, e[0]);
+  const double gxp = D(tr - tc, dcp, rcp, e[1]);
+  const double gyp = D(tp - tc, dy, rdy, e[2]);
+  const double pyp = m.half(uyp) * gyp;
+  const double adv1 = -(Cf(cm, uxm, e[4]) * gxm) - (Cf(cp, uxp, e[5]) * gxp);
+  const double adv2 = -pym - pyp;
+  const double dif1 = D(kappa * (gxp - gxm), df, rf, e[3]);
+  const double dif2 = D(kappa * (gyp - gym), dy, rdy, e[2]);
+  double A = adv1 + adv2;
+  if (!IMPX) A = A + dif1;
+  if (!IMPY) A = A + dif2;
+  double q = a.s.adt * A;
+  if (a.s.has_b) q = q + a.s.bdt * atr;
+  if (IMPX || IMPY) {
+    const double G = (IMPX && IMPY) ? dif1 + dif2 : (IMPX ? dif1 : dif2);
+    q = q + a.s.gdt * G;
+  }
+  o.A = A;
+  o.q = q;
+  o.gyp = gyp;
+  o.pyp = pyp;
+  return m.ok;
+}
+
+// src/temperature/update.c:11-87 (sources) and :114-122, :221-226 (RK3 update)
+// for column x, rows y0 .. y0+kRows-1. FAST: the products by powers of two in
+// the integer unit, a row outside their range recomputed with FP64 products.
+template <int IMPX, int IMPY, bool RCP, bool FAST>
+__device__ __forceinline__ void temp_column(const TempArgs &a, int x, int y0) {
+  const int nx = a.g.nx, ny = a.g.ny;
+  const int y1 = min(y0 + kRows, ny);
+  const double *T = a.t_in;
+  const double dcm = a.g.dxc[x], dcp = a.g.dxc[x + 1], df = a.g.dxf[x];
+  const double rcm = a.g.rdxc[x], rcp = a.g.rdxc[x + 1], rf = a.g.rdxf[x];
+  const double cm = a.g.c_cm[x], cp = a.g.c_cp[x];
+  const double dy = a.g.dy, rdy = a.g.rdy;
+  int e[6] = {0, 0, 0, 0, 0, 0};
+  if constexpr (FAST) {
+    e[0] = p2_field(rcm);
+    e[1] = p2_field(rcp);
+    e[2] = p2_field(rdy);
+    e[3] = p2_field(rf);
+    e[4] = p2_field(cm);
+    e[5] = p2_field(cp);
+  }
+  const bool left = x == 0, right = x == nx - 1;
+  double tc = T[(size_t)y0 * nx + x];
+  // y-face between rows y0-1 and y0 (periodic halo, src/temperature/boundary_conditions.c:13-14)
+  double gym = dv<RCP>(tc - T[(size_t)wrap_dn(y0, ny) * nx + x], dy, rdy);
+  double pym = (0.5 * a.uy[(size_t)y0 * nx + x]) * gym;
+  for (int y = y0; y < y1; ++y) {
+    const int yp = wrap_up(y, ny);
+    const size_t r = (size_t)y * nx + x;
+    const double tp = T[(size_t)yp * nx + x];
+    const double tl = left ? kTempXm : T[r - 1];
+    const double tr = right ? kTempXp : T[r + 1];
+    const double uyp = a.uy[(size_t)yp * nx + x];
+    const double uxm = a.ux[r];
+    const double uxp = right ? 0.0 : a.ux[r + 1];
+    const double atr = a.s.has_b ? a.at[r] : 0.0;
+    TempRow o;
+    if constexpr (FAST) {
+      if (!temp_row<IMPX, IMPY, RCP, true>(a, tc, gym, pym, tp, tl, tr, uyp, uxm, uxp, atr, dcm, dcp, df, rcm, rcp, rf,
+                                           cm, cp, e, o))
+        temp_row<IMPX, IMPY, RCP, false>(a, tc, gym, pym, tp, tl, tr, uyp, uxm, uxp, atr, dcm, dcp, df, rcm, rcp, rf,
+                                         cm, cp, e, o);
+    } else {
+      temp_row<IMPX, IMPY, RCP, false>(a, tc, gym, pym, tp, tl, tr, uyp, uxm, uxp, atr, dcm, dcp, df, rcm, rcp, rf, cm,
+                                       cp, e, o);
+    }
+    a.at[r] = o.A;
+    if (IMPX || IMPY) {
+      a.qt[r] = o.q;
+    } else {
+      a.t_out[r] = tc + o.q;
+    }
+    tc = tp;
+    gym = o.gyp;
+    pym = o.pyp;
+  }
+}
+
+template <int IMPX, int IMPY, bool RCP, bool FAST>
+__global__ void __launch_bounds__(128) k_temp(const TempArgs a) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= a.g.nx) return;
+  temp_column<IMPX, IMPY, RCP, FAST>(a, x, blockIdx.y * kRows);
+}
 
 // ------------------------------------------------------------------ velocity
 struct VelArgs {
@@ -944,7 +1002,13 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_poisson_fused(const FusedA
     const int xb = (nx + kFusedThreads - 1) / kFusedThreads, yb = (g.ny + kRows - 1) / kRows;
     for (int u = wk; u < xb * yb; u += W) {
       const int x = (u % xb) * kFusedThreads + threadIdx.x;
-      if (x < nx) temp_column<0, 0, RCP>(a.t, x, (u / xb) * kRows);
+      if (x < nx) {
+        if (RCP && g.p2) {
+          temp_column<0, 0, RCP, RCP>(a.t, x, (u / xb) * kRows);
+        } else {
+          temp_column<0, 0, RCP, false>(a.t, x, (u / xb) * kRows);
+        }
+      }
     }
   }
   // inverse DFT column groups, descending x, once every sweep warp passed them
@@ -1028,21 +1092,38 @@ __global__ void __launch_bounds__(128) k_corr(const CorrArgs a) {
           v[k] = a.uy[r];
           pp[k] = a.p[r];
         }
+        // the rows' new values; FAST: the products by 1/dx and 1/dy (powers of
+        // two on such grids) in the integer unit, false when out of range
+        auto rows = [&](auto fast, double *un, double *vn) -> bool {
+          Mul<decltype(fast)::value> m;
+          double s0 = sm;
+#pragma unroll
+          for (int k = 0; k < kCorrRows; ++k) {
+            const double sc = ps[k];
+            const double sl = left ? sc : pw[k];  // Neumann psi(0) = psi(1)
+            if constexpr (decltype(fast)::value) {
+              un[k] = u[k] - m.by(gdt * (sc - sl), dxi, p2_field(dxi));
+              vn[k] = v[k] - m.by(gdt * (sc - s0), rdy, p2_field(rdy));
+            } else {
+              un[k] = u[k] - ((gdt * (sc - sl)) * dxi);
+              vn[k] = v[k] - dv<RCP>(gdt * (sc - s0), dy, rdy);
+            }
+            s0 = sc;
+          }
+          return m.ok;
+        };
+        double un[kCorrRows], vn[kCorrRows];
+        if (!(RCP && a.g.p2 && rows(std::true_type{}, un, vn))) rows(std::false_type{}, un, vn);
 #pragma unroll
         for (int k = 0; k < kCorrRows; ++k) {
           const size_t r = (size_t)(y0 + k) * nx + x;
-          const double sc = ps[k];
-          const double sl = left ? sc : pw[k];  // Neumann psi(0) = psi(1)
           if (!left) {
-            const double un = u[k] - ((gdt * (sc - sl)) * dxi);
-            a.ux[r] = un;
-            mx = max(mx, abs_bits(un));
+            a.ux[r] = un[k];
+            mx = max(mx, abs_bits(un[k]));
           }
-          const double vn = v[k] - dv<RCP>(gdt * (sc - sm), dy, rdy);
-          a.uy[r] = vn;
-          my = max(my, abs_bits(vn));
-          a.p[r] = pp[k] + sc;
-          sm = sc;
+          a.uy[r] = vn[k];
+          my = max(my, abs_bits(vn[k]));
+          a.p[r] = pp[k] + ps[k];
         }
         y1 = y0;  // done: skip the row loop below
       }
@@ -1130,17 +1211,22 @@ cudaError_t launch_temp_update(const DevGrid &g, const StageScalars &s, int impx
                                const double *ux, const double *uy, cudaStream_t st) {
   const TempArgs a{g, s, t_in, t_out, at, qt, ux, uy};
   const dim3 grid = march_grid(g), block(kBlockX);
-#define SNS_T(X, Y, R) k_temp<X, Y, R><<<grid, block, 0, st>>>(a)
-  if (g.rcp) {
-    if (impx && impy) SNS_T(1, 1, true);
-    else if (impx) SNS_T(1, 0, true);
-    else if (impy) SNS_T(0, 1, true);
-    else SNS_T(0, 0, true);
+#define SNS_T(X, Y, R, F) k_temp<X, Y, R, F><<<grid, block, 0, st>>>(a)
+  if (g.p2) {
+    if (impx && impy) SNS_T(1, 1, true, true);
+    else if (impx) SNS_T(1, 0, true, true);
+    else if (impy) SNS_T(0, 1, true, true);
+    else SNS_T(0, 0, true, true);
+  } else if (g.rcp) {
+    if (impx && impy) SNS_T(1, 1, true, false);
+    else if (impx) SNS_T(1, 0, true, false);
+    else if (impy) SNS_T(0, 1, true, false);
+    else SNS_T(0, 0, true, false);
   } else {
-    if (impx && impy) SNS_T(1, 1, false);
-    else if (impx) SNS_T(1, 0, false);
-    else if (impy) SNS_T(0, 1, false);
-    else SNS_T(0, 0, false);
+    if (impx && impy) SNS_T(1, 1, false, false);
+    else if (impx) SNS_T(1, 0, false, false);
+    else if (impy) SNS_T(0, 1, false, false);
+    else SNS_T(0, 0, false, false);
   }
 #undef SNS_T
   count_launches(1);

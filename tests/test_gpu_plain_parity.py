@@ -129,11 +129,11 @@ def test_each_hot_path_call_matches(costs, stretch):
 
 @pytest.mark.parametrize("implicit", [0, 1], ids=["exp_exp", "imp_imp"])
 def test_velocity_update_with_extreme_magnitudes(implicit):
-    """On a uniform power-of-two grid the velocity kernel forms its products by
-    powers of two in integer arithmetic and recomputes a row with FP64
-    products when an operand is a subnormal, infinite or beyond 2^+-958.
-    Seeded fields with exact zeros, subnormals, tiny and huge normals must
-    still match the oracle bit for bit."""
+    """On a uniform power-of-two grid the velocity and temperature kernels form
+    their products by powers of two in integer arithmetic and recompute a row
+    with FP64 products when an operand is a subnormal, infinite or beyond
+    2^+-958. Seeded fields with exact zeros, subnormals, tiny and huge normals
+    must still match the oracle bit for bit."""
     cfg = Config(64, 32, ly=0.5, Ra=2e5, Pr=0.8)
     rng = np.random.default_rng(5)
     su, sc = (cfg.jtot + 2, cfg.itot + 1), (cfg.jtot + 2, cfg.itot + 2)
@@ -167,12 +167,46 @@ def test_velocity_update_with_extreme_magnitudes(implicit):
             c.temperature_compute_force()
             c.temperature_update_temp(rk)
             o.call("temperature_force_and_update", rk)
+            assert np.array_equal(c.get_state()["temp"], o.get_state()["temp"], equal_nan=True), f"temp after rk={rk}"
             c.fluid_update_velocity(rk)
             o.call("fluid_update_velocity", rk)
             # the huge seeds overflow by the second substage: NaN where the oracle has NaN
             for got, want in ((c.get_state(), o.get_state()), (c.get_sources(), o.get_sources())):
                 for k in set(got) & {"ux", "uy", "srcuxa", "srcuya"}:
                     assert np.array_equal(got[k], want[k], equal_nan=True), f"{k} after rk={rk}"
+
+
+@pytest.mark.parametrize("costs", [[1, 2, 2, 3], [4, 3, 2, 1]], ids=["exp_exp", "imp_imp"])
+def test_whole_steps_with_tiny_magnitudes(costs):
+    """Whole steps (the fused path: velocity, temperature, Poisson and the
+    correction/pressure kernel) from fields with exact zeros, subnormals and
+    normals below 2^-958 in every field: the rows that hold them take the
+    FP64 products, the others the integer ones, and the result is the
+    oracle's bit for bit."""
+    cfg = Config(64, 64, ly=1.0, Ra=1e6, Pr=0.8)
+    rng = np.random.default_rng(9)
+    su, sc = (cfg.jtot + 2, cfg.itot + 1), (cfg.jtot + 2, cfg.itot + 2)
+
+    def sprinkle(a):
+        pick = rng.uniform(size=a.shape)
+        sign = np.where(rng.uniform(size=a.shape) < 0.5, -1.0, 1.0)
+        a[pick < 0.05] = 0.0
+        a[(pick >= 0.05) & (pick < 0.08)] = (sign * 5e-320)[(pick >= 0.05) & (pick < 0.08)]
+        a[(pick >= 0.08) & (pick < 0.11)] = (sign * 3e-295)[(pick >= 0.08) & (pick < 0.11)]
+        return a
+
+    state = (sprinkle(0.2 * rng.uniform(-1, 1, su)), sprinkle(0.2 * rng.uniform(-1, 1, sc)),
+             sprinkle(0.05 * rng.uniform(-1, 1, sc)), sprinkle(rng.uniform(-0.5, 0.5, sc)))
+    o = OracleCase(cfg)
+    o.set_costs(costs)
+    o.set_state(*state)
+    with gpu_case(cfg, costs) as c:
+        c.set_state(*state)
+        o.call("update_boundaries")
+        c.run(2)
+        o.run(2)
+        assert c.get_dt() == o.get_dt()
+        assert_bitwise(c.get_state(), o.get_state(), FIELDS, "after 2 steps from tiny magnitudes")
 
 
 def test_rayleigh_benard_128x256_long_run_is_bitwise():
