@@ -861,14 +861,18 @@ __device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
   const size_t jp = (size_t)g.jpitch, vs = 2 * jp;
   double *col = reinterpret_cast<double *>(a.p.spec + Jc) + (lg & 1);
   const double *inv = g.pinv + Jc, *up = g.pup + Jc;
-  int vg = 0;  // groups 0 .. vg-1 are verified complete
+  int vg = 0;       // groups 0 .. vg-1 are verified complete
+  int ready = 0;    // rows below are readable: vg * C
   // make rows up to x readable: the lanes read the next 64
   // completion flags (two each, relaxed), the leading run of complete groups
   // is taken (polling while x's group is not among them), and one fence then
-  // orders the row reads after them
+  // orders the row reads after them. The test on the path taken once per
+  // chunk is one comparison (an integer division there cost ~12 us per
+  // launch at 512 x 1024: it runs between chunks, outside the latency
+  // shadows of the recurrence).
   auto need = [&](int x) -> bool {
+    if (x < ready) return true;
     const int gx = x / C;
-    if (gx < vg) return true;
     unsigned spin = 0;
     while (vg <= gx) {
       const int g0 = vg + lane, g1 = vg + 32 + lane;
@@ -882,6 +886,7 @@ __device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
         __nanosleep(64);
       }
     }
+    ready = min(vg * C, nx);
     __threadfence();
     return true;
   };
