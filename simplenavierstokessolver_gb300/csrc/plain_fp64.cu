@@ -964,9 +964,12 @@ __device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
         const double v = cq[k] - cu[k] * next;
         if (act) col[(size_t)x * vs] = v;
         next = v;
-        if (x % kFusedSpan == 0) signal(x / kFusedSpan);
       }
     }
+    // a span whose lowest element this chunk passed is final: signalled once
+    // per chunk, after it, instead of a test inside the recurrence
+    const int sb = (b / kFusedSpan) * kFusedSpan;
+    if (sb >= max(b - kLineChunk + 1, 0)) signal(sb / kFusedSpan);
 #pragma unroll
     for (int k = 0; k < kLineChunk; ++k) {
       cq[k] = nq[k];
