@@ -902,8 +902,9 @@ __device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
     cq[k] = e < nx ? __ldcg(col + (size_t)e * vs) : 0.0;
     ci[k] = e < nx ? __ldg(inv + (size_t)e * jp) : 0.0;
   }
-#pragma unroll 1
-  for (int b = 1; b < nx; b += kLineChunk) {
+  // one chunk of rows b .. b+kLineChunk-1; the full chunks run without a
+  // per-row guard inside the recurrence, only the last one needs it
+  auto forward_chunk = [&](int b, auto guarded) -> bool {
     double nq[kLineChunk], ni[kLineChunk];
     const int nb = b + kLineChunk;
     if (nb < nx && !need(min(nb + kLineChunk - 1, nx - 1))) return false;
@@ -916,7 +917,7 @@ __device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
 #pragma unroll
     for (int k = 0; k < kLineChunk; ++k) {
       const int x = b + k;
-      if (x < nx) {
+      if (!decltype(guarded)::value || x < nx) {
         const double iv = ci[k];
         // |pivot| < DBL_EPSILON rows carry 1/pivot = +0: the reference sets them to 0
         const double v = __double_as_longlong(iv) == 0 ? 0.0 : iv * (cq[k] - pl[x] * prev);
@@ -929,7 +930,13 @@ __device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
       cq[k] = nq[k];
       ci[k] = ni[k];
     }
-  }
+    return true;
+  };
+  int b = 1;
+#pragma unroll 1
+  for (; b + kLineChunk <= nx; b += kLineChunk)
+    if (!forward_chunk(b, std::false_type{})) return false;
+  if (b < nx && !forward_chunk(b, std::true_type{})) return false;
   // ---- back substitution (src/linalg.c:46-48), x = nx-2 .. 0; span s is
   // final once x passes its lowest element
   auto signal = [&](int s) {
@@ -948,8 +955,7 @@ __device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
     cq[k] = e >= 0 ? __ldcg(col + (size_t)e * vs) : 0.0;
     cu[k] = e >= 0 ? __ldg(up + (size_t)e * jp) : 0.0;
   }
-#pragma unroll 1
-  for (int b = hi; b >= 0; b -= kLineChunk) {
+  auto backward_chunk = [&](int b, auto guarded) {
     double nq[kLineChunk], nu[kLineChunk];
 #pragma unroll
     for (int k = 0; k < kLineChunk; ++k) {
@@ -960,7 +966,7 @@ __device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
 #pragma unroll
     for (int k = 0; k < kLineChunk; ++k) {
       const int x = b - k;
-      if (x >= 0) {
+      if (!decltype(guarded)::value || x >= 0) {
         const double v = cq[k] - cu[k] * next;
         if (act) col[(size_t)x * vs] = v;
         next = v;
@@ -975,7 +981,11 @@ __device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
       cq[k] = nq[k];
       cu[k] = nu[k];
     }
-  }
+  };
+  int bb = hi;
+#pragma unroll 1
+  for (; bb - kLineChunk + 1 >= 0; bb -= kLineChunk) backward_chunk(bb, std::false_type{});
+  if (bb >= 0) backward_chunk(bb, std::true_type{});
   return true;
 }
 
