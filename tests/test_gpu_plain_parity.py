@@ -231,6 +231,21 @@ def test_rayleigh_benard_512x1024_is_bitwise():
         assert_bitwise(c.get_state(), o.get_state(), FIELDS, "512x1024 after 4 steps")
 
 
+def test_rayleigh_benard_2048x4096_implicit_is_bitwise():
+    """The largest configuration, 2048 x 4096 at Ra 1e10: the cost table picks
+    Crank-Nicolson in x and y (lines of 2048 and 4096), the fused Poisson
+    launch runs column groups of two with four sweep warps per block."""
+    cfg = Config(2048, 4096, ly=2.0, Ra=1e10, Pr=1.0)
+    o = OracleCase(cfg, threads=16)
+    with gpu_case(cfg, [1, 2, 2, 3]) as c:
+        c.run(2)
+        o.run(2)
+        dt = c.get_dt()
+        assert dt == o.get_dt()
+        assert (dt["implicitx"], dt["implicity"]) == (1, 1)
+        assert_bitwise(c.get_state(), o.get_state(), FIELDS, "2048x4096 after 2 steps")
+
+
 def test_divergence_free_and_reference_diagnostics():
     """The projected velocity is solenoidal to round-off (the reference's own
     check, src/logging.c:36-80), and the log quantities computed from the
