@@ -397,21 +397,25 @@ __global__ void __launch_bounds__(kBTileXMax) k_b_corr(BCase *__restrict__ cases
     float *__restrict__ uyl = C.uyl[pu];
     const double *__restrict__ psi = C.psi;
     double *__restrict__ p = C.p;
-    const double gdt = C.gdt[rk], dxi = C.dxi[x], rdy = C.rdy;
+    const double gdt = C.gdt[rk];
     const float rxc = C.rdxc_f[x], rdyf = C.rdy_f;
+    // gamma dt / DXC and gamma dt / dy once per column: one FP64 product per
+    // increment instead of two (the same value on grids whose spacings are
+    // powers of two, where the division is an exact scaling)
+    const double gx = gdt * C.dxi[x], gy = gdt * C.rdy;
     double sm = psi[(size_t)wdn(y0, ny) * nx + x];
     for (int y = y0; y < y1; ++y) {
       const size_t r = (size_t)y * nx + x;
       const double sc = psi[r];
       if (x >= 1) {  // src/fluid/correct_velocity.c:19-25
         float u, ul;
-        acc2(ux[r], uxl[r], -(float)((gdt * (sc - psi[r - 1])) * dxi), u, ul);
+        acc2(ux[r], uxl[r], -(float)((sc - psi[r - 1]) * gx), u, ul);
         ux[r] = u;
         uxl[r] = ul;
         mx = fmaxf(mx, fabsf(u) * rxc);
       }
       float v, vlo;
-      acc2(uy[r], uyl[r], -(float)((gdt * (sc - sm)) * rdy), v, vlo);  // :31-37
+      acc2(uy[r], uyl[r], -(float)((sc - sm) * gy), v, vlo);  // :31-37
       uy[r] = v;
       uyl[r] = vlo;
       my = fmaxf(my, fabsf(v) * rdyf);
