@@ -264,7 +264,9 @@ def workload_config(args):
 
 # ------------------------------------------------------ FP32-stencil / batched
 def fp32_single(args, torch):
-    """throughput of the FP32-stencil / FP64-Poisson form on the same case"""
+    """throughput of the FP32-stencil / FP64-Poisson form on the same case,
+    with the launch shapes picked by sns_batch_autotune (the default shapes'
+    rate beside it; shapes change speed, not results)"""
     from simplenavierstokessolver_gb300.batch import Batch, Desc
 
     cells = args.nx * args.ny
@@ -274,17 +276,27 @@ def fp32_single(args, torch):
         flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
         b.step(args.warmup)
         b.synchronize()
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-        for a, e in ev:
-            a.record(stream)
-            b.step(1)
-            e.record(stream)
-            with torch.cuda.stream(stream):
-                flush.zero_()
+
+        def timed():
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                  for _ in range(args.steps)]
+            for a, e in ev:
+                a.record(stream)
+                b.step(1)
+                e.record(stream)
+                with torch.cuda.stream(stream):
+                    flush.zero_()
+            b.synchronize()
+            return sum(a.elapsed_time(e) for a, e in ev)
+
+        ms_default = timed()
+        shapes, _ = b.autotune(steps=5)
+        b.step(args.warmup)
         b.synchronize()
-        ms = sum(a.elapsed_time(e) for a, e in ev)
+        ms = timed()
         del b, s
     return {"value": cells * args.steps / (ms * 1e-3), "unit": "cell-steps/s", "ms_per_step": ms / args.steps,
+            "default_shapes_value": cells * args.steps / (ms_default * 1e-3), "autotuned_shapes": shapes,
             "l2": "flushed between timed steps (256 MiB write)"}
 
 
@@ -326,6 +338,8 @@ def large_instance(args, torch, nx=2048, ny=4096, Ra=1e10, steps=10):
         b.add(Desc(nx, ny, ly=2.0, Ra=Ra, Pr=1.0))
         stream = torch.cuda.ExternalStream(b.stream())
         b.step(3)
+        shapes, _ = b.autotune(steps=3)
+        b.step(2)
         b.synchronize()
         e0.record(stream)
         b.step(steps)
@@ -333,7 +347,7 @@ def large_instance(args, torch, nx=2048, ny=4096, Ra=1e10, steps=10):
         b.synchronize()
         ms = e0.elapsed_time(e1)
     out["fp32_stencil"] = {"value": cells * steps / (ms * 1e-3), "ms_per_step": ms / steps,
-                           "scheme": "explicit x / explicit y (batched form)"}
+                           "scheme": "explicit x / explicit y (batched form)", "autotuned_shapes": shapes}
     return out
 
 
