@@ -84,6 +84,11 @@ struct Context {
   // or unsupported for this size
   bool fused = true;
   bool fused_ready = false;
+  // ux, uy on the device change with every bump of `version`; colmax holds
+  // the max-|u| reduction of the state of version `red_version` (written by
+  // the last substage of sns_run / sns_integrate), so param_decide_dt and the
+  // next sns_run skip their reduction launch while nothing changed in between
+  unsigned long long version = 1, red_version = 0;
   FusedState fz;
   unsigned *fz_err_host = nullptr;  // pinned
   // asynchronous checkpoint (sns_checkpoint): a device snapshot of ux, uy, p
@@ -1243,6 +1248,7 @@ int fluid_update_velocity(const param_t *param, const parallel_t *parallel, cons
   if (!param || !parallel || !fe || rkstep < 0 || rkstep >= RKSTEPMAX)
     return fail(SNS_ERR_ARG, "fluid_update_velocity: bad argument");
   const TempExt *te = temperature ? as_temp(temperature) : nullptr;
+  fe->ctx->version++;
   return do_velocity_update(param, rkstep, fe, te);
 }
 
@@ -1260,6 +1266,7 @@ int fluid_correct_velocity(const param_t *param, const parallel_t *parallel, con
   if (!param || !parallel || !fe || rkstep < 0 || rkstep >= RKSTEPMAX)
     return fail(SNS_ERR_ARG, "fluid_correct_velocity: bad argument");
   Context *c = fe->ctx;
+  c->version++;
   Prof pf(c, K_CORR);
   SNS_CUDA(launch_correct(c->g, stage_scalars(param, rkstep), fe->f.psi, fe->f.ux, fe->f.uy, c->stream));
   return SNS_OK;
@@ -1356,7 +1363,9 @@ int sns_measure_cost(param_t *param, const parallel_t *parallel, int reps, doubl
 int param_decide_dt(param_t *param, const parallel_t *parallel, const fluid_t *fluid) {
   FluidExt *fe = as_fluid(fluid);
   if (!param || !parallel || !fe) return fail(SNS_ERR_ARG, "param_decide_dt: bad argument");
-  if (int rc = reduce_to_host(fe->ctx, fe->f, true)) return rc;
+  Context *c = fe->ctx;
+  if (int rc = reduce_to_host(c, fe->f, c->red_version != c->version)) return rc;
+  c->red_version = c->version;
   finish_decide_dt(param, fe->ctx);
   return SNS_OK;
 }
@@ -1443,6 +1452,7 @@ static int sync_to_device_impl(const param_t *param, fluid_t *fluid, temperature
   if (fe && te && fe->ctx != te->ctx) return fail(SNS_ERR_ARG, "%s: fluid and temperature of different cases", fn);
   Context *c = fe ? fe->ctx : te ? te->ctx : nullptr;
   if (!c) return SNS_OK;
+  c->version++;
   XferList L{};
   L.rows = c->ny;
   bool direct = true;
@@ -2031,7 +2041,13 @@ int sns_integrate(const param_t *param, const parallel_t *parallel, fluid_t *flu
   if (!param || !parallel || !fe) return fail(SNS_ERR_ARG, "sns_integrate: bad argument");
   if (parallel->mpisize != 1) return fail(SNS_ERR_UNSUPPORTED, "single-rank only");
   TempExt *te = temperature ? as_temp(temperature) : nullptr;
-  return integrate_impl(param, fe, te, false);
+  Context *c = fe->ctx;
+  c->version++;
+  // the last substage also leaves the max-|u| reduction for the next
+  // param_decide_dt
+  if (int rc = integrate_impl(param, fe, te, true)) return rc;
+  c->red_version = c->version;
+  return SNS_OK;
 }
 
 int sns_run(param_t *param, const parallel_t *parallel, fluid_t *fluid, temperature_t *temperature, int nsteps) {
@@ -2040,11 +2056,14 @@ int sns_run(param_t *param, const parallel_t *parallel, fluid_t *fluid, temperat
   if (parallel->mpisize != 1) return fail(SNS_ERR_UNSUPPORTED, "single-rank only");
   TempExt *te = temperature ? as_temp(temperature) : nullptr;
   Context *c = fe->ctx;
-  bool have_reduction = false;
+  // the reduction of the current state may be resident from the previous call
+  bool have_reduction = c->red_version == c->version;
   for (int s = 0; s < nsteps; s++) {
     if (int rc = reduce_to_host(c, fe->f, !have_reduction)) return rc;
     finish_decide_dt(param, c);
+    c->version++;
     if (int rc = integrate_impl(param, fe, te, true)) return rc;
+    c->red_version = c->version;
     have_reduction = true;
     param->step += 1;
     param->time += param->dt;

@@ -333,6 +333,34 @@ def test_state_only_syncs_around_whole_steps_are_bitwise(costs):
             assert np.array_equal(state[k], full[k]), k
 
 
+@pytest.mark.parametrize("costs", [[1, 2, 2, 3], [4, 3, 2, 1]], ids=["exp_exp", "imp_imp"])
+def test_resident_reduction_across_calls_is_bitwise(costs):
+    """The max-|u| reduction the last substage of sns_run / sns_integrate
+    leaves on the device stands in for the next call's own while nothing
+    changed the velocity in between: single-step sns_run calls,
+    param_decide_dt + sns_integrate steps, and reference-named calls and a
+    host round trip in between (which must force a fresh reduction) all
+    give the oracle's dt and state bit for bit."""
+    cfg = Config(48, 64, ly=1.0, Ra=1e7, Pr=0.8, stretch=3)
+    o = OracleCase(cfg)
+    o.set_costs(costs)
+    with gpu_case(cfg, costs) as c:
+        for _ in range(3):
+            c.run(1)
+        for _ in range(3):
+            c.param_decide_dt()
+            c.integrate()
+            c.set_time(c.get_dt()["time"] + c.get_dt()["dt"], c.get_dt()["step"] + 1)
+        c.run_calls(2)
+        c.run(1)
+        s = c.get_state()
+        c.set_state(s["ux"], s["uy"], s["p"], s["temp"], sources=c.get_sources())
+        c.run(2)
+        o.run(11)
+        assert c.get_dt() == o.get_dt()
+        assert_bitwise(c.get_state(), o.get_state(), FIELDS, "after mixed calls")
+
+
 @pytest.mark.parametrize("nx,ny,costs", [(64, 128, [1, 2, 2, 3]), (2048, 256, [1, 2, 2, 3]),
                                           (96, 64, [4, 3, 2, 1])], ids=["64x128", "2048x256", "impimp_96x64"])
 def test_fused_poisson_equals_three_kernels(nx, ny, costs):
