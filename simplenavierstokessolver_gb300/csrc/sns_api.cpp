@@ -64,6 +64,26 @@ static bool is_pow2_double(double v) {
 }
 
 // ------------------------------------------------------------------- context
+struct FluidExt;
+struct TempExt;
+
+// A reference-named call whose launch waits for a later call of the same
+// substage, to share its launch: the explicit temperature update runs inside
+// the next fluid_compute_potential's fused Poisson launch (as sns_run does),
+// the velocity correction together with the next fluid_update_pressure. Every
+// other entry point performs pending work first (flush_pending).
+struct PendingTemp {
+  TempExt *te = nullptr;  // set: an explicit temperature update not launched yet
+  int rk = -1, out = -1;
+  StageScalars s{};
+  const double *ux_k = nullptr, *uy_k = nullptr;  // the velocity it reads
+};
+struct PendingCorr {
+  FluidExt *fe = nullptr;  // set: a velocity correction not launched yet
+  int rk = -1, impx = 0, impy = 0;
+  StageScalars s{};
+};
+
 struct Context {
   const param_t *param = nullptr;
   int refs = 0;
@@ -89,6 +109,8 @@ struct Context {
   // the last substage of sns_run / sns_integrate), so param_decide_dt and the
   // next sns_run skip their reduction launch while nothing changed in between
   unsigned long long version = 1, red_version = 0;
+  PendingTemp ptemp;
+  PendingCorr pcorr;
   FusedState fz;
   unsigned *fz_err_host = nullptr;  // pinned
   // asynchronous checkpoint (sns_checkpoint): a device snapshot of ux, uy, p
@@ -962,6 +984,41 @@ static int reduce_to_host(Context *c, Fields &f, bool launch) {
   return fused_check(c);
 }
 
+static bool same_scalars(const StageScalars &a, const StageScalars &b) {
+  return a.adt == b.adt && a.bdt == b.bdt && a.gdt == b.gdt && a.has_b == b.has_b && a.kappa == b.kappa &&
+         a.nu == b.nu && a.rgdt == b.rgdt && a.rny == b.rny && a.pcorr == b.pcorr;
+}
+
+// launches the deferred work of the reference-named calls (PendingTemp,
+// PendingCorr) in call order: a temperature update is consumed before a
+// correction can be deferred, so at most one of them waits
+static int flush_pending(Context *c) {
+  if (!c) return SNS_OK;
+  if (TempExt *te = c->ptemp.te) {
+    const PendingTemp pt = c->ptemp;
+    c->ptemp = PendingTemp{};
+    {
+      Prof pf(c, K_TEMP);
+      SNS_CUDA(launch_temp_update(c->g, pt.s, 0, 0, te->f.t[te->cur], te->f.t[pt.out], te->f.at, nullptr, pt.ux_k,
+                                  pt.uy_k, c->stream));
+    }
+    te->cur = pt.out;
+  }
+  if (FluidExt *fe = c->pcorr.fe) {
+    const PendingCorr pc = c->pcorr;
+    c->pcorr = PendingCorr{};
+    Prof pf(c, K_CORR);
+    SNS_CUDA(launch_correct(c->g, pc.s, fe->f.psi, fe->f.ux, fe->f.uy, c->stream));
+  }
+  return SNS_OK;
+}
+
+static Context *ctx_of(const fluid_t *f, const temperature_t *t) {
+  if (FluidExt *fe = f ? as_fluid(f) : nullptr) return fe->ctx;
+  if (TempExt *te = t ? as_temp(t) : nullptr) return te->ctx;
+  return nullptr;
+}
+
 }  // namespace sns
 
 using namespace sns;
@@ -1104,6 +1161,7 @@ fluid_t *fluid_init(const param_t *param, const parallel_t *parallel) {
 int fluid_finalise(fluid_t *fluid) {
   FluidExt *fe = as_fluid(fluid);
   if (!fe) return fail(SNS_ERR_ARG, "fluid_finalise: not a fluid_t from fluid_init");
+  if (int rc = flush_pending(fe->ctx)) return rc;
   fluid_t &h = fe->pub;
   for (double *p : {h.ux, h.uy, h.p, h.psi, h.srcuxa, h.srcuxb, h.srcuxg, h.srcuya, h.srcuyb, h.srcuyg}) host_free(p);
   Context *c = fe->ctx;
@@ -1176,6 +1234,7 @@ temperature_t *temperature_init(const param_t *param, const parallel_t *parallel
 int temperature_finalise(temperature_t *temperature) {
   TempExt *te = as_temp(temperature);
   if (!te) return fail(SNS_ERR_ARG, "temperature_finalise: not a temperature_t from temperature_init");
+  if (int rc = flush_pending(te->ctx)) return rc;
   temperature_t &h = te->pub;
   for (double *p : {h.temp, h.tempforcex, h.srctempa, h.srctempb, h.srctempg}) host_free(p);
   Context *c = te->ctx;
@@ -1229,6 +1288,7 @@ int temperature_update_boundaries_temp(const param_t *param, const parallel_t *p
 int temperature_compute_force(const param_t *param, const parallel_t *parallel, temperature_t *temperature) {
   TempExt *te = as_temp(temperature);
   if (!param || !parallel || !te) return fail(SNS_ERR_ARG, "temperature_compute_force: bad argument");
+  if (int rc = flush_pending(te->ctx)) return rc;
   te->snap = param->with_thermal_forcing ? te->cur : -1;
   return SNS_OK;
 }
@@ -1239,6 +1299,21 @@ int temperature_update_temp(const param_t *param, const parallel_t *parallel, co
   FluidExt *fe = as_fluid(fluid);
   if (!param || !parallel || !te || !fe || rkstep < 0 || rkstep >= RKSTEPMAX)
     return fail(SNS_ERR_ARG, "temperature_update_temp: bad argument");
+  Context *c = te->ctx;
+  if (int rc = flush_pending(c)) return rc;
+  if (c->fused && fe->ctx == c && !param->implicitx && !param->implicity) {
+    // explicit: launched inside the next fluid_compute_potential (it reads the
+    // velocity of now, which that call's velocity update leaves in place)
+    PendingTemp &pt = c->ptemp;
+    pt.te = te;
+    pt.rk = rkstep;
+    pt.out = 0;
+    while (pt.out == te->cur || pt.out == te->snap) pt.out++;
+    pt.s = stage_scalars(param, rkstep);
+    pt.ux_k = fe->f.ux;
+    pt.uy_k = fe->f.uy;
+    return SNS_OK;
+  }
   return do_temp_update(param, rkstep, fe, te);
 }
 
@@ -1248,7 +1323,12 @@ int fluid_update_velocity(const param_t *param, const parallel_t *parallel, cons
   if (!param || !parallel || !fe || rkstep < 0 || rkstep >= RKSTEPMAX)
     return fail(SNS_ERR_ARG, "fluid_update_velocity: bad argument");
   const TempExt *te = temperature ? as_temp(temperature) : nullptr;
-  fe->ctx->version++;
+  Context *c = fe->ctx;
+  // a deferred temperature update may wait across this call (it reads the
+  // velocity buffer this call leaves alone) but not across a second one
+  if (c->pcorr.fe || (c->ptemp.te && c->ptemp.ux_k == fe->f.ux_alt))
+    if (int rc = flush_pending(c)) return rc;
+  c->version++;
   return do_velocity_update(param, rkstep, fe, te);
 }
 
@@ -1257,7 +1337,22 @@ int fluid_compute_potential(const param_t *param, const parallel_t *parallel, co
   if (!param || !parallel || !fe || rkstep < 0 || rkstep >= RKSTEPMAX)
     return fail(SNS_ERR_ARG, "fluid_compute_potential: bad argument");
   Context *c = fe->ctx;
-  if (int rc = poisson(c, stage_scalars(param, rkstep), fe->f)) return rc;
+  const StageScalars s = stage_scalars(param, rkstep);
+  PendingTemp &pt = c->ptemp;
+  if (pt.te && pt.rk == rkstep && same_scalars(pt.s, s)) {
+    // the substage's deferred temperature update inside the fused launch
+    TempExt *te = pt.te;
+    bool fused = false;
+    if (int rc = try_fused(c, s, fe->f, te->f.t[te->cur], te->f.t[pt.out], te->f.at, pt.ux_k, pt.uy_k, &fused))
+      return rc;
+    if (fused) {
+      te->cur = pt.out;
+      pt = PendingTemp{};
+      return SNS_OK;
+    }
+  }
+  if (int rc = flush_pending(c)) return rc;
+  if (int rc = poisson(c, s, fe->f)) return rc;
   return SNS_OK;
 }
 
@@ -1266,9 +1361,16 @@ int fluid_correct_velocity(const param_t *param, const parallel_t *parallel, con
   if (!param || !parallel || !fe || rkstep < 0 || rkstep >= RKSTEPMAX)
     return fail(SNS_ERR_ARG, "fluid_correct_velocity: bad argument");
   Context *c = fe->ctx;
+  if (int rc = flush_pending(c)) return rc;
   c->version++;
-  Prof pf(c, K_CORR);
-  SNS_CUDA(launch_correct(c->g, stage_scalars(param, rkstep), fe->f.psi, fe->f.ux, fe->f.uy, c->stream));
+  // launched with the next fluid_update_pressure of the substage (one kernel
+  // for both, the one sns_run uses), or by the next other call
+  PendingCorr &pc = c->pcorr;
+  pc.fe = fe;
+  pc.rk = rkstep;
+  pc.impx = param->implicitx;
+  pc.impy = param->implicity;
+  pc.s = stage_scalars(param, rkstep);
   return SNS_OK;
 }
 
@@ -1277,9 +1379,19 @@ int fluid_update_pressure(const param_t *param, const parallel_t *parallel, cons
   if (!param || !parallel || !fe || rkstep < 0 || rkstep >= RKSTEPMAX)
     return fail(SNS_ERR_ARG, "fluid_update_pressure: bad argument");
   Context *c = fe->ctx;
+  const StageScalars s = stage_scalars(param, rkstep);
+  PendingCorr &pc = c->pcorr;
+  if (pc.fe == fe && pc.rk == rkstep && pc.impx == param->implicitx && pc.impy == param->implicity &&
+      same_scalars(pc.s, s)) {
+    pc = PendingCorr{};
+    Prof pf(c, K_CORR_PRES);
+    SNS_CUDA(launch_correct_pressure(c->g, s, param->implicitx, param->implicity, fe->f.psi, fe->f.ux, fe->f.uy,
+                                     fe->f.p, nullptr, nullptr, c->stream));
+    return SNS_OK;
+  }
+  if (int rc = flush_pending(c)) return rc;
   Prof pf(c, K_PRES);
-  SNS_CUDA(launch_pressure(c->g, stage_scalars(param, rkstep), param->implicitx, param->implicity, fe->f.psi,
-                           fe->f.p, c->stream));
+  SNS_CUDA(launch_pressure(c->g, s, param->implicitx, param->implicity, fe->f.psi, fe->f.p, c->stream));
   return SNS_OK;
 }
 
@@ -1364,6 +1476,7 @@ int param_decide_dt(param_t *param, const parallel_t *parallel, const fluid_t *f
   FluidExt *fe = as_fluid(fluid);
   if (!param || !parallel || !fe) return fail(SNS_ERR_ARG, "param_decide_dt: bad argument");
   Context *c = fe->ctx;
+  if (int rc = flush_pending(c)) return rc;
   if (int rc = reduce_to_host(c, fe->f, c->red_version != c->version)) return rc;
   c->red_version = c->version;
   finish_decide_dt(param, fe->ctx);
@@ -1378,6 +1491,7 @@ int param_decide_dt(param_t *param, const parallel_t *parallel, const fluid_t *f
 static int sync_to_host_impl(const param_t *param, fluid_t *fluid, temperature_t *temperature, bool state_only,
                              const char *fn) {
   if (!param) return fail(SNS_ERR_ARG, "%s: NULL param", fn);
+  if (int rc = flush_pending(ctx_of(fluid, temperature))) return rc;
   const int nx = param->itot, ny = param->jtot;
   if (fluid) {
     FluidExt *fe = as_fluid(fluid);
@@ -1444,6 +1558,7 @@ int sns_sync_state_to_host(const param_t *param, fluid_t *fluid, temperature_t *
 static int sync_to_device_impl(const param_t *param, fluid_t *fluid, temperature_t *temperature, bool state_only,
                                const char *fn) {
   if (!param) return fail(SNS_ERR_ARG, "%s: NULL param", fn);
+  if (int rc = flush_pending(ctx_of(fluid, temperature))) return rc;
   const int nx = param->itot;
   FluidExt *fe = nullptr;
   TempExt *te = nullptr;
@@ -1509,6 +1624,7 @@ int sns_diagnostics(const param_t *param, const fluid_t *fluid, const temperatur
   TempExt *te = as_temp(temperature);
   if (!param || !fe || !te || !out) return fail(SNS_ERR_ARG, "sns_diagnostics: bad argument");
   Context *c = fe->ctx;
+  if (int rc = flush_pending(c)) return rc;
   const int nx = c->nx, ny = c->ny;
   const size_t words = diag_partials_words(nx, ny);
   if (!c->diag)
@@ -1605,6 +1721,7 @@ int sns_checkpoint(const param_t *param, const fluid_t *fluid, const temperature
   TempExt *te = temperature ? as_temp(temperature) : nullptr;
   if (!param || !fe || !dirname || (temperature && !te)) return fail(SNS_ERR_ARG, "sns_checkpoint: bad argument");
   Context *c = fe->ctx;
+  if (int rc = flush_pending(c)) return rc;
   if (c->ck_thread.joinable()) c->ck_thread.join();  // one checkpoint in flight per solver
   const int nx = c->nx, ny = c->ny;
   const size_t cells = (size_t)nx * ny;
@@ -1697,6 +1814,7 @@ int sns_restart(param_t *param, fluid_t *fluid, temperature_t *temperature, cons
   FluidExt *fe = as_fluid(fluid);
   TempExt *te = temperature ? as_temp(temperature) : nullptr;
   if (!param || !fe || !dirname || (temperature && !te)) return fail(SNS_ERR_ARG, "sns_restart: bad argument");
+  if (int rc = flush_pending(fe->ctx)) return rc;
   const int nx = param->itot, ny = param->jtot;
   const std::string dir(dirname);
   std::string err;
@@ -1802,6 +1920,7 @@ int statistics_collect(param_t *param, const parallel_t *parallel, const fluid_t
   if (!param || !parallel || !e || !fe || (temperature && !te))
     return fail(SNS_ERR_ARG, "statistics_collect: bad argument");
   Context *c = fe->ctx;
+  if (int rc = flush_pending(c)) return rc;
   if (e->nx != c->nx || e->ny != c->ny) return fail(SNS_ERR_ARG, "statistics_collect: grid size mismatch");
   if (e->ctx && e->ctx != c) return fail(SNS_ERR_ARG, "statistics_collect: statistics of another solver");
   const size_t nx = c->nx, ny = c->ny, words = 2 * (nx + 1) * ny + 4 * (nx + 2) * ny;
@@ -1896,6 +2015,7 @@ int sns_diagnostics_static(const param_t *param, const fluid_t *fluid, const tem
   FluidExt *fe = as_fluid(fluid);
   TempExt *te = as_temp(temperature);
   if (!param || !fe || !te || !out) return fail(SNS_ERR_ARG, "sns_diagnostics_static: bad argument");
+  if (int rc = flush_pending(fe->ctx)) return rc;
   Context *c = fe->ctx;
   const int nx = c->nx, ny = c->ny;
   const int nb = diag_blocks(nx, ny);
@@ -1951,6 +2071,7 @@ const char *sns_profile_kind_name(int kind) {
 int sns_synchronize(const fluid_t *fluid) {
   FluidExt *fe = as_fluid(fluid);
   if (!fe) return fail(SNS_ERR_ARG, "sns_synchronize: bad fluid");
+  if (int rc = flush_pending(fe->ctx)) return rc;
   if (int rc = fused_enqueue_err(fe->ctx)) return rc;
   SNS_CUDA(cudaStreamSynchronize(fe->ctx->stream));
   return fused_check(fe->ctx);
@@ -1959,6 +2080,7 @@ int sns_synchronize(const fluid_t *fluid) {
 int sns_set_fused(const fluid_t *fluid, int on) {
   FluidExt *fe = as_fluid(fluid);
   if (!fe) return fail(SNS_ERR_ARG, "sns_set_fused: bad fluid");
+  if (int rc = flush_pending(fe->ctx)) return rc;
   fe->ctx->fused = on != 0;
   return SNS_OK;
 }
@@ -2040,6 +2162,7 @@ int sns_integrate(const param_t *param, const parallel_t *parallel, fluid_t *flu
   FluidExt *fe = as_fluid(fluid);
   if (!param || !parallel || !fe) return fail(SNS_ERR_ARG, "sns_integrate: bad argument");
   if (parallel->mpisize != 1) return fail(SNS_ERR_UNSUPPORTED, "single-rank only");
+  if (int rc = flush_pending(fe->ctx)) return rc;
   TempExt *te = temperature ? as_temp(temperature) : nullptr;
   Context *c = fe->ctx;
   c->version++;
@@ -2054,6 +2177,7 @@ int sns_run(param_t *param, const parallel_t *parallel, fluid_t *fluid, temperat
   FluidExt *fe = as_fluid(fluid);
   if (!param || !parallel || !fe || nsteps < 0) return fail(SNS_ERR_ARG, "sns_run: bad argument");
   if (parallel->mpisize != 1) return fail(SNS_ERR_UNSUPPORTED, "single-rank only");
+  if (int rc = flush_pending(fe->ctx)) return rc;
   TempExt *te = temperature ? as_temp(temperature) : nullptr;
   Context *c = fe->ctx;
   // the reduction of the current state may be resident from the previous call

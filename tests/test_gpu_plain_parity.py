@@ -361,6 +361,41 @@ def test_resident_reduction_across_calls_is_bitwise(costs):
         assert_bitwise(c.get_state(), o.get_state(), FIELDS, "after mixed calls")
 
 
+def test_deferred_reference_calls_are_flushed_by_other_calls():
+    """temperature_update_temp waits for fluid_compute_potential and
+    fluid_correct_velocity for fluid_update_pressure (one launch each pair);
+    any other call in between performs the waiting work first. Substages with
+    diagnostics, host syncs and a fused-mode toggle wedged between the pairs
+    give the oracle's state bit for bit."""
+    cfg = Config(40, 64, ly=1.0, Ra=1e7, Pr=0.8)
+    o = OracleCase(cfg)
+    with gpu_case(cfg, [1, 2, 2, 3]) as c:
+        for step in range(3):
+            c.param_decide_dt()
+            for rk in range(3):
+                c.update_boundaries()
+                c.temperature_compute_force()
+                c.temperature_update_temp(rk)
+                if rk == 0:
+                    c.diagnostics()
+                if rk == 1:
+                    c.sync_state_to_host()
+                c.fluid_update_velocity(rk)
+                c.fluid_compute_potential(rk)
+                c.fluid_correct_velocity(rk)
+                if rk == 2:
+                    c.set_fused(step % 2 == 0)
+                if rk == 0:
+                    c.sync_to_host()
+                c.fluid_update_pressure(rk)
+            c.p.step += 1
+            c.p.time += c.p.dt
+        c.set_fused(True)
+        o.run(3)
+        assert c.get_dt() == o.get_dt()
+        assert_bitwise(c.get_state(), o.get_state(), FIELDS, "reference-named calls with calls in between")
+
+
 @pytest.mark.parametrize("nx,ny,costs", [(64, 128, [1, 2, 2, 3]), (2048, 256, [1, 2, 2, 3]),
                                           (96, 64, [4, 3, 2, 1])], ids=["64x128", "2048x256", "impimp_96x64"])
 def test_fused_poisson_equals_three_kernels(nx, ny, costs):
