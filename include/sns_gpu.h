@@ -141,7 +141,10 @@ extern int fluid_update_velocity(const param_t *param, const parallel_t *paralle
  * the scalar potential psi (real DFT along y, tridiagonal along x) */
 extern int fluid_compute_potential(const param_t *param, const parallel_t *parallel, const int rkstep,
                                    fluid_t *fluid);
-/* include/fluid.h:25 (src/fluid/correct_velocity.c:6-42) */
+/* include/fluid.h:25 (src/fluid/correct_velocity.c:6-42). Its launch waits
+ * for the next fluid_update_pressure of the same substage (one kernel for
+ * both); any other call of this solver launches it first, so every call sees
+ * the corrected velocity. */
 extern int fluid_correct_velocity(const param_t *param, const parallel_t *parallel, const int rkstep,
                                   fluid_t *fluid);
 /* include/fluid.h:26 (src/fluid/update_pressure.c:7-60) */
@@ -158,7 +161,11 @@ extern int temperature_finalise(temperature_t *temperature);
  * current temperature, consumed by the next fluid_update_velocity */
 extern int temperature_compute_force(const param_t *param, const parallel_t *parallel,
                                      temperature_t *temperature);
-/* include/temperature.h:18 (src/temperature/update.c:233-238) */
+/* include/temperature.h:18 (src/temperature/update.c:233-238). With the
+ * explicit scheme its launch waits for the next fluid_compute_potential of
+ * the same substage, which runs it inside the fused Poisson launch; any other
+ * call of this solver launches it first, so every call sees the updated
+ * temperature. */
 extern int temperature_update_temp(const param_t *param, const parallel_t *parallel, const int rkstep,
                                    const fluid_t *fluid, temperature_t *temperature);
 /* include/temperature.h:20 (src/temperature/boundary_conditions.c:6-21), same
