@@ -1384,9 +1384,17 @@ int fluid_update_pressure(const param_t *param, const parallel_t *parallel, cons
   if (pc.fe == fe && pc.rk == rkstep && pc.impx == param->implicitx && pc.impy == param->implicity &&
       same_scalars(pc.s, s)) {
     pc = PendingCorr{};
-    Prof pf(c, K_CORR_PRES);
-    SNS_CUDA(launch_correct_pressure(c->g, s, param->implicitx, param->implicity, fe->f.psi, fe->f.ux, fe->f.uy,
-                                     fe->f.p, nullptr, nullptr, c->stream));
+    // the last substage also leaves the max-|u| reduction for the next
+    // param_decide_dt (the velocity is final for the step)
+    const bool red = rkstep == RKSTEPMAX - 1;
+    if (red) SNS_CUDA(cudaMemsetAsync(fe->f.colmax, 0, sizeof(unsigned long long) * (c->nx + 1), c->stream));
+    {
+      Prof pf(c, K_CORR_PRES);
+      SNS_CUDA(launch_correct_pressure(c->g, s, param->implicitx, param->implicity, fe->f.psi, fe->f.ux, fe->f.uy,
+                                       fe->f.p, red ? fe->f.colmax : nullptr, red ? fe->f.uymax : nullptr,
+                                       c->stream));
+    }
+    if (red) c->red_version = c->version;
     return SNS_OK;
   }
   if (int rc = flush_pending(c)) return rc;
