@@ -117,7 +117,9 @@ def load_peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms, each sample
+    stamped with the host clock so that those inside a timed region can be
+    told apart (`mark`)."""
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -128,11 +130,12 @@ class ClockSampler:
         self.proc = None
         self.lines = []
         self.thread = None
+        self.region = None
 
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
@@ -142,7 +145,11 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
+
+    def mark(self, t0: float, t1: float):
+        """the timed region, in time.perf_counter() seconds"""
+        self.region = (t0, t1)
 
     def stop(self):
         if self.proc is None:
@@ -154,9 +161,9 @@ class ClockSampler:
             self.proc.kill()
         if self.thread:
             self.thread.join(timeout=2)
-        sm, smax, reasons, power = [], [], set(), []
+        sm, smax, reasons, power, inside = [], [], set(), [], []
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for t, ln in self.lines:
             parts = [x.strip() for x in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -166,13 +173,19 @@ class ClockSampler:
                 power.append(float(parts[3]))
             except ValueError:
                 continue
+            # a sample printed within 50 ms after the region's end was taken in it
+            if self.region and self.region[0] <= t <= self.region[1] + 0.05:
+                inside.append(sm[-1])
             for nm, v in zip(names, parts[5:9]):
                 if v.lower() == "active":
                     reasons.add(nm)
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
-                "samples": len(sm), "power_w_max": max(power) if power else None}
+        return {"sm_mhz": statistics.median(inside or sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm), "samples_in_timed_region": len(inside),
+                "sm_mhz_timed_region": statistics.median(inside) if inside else None,
+                "power_w_max": max(power) if power else None,
+                "window": "from before the warm-up to after the per-kernel pass (the same steps replayed)"}
 
 
 def dist_setup():
@@ -572,16 +585,17 @@ def gpu_arm(args, world, rank, local):
         with torch.cuda.stream(stream):
             flush.zero_()
 
+    clocks = ClockSampler(local)
+    clocks.start()
     for _ in range(args.warmup):
         case.run(1)
         flush_l2()
     torch.cuda.synchronize()
 
     # ---- pass A: headline, uninstrumented
-    clocks = ClockSampler(local)
-    clocks.start()
     barrier(world)
     torch.cuda.synchronize()
+    t_region = time.perf_counter()
     launches0 = kernel_launches()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     for a, b in ev:
@@ -590,9 +604,9 @@ def gpu_arm(args, world, rank, local):
         b.record(stream)
         flush_l2()
     torch.cuda.synchronize()
+    clocks.mark(t_region, time.perf_counter())
     barrier(world)
     launches = kernel_launches() - launches0
-    clk = clocks.stop()
     ms = sum(a.elapsed_time(b) for a, b in ev)
     ms = max_over_ranks(ms, world)
     value = cells * args.steps * world / (ms * 1e-3)
@@ -607,6 +621,7 @@ def gpu_arm(args, world, rank, local):
     kcnt = (N.c_longlong * kinds)()
     nk = lib.sns_profile_read(case.fluid, kms, kcnt, kinds)
     lib.sns_profile(case.fluid, 0)
+    clk = clocks.stop()
     kernels = {}
     total_k = sum(kms[k] for k in range(nk))
     for k in range(nk):
