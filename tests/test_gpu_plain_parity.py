@@ -396,6 +396,43 @@ def test_deferred_reference_calls_are_flushed_by_other_calls():
         assert_bitwise(c.get_state(), o.get_state(), FIELDS, "reference-named calls with calls in between")
 
 
+def test_state_only_syncs_of_one_structure_and_bad_arguments():
+    """Either structure may be NULL (only the other one's state moves); a
+    structure of another solver is rejected with SNS_ERR_ARG."""
+    from simplenavierstokessolver_gb300 import _native as N
+
+    cfg = Config(32, 32, ly=1.0, Ra=1e6, Pr=1.0)
+    with gpu_case(cfg, [1, 2, 2, 3]) as c, gpu_case(cfg, [1, 2, 2, 3]) as other:
+        c.run(2)
+        full = c.get_state()
+        h = c.host_arrays()
+        for k in ("ux", "uy", "p", "temp"):
+            h[k][...] = 0.0
+        N.check(c.lib.sns_sync_state_to_host(c.param, c.fluid, None), "sns_sync_state_to_host")
+        assert np.array_equal(h["ux"], full["ux"]) and np.array_equal(h["p"], full["p"])
+        assert not h["temp"].any()
+        N.check(c.lib.sns_sync_state_to_host(c.param, None, c.temperature), "sns_sync_state_to_host")
+        assert np.array_equal(h["temp"], full["temp"])
+        # upload the temperature alone: the velocity on the device stays as it was
+        h["temp"][...] = 0.25
+        N.check(c.lib.sns_sync_state_to_device(c.param, None, c.temperature), "sns_sync_state_to_device")
+        s = c.get_state()
+        assert np.array_equal(s["ux"], full["ux"]) and np.all(s["temp"][1:-1, 1:-1] == 0.25)
+        rc = c.lib.sns_sync_state_to_device(c.param, c.fluid, other.temperature)
+        assert rc == N.SNS_ERR_ARG
+        rc = c.lib.sns_sync_state_to_host(c.param, c.fluid, ctypes_cast_temperature(other.fluid))
+        assert rc == N.SNS_ERR_ARG
+
+
+def ctypes_cast_temperature(fluid_ptr):
+    """a fluid_t pointer passed where a temperature_t is expected"""
+    import ctypes
+
+    from simplenavierstokessolver_gb300 import _native as N
+
+    return ctypes.cast(fluid_ptr, ctypes.POINTER(N.Temperature))
+
+
 @pytest.mark.parametrize("nx,ny,costs", [(64, 128, [1, 2, 2, 3]), (2048, 256, [1, 2, 2, 3]),
                                           (96, 64, [4, 3, 2, 1])], ids=["64x128", "2048x256", "impimp_96x64"])
 def test_fused_poisson_equals_three_kernels(nx, ny, costs):
