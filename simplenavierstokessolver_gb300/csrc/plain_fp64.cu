@@ -881,10 +881,9 @@ __device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
       const unsigned n0 = __ballot_sync(0xffffffffu, !ok0), n1 = __ballot_sync(0xffffffffu, !ok1);
       const int run = n0 ? __ffs(n0) - 1 : (n1 ? 32 + __ffs(n1) - 1 : 64);
       vg = min(vg + run, a.groups);
-      if (vg <= gx) {
-        if (++spin >= kFusedSpin) return false;
-        __nanosleep(64);
-      }
+      // the warp owns its SM's FP64 work alone: poll back to back (each
+      // poll is an L2 round trip; a sleep between them delayed the start)
+      if (vg <= gx && ++spin >= kFusedSpin) return false;
     }
     ready = min(vg * C, nx);
     __threadfence();
@@ -1037,7 +1036,8 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_poisson_fused(const FusedA
       const int s = gi * C / kFusedSpan;
       unsigned spin = 0;
       unsigned long long v;
-      while ((v = ld_relaxed_u64(a.bwd_cnt + s)) < target && ++spin < kFusedSpin) __nanosleep(128);
+      while ((v = ld_relaxed_u64(a.bwd_cnt + s)) < target && ++spin < kFusedSpin) {
+      }
       s_ok = v >= target;
       if (!s_ok) atomicOr(a.err, 2u);
       __threadfence();
