@@ -889,6 +889,13 @@ __device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
     __threadfence();
     return true;
   };
+  // while the first spectrum columns are being computed: bring this line's
+  // factors into L2 (they come from HBM when the cache was flushed or evicted)
+#pragma unroll 1
+  for (int x = 0; x < nx; ++x) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(inv + (size_t)x * jp));
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(up + (size_t)x * jp));
+  }
   // ---- forward elimination (src/linalg.c:33-45)
   if (!need(0)) return false;
   double prev = __ldcg(col) / g.pd0[Jc];
