@@ -109,6 +109,7 @@ struct Context {
   // the last substage of sns_run / sns_integrate), so param_decide_dt and the
   // next sns_run skip their reduction launch while nothing changed in between
   unsigned long long version = 1, red_version = 0;
+  unsigned long long red_host_version = 0;  // state version whose reduction red_host holds
   PendingTemp ptemp;
   PendingCorr pcorr;
   FusedState fz;
@@ -972,6 +973,8 @@ static void finish_decide_dt(param_t *param, const Context *c) {
 }
 
 static int reduce_to_host(Context *c, Fields &f, bool launch) {
+  // copied to the host at the end of the call that computed it
+  if (!launch && c->red_host_version == c->version) return SNS_OK;
   if (launch) {
     SNS_CUDA(cudaMemsetAsync(f.colmax, 0, sizeof(unsigned long long) * (c->nx + 1), c->stream));
     Prof pf(c, K_UMAX);
@@ -981,7 +984,9 @@ static int reduce_to_host(Context *c, Fields &f, bool launch) {
                            c->stream));
   if (int rc = fused_enqueue_err(c)) return rc;
   SNS_CUDA(cudaStreamSynchronize(c->stream));
-  return fused_check(c);
+  if (int rc = fused_check(c)) return rc;
+  c->red_host_version = c->version;
+  return SNS_OK;
 }
 
 static bool same_scalars(const StageScalars &a, const StageScalars &b) {
@@ -2200,7 +2205,19 @@ int sns_run(param_t *param, const parallel_t *parallel, fluid_t *fluid, temperat
     param->step += 1;
     param->time += param->dt;
   }
+  if (nsteps > 0) {
+    // the last step's reduction to the host with this call's final wait, so
+    // that the next call decides dt without a round trip; launch errors of
+    // this call are reported by this call
+    SNS_CUDA(cudaMemcpyAsync(c->red_host, fe->f.colmax, sizeof(unsigned long long) * (c->nx + 1),
+                             cudaMemcpyDeviceToHost, c->stream));
+    if (int rc = fused_enqueue_err(c)) return rc;
+  }
   SNS_CUDA(cudaStreamSynchronize(c->stream));
+  if (nsteps > 0) {
+    if (int rc = fused_check(c)) return rc;
+    c->red_host_version = c->red_version;
+  }
   return SNS_OK;
 }
 
