@@ -1506,12 +1506,16 @@ static int sync_to_host_impl(const param_t *param, fluid_t *fluid, temperature_t
   if (!param) return fail(SNS_ERR_ARG, "%s: NULL param", fn);
   if (int rc = flush_pending(ctx_of(fluid, temperature))) return rc;
   const int nx = param->itot, ny = param->jtot;
-  if (fluid) {
-    FluidExt *fe = as_fluid(fluid);
-    if (!fe) return fail(SNS_ERR_ARG, "%s: foreign fluid_t", fn);
+  FluidExt *fe = nullptr;
+  TempExt *te = nullptr;
+  if (fluid && !(fe = as_fluid(fluid))) return fail(SNS_ERR_ARG, "%s: foreign fluid_t", fn);
+  if (temperature && !(te = as_temp(temperature))) return fail(SNS_ERR_ARG, "%s: foreign temperature_t", fn);
+  // every copy is enqueued before one wait (a wait between the fluid and the
+  // temperature copies left the link idle meanwhile)
+  int rc = SNS_OK;
+  if (fe) {
     Context *c = fe->ctx;
     fluid_t &h = fe->pub;
-    int rc = SNS_OK;
     if ((rc = download(c, fe->f.ux, h.ux, nx + 1, 0, 1)) || (rc = download(c, fe->f.uy, h.uy, nx + 2, 1, 0)) ||
         (rc = download(c, fe->f.p, h.p, nx + 2, 1, 0)))
       return rc;
@@ -1519,29 +1523,35 @@ static int sync_to_host_impl(const param_t *param, fluid_t *fluid, temperature_t
         ((rc = download(c, fe->f.psi, h.psi, nx + 2, 1, 0)) || (rc = download_src(c, fe->f.aux, h.srcuxa, 1)) ||
          (rc = download_src(c, fe->f.auy, h.srcuya, 0))))
       return rc;
-    SNS_CUDA(cudaStreamSynchronize(c->stream));
-    host_bc_ux(nx, ny, h.ux);
-    host_bc_uy(nx, ny, h.uy);
-    host_bc_p(nx, ny, h.p);
-    if (!state_only) host_bc_p(nx, ny, h.psi);
   }
-  if (temperature) {
-    TempExt *te = as_temp(temperature);
-    if (!te) return fail(SNS_ERR_ARG, "%s: foreign temperature_t", fn);
+  int snap = -1;
+  double *tf_alias = nullptr;
+  if (te) {
     Context *c = te->ctx;
     temperature_t &h = te->pub;
-    int rc = SNS_OK;
     if ((rc = download(c, te->f.t[te->cur], h.temp, nx + 2, 1, 0)) ||
         (!state_only && (rc = download_src(c, te->f.at, h.srctempa, 0))))
       return rc;
-    const int snap = state_only ? -1 : te->snap;
-    double *tf_alias = snap >= 0 ? dev_alias(h.tempforcex) : nullptr;
+    snap = state_only ? -1 : te->snap;
+    tf_alias = snap >= 0 ? dev_alias(h.tempforcex) : nullptr;
     if (tf_alias) {
       SNS_CUDA(launch_tempforce_to_host(c->g, te->f.t[snap], tf_alias, c->stream));
     } else if (snap >= 0) {
       if (int rc2 = fetch(c, te->f.t[snap])) return rc2;
     }
-    SNS_CUDA(cudaStreamSynchronize(c->stream));
+  }
+  if (fe) SNS_CUDA(cudaStreamSynchronize(fe->ctx->stream));
+  if (te && (!fe || te->ctx != fe->ctx)) SNS_CUDA(cudaStreamSynchronize(te->ctx->stream));
+  if (fe) {
+    fluid_t &h = fe->pub;
+    host_bc_ux(nx, ny, h.ux);
+    host_bc_uy(nx, ny, h.uy);
+    host_bc_p(nx, ny, h.p);
+    if (!state_only) host_bc_p(nx, ny, h.psi);
+  }
+  if (te) {
+    Context *c = te->ctx;
+    temperature_t &h = te->pub;
     host_bc_temp(nx, ny, h.temp);
     if (snap >= 0 && !tf_alias) {
       // tempforcex (src/temperature/force.c:17-23) from the snapshot buffer
