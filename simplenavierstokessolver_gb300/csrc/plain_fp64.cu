@@ -851,7 +851,12 @@ __device__ __forceinline__ void st_relaxed_u32(unsigned *p, unsigned v) {
   asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// one component of 32 modes (lines[lg]); false when a wait gave up
+// one component of 32 modes (lines[lg]); false when a wait gave up.
+// P2: the lower diagonal pl is 2^e (DevGrid::p2), so pl * prev, one of the
+// three dependent FP64 operations per element of the forward elimination,
+// is taken in the integer unit (~15 cycles on the chain instead of ~78); a
+// chunk with an operand out of range is recomputed with FP64 products.
+template <bool P2>
 __device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
   const DevGrid &g = a.p.g;
   const int lane = threadIdx.x & 31, nx = g.nx, C = a.p.cols;
@@ -920,16 +925,29 @@ __device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
       nq[k] = e < nx ? __ldcg(col + (size_t)e * vs) : 0.0;
       ni[k] = e < nx ? __ldg(inv + (size_t)e * jp) : 0.0;
     }
+    auto rows = [&](auto fast) -> bool {
+      Mul<decltype(fast)::value> m;
 #pragma unroll
-    for (int k = 0; k < kLineChunk; ++k) {
-      const int x = b + k;
-      if (!decltype(guarded)::value || x < nx) {
-        const double iv = ci[k];
-        // |pivot| < DBL_EPSILON rows carry 1/pivot = +0: the reference sets them to 0
-        const double v = __double_as_longlong(iv) == 0 ? 0.0 : iv * (cq[k] - pl[x] * prev);
-        if (act) col[(size_t)x * vs] = v;
-        prev = v;
+      for (int k = 0; k < kLineChunk; ++k) {
+        const int x = b + k;
+        if (!decltype(guarded)::value || x < nx) {
+          const double iv = ci[k], c = pl[x];
+          // |pivot| < DBL_EPSILON rows carry 1/pivot = +0: the reference sets them to 0
+          const double v = __double_as_longlong(iv) == 0 ? 0.0 : iv * (cq[k] - m.by(prev, c, p2_field(c)));
+          if (act) col[(size_t)x * vs] = v;
+          prev = v;
+        }
       }
+      return m.ok;
+    };
+    if constexpr (P2) {
+      const double p0 = prev;
+      if (!rows(std::true_type{})) {
+        prev = p0;
+        rows(std::false_type{});
+      }
+    } else {
+      rows(std::false_type{});
     }
 #pragma unroll
     for (int k = 0; k < kLineChunk; ++k) {
@@ -1007,7 +1025,8 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_poisson_fused(const FusedA
     const int w = threadIdx.x >> 5;
     const int lg = blockIdx.x * a.tri_warps + w;
     if (w >= a.tri_warps || lg >= a.lines) return;
-    if (!fused_sweep(a, pl, lg) && (threadIdx.x & 31) == 0) atomicOr(a.err, 1u);
+    const bool ok = RCP && g.p2 ? fused_sweep<RCP>(a, pl, lg) : fused_sweep<false>(a, pl, lg);
+    if (!ok && (threadIdx.x & 31) == 0) atomicOr(a.err, 1u);
     return;
   }
   __shared__ int s_ok;

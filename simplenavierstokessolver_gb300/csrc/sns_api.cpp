@@ -284,13 +284,14 @@ static int build_context(Context *c, const param_t *param) {
     dxi[i - 1] = 1. / DXC(i);  // src/fluid/correct_velocity.c:13
   }
   {
-    // the velocity kernel's power-of-two products in integer arithmetic
+    // the power-of-two products taken in integer arithmetic (velocity,
+    // temperature and correction kernels, the Poisson forward elimination)
     auto p2 = [](double v) {
       int e;
       return is_pow2_double(v) && (std::frexp(v, &e), std::abs(e - 1) <= 64);
     };
     bool ok = rcp && p2(g.rdy);
-    for (int i = 0; i < nx; i++) ok = ok && p2(rdxf[i]) && p2(ccm[i]) && p2(ccp[i]);
+    for (int i = 0; i < nx; i++) ok = ok && p2(rdxf[i]) && p2(ccm[i]) && p2(ccp[i]) && p2(pl[i]);
     for (int i = 0; i <= nx; i++) ok = ok && p2(rdxc[i]);
     for (int i = 1; i < nx; i++) ok = ok && p2(cfm[i]) && p2(cfp[i]);
     g.p2 = ok;

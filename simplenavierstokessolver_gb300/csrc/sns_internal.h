@@ -27,7 +27,7 @@ constexpr double kTempXp = -0.5;  // include/temperature.h:23
 struct DevGrid {
   int nx, ny, nh, jpitch;  // nh = ny/2 + 1 Fourier modes; jpitch >= nh
   bool rcp;                // every metric divisor is a power of two
-  bool p2;                 // rcp, and every reciprocal spacing and advective coefficient is 2^e, |e| <= 64
+  bool p2;                 // rcp, and every reciprocal spacing, advective and Poisson coefficient is 2^e, |e| <= 64
   double dy, rdy;
   const double *dxf;    // [nx]    DXF(i)
   const double *dxc;    // [nx+1]  DXC(i), i = 1..nx+1
