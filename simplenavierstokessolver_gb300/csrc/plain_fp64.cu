@@ -824,6 +824,7 @@ constexpr int kFusedTriWarps = 4;
 constexpr int kFusedMinWorkers = 130;
 constexpr int kFusedSpan = 64;
 constexpr unsigned kFusedSpin = 1u << 22;
+constexpr int kPoll = 128;  // completion flags read per poll by a sweep warp
 constexpr size_t kFusedMinSmem = 116 * 1024;  // above half an SM's shared memory: one block per SM
 
 struct FusedArgs {
@@ -868,10 +869,10 @@ __device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
   const double *inv = g.pinv + Jc, *up = g.pup + Jc;
   int vg = 0;       // groups 0 .. vg-1 are verified complete
   int ready = 0;    // rows below are readable: vg * C
-  // make rows up to x readable: the lanes read the next 64
-  // completion flags (two each, relaxed), the leading run of complete groups
-  // is taken (polling while x's group is not among them), and one fence then
-  // orders the row reads after them. The test on the path taken once per
+  // make rows up to x readable: the lanes read the next kPoll
+  // completion flags (kPoll / 32 each, relaxed), the leading run of complete
+  // groups is taken (polling while x's group is not among them), and one
+  // fence then orders the row reads after them. The test on the path taken once per
   // chunk is one comparison (an integer division there cost ~12 us per
   // launch at 512 x 1024: it runs between chunks, outside the latency
   // shadows of the recurrence).
@@ -880,11 +881,18 @@ __device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
     const int gx = x / C;
     unsigned spin = 0;
     while (vg <= gx) {
-      const int g0 = vg + lane, g1 = vg + 32 + lane;
-      const bool ok0 = g0 >= a.groups || ld_relaxed_u32(a.fwd_done + g0) == a.epoch;
-      const bool ok1 = g1 >= a.groups || ld_relaxed_u32(a.fwd_done + g1) == a.epoch;
-      const unsigned n0 = __ballot_sync(0xffffffffu, !ok0), n1 = __ballot_sync(0xffffffffu, !ok1);
-      const int run = n0 ? __ffs(n0) - 1 : (n1 ? 32 + __ffs(n1) - 1 : 64);
+      bool ok[kPoll / 32];
+#pragma unroll
+      for (int i = 0; i < kPoll / 32; ++i) {
+        const int gi = vg + 32 * i + lane;
+        ok[i] = gi >= a.groups || ld_relaxed_u32(a.fwd_done + gi) == a.epoch;
+      }
+      int run = kPoll;
+#pragma unroll
+      for (int i = kPoll / 32 - 1; i >= 0; --i) {
+        const unsigned n = __ballot_sync(0xffffffffu, !ok[i]);
+        if (n) run = 32 * i + __ffs(n) - 1;
+      }
       vg = min(vg + run, a.groups);
       // the warp owns its SM's FP64 work alone: poll back to back (each
       // poll is an L2 round trip; a sleep between them delayed the start)
