@@ -276,15 +276,16 @@ def workload_config(args):
 
 
 # ------------------------------------------------------ FP32-stencil / batched
-def fp32_single(args, torch):
+def fp32_single(args, torch, compensated=False):
     """throughput of the FP32-stencil / FP64-Poisson form on the same case,
     with the launch shapes picked by sns_batch_autotune (the default shapes'
-    rate beside it; shapes change speed, not results)"""
+    rate beside it; shapes change speed, not results); compensated: the
+    float-float stencil terms and increments"""
     from simplenavierstokessolver_gb300.batch import Batch, Desc
 
     cells = args.nx * args.ny
     with Batch(8 << 30) as b:
-        s = b.add(Desc(args.nx, args.ny, ly=2.0, Ra=args.Ra, Pr=args.Pr))
+        s = b.add(Desc(args.nx, args.ny, ly=2.0, Ra=args.Ra, Pr=args.Pr, compensated=compensated))
         stream = torch.cuda.ExternalStream(b.stream())
         flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
         b.step(args.warmup)
@@ -364,7 +365,7 @@ def large_instance(args, torch, nx=2048, ny=4096, Ra=1e10, steps=10):
     return out
 
 
-def fp32_accuracy(args):
+def fp32_accuracy(args, compensated=False):
     """The FP32-stencil form against the bit-exact FP64 path (identical to the
     reference) over args.acc_steps steps with the same dt sequence: the
     batch's own CFL dt is replayed into the FP64 solver. Returns relative L2
@@ -375,7 +376,7 @@ def fp32_accuracy(args):
     from simplenavierstokessolver_gb300.batch import Batch, Desc
 
     nsteps = args.acc_steps
-    desc = Desc(args.nx, args.ny, ly=2.0, Ra=args.Ra, Pr=args.Pr)
+    desc = Desc(args.nx, args.ny, ly=2.0, Ra=args.Ra, Pr=args.Pr, compensated=compensated)
     dts = []
     with Batch(8 << 30) as b:
         s = b.add(desc)
@@ -404,16 +405,18 @@ def fp32_accuracy(args):
             "divergence_max_fp32_stencil": float(diag32[0]), "divergence_max_fp64": float(diag64[0])}
 
 
-def ensemble_throughput(args, torch):
+def ensemble_throughput(args, torch, compensated=False):
     """64-case ensemble: batched FP32-stencil form (one graph launch per step
     for all cases, launch shapes picked by sns_batch_autotune; the default
     shapes' rate beside it) against the plain FP64 path stepping the cases
-    one by one"""
+    one by one (compensated: the batched rates only)"""
     from simplenavierstokessolver_gb300 import Case
     from simplenavierstokessolver_gb300.batch import Batch
     from simplenavierstokessolver_gb300.workloads import ensemble
 
     descs = ensemble(64)
+    for d in descs:
+        d.compensated = compensated
     cells = sum(d.itot * d.jtot for d in descs)
     with Batch(8 << 30) as b:
         for d in descs:
@@ -436,6 +439,10 @@ def ensemble_throughput(args, torch):
         ms_b = timed()
     batched = cells * args.ens_steps / (ms_b * 1e-3)
     batched_default = cells * args.ens_steps / (ms_default * 1e-3)
+    if compensated:
+        return {"cases": len(descs), "cells": cells, "batched_compensated": batched,
+                "batched_default_shapes": batched_default, "autotuned_shapes": tuned_shapes,
+                "unit": "cell-steps/s", "batched_steps": args.ens_steps}
     plain_steps = max(2, args.ens_steps // 5)
     total_s, plain_cells = 0.0, 0
     for d in descs:
@@ -478,12 +485,14 @@ def ensemble_throughput(args, torch):
             "workload": "nx in {64,128,256}, ny=2nx, log10 Ra in [6,9], Pr in [0.7,7], SplitMix64 seeds 20261203+k"}
 
 
-def ensemble_accuracy(args):
+def ensemble_accuracy(args, compensated=False):
     """The 64-case ensemble in the batched FP32-stencil form against the FP64
     path (bit-identical to the reference) over args.ens_acc_steps steps: each
     case starts from its seeded initial temperature in both runs, and the
     batch's CFL dt sequence is replayed into the FP64 run. Relative L2 per
-    field over the interior (p modulo its mean); max and median over cases."""
+    field over the interior (p modulo its mean); max and median over cases.
+    The sensitivity control (FP64 from a perturbed start) runs for the FP32
+    form only."""
     import numpy as np
 
     from simplenavierstokessolver_gb300 import Case
@@ -491,6 +500,8 @@ def ensemble_accuracy(args):
     from simplenavierstokessolver_gb300.workloads import ensemble
 
     descs = ensemble(64)
+    for d in descs:
+        d.compensated = compensated
     n = args.ens_acc_steps
     dts = [[] for _ in descs]
     with Batch(8 << 30) as b:
@@ -530,11 +541,20 @@ def ensemble_accuracy(args):
         t0 = initial_temperature(d)
         ref = fp64_run(d, dts[k], t0)
         errs.append(rel(got[k], ref))
+        if compensated:
+            continue
         tp = t0.copy()
         tp[1:-1, 1:-1] *= 1.0 + eps * rng.uniform(-1.0, 1.0, tp[1:-1, 1:-1].shape)
         growth.append(max(rel(fp64_run(d, dts[k], tp), ref).values()) / eps)
     worst = [max(e.values()) for e in errs]
     within = [w <= 1e-5 for w in worst]
+    if compensated:
+        return {"steps": n, "dt": "CFL dt of the compensated run, replayed in the FP64 run",
+                "rel_l2_max": {f: max(e[f] for e in errs) for f in fields},
+                "rel_l2_median": {f: float(np.median([e[f] for e in errs])) for f in fields},
+                "target": 1e-5, "cases_within_target": int(sum(within)),
+                "worst_case": {"nx": descs[int(np.argmax(worst))].itot, "Ra": descs[int(np.argmax(worst))].Ra,
+                               "rel_l2_max": max(worst)}}
     outside = [{"nx": descs[k].itot, "Ra": descs[k].Ra, "Pr": descs[k].Pr, "rel_l2_max": worst[k],
                 "fp64_growth_of_1e-9": growth[k]} for k in range(len(descs)) if not within[k]]
     return {"steps": n, "dt": "CFL dt of the FP32 run, replayed in the FP64 run",
@@ -712,6 +732,18 @@ def gpu_arm(args, world, rank, local):
         extra["ensemble_64"] = ensemble_throughput(args, torch)
         if args.ens_acc_steps > 0:
             extra["ensemble_64"]["accuracy_vs_fp64"] = ensemble_accuracy(args)
+        # the same case and ensemble with float-float stencil terms and increments
+        comp = fp32_single(args, torch, compensated=True)
+        comp["vs_plain_fp64"] = comp["value"] / value
+        comp["accuracy_vs_fp64"] = fp32_accuracy(args, compensated=True)
+        ens = ensemble_throughput(args, torch, compensated=True)
+        ens["ratio_vs_plain_concurrent"] = ens["batched_compensated"] / extra["ensemble_64"][
+            "plain_fp64_concurrent_streams"]
+        ens["ratio_vs_plain_one_by_one"] = ens["batched_compensated"] / extra["ensemble_64"]["plain_fp64_one_by_one"]
+        if args.ens_acc_steps > 0:
+            ens["accuracy_vs_fp64"] = ensemble_accuracy(args, compensated=True)
+        comp["ensemble_64"] = ens
+        extra["fp32_compensated"] = comp
         extra["serving"] = serving(args)
         if args.large_steps > 0:
             extra["large_instance"] = large_instance(args, torch, steps=args.large_steps)

@@ -44,6 +44,9 @@ typedef struct sns_case_desc {
   unsigned long long seed;   /* 0: the reference's own initial noise (srand(0); rand()),
                                 else SplitMix64(seed) uniform noise in [-0.05, 0.05] */
   double fixed_dt;           /* > 0: use this dt every step instead of the CFL decision */
+  int compensated;           /* 1: stencil terms, coefficients and increments as float-float
+                                pairs (about 48 bits, on the FP32 pipes) and the divergence
+                                from both words in FP64; 0: FP32 terms */
 } sns_case_desc;
 
 /* Launch shapes of the step's kernels. The defaults (64, 8, 4, 0) are set at

@@ -339,8 +339,9 @@ extern long long sns_kernel_launches(void);
 /* struct layout as compiled into the library, for binding checks: writes up to
  * n values -- sizeof(param_t), offsetof(param_t, itot / dy / rkcoefs / time /
  * dt / step / expimp_wtimes / timemax / log / stat), sizeof(parallel_t),
- * sizeof(fluid_t), offsetof(fluid_t, srcuyg), sizeof(temperature_t) -- and
- * returns how many it wrote (15) */
+ * sizeof(fluid_t), offsetof(fluid_t, srcuyg), sizeof(temperature_t),
+ * sizeof(sns_case_desc), offsetof(sns_case_desc, fixed_dt / compensated)
+ * (include/sns_batch.h) -- and returns how many it wrote (18) */
 extern int sns_abi_layout(size_t *out, int n);
 
 #ifdef __cplusplus

@@ -73,7 +73,8 @@ class CaseDesc(ctypes.Structure):
 
     _fields_ = [("itot", c_int), ("jtot", c_int), ("ly", c_double), ("stretch", c_double), ("Ra", c_double),
                 ("Pr", c_double), ("with_temperature", c_int), ("with_thermal_forcing", c_int),
-                ("steps", c_longlong), ("seed", ctypes.c_ulonglong), ("fixed_dt", c_double)]
+                ("steps", c_longlong), ("seed", ctypes.c_ulonglong), ("fixed_dt", c_double),
+                ("compensated", c_int)]
 
 
 class Tuning(ctypes.Structure):

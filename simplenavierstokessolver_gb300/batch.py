@@ -33,10 +33,13 @@ class Desc:
     steps: int = 0
     seed: int = 0
     fixed_dt: float = 0.0
+    # float-float stencil terms and increments (about 48 bits) instead of FP32
+    compensated: bool = False
 
     def c(self) -> CaseDesc:
         return CaseDesc(self.itot, self.jtot, self.ly, self.stretch, self.Ra, self.Pr, int(self.with_temperature),
-                        int(self.with_thermal_forcing), int(self.steps), int(self.seed), float(self.fixed_dt))
+                        int(self.with_thermal_forcing), int(self.steps), int(self.seed), float(self.fixed_dt),
+                        int(self.compensated))
 
 
 def _ptr(a):

@@ -51,13 +51,15 @@ static size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 // byte layout of one case inside its arena block
 struct CaseLayout {
   size_t rdxf_f, rdxc_f, ccm_f, ccp_f, cfm_f, cfp_f;
-  size_t rdxf, rdxc, dxi, dxf, dxc, tw, lo, hi, pfac;
-  size_t ux[2], uy[2], t[2], uxl[2], uyl[2], tl[2], aux, auy, at, p, psi, spec;
+  size_t rdxf, rdxc, dxi, dxf, dxc, tw, lo, hi, pfac, ccm, ccp, cfm, cfp;
+  size_t ux[2], uy[2], t[2], uxl[2], uyl[2], tl[2], aux, auy, at, auxl, auyl, atl, p, psi, spec;
   size_t total;
   size_t pstride;
 };
 
-static CaseLayout layout_for(int nx, int ny) {
+// x2: a compensated case (sns_case_desc::compensated), which also keeps the
+// low words of the previous right-hand sides
+static CaseLayout layout_for(int nx, int ny, bool x2) {
   CaseLayout L{};
   const int nh = ny / 2 + 1;
   size_t off = 0;
@@ -83,6 +85,10 @@ static CaseLayout layout_for(int nx, int ny) {
   L.hi = take(sizeof(double) * nx);
   L.pstride = 4 * (size_t)nx + 2 * kPcrLevels * kSeg + kSeg;
   L.pfac = take(sizeof(double) * L.pstride * nh);
+  L.ccm = take(sizeof(double) * nx);
+  L.ccp = take(sizeof(double) * nx);
+  L.cfm = take(sizeof(double) * nx);
+  L.cfp = take(sizeof(double) * nx);
   for (int k = 0; k < 2; k++) {
     L.ux[k] = take(sizeof(float) * cells);
     L.uy[k] = take(sizeof(float) * cells);
@@ -96,6 +102,11 @@ static CaseLayout layout_for(int nx, int ny) {
   L.aux = take(sizeof(float) * cells);
   L.auy = take(sizeof(float) * cells);
   L.at = take(sizeof(float) * cells);
+  if (x2) {
+    L.auxl = take(sizeof(float) * cells);
+    L.auyl = take(sizeof(float) * cells);
+    L.atl = take(sizeof(float) * cells);
+  }
   L.p = take(sizeof(double) * cells);
   L.psi = take(sizeof(double) * cells);
   L.spec = take(sizeof(double2) * (size_t)nh * nx);
@@ -250,6 +261,8 @@ struct sns_batch {
   BModes *d_modes = nullptr;
   size_t cap_tiles = 0, cap_cols = 0, cap_modes = 0;
   int ntiles = 0, ncols = 0, nmodes = 0;
+  int ntiles_x2 = 0;  // the last ntiles_x2 tiles belong to compensated cases
+  int graph_launches = 0;  // kernel launches per replay of the step graph
   size_t fft_smem = 0;
   int fft_threads = 64;
   cudaGraph_t graph = nullptr;
@@ -319,7 +332,7 @@ static int tuned_fcols(const sns_batch *b, const CaseHost &h) {
 }
 
 static int rebuild(sns_batch *b) {
-  std::vector<BTile> tiles;
+  std::vector<BTile> tiles, tiles_x2;
   std::vector<BCols> cols;
   std::vector<BModes> modes;
   size_t smem = 0;
@@ -344,12 +357,14 @@ static int rebuild(sns_batch *b) {
                             sizeof(int), cudaMemcpyHostToDevice, b->stream));
     }
     for (int y0 = 0; y0 < ny; y0 += ty)
-      for (int x0 = 0; x0 < nx; x0 += tx) tiles.push_back({c, x0, y0});
+      for (int x0 = 0; x0 < nx; x0 += tx) (h.d.compensated ? tiles_x2 : tiles).push_back({c, x0, y0});
     for (int x0 = 0; x0 < nx; x0 += fc) cols.push_back({c, x0});
     for (int j0 = 0; j0 < nh; j0 += mpb) modes.push_back({c, j0});
     smem = std::max(smem, sizeof(double) * (size_t)fc * ny);
     threads = std::max(threads, std::min(256, (fc * (ny / 2) / 4 + 31) / 32 * 32));
   }
+  const int nx2 = (int)tiles_x2.size();
+  tiles.insert(tiles.end(), tiles_x2.begin(), tiles_x2.end());
   if (int rc = ensure_device_list(&b->d_tiles, &b->cap_tiles, std::max<size_t>(tiles.size(), 1))) return rc;
   if (int rc = ensure_device_list(&b->d_cols, &b->cap_cols, std::max<size_t>(cols.size(), 1))) return rc;
   if (int rc = ensure_device_list(&b->d_modes, &b->cap_modes, std::max<size_t>(modes.size(), 1))) return rc;
@@ -361,6 +376,10 @@ static int rebuild(sns_batch *b) {
     BCUDA(cudaMemcpyAsync(b->d_modes, modes.data(), sizeof(BModes) * modes.size(), cudaMemcpyHostToDevice,
                           b->stream));
   b->ntiles = (int)tiles.size();
+  b->ntiles_x2 = nx2;
+  // per substage: the stencil launch(es), forward DFT, tridiagonal, inverse
+  // DFT, correction; then the dt update
+  b->graph_launches = 3 * ((b->ntiles > nx2) + (nx2 > 0) + 4) + 1;
   b->ncols = (int)cols.size();
   b->nmodes = (int)modes.size();
   b->fft_smem = smem;
@@ -378,7 +397,9 @@ static int rebuild(sns_batch *b) {
   BCUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   cudaError_t err = cudaSuccess;
   for (int rk = 0; rk < 3 && err == cudaSuccess; rk++) {
-    if ((err = launch_batch_stencil(b->d_cases, b->d_tiles, b->ntiles, rk, tx, ty, b->stream)) != cudaSuccess) break;
+    if ((err = launch_batch_stencil(b->d_cases, b->d_tiles, b->ntiles, b->ntiles_x2, rk, tx, ty, b->stream)) !=
+        cudaSuccess)
+      break;
     if ((err = launch_batch_fwd(b->d_cases, b->d_cols, b->ncols, rk, b->fft_smem, b->fft_threads, b->stream)) !=
         cudaSuccess)
       break;
@@ -403,7 +424,7 @@ extern "C" {
 
 size_t sns_batch_case_bytes(const sns_case_desc *desc) {
   if (check_desc(desc) != SNS_OK) return 0;
-  return layout_for(desc->itot, desc->jtot).total;
+  return layout_for(desc->itot, desc->jtot, desc->compensated != 0).total;
 }
 
 sns_batch *sns_batch_create(size_t hbm_bytes, int max_cases) {
@@ -489,7 +510,8 @@ static int admit(sns_batch *b, const sns_case_desc *d, const double *temp_init, 
     }
   if (slot < 0) return bfail(SNS_ERR_OOM, "batch full (%d cases)", b->max_cases);
   const int nx = d->itot, ny = d->jtot, nh = ny / 2 + 1;
-  const CaseLayout L = layout_for(nx, ny);
+  const bool x2 = d->compensated != 0;
+  const CaseLayout L = layout_for(nx, ny, x2);
   size_t off;
   if (!arena_alloc(b, L.total, &off))
     return bfail(SNS_ERR_OOM, "case needs %zu bytes, largest free block %zu", L.total, sns_batch_free_bytes(b));
@@ -501,15 +523,20 @@ static int admit(sns_batch *b, const sns_case_desc *d, const double *temp_init, 
   auto DXF = [&](int i) { return dxf[i - 1]; };
   auto DXC = [&](int i) { return dxc[i - 1]; };
   std::vector<float> rdxf_f(nx), rdxc_f(nx + 1), ccm(nx), ccp(nx), cfm(nx, 0.f), cfp(nx, 0.f);
+  std::vector<double> ccm_d(nx), ccp_d(nx), cfm_d(nx, 0.0), cfp_d(nx, 0.0);
   std::vector<double> rdxf(nx), rdxc(nx + 1), dxi(nx + 1), lo(nx), hi(nx), l_raw(nx), u_raw(nx);
   for (int i = 1; i <= nx; i++) {
     rdxf[i - 1] = 1.0 / DXF(i);
     rdxf_f[i - 1] = (float)rdxf[i - 1];
-    ccm[i - 1] = (float)(DXC(i) / (2. * DXF(i)));
-    ccp[i - 1] = (float)(DXC(i + 1) / (2. * DXF(i)));
+    ccm_d[i - 1] = DXC(i) / (2. * DXF(i));
+    ccp_d[i - 1] = DXC(i + 1) / (2. * DXF(i));
+    ccm[i - 1] = (float)ccm_d[i - 1];
+    ccp[i - 1] = (float)ccp_d[i - 1];
     if (i >= 2) {
-      cfm[i - 1] = (float)(DXF(i - 1) / (2. * DXC(i)));
-      cfp[i - 1] = (float)(DXF(i) / (2. * DXC(i)));
+      cfm_d[i - 1] = DXF(i - 1) / (2. * DXC(i));
+      cfp_d[i - 1] = DXF(i) / (2. * DXC(i));
+      cfm[i - 1] = (float)cfm_d[i - 1];
+      cfp[i - 1] = (float)cfp_d[i - 1];
     }
     l_raw[i - 1] = 1. / DXC(i) / DXF(i);
     u_raw[i - 1] = 1. / DXC(i + 1) / DXF(i);
@@ -564,6 +591,10 @@ static int admit(sns_batch *b, const sns_case_desc *d, const double *temp_init, 
   chk(put(L.lo, lo.data(), sizeof(double) * nx));
   chk(put(L.hi, hi.data(), sizeof(double) * nx));
   chk(put(L.pfac, pfac.data(), sizeof(double) * pfac.size()));
+  chk(put(L.ccm, ccm_d.data(), sizeof(double) * nx));
+  chk(put(L.ccp, ccp_d.data(), sizeof(double) * nx));
+  chk(put(L.cfm, cfm_d.data(), sizeof(double) * nx));
+  chk(put(L.cfp, cfp_d.data(), sizeof(double) * nx));
   for (int k = 0; k < 2; k++) {
     chk(cudaMemsetAsync(base + L.ux[k], 0, sizeof(float) * cells, b->stream));
     chk(cudaMemsetAsync(base + L.uy[k], 0, sizeof(float) * cells, b->stream));
@@ -608,6 +639,8 @@ static int admit(sns_batch *b, const sns_case_desc *d, const double *temp_init, 
   }
   chk(cudaMemsetAsync(base + L.t[1], 0, sizeof(float) * cells, b->stream));
   for (size_t o : {L.aux, L.auy, L.at}) chk(cudaMemsetAsync(base + o, 0, sizeof(float) * cells, b->stream));
+  if (x2)
+    for (size_t o : {L.auxl, L.auyl, L.atl}) chk(cudaMemsetAsync(base + o, 0, sizeof(float) * cells, b->stream));
   if (st) {
     chk(put(L.p, p_d.data(), sizeof(double) * cells));
   } else {
@@ -633,6 +666,9 @@ static int admit(sns_batch *b, const sns_case_desc *d, const double *temp_init, 
   t.rdy_f = (float)t.rdy;
   t.kappa_f = (float)(1. / sqrt(d->Pr) / sqrt(d->Ra));
   t.nu_f = (float)(sqrt(d->Pr) / sqrt(d->Ra));
+  t.kappa = 1. / sqrt(d->Pr) / sqrt(d->Ra);
+  t.nu = sqrt(d->Pr) / sqrt(d->Ra);
+  t.x2 = x2 ? 1 : 0;
   {  // explicit diffusive limits (src/param/decide_dt.c:62-74)
     const double diffusivity = fmax(sqrt(d->Pr) / sqrt(d->Ra), 1. / sqrt(d->Pr) / sqrt(d->Ra));
     double dx = 1.0;
@@ -651,6 +687,10 @@ static int admit(sns_batch *b, const sns_case_desc *d, const double *temp_init, 
   t.rdxf = reinterpret_cast<const double *>(base + L.rdxf);
   t.rdxc = reinterpret_cast<const double *>(base + L.rdxc);
   t.dxi = reinterpret_cast<const double *>(base + L.dxi);
+  t.ccm = reinterpret_cast<const double *>(base + L.ccm);
+  t.ccp = reinterpret_cast<const double *>(base + L.ccp);
+  t.cfm = reinterpret_cast<const double *>(base + L.cfm);
+  t.cfp = reinterpret_cast<const double *>(base + L.cfp);
   t.dxf = reinterpret_cast<const double *>(base + L.dxf);
   t.dxc = reinterpret_cast<const double *>(base + L.dxc);
   t.tw = reinterpret_cast<const double *>(base + L.tw);
@@ -671,6 +711,9 @@ static int admit(sns_batch *b, const sns_case_desc *d, const double *temp_init, 
   t.aux = reinterpret_cast<float *>(base + L.aux);
   t.auy = reinterpret_cast<float *>(base + L.auy);
   t.at = reinterpret_cast<float *>(base + L.at);
+  t.auxl = x2 ? reinterpret_cast<float *>(base + L.auxl) : nullptr;
+  t.auyl = x2 ? reinterpret_cast<float *>(base + L.auyl) : nullptr;
+  t.atl = x2 ? reinterpret_cast<float *>(base + L.atl) : nullptr;
   t.p = reinterpret_cast<double *>(base + L.p);
   t.psi = reinterpret_cast<double *>(base + L.psi);
   t.spec = reinterpret_cast<double2 *>(base + L.spec);
@@ -774,7 +817,7 @@ int sns_batch_step(sns_batch *b, int nsteps) {
       if (int rc = rebuild(b)) return rc;
     if (b->ntiles == 0) break;
     BCUDA(cudaGraphLaunch(b->exec, b->stream));
-    count_launches(16);
+    count_launches(b->graph_launches);
     bool finished_one = false;
     for (CaseHost &h : b->hc) {
       if (!h.used || (h.d.steps > 0 && h.steps_done >= h.d.steps)) continue;
@@ -1131,7 +1174,7 @@ extern "C" int sns_serve(const sns_case_desc *reqs, const double *arrival_s, int
     if (int rc = check_desc(&reqs[r])) return rc;
     if (reqs[r].steps <= 0) return bfail(SNS_ERR_ARG, "sns_serve: request %d has no step count", r);
     if (r > 0 && arrival_s[r] < arrival_s[r - 1]) return bfail(SNS_ERR_ARG, "sns_serve: arrivals must not decrease");
-    if (layout_for(reqs[r].itot, reqs[r].jtot).total > hbm_bytes)
+    if (layout_for(reqs[r].itot, reqs[r].jtot, reqs[r].compensated != 0).total > hbm_bytes)
       return bfail(SNS_ERR_OOM, "sns_serve: request %d is larger than the arena", r);
   }
   sns_batch *b = sns_batch_create(hbm_bytes, max_cases);

@@ -56,6 +56,185 @@ __device__ __forceinline__ F2 ld2(const float *__restrict__ h, const float *__re
 }
 __device__ __forceinline__ float dif(F2 a, F2 b) { return (a.h - b.h) + (a.l - b.l); }
 
+// ------------------------------------------- float-float (compensated) terms
+// Values as unevaluated sums h + l of two FP32 words (about 48 significant
+// bits), built from error-free transformations: Knuth's TwoSum, Dekker's
+// Fast2Sum (|a| >= |b| or a = 0) and the exact product error of one fused
+// multiply-add. Cases with sns_case_desc::compensated compute every stencil
+// term, coefficient and increment this way on the FP32 pipes, so the per-step
+// rounding of the increments drops from FP32's 2^-24 to about 2^-44.
+__device__ __forceinline__ F2 two_sum(float a, float b) {
+  const float s = a + b;
+  const float bp = s - a;
+  return F2{s, (a - (s - bp)) + (b - bp)};
+}
+__device__ __forceinline__ F2 fast_two_sum(float a, float b) {
+  const float s = a + b;
+  return F2{s, b - (s - a)};
+}
+__device__ __forceinline__ F2 operator+(F2 x, F2 y) {
+  const F2 s = two_sum(x.h, y.h);
+  return fast_two_sum(s.h, s.l + (x.l + y.l));
+}
+__device__ __forceinline__ F2 operator-(F2 x) { return F2{-x.h, -x.l}; }
+__device__ __forceinline__ F2 operator-(F2 x, F2 y) { return x + (-y); }
+__device__ __forceinline__ F2 operator*(F2 x, F2 y) {
+  const float p = x.h * y.h;
+  float e = fmaf(x.h, y.h, -p);
+  e = fmaf(x.h, y.l, e);
+  e = fmaf(x.l, y.h, e);
+  return fast_two_sum(p, e);
+}
+__device__ __forceinline__ F2 halve(F2 x) { return F2{0.5f * x.h, 0.5f * x.l}; }
+__device__ __forceinline__ F2 ff(double d) {
+  const float h = (float)d;
+  return F2{h, (float)(d - (double)h)};
+}
+
+// The stencil of k_b_stencil below for a compensated case: the same terms in
+// the same order on float-float values; the previous right-hand sides are
+// stored as pairs too (at/atl, aux/auxl, auy/auyl).
+__device__ void stencil_x2(const BCase &C, int x, int y0, int y1, int rk) {
+  const int nx = C.nx, ny = C.ny;
+  const int pin = C.par ^ (rk & 1), pout = pin ^ 1;
+  const float *__restrict__ ux = C.ux[pin];
+  const float *__restrict__ uy = C.uy[pin];
+  const float *__restrict__ T = C.t[pin];
+  const float *__restrict__ uxl = C.uxl[pin];
+  const float *__restrict__ uyl = C.uyl[pin];
+  const float *__restrict__ Tl = C.tl[pin];
+  float *__restrict__ uxo = C.ux[pout];
+  float *__restrict__ uyo = C.uy[pout];
+  float *__restrict__ To = C.t[pout];
+  float *__restrict__ uxlo = C.uxl[pout];
+  float *__restrict__ uylo = C.uyl[pout];
+  float *__restrict__ Tlo = C.tl[pout];
+  float *__restrict__ aux = C.aux;
+  float *__restrict__ auy = C.auy;
+  float *__restrict__ at = C.at;
+  float *__restrict__ auxl = C.auxl;
+  float *__restrict__ auyl = C.auyl;
+  float *__restrict__ atl = C.atl;
+  const double *__restrict__ p = C.p;
+  const F2 adt = ff(C.adt[rk]), bdt = ff(C.bdt[rk]), gdt = ff(C.gdt[rk]);
+  const bool hasb = rk > 0;
+  const bool with_t = C.with_t != 0, force = C.with_t && C.with_force;
+  const bool left = x == 0, right = x == nx - 1, has_ux = x >= 1;
+  const F2 rdy = ff(C.rdy), kappa = ff(C.kappa), nu = ff(C.nu);
+  const F2 rxc_m = ff(C.rdxc[x]), rxc_p = ff(C.rdxc[x + 1]), rxf = ff(C.rdxf[x]);
+  const F2 rxf_m = has_ux ? ff(C.rdxf[x - 1]) : F2{0.f, 0.f};
+  const F2 ccm = ff(C.ccm[x]), ccp = ff(C.ccp[x]), cfm = ff(C.cfm[x]), cfp = ff(C.cfp[x]);
+  const double rdxc_d = C.rdxc[x], rdy_d = C.rdy;
+  const F2 Z{0.f, 0.f};
+
+  const int ym = wdn(y0, ny);
+  const size_t r0 = (size_t)y0 * nx + x, rm = (size_t)ym * nx + x;
+  F2 u0 = ld2(ux, uxl, r0), u1 = right ? Z : ld2(ux, uxl, r0 + 1);
+  F2 um0 = ld2(ux, uxl, rm), um1 = right ? Z : ld2(ux, uxl, rm + 1);
+  F2 v0 = ld2(uy, uyl, r0), vl = left ? Z : ld2(uy, uyl, r0 - 1);
+  const F2 vm = ld2(uy, uyl, rm);
+  F2 tc = ld2(T, Tl, r0);
+  const F2 tm = ld2(T, Tl, rm);
+  double pm = p[rm];
+  F2 gym_u = (u0 - um0) * rdy;
+  F2 pym_u = has_ux ? halve(cfm * vl + cfp * v0) * gym_u : Z;
+  F2 gym_v = (v0 - vm) * rdy;
+  F2 pym_v = halve(halve(vm + v0)) * gym_v;
+  F2 gym_t = (tc - tm) * rdy;
+  F2 pym_t = halve(v0) * gym_t;
+
+  for (int y = y0; y < y1; ++y) {
+    const int yp = wup(y, ny);
+    const size_t r = (size_t)y * nx + x, rp = (size_t)yp * nx + x;
+    const F2 u0n = ld2(ux, uxl, rp);
+    const F2 u1n = right ? Z : ld2(ux, uxl, rp + 1);
+    const F2 v0n = ld2(uy, uyl, rp);
+    const F2 vln = left ? Z : ld2(uy, uyl, rp - 1);
+    const F2 vr = right ? Z : ld2(uy, uyl, r + 1);
+    const F2 tn = ld2(T, Tl, rp);
+    const F2 tlv = left ? F2{0.5f, 0.f} : ld2(T, Tl, r - 1);  // T(0, j) = +0.5 (include/temperature.h)
+    const double pc = p[r];
+    if (with_t) {  // src/temperature/update.c:32-85
+      const F2 trv = right ? F2{-0.5f, 0.f} : ld2(T, Tl, r + 1);
+      const F2 gxm = (tc - tlv) * rxc_m, gxp = (trv - tc) * rxc_p, gyp = (tn - tc) * rdy;
+      const F2 pyp = halve(v0n) * gyp;
+      const F2 adv1 = -(ccm * u0 * gxm) - (ccp * u1 * gxp);
+      const F2 adv2 = -pym_t - pyp;
+      const F2 dfs = kappa * ((gxp - gxm) * rxf + (gyp - gym_t) * rdy);
+      const F2 A = adv1 + adv2 + dfs;
+      const F2 q = hasb ? adt * A + bdt * ld2(at, atl, r) : adt * A;
+      at[r] = A.h;
+      atl[r] = A.l;
+      const F2 tn2 = tc + q;
+      To[r] = tn2.h;
+      Tlo[r] = tn2.l;
+      gym_t = gyp;
+      pym_t = pyp;
+    } else {
+      To[r] = tc.h;
+      Tlo[r] = tc.l;
+    }
+    if (has_ux) {  // src/fluid/update_velocity.c:136-203
+      const F2 ul = ld2(ux, uxl, r - 1);
+      const F2 gxm = (u0 - ul) * rxf_m, gxp = (u1 - u0) * rxf, gyp = (u0n - u0) * rdy;
+      const F2 vxm = halve(ul + u0), vxp = halve(u0 + u1);
+      const F2 adv1 = -(cfm * vxm * gxm) - (cfp * vxp * gxp);
+      const F2 pyp = halve(cfm * vln + cfp * v0n) * gyp;
+      const F2 adv2 = -pym_u - pyp;
+      const F2 dfs = nu * ((gxp - gxm) * rxc_m + (gyp - gym_u) * rdy);
+      const F2 pre = ff(-((pc - p[r - 1]) * rdxc_d));
+      F2 A = adv1 + adv2 + dfs;
+      if (force) A = A + halve(tlv + tc);
+      const F2 q = (hasb ? adt * A + bdt * ld2(aux, auxl, r) : adt * A) + gdt * pre;
+      aux[r] = A.h;
+      auxl[r] = A.l;
+      const F2 un = u0 + q;
+      uxo[r] = un.h;
+      uxlo[r] = un.l;
+      gym_u = gyp;
+      pym_u = pyp;
+    }
+    {  // src/fluid/update_velocity.c:230-291
+      const F2 gxm = (v0 - vl) * rxc_m, gxp = (vr - v0) * rxc_p, gyp = (v0n - v0) * rdy;
+      const F2 wxm = halve(um0 + u0), wxp = halve(um1 + u1);
+      const F2 adv1 = -(ccm * wxm * gxm) - (ccp * wxp * gxp);
+      const F2 pyp = halve(halve(v0 + v0n)) * gyp;
+      const F2 adv2 = -pym_v - pyp;
+      const F2 dfs = nu * ((gxp - gxm) * rxf + (gyp - gym_v) * rdy);
+      const F2 pre = ff(-((pc - pm) * rdy_d));
+      const F2 A = adv1 + adv2 + dfs;
+      const F2 q = (hasb ? adt * A + bdt * ld2(auy, auyl, r) : adt * A) + gdt * pre;
+      auy[r] = A.h;
+      auyl[r] = A.l;
+      const F2 vn = v0 + q;
+      uyo[r] = vn.h;
+      uylo[r] = vn.l;
+      gym_v = gyp;
+      pym_v = pyp;
+    }
+    um0 = u0;
+    um1 = u1;
+    u0 = u0n;
+    u1 = u1n;
+    vl = vln;
+    v0 = v0n;
+    pm = pc;
+    tc = tn;
+  }
+}
+
+// the tiles of compensated cases (listed after the FP32 ones): a launch of
+// its own, so that the FP32 stencil keeps its register budget
+__global__ void __launch_bounds__(kBTileXMax) k_b_stencil_x2(const BCase *__restrict__ cases,
+                                                            const BTile *__restrict__ tiles, int rk, int rows) {
+  const BTile tile = tiles[blockIdx.x];
+  const BCase &C = cases[tile.c];
+  if (C.done) return;
+  const int x = tile.x0 + threadIdx.x;
+  if (x >= C.nx) return;
+  stencil_x2(C, x, tile.y0, min(tile.y0 + rows, C.ny), rk);
+}
+
 __global__ void __launch_bounds__(kBTileXMax) k_b_stencil(const BCase *__restrict__ cases,
                                                          const BTile *__restrict__ tiles, int rk, int rows) {
   const BTile tile = tiles[blockIdx.x];
@@ -205,9 +384,16 @@ __global__ void __launch_bounds__(256) k_b_fwd(const BCase *__restrict__ cases, 
     if (x < nx) {
       const size_t r = (size_t)y * nx + x;
       const size_t ry = (size_t)wup(y, ny) * nx + x;
-      const float dux = x == nx - 1 ? -(ux[r] + uxl[r]) : (ux[r + 1] - ux[r]) + (uxl[r + 1] - uxl[r]);
-      const float duy = (uy[ry] - uy[r]) + (uyl[ry] - uyl[r]);
-      d = rgdt * ((double)dux * C.rdxf[x] + (double)duy * rdy);
+      if (C.x2) {  // the differences of the pairs in FP64, exact up to one rounding
+        const double dux = x == nx - 1 ? -((double)ux[r] + (double)uxl[r])
+                                       : ((double)ux[r + 1] - (double)ux[r]) + ((double)uxl[r + 1] - (double)uxl[r]);
+        const double duy = ((double)uy[ry] - (double)uy[r]) + ((double)uyl[ry] - (double)uyl[r]);
+        d = rgdt * (dux * C.rdxf[x] + duy * rdy);
+      } else {
+        const float dux = x == nx - 1 ? -(ux[r] + uxl[r]) : (ux[r + 1] - ux[r]) + (uxl[r + 1] - uxl[r]);
+        const float duy = (uy[ry] - uy[r]) + (uyl[ry] - uyl[r]);
+        d = rgdt * ((double)dux * C.rdxf[x] + (double)duy * rdy);
+      }
     }
     zd[2 * (c * M + fft::fft_slot(y >> 1, M, C.fft_nst, C.fft_first2)) + (y & 1)] = d;
   }
@@ -409,13 +595,27 @@ __global__ void __launch_bounds__(kBTileXMax) k_b_corr(BCase *__restrict__ cases
       const double sc = psi[r];
       if (x >= 1) {  // src/fluid/correct_velocity.c:19-25
         float u, ul;
-        acc2(ux[r], uxl[r], -(float)((sc - psi[r - 1]) * gx), u, ul);
+        const double du = -((sc - psi[r - 1]) * gx);
+        if (C.x2) {
+          const F2 w = F2{ux[r], uxl[r]} + ff(du);
+          u = w.h;
+          ul = w.l;
+        } else {
+          acc2(ux[r], uxl[r], (float)du, u, ul);
+        }
         ux[r] = u;
         uxl[r] = ul;
         mx = fmaxf(mx, fabsf(u) * rxc);
       }
       float v, vlo;
-      acc2(uy[r], uyl[r], -(float)((sc - sm) * gy), v, vlo);  // :31-37
+      const double dv = -((sc - sm) * gy);  // :31-37
+      if (C.x2) {
+        const F2 w = F2{uy[r], uyl[r]} + ff(dv);
+        v = w.h;
+        vlo = w.l;
+      } else {
+        acc2(uy[r], uyl[r], (float)dv, v, vlo);
+      }
       uy[r] = v;
       uyl[r] = vlo;
       my = fmaxf(my, fabsf(v) * rdyf);
@@ -481,10 +681,15 @@ cudaError_t batch_kernels_init() {
 }
 
 // the launch helpers below only enqueue: the graph replays are counted by sns_batch_step
-cudaError_t launch_batch_stencil(const BCase *cases, const BTile *tiles, int ntiles, int rk, int tile_x, int rows,
-                                 cudaStream_t st) {
-  if (ntiles == 0) return cudaSuccess;
-  k_b_stencil<<<ntiles, tile_x, 0, st>>>(cases, tiles, rk, rows);
+cudaError_t launch_batch_stencil(const BCase *cases, const BTile *tiles, int ntiles, int ntiles_x2, int rk,
+                                 int tile_x, int rows, cudaStream_t st) {
+  const int nf = ntiles - ntiles_x2;
+  if (nf > 0) {
+    k_b_stencil<<<nf, tile_x, 0, st>>>(cases, tiles, rk, rows);
+  }
+  if (ntiles_x2 > 0) {
+    k_b_stencil_x2<<<ntiles_x2, tile_x, 0, st>>>(cases, tiles + nf, rk, rows);
+  }
   return cudaGetLastError();
 }
 

@@ -25,6 +25,8 @@ struct BCase {
   int seg;                         // rows per segment = nx / kSeg
   double dy, rdy;
   float rdy_f, kappa_f, nu_f;
+  int x2;                          // compensated increments (sns_case_desc::compensated)
+  double kappa, nu;
   double dt_dif;                   // explicit diffusive limit min(dt_dif_x, dt_dif_y)
   double fixed_dt;
   long long target_steps;
@@ -32,6 +34,7 @@ struct BCase {
   const float *ccm_f, *ccp_f;      // DXC(i)/(2 DXF(i)), DXC(i+1)/(2 DXF(i))
   const float *cfm_f, *cfp_f;      // DXF(i-1)/(2 DXC(i)), DXF(i)/(2 DXC(i))
   const double *rdxf, *rdxc, *dxi; // FP64 metrics
+  const double *ccm, *ccp, *cfm, *cfp;  // the advective coefficients above in FP64 (compensated cases)
   const double *dxf, *dxc;         // DXF(i), DXC(i) (diagnostics)
   const double *tw;                // [2*ny]
   const double *lo, *hi;           // Poisson sub/super diagonals a_i, c_i (mode independent) [nx]
@@ -43,6 +46,7 @@ struct BCase {
   // double-buffered like the high words
   float *uxl[2], *uyl[2], *tl[2];
   float *aux, *auy, *at;
+  float *auxl, *auyl, *atl;        // low words of the previous right-hand sides (compensated cases)
   double *p, *psi;
   double2 *spec;
   // ---- dynamic (device-owned)
@@ -72,8 +76,9 @@ constexpr int kBModesPerBlock = 4;     // default tridiagonal warps per block (t
 constexpr int kBModesPerBlockMax = 8;
 
 cudaError_t batch_kernels_init();
-cudaError_t launch_batch_stencil(const BCase *cases, const BTile *tiles, int ntiles, int rk, int tile_x, int rows,
-                                 cudaStream_t st);
+// tiles[ntiles - ntiles_x2 ..] belong to compensated cases
+cudaError_t launch_batch_stencil(const BCase *cases, const BTile *tiles, int ntiles, int ntiles_x2, int rk,
+                                 int tile_x, int rows, cudaStream_t st);
 cudaError_t launch_batch_fwd(const BCase *cases, const BCols *cols, int ncols, int rk, size_t smem, int threads,
                              cudaStream_t st);
 // shared memory of the tridiagonal launch for lines up to nmax long

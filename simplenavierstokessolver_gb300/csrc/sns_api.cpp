@@ -24,6 +24,7 @@
 #include "diag_internal.h"
 #include "host_common.h"
 #include "npy.h"
+#include "sns_batch.h"
 #include "sns_gpu.h"
 #include "sns_internal.h"
 
@@ -1040,7 +1041,8 @@ int sns_abi_layout(size_t *out, int n) {
                       offsetof(param_t, rkcoefs), offsetof(param_t, time),  offsetof(param_t, dt),
                       offsetof(param_t, step),  offsetof(param_t, expimp_wtimes), offsetof(param_t, timemax),
                       offsetof(param_t, log),   offsetof(param_t, stat),    sizeof(parallel_t),
-                      sizeof(fluid_t),          offsetof(fluid_t, srcuyg),  sizeof(temperature_t)};
+                      sizeof(fluid_t),          offsetof(fluid_t, srcuyg),  sizeof(temperature_t),
+                      sizeof(sns_case_desc),    offsetof(sns_case_desc, fixed_dt), offsetof(sns_case_desc, compensated)};
   const int m = (int)(sizeof v / sizeof v[0]);
   for (int k = 0; k < m && k < n; k++) out[k] = v[k];
   return m;

@@ -53,7 +53,8 @@ def test_struct_layout_matches_bindings(native):
     expect = [ctypes.sizeof(P), P.itot.offset, P.dy.offset, P.rkcoefs.offset, P.time.offset, P.dt.offset,
               P.step.offset, P.expimp_wtimes.offset, P.timemax.offset, getattr(P, "log").offset, P.stat.offset,
               ctypes.sizeof(native.Parallel), ctypes.sizeof(native.Fluid), native.Fluid.srcuyg.offset,
-              ctypes.sizeof(native.Temperature)]
+              ctypes.sizeof(native.Temperature), ctypes.sizeof(native.CaseDesc), native.CaseDesc.fixed_dt.offset,
+              native.CaseDesc.compensated.offset]
     assert n == len(expect)
     assert list(out[:n]) == expect
 

@@ -86,6 +86,48 @@ def test_single_case_matches_fp64_oracle(stretch):
     assert max(err.values()) < 1e-5, err
 
 
+@pytest.mark.parametrize("stretch", [1e9, 3], ids=["uniform", "stretched"])
+def test_compensated_case_matches_fp64_oracle(stretch):
+    """float-float stencil terms and increments: the error against the FP64
+    oracle drops by orders of magnitude below the FP32 case's"""
+    from simplenavierstokessolver_gb300.batch import Batch, Desc
+
+    errs = {}
+    for comp in (False, True):
+        desc = Desc(64, 128, ly=2.0, stretch=stretch, Ra=1e6, Pr=1.0, seed=7, compensated=comp)
+        dt = explicit_dt(desc)
+        desc.fixed_dt = dt
+        with Batch(256 << 20) as b:
+            s = b.add(desc)
+            b.step(60)
+            got = b.state(s)
+        errs[comp] = errors(got, oracle_fixed_dt(desc, 60, dt).get_state())
+    assert max(errs[True].values()) < 1e-10, errs
+    assert max(errs[True].values()) < 1e-3 * max(errs[False].values()), errs
+
+
+def test_compensated_alone_and_next_to_fp32_cases_are_identical():
+    """compensated cases run in a launch of their own over the tail of the
+    tile list: mixing them with FP32 cases changes no case"""
+    from simplenavierstokessolver_gb300.batch import Batch, Desc
+
+    descs = [Desc(64, 128, Ra=3e6, Pr=0.7, seed=1, compensated=True), Desc(128, 256, Ra=1e8, Pr=5.0, seed=2),
+             Desc(96, 64, ly=0.5, Ra=1e5, Pr=2.0, seed=3, stretch=4, compensated=True)]
+    alone = []
+    for d in descs:
+        with Batch(512 << 20) as b:
+            s = b.add(d)
+            b.step(20)
+            alone.append(b.state(s))
+    with Batch(1 << 30) as b:
+        slots = [b.add(d) for d in descs]
+        b.step(20)
+        mixed = [b.state(s) for s in slots]
+    for a, m in zip(alone, mixed):
+        for k in a:
+            assert np.array_equal(a[k], m[k]), k
+
+
 def test_cfl_dt_tracks_the_oracle():
     """dt from the device max-|u| reduction follows the reference's rule."""
     from simplenavierstokessolver_gb300.batch import Batch, Desc, initial_temperature
