@@ -50,7 +50,7 @@ static size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 
 // byte layout of one case inside its arena block
 struct CaseLayout {
-  size_t rdxf_f, rdxc_f, ccm_f, ccp_f, cfm_f, cfp_f;
+  size_t rdxf_f, rdxc_f, ccm_f, ccp_f, cfm_f, cfp_f, rdxf_l;
   size_t rdxf, rdxc, dxi, dxf, dxc, tw, lo, hi, pfac, ccm, ccp, cfm, cfp;
   size_t ux[2], uy[2], t[2], uxl[2], uyl[2], tl[2], aux, auy, at, auxl, auyl, atl, p, psi, spec;
   size_t total;
@@ -70,6 +70,7 @@ static CaseLayout layout_for(int nx, int ny, bool x2) {
   };
   const size_t cells = (size_t)nx * ny;
   L.rdxf_f = take(sizeof(float) * nx);
+  L.rdxf_l = take(sizeof(float) * nx);
   L.rdxc_f = take(sizeof(float) * (nx + 1));
   L.ccm_f = take(sizeof(float) * nx);
   L.ccp_f = take(sizeof(float) * nx);
@@ -522,12 +523,13 @@ static int admit(sns_batch *b, const sns_case_desc *d, const double *temp_init, 
   make_grid(nx, ny, 1.0, d->ly, d->stretch, xf.data(), xc.data(), dxf.data(), dxc.data(), nullptr, nullptr, &dy);
   auto DXF = [&](int i) { return dxf[i - 1]; };
   auto DXC = [&](int i) { return dxc[i - 1]; };
-  std::vector<float> rdxf_f(nx), rdxc_f(nx + 1), ccm(nx), ccp(nx), cfm(nx, 0.f), cfp(nx, 0.f);
+  std::vector<float> rdxf_f(nx), rdxf_l(nx), rdxc_f(nx + 1), ccm(nx), ccp(nx), cfm(nx, 0.f), cfp(nx, 0.f);
   std::vector<double> ccm_d(nx), ccp_d(nx), cfm_d(nx, 0.0), cfp_d(nx, 0.0);
   std::vector<double> rdxf(nx), rdxc(nx + 1), dxi(nx + 1), lo(nx), hi(nx), l_raw(nx), u_raw(nx);
   for (int i = 1; i <= nx; i++) {
     rdxf[i - 1] = 1.0 / DXF(i);
     rdxf_f[i - 1] = (float)rdxf[i - 1];
+    rdxf_l[i - 1] = (float)(rdxf[i - 1] - (double)rdxf_f[i - 1]);
     ccm_d[i - 1] = DXC(i) / (2. * DXF(i));
     ccp_d[i - 1] = DXC(i + 1) / (2. * DXF(i));
     ccm[i - 1] = (float)ccm_d[i - 1];
@@ -577,6 +579,7 @@ static int admit(sns_batch *b, const sns_case_desc *d, const double *temp_init, 
     if (e == cudaSuccess) e = x;
   };
   chk(put(L.rdxf_f, rdxf_f.data(), sizeof(float) * nx));
+  chk(put(L.rdxf_l, rdxf_l.data(), sizeof(float) * nx));
   chk(put(L.rdxc_f, rdxc_f.data(), sizeof(float) * (nx + 1)));
   chk(put(L.ccm_f, ccm.data(), sizeof(float) * nx));
   chk(put(L.ccp_f, ccp.data(), sizeof(float) * nx));
@@ -664,6 +667,7 @@ static int admit(sns_batch *b, const sns_case_desc *d, const double *temp_init, 
   t.dy = dy;
   t.rdy = 1.0 / dy;
   t.rdy_f = (float)t.rdy;
+  t.rdy_l = (float)(t.rdy - (double)t.rdy_f);
   t.kappa_f = (float)(1. / sqrt(d->Pr) / sqrt(d->Ra));
   t.nu_f = (float)(sqrt(d->Pr) / sqrt(d->Ra));
   t.kappa = 1. / sqrt(d->Pr) / sqrt(d->Ra);
@@ -679,6 +683,7 @@ static int admit(sns_batch *b, const sns_case_desc *d, const double *temp_init, 
   t.fixed_dt = d->fixed_dt;
   t.target_steps = d->steps;
   t.rdxf_f = reinterpret_cast<const float *>(base + L.rdxf_f);
+  t.rdxf_l = reinterpret_cast<const float *>(base + L.rdxf_l);
   t.rdxc_f = reinterpret_cast<const float *>(base + L.rdxc_f);
   t.ccm_f = reinterpret_cast<const float *>(base + L.ccm_f);
   t.ccp_f = reinterpret_cast<const float *>(base + L.ccp_f);

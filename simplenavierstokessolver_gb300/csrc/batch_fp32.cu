@@ -377,6 +377,7 @@ __global__ void __launch_bounds__(256) k_b_fwd(const BCase *__restrict__ cases, 
   const float *__restrict__ uxl = C.uxl[pu];
   const float *__restrict__ uyl = C.uyl[pu];
   const double rgdt = C.rgdt[rk], rdy = C.rdy;
+  const F2 rg2 = ff(rgdt);
   double *zd = reinterpret_cast<double *>(zs);
   for (int e = threadIdx.x; e < nc * ny; e += blockDim.x) {
     const int c = e % nc, y = e / nc, x = x0 + c;
@@ -384,11 +385,12 @@ __global__ void __launch_bounds__(256) k_b_fwd(const BCase *__restrict__ cases, 
     if (x < nx) {
       const size_t r = (size_t)y * nx + x;
       const size_t ry = (size_t)wup(y, ny) * nx + x;
-      if (C.x2) {  // the differences of the pairs in FP64, exact up to one rounding
-        const double dux = x == nx - 1 ? -((double)ux[r] + (double)uxl[r])
-                                       : ((double)ux[r + 1] - (double)ux[r]) + ((double)uxl[r + 1] - (double)uxl[r]);
-        const double duy = ((double)uy[ry] - (double)uy[r]) + ((double)uyl[ry] - (double)uyl[r]);
-        d = rgdt * (dux * C.rdxf[x] + duy * rdy);
+      if (C.x2) {  // float-float on the FP32 pipes, one conversion pair at the end
+        const F2 u0{ux[r], uxl[r]};
+        const F2 dux = x == nx - 1 ? -u0 : F2{ux[r + 1], uxl[r + 1]} - u0;
+        const F2 duy = F2{uy[ry], uyl[ry]} - F2{uy[r], uyl[r]};
+        const F2 v = (dux * F2{C.rdxf_f[x], C.rdxf_l[x]} + duy * F2{C.rdy_f, C.rdy_l}) * rg2;
+        d = (double)v.h + (double)v.l;
       } else {
         const float dux = x == nx - 1 ? -(ux[r] + uxl[r]) : (ux[r + 1] - ux[r]) + (uxl[r + 1] - uxl[r]);
         const float duy = (uy[ry] - uy[r]) + (uyl[ry] - uyl[r]);

@@ -31,6 +31,8 @@ struct BCase {
   double fixed_dt;
   long long target_steps;
   const float *rdxf_f, *rdxc_f;    // [nx], [nx+1]
+  const float *rdxf_l;             // [nx] low words of 1/DXF(i) (compensated cases: rdxf_f + rdxf_l)
+  float rdy_l;                     // low word of 1/dy
   const float *ccm_f, *ccp_f;      // DXC(i)/(2 DXF(i)), DXC(i+1)/(2 DXF(i))
   const float *cfm_f, *cfp_f;      // DXF(i-1)/(2 DXC(i)), DXF(i)/(2 DXC(i))
   const double *rdxf, *rdxc, *dxi; // FP64 metrics
