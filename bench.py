@@ -76,6 +76,25 @@ PROFILED_TRAFFIC = {
 }
 
 
+# algorithmic DRAM bytes per cell of the plain path's implicit-scheme
+# launches (2048 x 4096 at Ra 1e10): each Crank-Nicolson launch solves the
+# temperature, ux and uy lines side by side (increment read and written per
+# field), the increment launch adds them to the three fields
+IMPLICIT_MODEL = {"cn_solve_x": 48.0, "cn_solve_y": 48.0, "add_increment": 72.0}
+
+
+def batched_bytes_per_cell_step(compensated: bool) -> float:
+    """algorithmic DRAM bytes per cell and time step of the batched form:
+    per substage the stencil (hi and lo words of ux, uy, T read and written,
+    24 + 24 B; previous right-hand sides 12 + 12 B, their low words too when
+    compensated; p 8 B), the divergence and forward DFT (ux, uy pairs 16 B,
+    half-spectrum 8 B), the tridiagonal solve (spectrum 8 + 8 B, factors
+    16 B), the inverse DFT (8 + 8 B) and the correction (psi, p 16 B, the
+    velocity pairs 16 + 16 B, p 8 B)"""
+    stencil = 80.0 + (24.0 if compensated else 0.0)
+    return 3 * (stencil + 24.0 + 32.0 + 16.0 + 56.0)
+
+
 def power_of_two_grid(grid: dict) -> bool:
     """every spacing a power of two 2^e, |e| <= 64: the velocity kernel then
     forms its power-of-two products in integer arithmetic"""
@@ -309,9 +328,20 @@ def fp32_single(args, torch, compensated=False):
         b.synchronize()
         ms = timed()
         del b, s
-    return {"value": cells * args.steps / (ms * 1e-3), "unit": "cell-steps/s", "ms_per_step": ms / args.steps,
+    value = cells * args.steps / (ms * 1e-3)
+    return {"value": value, "unit": "cell-steps/s", "ms_per_step": ms / args.steps,
             "default_shapes_value": cells * args.steps / (ms_default * 1e-3), "autotuned_shapes": shapes,
-            "l2": "flushed between timed steps (256 MiB write)"}
+            "l2": "flushed between timed steps (256 MiB write)", "hbm_roofline": hbm_roofline(value, compensated)}
+
+
+def hbm_roofline(cell_steps_per_s: float, compensated: bool) -> dict:
+    """the batched form's whole step against the measured HBM bandwidth"""
+    peak, kind = load_peaks()
+    bpc = batched_bytes_per_cell_step(compensated)
+    gbs = cell_steps_per_s * bpc / 1e9
+    return {"bytes_per_cell_step": bpc, "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+            "peak_source": f"{kind} (MEASURED_PEAKS.json hbm_gbs)" if kind == "measured" else "fallback",
+            "note": "algorithmic bytes of the whole step over its event time; the FP64 DFTs bound the step"}
 
 
 def large_instance(args, torch, nx=2048, ny=4096, Ra=1e10, steps=10):
@@ -345,9 +375,16 @@ def large_instance(args, torch, nx=2048, ny=4096, Ra=1e10, steps=10):
         n = lib.sns_profile_read(c.fluid, kms, kcnt, 32)
         lib.sns_profile(c.fluid, 0)
         kernels = {lib.sns_profile_kind_name(k).decode(): round(1e3 * kms[k] / kcnt[k], 1) for k in range(n) if kcnt[k]}
+    peak, _ = load_peaks()
+    kgbs = {}
+    for k, us in kernels.items():
+        bpc = IMPLICIT_MODEL.get(k, KERNEL_MODEL.get(k, (None,))[0])
+        if bpc and us > 0:
+            gbs = bpc * cells / (us * 1e-6) / 1e9
+            kgbs[k] = {"bytes_per_cell": bpc, "achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4)}
     out["plain_fp64"] = {"value": cells * steps / (ms * 1e-3), "ms_per_step": ms / steps,
                          "scheme": f"implicit x {d['implicitx']}, implicit y {d['implicity']}",
-                         "kernel_avg_us": kernels}
+                         "kernel_avg_us": kernels, "kernel_hbm": kgbs, "hbm_peak_gbs": peak}
     with Batch(16 << 30) as b:
         b.add(Desc(nx, ny, ly=2.0, Ra=Ra, Pr=1.0))
         stream = torch.cuda.ExternalStream(b.stream())
@@ -360,8 +397,10 @@ def large_instance(args, torch, nx=2048, ny=4096, Ra=1e10, steps=10):
         e1.record(stream)
         b.synchronize()
         ms = e0.elapsed_time(e1)
-    out["fp32_stencil"] = {"value": cells * steps / (ms * 1e-3), "ms_per_step": ms / steps,
-                           "scheme": "explicit x / explicit y (batched form)", "autotuned_shapes": shapes}
+    v32 = cells * steps / (ms * 1e-3)
+    out["fp32_stencil"] = {"value": v32, "ms_per_step": ms / steps,
+                           "scheme": "explicit x / explicit y (batched form)", "autotuned_shapes": shapes,
+                           "hbm_roofline": hbm_roofline(v32, False)}
     return out
 
 
@@ -442,7 +481,8 @@ def ensemble_throughput(args, torch, compensated=False):
     if compensated:
         return {"cases": len(descs), "cells": cells, "batched_compensated": batched,
                 "batched_default_shapes": batched_default, "autotuned_shapes": tuned_shapes,
-                "unit": "cell-steps/s", "batched_steps": args.ens_steps}
+                "unit": "cell-steps/s", "batched_steps": args.ens_steps,
+                "hbm_roofline": hbm_roofline(batched, True)}
     plain_steps = max(2, args.ens_steps // 5)
     total_s, plain_cells = 0.0, 0
     for d in descs:
@@ -481,6 +521,7 @@ def ensemble_throughput(args, torch, compensated=False):
             "plain_fp64_concurrent_streams": plain_concurrent,
             "ratio_vs_concurrent": batched / plain_concurrent,
             "ratio": batched / plain, "unit": "cell-steps/s", "batched_steps": args.ens_steps,
+            "hbm_roofline": hbm_roofline(batched, False),
             "plain_steps_per_case": plain_steps,
             "workload": "nx in {64,128,256}, ny=2nx, log10 Ra in [6,9], Pr in [0.7,7], SplitMix64 seeds 20261203+k"}
 
