@@ -115,7 +115,10 @@ extern int sns_serve(const sns_case_desc *reqs, const double *arrival_s, int n, 
 
 /* A case's state in the reference's save layout (src/save.c:13-68): the
  * files sns_checkpoint (sns_gpu.h) writes for the plain path, with velocity
- * and temperature widened from their compensated FP32 pairs. Blocks. */
+ * and temperature widened from their compensated FP32 pairs. An FP32 case's
+ * pairs fit FP64 exactly, so a restart continues bit for bit; a compensated
+ * case's pairs may hold more bits, and its restart resumes from them
+ * rounded to FP64 (a relative 2^-53 per value). Blocks. */
 extern int sns_batch_checkpoint(sns_batch *batch, int slot, const char *dirname);
 /* Admits a case from a directory in that layout (written by the reference's
  * save(), sns_checkpoint or sns_batch_checkpoint): step, time, ux, uy, p and

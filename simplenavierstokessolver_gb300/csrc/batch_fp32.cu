@@ -72,9 +72,11 @@ __device__ __forceinline__ F2 fast_two_sum(float a, float b) {
   const float s = a + b;
   return F2{s, b - (s - a)};
 }
+// the final renormalisation is a TwoSum too: under cancellation the low
+// parts can outweigh the high sum, where Fast2Sum would not be exact
 __device__ __forceinline__ F2 operator+(F2 x, F2 y) {
   const F2 s = two_sum(x.h, y.h);
-  return fast_two_sum(s.h, s.l + (x.l + y.l));
+  return two_sum(s.h, s.l + (x.l + y.l));
 }
 __device__ __forceinline__ F2 operator-(F2 x) { return F2{-x.h, -x.l}; }
 __device__ __forceinline__ F2 operator-(F2 x, F2 y) { return x + (-y); }

@@ -239,7 +239,9 @@ def test_serving_results_equal_standalone_runs():
     case run alone."""
     from simplenavierstokessolver_gb300.batch import Batch, Desc, case_bytes, serve
 
-    descs = [Desc(64, 128, Ra=1e6 * (k + 1), Pr=1.0 + 0.3 * k, seed=100 + k, steps=20 + 7 * k) for k in range(5)]
+    # every other request compensated: both kinds share the launches
+    descs = [Desc(64, 128, Ra=1e6 * (k + 1), Pr=1.0 + 0.3 * k, seed=100 + k, steps=20 + 7 * k, compensated=k % 2 == 1)
+             for k in range(5)]
     descs.append(Desc(128, 256, Ra=1e8, Pr=0.8, seed=200, steps=25))
     arrivals = [0.0, 0.0, 0.05, 0.1, 0.1, 0.15]
     arena = case_bytes(descs[-1]) + case_bytes(descs[0])  # at most ~2 cases resident
@@ -314,13 +316,17 @@ def test_tuning_changes_speed_not_results():
             assert np.array_equal(a[k], m[k]), k
 
 
-def test_checkpoint_and_restart_continue_bit_for_bit(tmp_path):
+@pytest.mark.parametrize("compensated", [False, True], ids=["fp32", "compensated"])
+def test_checkpoint_and_restart_continue_bit_for_bit(tmp_path, compensated):
     """serving snapshot and resume: a case checkpointed after 15 steps and
-    admitted from the files into another batch continues exactly as the
-    uninterrupted case; the files read back as the reference's save layout"""
+    admitted from the files into another batch continues as the uninterrupted
+    case; the files read back as the reference's save layout. An FP32 case
+    continues bit for bit (its pairs carry the increments' FP32 precision and
+    fit the file's FP64 values); a compensated pair can hold more bits than
+    an FP64 value, so that case resumes from the pair rounded to FP64"""
     from simplenavierstokessolver_gb300.batch import Batch, Desc
 
-    d = Desc(128, 256, Ra=1e8, Pr=1.0, seed=5)
+    d = Desc(128, 256, Ra=1e8, Pr=1.0, seed=5, compensated=compensated)
     with Batch(512 << 20) as b:
         s = b.add(d)
         b.step(15)
@@ -338,7 +344,11 @@ def test_checkpoint_and_restart_continue_bit_for_bit(tmp_path):
         st_resumed = b.status(s)
     assert st_resumed["step"] == st_straight["step"] and st_resumed["time"] == st_straight["time"]
     for k in ("ux", "uy", "p", "temp"):
-        assert np.array_equal(straight[k], resumed[k]), k
+        if compensated:
+            a, r = resumed[k][1:-1, 1:-1], straight[k][1:-1, 1:-1]
+            assert np.linalg.norm(a - r) <= 1e-13 * np.linalg.norm(r), k
+        else:
+            assert np.array_equal(straight[k], resumed[k]), k
 
 
 def test_restart_from_a_plain_checkpoint(tmp_path):
