@@ -452,33 +452,43 @@ __global__ void __launch_bounds__(128) k_vel(const VelArgs a) {
 // their factors, uniform across the warp) is loaded into registers while the
 // current chunk is eliminated, so the loads stay off the dependent chain.
 constexpr int kLineChunk = 8;
+// elements per chunk of the row-wise solve along x: its lanes walk 32
+// different rows, so every load touches 32 cache lines and the prefetch
+// distance sets the pace (2048 x 4096: chunks of 8 / 10 / 16 take 1015 /
+// 585 / 547 us per launch, 12 to 20 alike); the column-wise solve along y is
+// coalesced and fastest with kLineChunk
+constexpr int kSolveXChunk = 16;
+// elements per chunk of the periodic solve's final pass (no recurrence: the
+// next chunk's loads are issued before the current chunk's stores)
+constexpr int kFixChunk = 16;
 
 __device__ __forceinline__ bool is_zero_bits(double v) { return (__double_as_longlong(v) << 1) == 0; }
 
 // forward elimination (src/linalg.c:14-23) over e = e0..e1-1 with element
 // stride s; prev is the eliminated value at e0-1. Returns the value at e1-1.
+template <int CH>
 __device__ __forceinline__ double line_forward(double *q, size_t s, const double *inv, const double *l, int e0, int e1,
                                                double prev) {
-  double cq[kLineChunk], ci[kLineChunk], cl[kLineChunk];
+  double cq[CH], ci[CH], cl[CH];
 #pragma unroll
-  for (int k = 0; k < kLineChunk; ++k) {
+  for (int k = 0; k < CH; ++k) {
     const int e = e0 + k;
     cq[k] = e < e1 ? q[(size_t)e * s] : 0.0;
     ci[k] = e < e1 ? __ldg(inv + e) : 0.0;
     cl[k] = e < e1 ? __ldg(l + e) : 0.0;
   }
 #pragma unroll 1
-  for (int b = e0; b < e1; b += kLineChunk) {
-    double nq[kLineChunk], ni[kLineChunk], nl[kLineChunk];
+  for (int b = e0; b < e1; b += CH) {
+    double nq[CH], ni[CH], nl[CH];
 #pragma unroll
-    for (int k = 0; k < kLineChunk; ++k) {
-      const int e = b + kLineChunk + k;
+    for (int k = 0; k < CH; ++k) {
+      const int e = b + CH + k;
       nq[k] = e < e1 ? q[(size_t)e * s] : 0.0;
       ni[k] = e < e1 ? __ldg(inv + e) : 0.0;
       nl[k] = e < e1 ? __ldg(l + e) : 0.0;
     }
 #pragma unroll
-    for (int k = 0; k < kLineChunk; ++k) {
+    for (int k = 0; k < CH; ++k) {
       const int e = b + k;
       if (e < e1) {
         const double v = is_zero_bits(ci[k]) ? 0.0 : ci[k] * (cq[k] - cl[k] * prev);
@@ -487,7 +497,7 @@ __device__ __forceinline__ double line_forward(double *q, size_t s, const double
       }
     }
 #pragma unroll
-    for (int k = 0; k < kLineChunk; ++k) {
+    for (int k = 0; k < CH; ++k) {
       cq[k] = nq[k];
       ci[k] = ni[k];
       cl[k] = nl[k];
@@ -498,25 +508,26 @@ __device__ __forceinline__ double line_forward(double *q, size_t s, const double
 
 // back substitution (src/linalg.c:25-27) over e = hi down to lo; next is the
 // value at hi+1.
+template <int CH>
 __device__ __forceinline__ void line_backward(double *q, size_t s, const double *up, int hi, int lo, double next) {
-  double cq[kLineChunk], cu[kLineChunk];
+  double cq[CH], cu[CH];
 #pragma unroll
-  for (int k = 0; k < kLineChunk; ++k) {
+  for (int k = 0; k < CH; ++k) {
     const int e = hi - k;
     cq[k] = e >= lo ? q[(size_t)e * s] : 0.0;
     cu[k] = e >= lo ? __ldg(up + e) : 0.0;
   }
 #pragma unroll 1
-  for (int b = hi; b >= lo; b -= kLineChunk) {
-    double nq[kLineChunk], nu[kLineChunk];
+  for (int b = hi; b >= lo; b -= CH) {
+    double nq[CH], nu[CH];
 #pragma unroll
-    for (int k = 0; k < kLineChunk; ++k) {
-      const int e = b - kLineChunk - k;
+    for (int k = 0; k < CH; ++k) {
+      const int e = b - CH - k;
       nq[k] = e >= lo ? q[(size_t)e * s] : 0.0;
       nu[k] = e >= lo ? __ldg(up + e) : 0.0;
     }
 #pragma unroll
-    for (int k = 0; k < kLineChunk; ++k) {
+    for (int k = 0; k < CH; ++k) {
       const int e = b - k;
       if (e >= lo) {
         const double v = cq[k] - cu[k] * next;
@@ -525,7 +536,7 @@ __device__ __forceinline__ void line_backward(double *q, size_t s, const double 
       }
     }
 #pragma unroll
-    for (int k = 0; k < kLineChunk; ++k) {
+    for (int k = 0; k < CH; ++k) {
       cq[k] = nq[k];
       cu[k] = nu[k];
     }
@@ -549,9 +560,9 @@ __global__ void __launch_bounds__(32) k_solve_x(int nx, int ny, const SolveXSet 
     prev = row[0] / f.d0;
     row[0] = prev;
   }
-  prev = line_forward(row, 1, f.inv, f.l, 1, nx, prev);
+  prev = line_forward<kSolveXChunk>(row, 1, f.inv, f.l, 1, nx, prev);
   // mode 1: the identity row itot+1 is zero, so row itot-1 is final already
-  line_backward(row, 1, f.up, nx - 2, mode == 0 ? 0 : 1, prev);
+  line_backward<kSolveXChunk>(row, 1, f.up, nx - 2, mode == 0 ? 0 : 1, prev);
 }
 
 // src/linalg.c:52-108 applied per column along y (periodic), coalesced across x.
@@ -565,24 +576,36 @@ __global__ void __launch_bounds__(32) k_solve_y(int nx, int ny, const SolveYSet 
   const LineFactors &sub = f.sub;
   double prev = col[0] / sub.d0;
   col[0] = prev;
-  prev = line_forward(col, s, sub.inv, sub.l, 1, n - 1, prev);
-  line_backward(col, s, sub.up, n - 3, 0, prev);
+  prev = line_forward<kLineChunk>(col, s, sub.inv, sub.l, 1, n - 1, prev);
+  line_backward<kLineChunk>(col, s, sub.up, n - 3, 0, prev);
   const double q00 = col[0], q0l = col[(size_t)(n - 2) * s];
   const double last = (col[(size_t)(n - 1) * s] - f.u_last * q00 - f.l_last * q0l) / f.den;
   col[(size_t)(n - 1) * s] = last;
-#pragma unroll 1
-  for (int b = 0; b <= n - 2; b += kLineChunk) {
-    double cq[kLineChunk], c1[kLineChunk];
+  double cq[kFixChunk], c1[kFixChunk];
 #pragma unroll
-    for (int k = 0; k < kLineChunk; ++k) {
-      const int y = b + k;
-      cq[k] = y <= n - 2 ? col[(size_t)y * s] : 0.0;
-      c1[k] = y <= n - 2 ? __ldg(f.q1 + y) : 0.0;
+  for (int k = 0; k < kFixChunk; ++k) {
+    const int y = k;
+    cq[k] = y <= n - 2 ? col[(size_t)y * s] : 0.0;
+    c1[k] = y <= n - 2 ? __ldg(f.q1 + y) : 0.0;
+  }
+#pragma unroll 1
+  for (int b = 0; b <= n - 2; b += kFixChunk) {
+    double nq[kFixChunk], n1[kFixChunk];
+#pragma unroll
+    for (int k = 0; k < kFixChunk; ++k) {
+      const int y = b + kFixChunk + k;
+      nq[k] = y <= n - 2 ? col[(size_t)y * s] : 0.0;
+      n1[k] = y <= n - 2 ? __ldg(f.q1 + y) : 0.0;
     }
 #pragma unroll
-    for (int k = 0; k < kLineChunk; ++k) {
+    for (int k = 0; k < kFixChunk; ++k) {
       const int y = b + k;
       if (y <= n - 2) col[(size_t)y * s] = cq[k] + last * c1[k];
+    }
+#pragma unroll
+    for (int k = 0; k < kFixChunk; ++k) {
+      cq[k] = nq[k];
+      c1[k] = n1[k];
     }
   }
 }
