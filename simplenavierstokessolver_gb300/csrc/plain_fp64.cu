@@ -846,10 +846,11 @@ constexpr int kFusedThreads = 512;
 constexpr int kFusedTriWarps = 4;
 constexpr int kFusedMinWorkers = 130;
 constexpr int kFusedSpan = 64;
-// elements per chunk of the fused back substitution (the forward elimination
-// and the Crank-Nicolson sweeps use kLineChunk = 8): measured at 512 x 1024,
-// chunks of 6 finish the back substitution in 50 us against 54.5 us with 8
-// (5: 51 us, 7: 60 us)
+// elements per chunk of the fused forward elimination and back substitution,
+// measured at 512 x 1024 (launch, CUDA events): forward 8 / 6 / 10 with back
+// 6: 143.1 / 143.9 / 147.3 us; back 6 / 5 / 7 / 8 with forward 8: 143.1 /
+// 144.1 / 152.7 / 153.5 us
+constexpr int kForwardChunk = 8;
 constexpr int kBackChunk = 6;
 constexpr unsigned kFusedSpin = 1u << 22;
 constexpr int kPoll = 128;  // completion flags read per poll by a sweep warp
@@ -941,22 +942,22 @@ __device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
   if (!need(0)) return false;
   double prev = __ldcg(col) / g.pd0[Jc];
   if (act) col[0] = prev;
-  double cq[kLineChunk], ci[kLineChunk];
-  if (nx > 1 && !need(min(kLineChunk, nx - 1))) return false;
+  double cq[kForwardChunk], ci[kForwardChunk];
+  if (nx > 1 && !need(min(kForwardChunk, nx - 1))) return false;
 #pragma unroll
-  for (int k = 0; k < kLineChunk; ++k) {
+  for (int k = 0; k < kForwardChunk; ++k) {
     const int e = 1 + k;
     cq[k] = e < nx ? __ldcg(col + (size_t)e * vs) : 0.0;
     ci[k] = e < nx ? __ldg(inv + (size_t)e * jp) : 0.0;
   }
-  // one chunk of rows b .. b+kLineChunk-1; the full chunks run without a
+  // one chunk of rows b .. b+kForwardChunk-1; the full chunks run without a
   // per-row guard inside the recurrence, only the last one needs it
   auto forward_chunk = [&](int b, auto guarded) -> bool {
-    double nq[kLineChunk], ni[kLineChunk];
-    const int nb = b + kLineChunk;
-    if (nb < nx && !need(min(nb + kLineChunk - 1, nx - 1))) return false;
+    double nq[kForwardChunk], ni[kForwardChunk];
+    const int nb = b + kForwardChunk;
+    if (nb < nx && !need(min(nb + kForwardChunk - 1, nx - 1))) return false;
 #pragma unroll
-    for (int k = 0; k < kLineChunk; ++k) {
+    for (int k = 0; k < kForwardChunk; ++k) {
       const int e = nb + k;
       nq[k] = e < nx ? __ldcg(col + (size_t)e * vs) : 0.0;
       ni[k] = e < nx ? __ldg(inv + (size_t)e * jp) : 0.0;
@@ -964,7 +965,7 @@ __device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
     auto rows = [&](auto fast) -> bool {
       Mul<decltype(fast)::value> m;
 #pragma unroll
-      for (int k = 0; k < kLineChunk; ++k) {
+      for (int k = 0; k < kForwardChunk; ++k) {
         const int x = b + k;
         if (!decltype(guarded)::value || x < nx) {
           const double iv = ci[k], c = pl[x];
@@ -986,7 +987,7 @@ __device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
       rows(std::false_type{});
     }
 #pragma unroll
-    for (int k = 0; k < kLineChunk; ++k) {
+    for (int k = 0; k < kForwardChunk; ++k) {
       cq[k] = nq[k];
       ci[k] = ni[k];
     }
@@ -994,7 +995,7 @@ __device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
   };
   int b = 1;
 #pragma unroll 1
-  for (; b + kLineChunk <= nx; b += kLineChunk)
+  for (; b + kForwardChunk <= nx; b += kForwardChunk)
     if (!forward_chunk(b, std::false_type{})) return false;
   if (b < nx && !forward_chunk(b, std::true_type{})) return false;
   // ---- back substitution (src/linalg.c:46-48), x = nx-2 .. 0; span s is
