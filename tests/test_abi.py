@@ -128,3 +128,18 @@ def test_argument_validation_before_any_device_call(native):
     finally:
         lib.sns_param_destroy(p)
         lib.sns_param_destroy(q)
+
+
+def test_batch_case_footprint(native):
+    """sns_batch_case_bytes (host-only): a compensated case also keeps the
+    low words of its three previous right-hand sides, one 256-byte aligned
+    FP32 field each; unsupported sizes report 0"""
+    from simplenavierstokessolver_gb300.batch import Desc, case_bytes
+
+    for nx, ny in ((64, 128), (96, 64), (512, 1024)):
+        plain = case_bytes(Desc(nx, ny))
+        comp = case_bytes(Desc(nx, ny, compensated=True))
+        field = (nx * ny * 4 + 255) // 256 * 256
+        assert plain > 0 and comp - plain == 3 * field, (nx, ny, plain, comp)
+    assert case_bytes(Desc(64, 100)) == 0  # jtot not a power of two
+    assert case_bytes(Desc(40, 128)) == 0  # itot not a multiple of 32
