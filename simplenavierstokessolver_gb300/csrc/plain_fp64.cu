@@ -832,7 +832,7 @@ __global__ void __launch_bounds__(256) k_poisson_bwd(const PoissonArgs a) {
 // written (release: block barrier, fence, store); a sweep warp reads flags
 // with relaxed loads and issues one fence before reading the rows it
 // verified (acquire). bwd_cnt[s] counts the sweep warps that finished span s
-// (span = kFusedSpan x elements), cumulative over launches, so a worker waits
+// (span = 2^span_shift x elements), cumulative over launches, so a worker waits
 // for epoch * lines. Spectrum reads of data written in this launch go
 // through L2 (__ldcg). Every wait polls at most kFusedSpin times; a wait that
 // gives up sets *err and its warp or block stops, so the launch always ends.
@@ -845,7 +845,12 @@ constexpr int kFusedThreads = 512;
 // against 183 us with four), four per block beyond (1024 x 2048, 2048 x 4096).
 constexpr int kFusedTriWarps = 4;
 constexpr int kFusedMinWorkers = 130;
-constexpr int kFusedSpan = 64;
+// x elements per span of the back substitution's signals: 128 when the
+// workers can invert a whole span at once (the last span starts only when the
+// sweeps end), else 64; 512 x 1024: 140.2 us per launch against 143.1 (64)
+// and 148.9 (32). The counters are sized for the smaller span.
+constexpr int kFusedSpanMin = 64;
+constexpr int kFusedSpanShiftMax = 7;
 // elements per chunk of the fused forward elimination and back substitution,
 // measured at 512 x 1024 (launch, CUDA events): forward 8 / 6 / 10 with back
 // 6: 143.1 / 143.9 / 147.3 us; back 6 / 5 / 7 / 8 with forward 8: 143.1 /
@@ -865,6 +870,7 @@ struct FusedArgs {
   unsigned *err;                   // 1: a sweep wait gave up, 2: a worker wait gave up
   unsigned epoch;
   int tri_blocks, tri_warps, lines, groups;
+  int span_shift;                  // span = 2^span_shift x elements
 };
 
 __device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned *p) {
@@ -1005,8 +1011,9 @@ __device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
     __syncwarp();
     if (lane == 0) atomicAdd(a.bwd_cnt + s, 1ull);
   };
-  const int top = (nx - 1) / kFusedSpan;
-  if (top * kFusedSpan > nx - 2) signal(top);  // a top span holding only x = nx-1
+  const int sh = a.span_shift;
+  const int top = (nx - 1) >> sh;
+  if ((top << sh) > nx - 2) signal(top);  // a top span holding only x = nx-1
   double next = prev;
   double bq[kBackChunk], cu[kBackChunk];
   const int hi = nx - 2;
@@ -1035,8 +1042,8 @@ __device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
     }
     // a span whose lowest element this chunk passed is final: signalled once
     // per chunk, after it, instead of a test inside the recurrence
-    const int sb = (b / kFusedSpan) * kFusedSpan;
-    if (sb >= max(b - kBackChunk + 1, 0)) signal(sb / kFusedSpan);
+    const int sb = (b >> sh) << sh;
+    if (sb >= max(b - kBackChunk + 1, 0)) signal(sb >> sh);
 #pragma unroll
     for (int k = 0; k < kBackChunk; ++k) {
       bq[k] = nq[k];
@@ -1096,7 +1103,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_poisson_fused(const FusedA
   for (int k = wk; k < a.groups; k += W) {
     const int gi = a.groups - 1 - k;
     if (threadIdx.x == 0) {
-      const int s = gi * C / kFusedSpan;
+      const int s = (gi * C) >> a.span_shift;
       unsigned spin = 0;
       unsigned long long v;
       while ((v = ld_relaxed_u64(a.bwd_cnt + s)) < target && ++spin < kFusedSpin) {
@@ -1502,7 +1509,7 @@ static int fused_cols(const DevGrid &g) {
 void fused_layout(const DevGrid &g, int *groups, int *spans) {
   const int C = fused_cols(g);
   *groups = (g.nx + C - 1) / C;
-  *spans = (g.nx + kFusedSpan - 1) / kFusedSpan;
+  *spans = (g.nx + kFusedSpanMin - 1) / kFusedSpanMin;
 }
 
 cudaError_t launch_poisson_fused(const DevGrid &g, const StageScalars &s, const double *ux, const double *uy,
@@ -1545,6 +1552,8 @@ cudaError_t launch_poisson_fused(const DevGrid &g, const StageScalars &s, const 
   a.lines = lines;
   int spans = 0;
   fused_layout(g, &a.groups, &spans);
+  // the larger span when the workers can take all of its column groups at once
+  a.span_shift = ((1 << kFusedSpanShiftMax) / C <= sms - tri_blocks) ? kFusedSpanShiftMax : kFusedSpanShiftMax - 1;
   void *args[] = {&a};
   e = cudaLaunchCooperativeKernel(g.rcp ? (const void *)k_poisson_fused<true> : (const void *)k_poisson_fused<false>,
                                   dim3(sms), dim3(kFusedThreads), args, smem, st);
