@@ -332,6 +332,13 @@ extern int sns_profile(const fluid_t *fluid, int enable);
 extern int sns_profile_read(const fluid_t *fluid, double *ms, long long *count, int n);
 extern const char *sns_profile_kind_name(int kind);
 
+/* FP64 issue rate of the current device in Gop/s, no counterpart in the
+ * reference: out[0] additions, out[1] multiplications, each from eight
+ * independent chains per thread on every SM, timed by CUDA events. The plain
+ * FP64 kernels are bound by FP64 issue on GB300; this is the denominator of
+ * their FP64 roofline. Takes a few milliseconds. */
+extern int sns_fp64_issue_rate(double out[2]);
+
 /* message of the last error on this thread ("" if none) */
 extern const char *sns_last_error(void);
 /* number of kernel launches issued by this process so far */

@@ -143,6 +143,7 @@ PROTOTYPES = {
     "sns_profile": (c_int, [PF, c_int]),
     "sns_profile_read": (c_int, [PF, POINTER(c_double), POINTER(c_longlong), c_int]),
     "sns_profile_kind_name": (c_char_p, [c_int]),
+    "sns_fp64_issue_rate": (c_int, [_PD]),
     # include/sns_batch.h
     "sns_batch_create": (c_void_p, [c_size_t, c_int]),
     "sns_batch_destroy": (c_int, [c_void_p]),
@@ -201,3 +202,11 @@ class SnsError(RuntimeError):
 def check(code: int, what: str) -> None:
     if code != SNS_OK:
         raise SnsError(code, what)
+
+
+def fp64_issue_rate() -> dict:
+    """FP64 additions and multiplications per second of the current device
+    (sns_fp64_issue_rate), in Gop/s"""
+    out = (c_double * 2)()
+    check(lib().sns_fp64_issue_rate(out), "sns_fp64_issue_rate")
+    return {"dadd_gops": out[0], "dmul_gops": out[1]}

@@ -38,6 +38,7 @@ UNITS = {
     "plain_fp64.cu": ["--fmad=false"],
     "batch_fp32.cu": [],
     "diagnostics.cu": [],
+    "fp64_rate.cu": [],
     "sns_api.cpp": [],
     "batch_api.cpp": [],
     "npy.cpp": [],

@@ -187,6 +187,8 @@ enum KernelKind {
 
 // counts kernel launches (process-wide)
 void count_launches(long long n);
+// message returned by sns_last_error on this thread
+void record_error(const char *msg);
 // predicted seconds per RK substage, out[implicity][implicitx] (cost_model.cpp)
 void cost_model(int nx, int ny, int sms, double clock_hz, bool with_t, double out[2][2]);
 
