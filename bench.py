@@ -49,6 +49,9 @@ KERNEL_MODEL = {
     "velocity_update_p2": (80.0, 52.0),
     "poisson_forward_fft": (24.0, None),
     "poisson_tridiagonal": (40.0, 5.0),
+    # partition-method solve of the parallel form: the spectrum read and
+    # written once (its RHS-independent factor blocks stay in L2)
+    "poisson_pcr": (16.0, None),
     "poisson_inverse_fft": (16.0, None),
     "correct_and_pressure": (56.0, 9.0),
     "max_velocity": (16.0, 0.0),
@@ -639,6 +642,14 @@ def gpu_arm(args, world, rank, local):
 
     lib = N.lib()
     case = Case(args.nx, args.ny, ly=2.0, Ra=args.Ra, Pr=args.Pr)
+    # the headline's arithmetic form: the parallel form (within 1e-12 of the
+    # oracle after the stated step counts) where the grid supports it
+    form = args.form
+    if form == "parallel":
+        try:
+            case.set_form(True)
+        except N.SnsError:
+            form = "exact"
     stream = torch.cuda.ExternalStream(case.stream())
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     cells = args.nx * args.ny
@@ -719,16 +730,67 @@ def gpu_arm(args, world, rank, local):
     if opc:
         ach = opc * cells / avg_s / 1e9
         fp64 = {"kernel": dom, "achieved": ach, "peak": fp64_peak, "unit": "Gop/s (FP64 instructions)",
-                "frac": ach / fp64_peak, "ops_per_cell": opc, "peak_source": fp64_source}
+                "frac": ach / fp64_peak, "ops_per_cell": opc, "peak_source": fp64_source,
+                "ops_counted_for": "the exact form (the parallel form's contracted kernels issue fewer)"}
     # the whole explicit step against the FP64 issue rate: FP64 operations per
     # cell-step from the kernels' counts (3 substages of temperature, velocity,
     # forward DFT, sweep, inverse DFT and correction)
+    # (counted for the exact form; the parallel form's contracted kernels
+    # issue fewer FP64 instructions than these counts)
     ops_step = 3 * (KERNEL_MODEL["temperature_update"][1] + KERNEL_MODEL[vel_model][1] +
                     fft_ops_per_cell(args.ny, True) + KERNEL_MODEL["poisson_tridiagonal"][1] +
                     fft_ops_per_cell(args.ny, False) + KERNEL_MODEL["correct_and_pressure"][1])
-    step_fp64 = {"ops_per_cell_step": ops_step, "achieved": value * ops_step / 1e9, "peak": fp64_peak,
+    step_fp64 = {"form": form, "ops_per_cell_step": ops_step, "achieved": value * ops_step / 1e9, "peak": fp64_peak,
                  "unit": "Gop/s (FP64 instructions)", "frac": value * ops_step / 1e9 / fp64_peak,
                  "peak_source": fp64_source}
+
+    # ---- the same workload in the other arithmetic form, same protocol
+    other_form = "exact" if form == "parallel" else "parallel"
+    other = None
+    with Case(args.nx, args.ny, ly=2.0, Ra=args.Ra, Pr=args.Pr) as pc:
+        try:
+            pc.set_form(other_form == "parallel")
+        except N.SnsError as err:
+            other = {"unavailable": str(err)}
+        if other is None:
+            pstream = torch.cuda.ExternalStream(pc.stream())
+            for _ in range(args.warmup):
+                pc.run(1)
+                with torch.cuda.stream(pstream):
+                    flush.zero_()
+            torch.cuda.synchronize()
+            pev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                   for _ in range(args.steps)]
+            for a, b in pev:
+                a.record(pstream)
+                pc.run(1)
+                b.record(pstream)
+                with torch.cuda.stream(pstream):
+                    flush.zero_()
+            torch.cuda.synchronize()
+            pms = max_over_ranks(sum(a.elapsed_time(b) for a, b in pev), world)
+            lib.sns_profile(pc.fluid, 1)
+            for _ in range(args.steps):
+                pc.run(1)
+                with torch.cuda.stream(pstream):
+                    flush.zero_()
+            pkms = (N.c_double * kinds)()
+            pkcnt = (N.c_longlong * kinds)()
+            pnk = lib.sns_profile_read(pc.fluid, pkms, pkcnt, kinds)
+            lib.sns_profile(pc.fluid, 0)
+            ptot = sum(pkms[k] for k in range(pnk))
+            pkern = {lib.sns_profile_kind_name(k).decode(): {"launches": int(pkcnt[k]),
+                                                             "avg_us": 1e3 * pkms[k] / pkcnt[k],
+                                                             "share": pkms[k] / ptot if ptot else None}
+                     for k in range(pnk) if pkcnt[k]}
+            other = {"form": other_form, "value": cells * args.steps * world / (pms * 1e-3), "unit": "cell-steps/s",
+                     "ms_per_step": pms / args.steps, "headline_speedup_over_this": pms / ms, "kernels": pkern}
+    forms = {"headline": form, "other": other,
+             "exact": "every operation of the reference in its order, Thomas recurrence: identical to the oracle "
+                      "bit for bit (tests/test_gpu_long_parity.py)",
+             "parallel": "Poisson lines by the partition method + warp-shuffle PCR, FMA-contracted kernels: within "
+                         "1e-12 relative L2 of the oracle per field after 1000 / 2000 steps "
+                         "(tests/test_gpu_parallel_form.py)"}
 
     # ---- end to end through the C ABI with host buffers
     # each step: host arrays -> device, one time step (param_decide_dt + the 3
@@ -814,8 +876,9 @@ def gpu_arm(args, world, rank, local):
             "metric": METRIC, "value": value, "unit": "cell-steps/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (reference initial condition, srand(0))", "config": workload_config(args),
-            "roofline": roofline, "fp64_roofline": fp64, "step_fp64_roofline": step_fp64, "kernels": kernels, "cpu_baseline": cpu, "e2e": e2e,
+            "data": "synthetic (reference initial condition, srand(0))", "config": dict(workload_config(args), form=form),
+            "roofline": roofline, "fp64_roofline": fp64, "step_fp64_roofline": step_fp64, "kernels": kernels,
+            "forms": forms, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(launches), "clocks": clk,
         }
         line.update(extra)
@@ -836,6 +899,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--plain-only", action="store_true", help="skip the FP32-stencil, ensemble and serving parts")
+    ap.add_argument("--form", default="parallel", choices=["parallel", "exact"],
+                    help="arithmetic form of the headline plain FP64 step (sns_set_form)")
     ap.add_argument("--acc-steps", type=int, default=2000, help="steps of the FP32-vs-FP64 accuracy run")
     ap.add_argument("--ens-steps", type=int, default=50)
     ap.add_argument("--ens-acc-steps", type=int, default=500, help="steps of the ensemble FP32-vs-FP64 accuracy run")

@@ -322,6 +322,40 @@ extern int sns_npy_read(const char *path, const char *dtype, int ndim, const siz
  * by themselves. */
 extern int sns_set_fused(const fluid_t *fluid, int on);
 
+/* Arithmetic form of the plain path; no counterpart in the reference.
+ * SNS_FORM_EXACT (default): every operation of the reference in its order,
+ * without contraction, the Poisson lines by the reference's Thomas
+ * recurrence (src/fluid/compute_potential.c:109-136, src/linalg.c:32-50):
+ * results identical to the reference's bit for bit. On GB300 the
+ * recurrence's serial chain of dependent FP64 operations sets the step's
+ * critical path.
+ * SNS_FORM_PARALLEL: the Poisson lines by the partition method with
+ * warp-shuffle parallel cyclic reduction (one warp per Fourier mode, one lane
+ * per segment of itot/32 rows), and every kernel compiled with fused
+ * multiply-adds (fewer FP64 instructions, shorter Crank-Nicolson chains).
+ * Results differ from the reference's by rounding, held to 1e-12 relative L2
+ * per field after the stated step counts. Needs itot a multiple of 32 in
+ * [64, 3968] and a grid on which the mean mode's last Thomas pivot vanishes
+ * (uniform grids), otherwise SNS_ERR_UNSUPPORTED and the form is unchanged.
+ * The first switch to it computes the factors (host, O(itot * jtot)) and
+ * allocates them on the device. */
+#define SNS_FORM_EXACT 0
+#define SNS_FORM_PARALLEL 1
+extern int sns_set_form(const fluid_t *fluid, int form);
+/* the current form, or -1 for a foreign structure */
+extern int sns_get_form(const fluid_t *fluid);
+
+/* Bounded device waits, no counterpart in the reference. The fused Poisson
+ * launch (SNS_FORM_EXACT) polls completion flags written by other blocks
+ * of the same launch, and the partition-method launch (SNS_FORM_PARALLEL) waits for its
+ * bulk copies; every such wait gives up after `polls` polls (0: the default,
+ * about a second), sets an error word, and the next synchronising call of
+ * this solver returns SNS_ERR_STATE (the fused form is then switched off for
+ * this solver, see sns_set_fused). stale != 0 makes the next launch wait for
+ * a flag that nothing sets (fused form) or issue no copy (parallel form), so
+ * that its wait runs out: a test of the error path that faults nothing. */
+extern int sns_set_wait_limit(const fluid_t *fluid, unsigned polls, int stale);
+
 /* per-kernel device time: with profiling enabled every kernel launched for
  * this solver is bracketed by CUDA events on its stream. sns_profile(f, 1)
  * resets the totals and starts, sns_profile(f, 0) stops. sns_profile_read

@@ -21,6 +21,9 @@ SNS_ERR_CUDA = 3
 SNS_ERR_OOM = 4
 SNS_ERR_STATE = 5
 
+SNS_FORM_EXACT = 0
+SNS_FORM_PARALLEL = 1
+
 _PD = POINTER(c_double)
 
 
@@ -128,6 +131,9 @@ PROTOTYPES = {
     "sns_diagnostics_static": (c_int, [PP, PF, PT, _PD]),
     "param_estimate_cost": (c_int, [PP, PL]),
     "sns_set_fused": (c_int, [PF, c_int]),
+    "sns_set_form": (c_int, [PF, c_int]),
+    "sns_get_form": (c_int, [PF]),
+    "sns_set_wait_limit": (c_int, [PF, ctypes.c_uint, c_int]),
     "sns_cost_model": (c_int, [c_int, c_int, c_int, c_double, c_int, _PD]),
     "sns_measure_cost": (c_int, [PP, PL, c_int, _PD]),
     "statistics_init": (PS, [PP, PL]),

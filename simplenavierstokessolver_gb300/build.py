@@ -36,9 +36,12 @@ def cuda_home() -> str:
 # translation unit -> extra flags. fmad=false: bit-identical FP64 path.
 UNITS = {
     "plain_fp64.cu": ["--fmad=false"],
+    # the same kernels with contraction (the parallel form)
+    "plain_fp64_contract.cu": ["--fmad=true"],
     "batch_fp32.cu": [],
     "diagnostics.cu": [],
     "fp64_rate.cu": [],
+    "plain_parallel.cu": [],
     "sns_api.cpp": [],
     "batch_api.cpp": [],
     "npy.cpp": [],
@@ -46,9 +49,13 @@ UNITS = {
 }
 
 
+# units that include another unit's source
+INCLUDES = {"plain_fp64_contract.cu": ["plain_fp64.cu"]}
+
+
 def _headers():
     hs = [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE) if f.endswith(".h")]
-    hs += [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
+    hs += [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh", ".inc"))]
     return hs
 
 
@@ -62,7 +69,9 @@ def _stale(target: str, deps: list[str]) -> bool:
 def _compile(unit: str, extra: list[str], cuda: str) -> str:
     src = os.path.join(CSRC, unit)
     obj = os.path.join(BUILD, unit + ".o")
-    if not _stale(obj, [src, __file__] + _headers()):
+    # a unit that includes another .cu rebuilds with it
+    deps = [src, __file__] + _headers() + [os.path.join(CSRC, u) for u in INCLUDES.get(unit, [])]
+    if not _stale(obj, deps):
         return obj
     nvcc = os.path.join(cuda, "bin", "nvcc")
     if unit.endswith(".cu"):

@@ -29,6 +29,8 @@
 
 namespace sns {
 
+static_assert(kSeg == kPartSeg && kPcrLevels == kPartLevels, "one partition layout for both forms");
+
 static int bfail(int code, const char *fmt, ...) {
   char buf[512];
   va_list ap;
@@ -159,81 +161,6 @@ static void initial_temperature(const sns_case_desc *d, const double *xc, double
     temp[i] = temp[(size_t)ny * (nx + 2) + i];
     temp[(size_t)(ny + 1) * (nx + 2) + i] = temp[(size_t)(nx + 2) + i];
   }
-}
-
-// Partition-method factors of the per-mode Poisson lines (see batch_fp32.cu):
-// rows i = 0..n-1, sub-diagonal a_i (a_0 = 0), super-diagonal c_i
-// (c_{n-1} = 0), diagonal d_i = -a_i - c_i + eig with the reference's Neumann
-// closure (src/fluid/compute_potential.c:116-127).
-static void mode_factors(int n, const double *a, const double *c, const double *l_raw, const double *u_raw, double eig,
-                         bool pin_last, double *out) {
-  const int m = n / kSeg;
-  std::vector<double> d(n);
-  for (int i = 0; i < n; i++) d[i] = -l_raw[i] - u_raw[i] + eig;
-  d[0] += l_raw[0];
-  d[n - 1] += u_raw[n - 1];
-  double *inv = out, *up = out + n, *v = out + 2 * n, *w = out + 3 * n;
-  double *alpha = out + 4 * n, *beta = alpha + kPcrLevels * kSeg, *rD = beta + kPcrLevels * kSeg;
-  std::fill(out, out + 4 * n, 0.0);
-  std::vector<double> L(kSeg), D(kSeg), U(kSeg);
-  for (int k = 0; k < kSeg; k++) {
-    const int s = k * m, e = s + m - 1;
-    // interior block rows s..e-1
-    inv[s] = 1.0 / d[s];
-    up[s] = c[s] * inv[s];
-    for (int i = s + 1; i < e; i++) {
-      inv[i] = 1.0 / (d[i] - a[i] * up[i - 1]);
-      up[i] = c[i] * inv[i];
-    }
-    auto solve = [&](std::vector<double> &r) {  // r over rows s..e-1 (index i - s)
-      r[0] *= inv[s];
-      for (int i = s + 1; i < e; i++) r[i - s] = inv[i] * (r[i - s] - a[i] * r[i - s - 1]);
-      for (int i = e - 2; i >= s; i--) r[i - s] -= up[i] * r[i - s + 1];
-    };
-    std::vector<double> rv(m - 1, 0.0), rw(m - 1, 0.0);
-    rv[0] = -a[s];
-    rw[m - 2] = -c[e - 1];
-    solve(rv);
-    solve(rw);
-    for (int i = s; i < e; i++) {
-      v[i] = rv[i - s];
-      w[i] = rw[i - s];
-    }
-  }
-  for (int k = 0; k < kSeg; k++) {
-    const int s = k * m, e = s + m - 1;
-    const double ae = a[e], ce = c[e];
-    L[k] = ae * v[e - 1];
-    D[k] = ae * w[e - 1] + d[e];
-    U[k] = 0.0;
-    if (k < kSeg - 1) {
-      const int s1 = s + m;
-      D[k] += ce * v[s1];
-      U[k] = ce * w[s1];
-    }
-  }
-  if (pin_last) {  // singular mean mode: x_{n-1} = 0 (the reference's zero last pivot)
-    L[kSeg - 1] = 0.0;
-    D[kSeg - 1] = 1.0;
-    U[kSeg - 1] = 0.0;
-  }
-  for (int lev = 0; lev < kPcrLevels; lev++) {
-    const int dd = 1 << lev;
-    std::vector<double> L2(kSeg), D2(kSeg), U2(kSeg);
-    for (int k = 0; k < kSeg; k++) {
-      const double al = k - dd >= 0 ? -L[k] / D[k - dd] : 0.0;
-      const double be = k + dd < kSeg ? -U[k] / D[k + dd] : 0.0;
-      alpha[lev * kSeg + k] = al;
-      beta[lev * kSeg + k] = be;
-      L2[k] = k - dd >= 0 ? al * L[k - dd] : 0.0;
-      U2[k] = k + dd < kSeg ? be * U[k + dd] : 0.0;
-      D2[k] = D[k] + (k - dd >= 0 ? al * U[k - dd] : 0.0) + (k + dd < kSeg ? be * L[k + dd] : 0.0);
-    }
-    L = L2;
-    D = D2;
-    U = U2;
-  }
-  for (int k = 0; k < kSeg; k++) rD[k] = 1.0 / D[k];
 }
 
 struct CaseHost {
@@ -552,8 +479,8 @@ static int admit(sns_batch *b, const sns_case_desc *d, const double *temp_init, 
   }
   std::vector<double> pfac(L.pstride * nh);
   for (int J = 0; J < nh; J++)
-    mode_factors(nx, lo.data(), hi.data(), l_raw.data(), u_raw.data(), poisson_eigenvalue(dy, ny, J), J == 0,
-                 pfac.data() + L.pstride * J);
+    partition_factors(nx, lo.data(), hi.data(), l_raw.data(), u_raw.data(), poisson_eigenvalue(dy, ny, J), J == 0,
+                      false, pfac.data() + L.pstride * J);
   const std::vector<double> tw = twiddle_table(ny);
   std::vector<double> temp((size_t)(nx + 2) * (ny + 2));
   if (st) temp_init = st->temp;

@@ -99,6 +99,109 @@ inline double poisson_eigenvalue(double dy, int jtot, int J) {
   return -4. / pow(dy, 2.) * pow(sin(kPiRef * (J) / (1. * jtot)), 2.);
 }
 
+// ------------------------------------------------ partition method (PCR)
+// A tridiagonal line of n rows is split into kPartSeg segments of m = n /
+// kPartSeg rows, one per lane of a warp. Row e = k m + m - 1, the last of
+// segment k, is its interface unknown; the m - 1 rows before it are the
+// segment's interior. With the interface values known, an interior is the
+// solution y of its own block (zero boundary values) plus multiples of two
+// spikes: x_i = y_i + v_i x_{e(k-1)} + w_i x_{e(k)}. Substituting into the
+// interface rows gives a tridiagonal system of kPartSeg unknowns, solved by
+// parallel cyclic reduction in kPartLevels levels of warp shuffles.
+// Everything here is independent of the right-hand side and computed once.
+constexpr int kPartSeg = 32;
+constexpr int kPartLevels = 5;  // log2(kPartSeg)
+
+// doubles per line of the factor block written by partition_factors
+inline size_t partition_stride(int n) { return 4 * (size_t)n + 2 * kPartLevels * kPartSeg + kPartSeg; }
+
+// Factors of one line: sub-diagonal a_i (a_0 = 0), super-diagonal c_i
+// (c_{n-1} = 0), diagonal d_i = -l_raw_i - u_raw_i + eig with the Poisson
+// lines' Neumann closure (src/fluid/compute_potential.c:116-127: the first
+// and last diagonal entries absorb l_raw_0 and u_raw_{n-1}). pin_last: the
+// singular mean mode, whose last unknown the reference's Thomas solve sets
+// to zero (its last pivot vanishes, src/linalg.c:36-38). Output (doubles):
+// inv[n] up[n] v[n] w[n] (interior Thomas factors and spikes by row)
+// alpha[kPartLevels][kPartSeg] beta[kPartLevels][kPartSeg] rD[kPartSeg].
+// interleave: the four row arrays hold row k m + r at index r kPartSeg + k,
+// so that the 32 lanes, each walking its own segment, touch 32 consecutive
+// words at every step.
+inline void partition_factors(int n, const double *a, const double *c, const double *l_raw, const double *u_raw,
+                              double eig, bool pin_last, bool interleave, double *out) {
+  const int m = n / kPartSeg;
+  std::vector<double> d(n), inv(n, 0.0), up(n, 0.0), v(n, 0.0), w(n, 0.0);
+  for (int i = 0; i < n; i++) d[i] = -l_raw[i] - u_raw[i] + eig;
+  d[0] += l_raw[0];
+  d[n - 1] += u_raw[n - 1];
+  double *alpha = out + 4 * (size_t)n, *beta = alpha + kPartLevels * kPartSeg, *rD = beta + kPartLevels * kPartSeg;
+  std::vector<double> L(kPartSeg), D(kPartSeg), U(kPartSeg);
+  for (int k = 0; k < kPartSeg; k++) {
+    const int s = k * m, e = s + m - 1;
+    // interior block rows s..e-1
+    inv[s] = 1.0 / d[s];
+    up[s] = c[s] * inv[s];
+    for (int i = s + 1; i < e; i++) {
+      inv[i] = 1.0 / (d[i] - a[i] * up[i - 1]);
+      up[i] = c[i] * inv[i];
+    }
+    auto solve = [&](std::vector<double> &r) {  // r over rows s..e-1 (index i - s)
+      r[0] *= inv[s];
+      for (int i = s + 1; i < e; i++) r[i - s] = inv[i] * (r[i - s] - a[i] * r[i - s - 1]);
+      for (int i = e - 2; i >= s; i--) r[i - s] -= up[i] * r[i - s + 1];
+    };
+    std::vector<double> rv(m - 1, 0.0), rw(m - 1, 0.0);
+    rv[0] = -a[s];
+    rw[m - 2] = -c[e - 1];
+    solve(rv);
+    solve(rw);
+    for (int i = s; i < e; i++) {
+      v[i] = rv[i - s];
+      w[i] = rw[i - s];
+    }
+  }
+  for (int k = 0; k < kPartSeg; k++) {
+    const int s = k * m, e = s + m - 1;
+    const double ae = a[e], ce = c[e];
+    L[k] = ae * v[e - 1];
+    D[k] = ae * w[e - 1] + d[e];
+    U[k] = 0.0;
+    if (k < kPartSeg - 1) {
+      const int s1 = s + m;
+      D[k] += ce * v[s1];
+      U[k] = ce * w[s1];
+    }
+  }
+  if (pin_last) {
+    L[kPartSeg - 1] = 0.0;
+    D[kPartSeg - 1] = 1.0;
+    U[kPartSeg - 1] = 0.0;
+  }
+  for (int lev = 0; lev < kPartLevels; lev++) {
+    const int dd = 1 << lev;
+    std::vector<double> L2(kPartSeg), D2(kPartSeg), U2(kPartSeg);
+    for (int k = 0; k < kPartSeg; k++) {
+      const double al = k - dd >= 0 ? -L[k] / D[k - dd] : 0.0;
+      const double be = k + dd < kPartSeg ? -U[k] / D[k + dd] : 0.0;
+      alpha[lev * kPartSeg + k] = al;
+      beta[lev * kPartSeg + k] = be;
+      L2[k] = k - dd >= 0 ? al * L[k - dd] : 0.0;
+      U2[k] = k + dd < kPartSeg ? be * U[k + dd] : 0.0;
+      D2[k] = D[k] + (k - dd >= 0 ? al * U[k - dd] : 0.0) + (k + dd < kPartSeg ? be * L[k + dd] : 0.0);
+    }
+    L = L2;
+    D = D2;
+    U = U2;
+  }
+  for (int k = 0; k < kPartSeg; k++) rD[k] = 1.0 / D[k];
+  for (int i = 0; i < n; i++) {
+    const size_t o = interleave ? (size_t)(i % m) * kPartSeg + i / m : (size_t)i;
+    out[o] = inv[i];
+    out[n + o] = up[i];
+    out[2 * (size_t)n + o] = v[i];
+    out[3 * (size_t)n + o] = w[i];
+  }
+}
+
 // stage layout of the length-jtot/2 complex FFT: radix 2 first when
 // log2(jtot/2) is odd, then radix 4
 inline void fft_layout(int jtot, int *nst, int *first2) {

@@ -20,7 +20,20 @@
 #include "fft_dev.cuh"
 #include "sns_internal.h"
 
+// plain_fp64_contract.cu compiles this file a second time, with fused
+// multiply-add contraction, into namespace sns::contract (the parallel form)
+#ifdef SNS_PLAIN_CONTRACT
+#define SNS_PLAIN_FORM contract
+#else
+#define SNS_PLAIN_FORM exact
+#endif
+
 namespace sns {
+#ifdef SNS_PLAIN_CONTRACT
+namespace contract {
+#else
+inline namespace exact {
+#endif
 namespace {
 
 template <bool RCP>
@@ -834,8 +847,9 @@ __global__ void __launch_bounds__(256) k_poisson_bwd(const PoissonArgs a) {
 // verified (acquire). bwd_cnt[s] counts the sweep warps that finished span s
 // (span = 2^span_shift x elements), cumulative over launches, so a worker waits
 // for epoch * lines. Spectrum reads of data written in this launch go
-// through L2 (__ldcg). Every wait polls at most kFusedSpin times; a wait that
-// gives up sets *err and its warp or block stops, so the launch always ends.
+// through L2 (__ldcg). Every wait polls at most `spin` times (kFusedSpin by
+// default, about a second; the host may set fewer); a wait that gives up sets
+// *err and its warp or block stops, so the launch always ends.
 constexpr int kFusedThreads = 512;
 // sweep warps per block, one per SM sub-partition. Dependent FP64 chains run
 // ~20% slower with four warps on one SM than with one, but every SM given to
@@ -871,6 +885,8 @@ struct FusedArgs {
   unsigned epoch;
   int tri_blocks, tri_warps, lines, groups;
   int span_shift;                  // span = 2^span_shift x elements
+  unsigned spin;                   // polls of a wait before it gives up
+  unsigned want;                   // the flag value a sweep waits for: epoch (epoch + 1 in tests of the waits)
 };
 
 __device__ __forceinline__ unsigned ld_relaxed_u32(const unsigned *p) {
@@ -920,7 +936,7 @@ __device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
 #pragma unroll
       for (int i = 0; i < kPoll / 32; ++i) {
         const int gi = vg + 32 * i + lane;
-        ok[i] = gi >= a.groups || ld_relaxed_u32(a.fwd_done + gi) == a.epoch;
+        ok[i] = gi >= a.groups || ld_relaxed_u32(a.fwd_done + gi) == a.want;
       }
       int run = kPoll;
 #pragma unroll
@@ -931,7 +947,7 @@ __device__ bool fused_sweep(const FusedArgs &a, const double *pl, int lg) {
       vg = min(vg + run, a.groups);
       // the warp owns its SM's FP64 work alone: poll back to back (each
       // poll is an L2 round trip; a sleep between them delayed the start)
-      if (vg <= gx && ++spin >= kFusedSpin) return false;
+      if (vg <= gx && ++spin >= a.spin) return false;
     }
     ready = min(vg * C, nx);
     __threadfence();
@@ -1106,7 +1122,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1) k_poisson_fused(const FusedA
       const int s = (gi * C) >> a.span_shift;
       unsigned spin = 0;
       unsigned long long v;
-      while ((v = ld_relaxed_u64(a.bwd_cnt + s)) < target && ++spin < kFusedSpin) {
+      while ((v = ld_relaxed_u64(a.bwd_cnt + s)) < target && ++spin < a.spin) {
       }
       s_ok = v >= target;
       if (!s_ok) atomicOr(a.err, 2u);
@@ -1369,7 +1385,7 @@ cudaError_t launch_solve_x(const DevGrid &g, const LineFactors &f, int mode, dou
   set.mode[0] = mode;
   set.q[0] = q;
   set.n = 1;
-  return launch_solve_x_set(g, set, st);
+  return SNS_PLAIN_FORM::launch_solve_x_set(g, set, st);
 }
 
 cudaError_t launch_solve_y(const DevGrid &g, const PeriodicFactors &f, int first_col, double *q, cudaStream_t st) {
@@ -1378,7 +1394,7 @@ cudaError_t launch_solve_y(const DevGrid &g, const PeriodicFactors &f, int first
   set.first_col[0] = first_col;
   set.q[0] = q;
   set.n = 1;
-  return launch_solve_y_set(g, set, st);
+  return SNS_PLAIN_FORM::launch_solve_y_set(g, set, st);
 }
 
 cudaError_t launch_add_increment(const DevGrid &g, int kind, const double *in, const double *q, double *out,
@@ -1547,11 +1563,14 @@ cudaError_t launch_poisson_fused(const DevGrid &g, const StageScalars &s, const 
   a.bwd_cnt = fs.bwd_cnt;
   a.err = fs.err;
   a.epoch = ++fs.epoch;
+  a.spin = fs.spin_limit ? fs.spin_limit : kFusedSpin;
+  a.want = a.epoch + (fs.stale ? 1u : 0u);
+  fs.stale = 0;  // a test's stale wait applies to one launch
   a.tri_blocks = tri_blocks;
   a.tri_warps = tri_warps;
   a.lines = lines;
   int spans = 0;
-  fused_layout(g, &a.groups, &spans);
+  SNS_PLAIN_FORM::fused_layout(g, &a.groups, &spans);
   // the larger span when the workers can take all of its column groups at once
   a.span_shift = ((1 << kFusedSpanShiftMax) / C <= sms - tri_blocks) ? kFusedSpanShiftMax : kFusedSpanShiftMax - 1;
   void *args[] = {&a};
@@ -1622,4 +1641,5 @@ cudaError_t launch_umax(const DevGrid &g, const double *ux, const double *uy, un
   return cudaGetLastError();
 }
 
+}  // namespace SNS_PLAIN_FORM
 }  // namespace sns

@@ -1,0 +1,321 @@
+// Parallel tridiagonal form of the plain FP64 Poisson solve on GB300.
+//
+// The reference solves each Fourier mode's x-line with a serial Thomas
+// recurrence (src/fluid/compute_potential.c:109-136, src/linalg.c:32-50).
+// Reproduced bit for bit, that recurrence is a chain of 3 + 2 dependent FP64
+// operations per x, which on GB300 (~70 cycles per dependent FP64 operation)
+// bounds the plain step no matter how many lines run side by side. This
+// form solves the same lines by the partition method with warp-shuffle
+// parallel cyclic reduction (PCR): one warp per mode, one lane per segment of
+// nx/32 rows, a 32-unknown interface system reduced in 5 shuffle levels. All
+// RHS-independent factors (interior Thomas factors, spikes, PCR coefficients)
+// are computed once on the host. Its results differ from the Thomas
+// recurrence by rounding only, so the form is held to the path's tolerance
+// (1e-12 relative L2 per field after the stated step counts) rather than to
+// bit identity, and this unit is compiled with floating-point contraction.
+//
+// Layout: the spectrum is mode-major, spec[J * nx + p], with the rows of a
+// mode line in the interleaved order p = (x % m) * 32 + x / m (m = nx / 32):
+// lane k walks segment k, and at every step the 32 lanes touch 32
+// consecutive elements, in global and in shared memory alike. The forward
+// and inverse DFTs (the same FFT as the Thomas form) write and read that
+// order.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "fft_dev.cuh"
+#include "host_common.h"
+#include "sns_gpu.h"
+#include "sns_internal.h"
+
+namespace sns {
+namespace {
+
+constexpr int kParWarpsMax = 4;  // mode lines per block of the PCR kernel
+constexpr size_t kParSmemMax = 220 * 1024;
+
+struct ParArgs {
+  DevGrid g;
+  StageScalars s;
+  const double *ux, *uy;
+  double2 *spec;  // [nh][nx], interleaved rows
+  double *psi;
+  int cols;       // line positions per block of the DFT kernels
+  int m;          // rows per segment, nx / 32
+};
+
+// x of line position p (p = (x % m) * 32 + x / m)
+__device__ __forceinline__ int par_x(int p, int m) { return (p % kPartSeg) * m + p / kPartSeg; }
+
+// src/fluid/compute_potential.c:69-92: (div u*)/(gamma dt) and its real DFT
+// along y, for the columns at line positions p0 .. p0+cols-1
+__global__ void __launch_bounds__(256) k_par_fwd(const ParArgs a) {
+  extern __shared__ double2 z[];
+  const int nx = a.g.nx, ny = a.g.ny, M = ny / 2, C = a.cols;
+  const int p0 = blockIdx.x * C;
+  double *zd = reinterpret_cast<double *>(z);
+  const double rdy = a.g.rdy, rgdt = a.s.rgdt;
+  for (int e = threadIdx.x; e < C * ny; e += blockDim.x) {
+    const int c = e % C, y = e / C, p = p0 + c;
+    double d = 0.0;
+    if (p < nx) {
+      const int x = par_x(p, a.m);
+      const size_t r = (size_t)y * nx + x;
+      const double uxm = a.ux[r];
+      const double uxp = x == nx - 1 ? 0.0 : a.ux[r + 1];
+      const double uym = a.uy[r];
+      const double uyp = a.uy[(size_t)(y + 1 == ny ? 0 : y + 1) * nx + x];
+      d = rgdt * ((uxp - uxm) * a.g.rdxf[x] + (uyp - uym) * rdy);
+    }
+    zd[2 * (c * M + fft::fft_slot(y >> 1, M, a.g.fft_nst, a.g.fft_first2)) + (y & 1)] = d;
+  }
+  __syncthreads();
+  const double2 *tw = reinterpret_cast<const double2 *>(a.g.tw);
+  fft::fft_stages<true>(z, C, M, ny, a.g.fft_nst, a.g.fft_first2, tw);
+  const int half = M / 2 + 1;
+  for (int e = threadIdx.x; e < C * half; e += blockDim.x) {
+    const int c = e % C, k = e / C, p = p0 + c;
+    if (p < nx) fft::rfft_post(z + c * M, a.spec + p, M, k, tw, (size_t)nx);
+  }
+}
+
+// src/fluid/compute_potential.c:146-157: inverse real DFT and 1/jtot
+__global__ void __launch_bounds__(256) k_par_bwd(const ParArgs a) {
+  extern __shared__ double2 z[];
+  const int nx = a.g.nx, ny = a.g.ny, M = ny / 2, C = a.cols;
+  const int p0 = blockIdx.x * C;
+  const double2 *tw = reinterpret_cast<const double2 *>(a.g.tw);
+  const int half = M / 2 + 1;
+  for (int e = threadIdx.x; e < C * half; e += blockDim.x) {
+    const int c = e % C, k = e / C, p = p0 + c;
+    double2 *zc = z + c * M;
+    if (p >= nx) {
+      zc[fft::fft_slot(k, M, a.g.fft_nst, a.g.fft_first2)] = make_double2(0.0, 0.0);
+      if (k > 0) zc[fft::fft_slot(M - k, M, a.g.fft_nst, a.g.fft_first2)] = make_double2(0.0, 0.0);
+      continue;
+    }
+    fft::rfft_pre(a.spec + p, zc, M, k, tw, a.g.fft_nst, a.g.fft_first2, (size_t)nx);
+  }
+  __syncthreads();
+  fft::fft_stages<false>(z, C, M, ny, a.g.fft_nst, a.g.fft_first2, tw);
+  const double *zd = reinterpret_cast<const double *>(z);
+  for (int e = threadIdx.x; e < C * ny; e += blockDim.x) {
+    const int c = e % C, y = e / C, p = p0 + c;
+    if (p >= nx) continue;
+    a.psi[(size_t)y * nx + par_x(p, a.m)] = zd[2 * (c * M + (y >> 1)) + (y & 1)] * a.s.rny;
+  }
+}
+
+struct ParTriArgs {
+  double2 *spec;       // [nh][nx], interleaved rows
+  const double *fac;   // [nh][stride]: inv g up v w (interleaved rows, g = a inv), alpha, beta, rD
+  const double *lo;    // [nx] sub-diagonal a_i, interleaved rows (a_0 = 0)
+  const double *hi;    // [nx] super-diagonal c_i, interleaved rows (c_{nx-1} = 0)
+  size_t stride;       // doubles per mode in fac
+  int nx, nh, m;
+  unsigned *err;       // set to 1 when a copy wait gave up (the line is then left unsolved)
+  unsigned spin_limit; // polls of a copy wait before it gives up
+  int stale;           // test of the bounded wait: issue no copy, so the wait runs out
+};
+
+// polls of the wait that lets a warp's copies land after its first wait gave
+// up, so that no copy into the warp's shared memory outlives the warp
+constexpr unsigned kParDrainSpins = 1u << 22;
+
+__device__ __forceinline__ bool mbar_try(unsigned bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+// src/fluid/compute_potential.c:109-136 by the partition method: one warp per
+// mode line. The warp's lane 0 moves the line (16 nx bytes) and its factor
+// block into shared memory with two bulk asynchronous copies (completion on
+// an mbarrier, bounded wait), the warp solves there and writes the line back
+// with coalesced stores. Real and imaginary parts see the same real matrix.
+__global__ void __launch_bounds__(32 * kParWarpsMax) k_par_tri(const ParTriArgs a) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int J = blockIdx.x * (blockDim.x >> 5) + w;
+  if (J >= a.nh) return;  // the whole warp
+  const int n = a.nx, m = a.m;
+  const size_t per_warp = 16 * (size_t)n + 8 * a.stride;
+  double2 *line = reinterpret_cast<double2 *>(sm + 128 + (size_t)w * per_warp);
+  double *f = reinterpret_cast<double *>(line + n);
+  double2 *gline = a.spec + (size_t)J * n;
+  const unsigned bar = smem_u32(reinterpret_cast<unsigned long long *>(sm) + w);
+  const unsigned line_bytes = 16u * (unsigned)n, fac_bytes = 8u * (unsigned)a.stride;
+  if (lane == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(line_bytes + fac_bytes)
+                 : "memory");
+  }
+  if (lane == 0 && !a.stale) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(line)),
+                 "l"(__cvta_generic_to_global(gline)), "r"(line_bytes), "r"(bar)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(f)),
+                 "l"(__cvta_generic_to_global(a.fac + (size_t)J * a.stride)), "r"(fac_bytes), "r"(bar)
+                 : "memory");
+  }
+  __syncwarp();
+  bool done = false;
+  for (unsigned k = 0; k < a.spin_limit && !done; ++k) done = mbar_try(bar, 0u);
+  if (!done) {
+    if (lane == 0) atomicOr(a.err, 1u);
+    // leave the line unsolved, but only once the copies issued into this
+    // warp's shared memory have landed (bounded as well)
+    if (!a.stale)
+      for (unsigned k = 0; k < kParDrainSpins && !mbar_try(bar, 0u); ++k) {
+      }
+    return;
+  }
+  const double *inv = f, *gg = f + n, *up = f + 2 * n, *vv = f + 3 * n, *ww = f + 4 * n;
+  const double *alpha = f + 5 * n, *beta = alpha + kPartLevels * kPartSeg, *rD = beta + kPartLevels * kPartSeg;
+  // 1) the segment's interior rows r = 0 .. m-2 (line index r*32 + lane)
+  //    with zero boundary values: forward elimination and back substitution.
+  //    y_r = inv_r q_r - g_r y_{r-1} with g_r = a_r inv_r: one FMA per row on
+  //    the dependent chain, the product inv_r q_r off it
+  double2 y = line[lane];
+  y.x *= inv[lane];
+  y.y *= inv[lane];
+  line[lane] = y;
+#pragma unroll 4
+  for (int r = 1; r < m - 1; ++r) {
+    const int i = r * kPartSeg + lane;
+    double2 q = line[i];
+    const double iv = inv[i], g = gg[i];
+    q.x = fma(-g, y.x, iv * q.x);
+    q.y = fma(-g, y.y, iv * q.y);
+    line[i] = q;
+    y = q;
+  }
+  const double2 ylast = y;  // row m-2
+#pragma unroll 4
+  for (int r = m - 3; r >= 0; --r) {
+    const int i = r * kPartSeg + lane;
+    double2 q = line[i];
+    const double u = up[i];
+    q.x = fma(-u, y.x, q.x);
+    q.y = fma(-u, y.y, q.y);
+    line[i] = q;
+    y = q;
+  }
+  // y: the first interior value (row 0). 2) right-hand side of the interface
+  // row e: r_e - a_e y_{e-1} - c_e y'_0 (y'_0 of the next segment)
+  const int ie = (m - 1) * kPartSeg + lane;
+  const double ynx = __shfl_down_sync(0xffffffffu, y.x, 1);
+  const double yny = __shfl_down_sync(0xffffffffu, y.y, 1);
+  const double2 re = line[ie];
+  const double ae = __ldg(a.lo + ie), ce = lane < kPartSeg - 1 ? __ldg(a.hi + ie) : 0.0;
+  double Rx = re.x - ae * ylast.x - ce * (lane < kPartSeg - 1 ? ynx : 0.0);
+  double Ry = re.y - ae * ylast.y - ce * (lane < kPartSeg - 1 ? yny : 0.0);
+  if (J == 0 && lane == kPartSeg - 1) {  // the mean mode: last unknown pinned to 0
+    Rx = 0.0;
+    Ry = 0.0;
+  }
+  // 3) parallel cyclic reduction of the 32 interface equations
+#pragma unroll
+  for (int lev = 0; lev < kPartLevels; ++lev) {
+    const int d = 1 << lev;
+    const double mx = __shfl_up_sync(0xffffffffu, Rx, d), my = __shfl_up_sync(0xffffffffu, Ry, d);
+    const double px = __shfl_down_sync(0xffffffffu, Rx, d), py = __shfl_down_sync(0xffffffffu, Ry, d);
+    const double al = alpha[lev * kPartSeg + lane], be = beta[lev * kPartSeg + lane];
+    const double lmx = lane >= d ? mx : 0.0, lmy = lane >= d ? my : 0.0;
+    const double lpx = lane + d < kPartSeg ? px : 0.0, lpy = lane + d < kPartSeg ? py : 0.0;
+    Rx = fma(be, lpx, fma(al, lmx, Rx));
+    Ry = fma(be, lpy, fma(al, lmy, Ry));
+  }
+  const double xe_x = Rx * rD[lane], xe_y = Ry * rD[lane];
+  line[ie] = make_double2(xe_x, xe_y);
+  // 4) interiors from the spikes: x_i = y_i + v_i x_{e(k-1)} + w_i x_{e(k)}
+  const double xl_x = __shfl_up_sync(0xffffffffu, xe_x, 1), xl_y = __shfl_up_sync(0xffffffffu, xe_y, 1);
+  const double lx = lane > 0 ? xl_x : 0.0, ly = lane > 0 ? xl_y : 0.0;
+#pragma unroll 4
+  for (int r = 0; r < m - 1; ++r) {
+    const int i = r * kPartSeg + lane;
+    double2 q = line[i];
+    q.x = fma(ww[i], xe_x, fma(vv[i], lx, q.x));
+    q.y = fma(ww[i], xe_y, fma(vv[i], ly, q.y));
+    line[i] = q;
+  }
+  __syncwarp();
+  for (int i = lane; i < n; i += 32) gline[i] = line[i];
+}
+
+int par_cols(const DevGrid &g) {
+  // enough blocks to cover the SMs at least twice, at most 64 KiB of shared memory each
+  int c = 1;
+  while (c < 16 && (size_t)(2 * c) * g.ny * sizeof(double) <= 65536 && g.nx / (2 * c) >= 304) c *= 2;
+  return c;
+}
+
+int par_threads(const DevGrid &g, int cols) {
+  const int b = cols * (g.ny / 2) / 4;
+  return b <= 64 ? 64 : b >= 256 ? 256 : (b + 31) / 32 * 32;
+}
+
+int par_warps(int nx, size_t stride) {
+  const size_t per_warp = 16 * (size_t)nx + 8 * stride;
+  int w = (int)std::min<size_t>(kParWarpsMax, (kParSmemMax - 128) / per_warp);
+  return std::max(w, 0);
+}
+
+}  // namespace
+
+bool parallel_tri_supported(int nx, int ny) {
+  return nx >= 2 * kPartSeg && nx % kPartSeg == 0 && ny >= 4 && par_warps(nx, partition_stride(nx) + nx) >= 1;
+}
+
+cudaError_t launch_par_fwd(const DevGrid &g, const StageScalars &s, const double *ux, const double *uy,
+                           double2 *spec, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_par_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(k_par_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    attr = true;
+  }
+  const int C = par_cols(g);
+  const ParArgs a{g, s, ux, uy, spec, nullptr, C, g.nx / kPartSeg};
+  k_par_fwd<<<(g.nx + C - 1) / C, par_threads(g, C), (size_t)C * g.ny * sizeof(double), st>>>(a);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_par_tri(const DevGrid &g, double2 *spec, const ParFactors &pf, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_par_tri, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kParSmemMax);
+    attr = true;
+  }
+  const int wpb = par_warps(g.nx, pf.stride);
+  if (wpb < 1) return cudaErrorInvalidValue;
+  const ParTriArgs a{spec,  pf.fac, pf.lo, pf.hi, pf.stride, g.nx, g.nh, g.nx / kPartSeg, pf.err, pf.spin_limit,
+                     pf.stale};
+  const size_t smem = 128 + (size_t)wpb * (16 * (size_t)g.nx + 8 * pf.stride);
+  k_par_tri<<<(g.nh + wpb - 1) / wpb, 32 * wpb, smem, st>>>(a);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_par_bwd(const DevGrid &g, const StageScalars &s, const double2 *spec, double *psi,
+                           cudaStream_t st) {
+  const int C = par_cols(g);
+  const ParArgs a{g, s, nullptr, nullptr, const_cast<double2 *>(spec), psi, C, g.nx / kPartSeg};
+  k_par_bwd<<<(g.nx + C - 1) / C, par_threads(g, C), (size_t)C * g.ny * sizeof(double), st>>>(a);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+}  // namespace sns

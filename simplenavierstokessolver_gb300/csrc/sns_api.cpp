@@ -115,6 +115,13 @@ struct Context {
   PendingCorr pcorr;
   FusedState fz;
   unsigned *fz_err_host = nullptr;  // pinned
+  // the Poisson lines' solver: SNS_FORM_EXACT (the reference's
+  // recurrence, identical results) or SNS_FORM_PARALLEL (partition
+  // method with parallel cyclic reduction, held to the path's tolerance)
+  int form = SNS_FORM_EXACT;
+  ParFactors par{};
+  bool par_ready = false;
+  unsigned *par_err_host = nullptr;  // pinned
   // asynchronous checkpoint (sns_checkpoint): a device snapshot of ux, uy, p
   // and T taken on the solver's stream, its copy to pinned memory on ck_stream,
   // and a host thread that writes the files
@@ -175,6 +182,10 @@ struct Prof {
     if (idx >= 0) cudaEventRecord(c->prof_ev[2 * idx + 1], st);
   }
 };
+
+// the plain kernels of the context's arithmetic form: sns::exact (the
+// reference's roundings) or sns::contract (fused multiply-adds)
+#define FORM(c, fn) ((c)->form == SNS_FORM_PARALLEL ? contract::fn : exact::fn)
 
 static std::mutex g_mu;
 static std::vector<Context *> g_contexts;
@@ -237,6 +248,7 @@ static void destroy_context(Context *c) {
   if (c->staging) cudaFreeHost(c->staging);
   if (c->red_host) cudaFreeHost(c->red_host);
   if (c->fz_err_host) cudaFreeHost(c->fz_err_host);
+  if (c->par_err_host) cudaFreeHost(c->par_err_host);
   if (c->ev_fwd) cudaEventDestroy(c->ev_fwd);
   if (c->ev_temp) cudaEventDestroy(c->ev_temp);
   if (c->side) cudaStreamDestroy(c->side);
@@ -658,7 +670,7 @@ static int implicit_x(Context *c, const param_t *param, int rk, int kind, double
   LineFactors lf{};
   if (int rc = push_factors(c, hf, 0, lf)) return rc;
   Prof pf(c, K_SOLVE_X);
-  SNS_CUDA(launch_solve_x(c->g, lf, kind == 1 ? 1 : 0, q, c->stream));
+  SNS_CUDA(FORM(c, launch_solve_x)(c->g, lf, kind == 1 ? 1 : 0, q, c->stream));
   return SNS_OK;
 }
 
@@ -673,7 +685,7 @@ static int implicit_y(Context *c, const param_t *param, int rk, int is_temp, int
   SNS_CUDA(cudaMemcpyAsync(c->fac + qoff, q1.data(), q1.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   pf.q1 = c->fac + qoff;
   Prof pr(c, K_SOLVE_Y);
-  SNS_CUDA(launch_solve_y(c->g, pf, first_col, q, c->stream));
+  SNS_CUDA(FORM(c, launch_solve_y)(c->g, pf, first_col, q, c->stream));
   return SNS_OK;
 }
 
@@ -702,7 +714,7 @@ static int do_temp_update(const param_t *param, int rk, FluidExt *fe, TempExt *t
   }
   {
     Prof pf(c, K_TEMP);
-    SNS_CUDA(launch_temp_update(c->g, s, impx, impy, te->f.t[te->cur], te->f.t[out], te->f.at, te->f.qt, fe->f.ux,
+    SNS_CUDA(FORM(c, launch_temp_update)(c->g, s, impx, impy, te->f.t[te->cur], te->f.t[out], te->f.at, te->f.qt, fe->f.ux,
                                 fe->f.uy, c->stream));
   }
   if (impx || impy) {
@@ -727,7 +739,7 @@ static int do_velocity_update(const param_t *param, int rk, FluidExt *fe, const 
   Fields &f = fe->f;
   {
     Prof pf(c, K_VEL);
-    SNS_CUDA(launch_velocity_update(c->g, s, impx, impy, f.ux, f.uy, f.p, tf, f.ux_alt, f.uy_alt, f.aux, f.auy,
+    SNS_CUDA(FORM(c, launch_velocity_update)(c->g, s, impx, impy, f.ux, f.uy, f.p, tf, f.ux_alt, f.uy_alt, f.aux, f.auy,
                                     f.qx, f.qy, c->stream));
   }
   if (impx || impy) {
@@ -767,13 +779,13 @@ static int implicit_updates(const param_t *param, int rk, FluidExt *fe, TempExt 
       if (int rc = dev_alloc(c, &te->f.qt, (size_t)c->nx * c->ny)) return rc;
     while (out == te->cur || out == te->snap) out++;
     Prof pf(c, K_TEMP);
-    SNS_CUDA(launch_temp_update(c->g, s, impx, impy, te->f.t[te->cur], te->f.t[out], te->f.at, te->f.qt, f.ux, f.uy,
+    SNS_CUDA(FORM(c, launch_temp_update)(c->g, s, impx, impy, te->f.t[te->cur], te->f.t[out], te->f.at, te->f.qt, f.ux, f.uy,
                                 c->stream));
   }
   const double *tf = (te && te->snap >= 0) ? te->f.t[te->snap] : nullptr;
   {
     Prof pf(c, K_VEL);
-    SNS_CUDA(launch_velocity_update(c->g, s, impx, impy, f.ux, f.uy, f.p, tf, f.ux_alt, f.uy_alt, f.aux, f.auy, f.qx,
+    SNS_CUDA(FORM(c, launch_velocity_update)(c->g, s, impx, impy, f.ux, f.uy, f.p, tf, f.ux_alt, f.uy_alt, f.aux, f.auy, f.qx,
                                     f.qy, c->stream));
   }
   // fields: temperature (if coupled), ux, uy
@@ -790,7 +802,7 @@ static int implicit_updates(const param_t *param, int rk, FluidExt *fe, TempExt 
       set.n++;
     }
     Prof pf(c, K_SOLVE_X);
-    SNS_CUDA(launch_solve_x_set(c->g, set, c->stream));
+    SNS_CUDA(FORM(c, launch_solve_x_set)(c->g, set, c->stream));
   }
   if (impy) {
     SolveYSet set{};
@@ -819,7 +831,7 @@ static int implicit_updates(const param_t *param, int rk, FluidExt *fe, TempExt 
       }
     }
     Prof pr(c, K_SOLVE_Y);
-    SNS_CUDA(launch_solve_y_set(c->g, set, c->stream));
+    SNS_CUDA(FORM(c, launch_solve_y_set)(c->g, set, c->stream));
   }
   {
     Prof pf(c, K_ADD_INC);
@@ -835,11 +847,25 @@ static int implicit_updates(const param_t *param, int rk, FluidExt *fe, TempExt 
 
 static int poisson_forward(Context *c, const StageScalars &s, Fields &f) {
   Prof pf(c, K_POI_FWD);
-  SNS_CUDA(launch_poisson_fwd(c->g, s, f.ux, f.uy, f.spec, c->stream));
+  if (c->form == SNS_FORM_PARALLEL) {
+    SNS_CUDA(launch_par_fwd(c->g, s, f.ux, f.uy, f.spec, c->stream));
+  } else {
+    SNS_CUDA(launch_poisson_fwd(c->g, s, f.ux, f.uy, f.spec, c->stream));
+  }
   return SNS_OK;
 }
 
 static int poisson_rest(Context *c, const StageScalars &s, Fields &f) {
+  if (c->form == SNS_FORM_PARALLEL) {
+    {
+      Prof pf(c, K_POI_PCR);
+      SNS_CUDA(launch_par_tri(c->g, f.spec, c->par, c->stream));
+      c->par.stale = 0;  // a test's stale wait applies to one launch
+    }
+    Prof pf(c, K_POI_BWD);
+    SNS_CUDA(launch_par_bwd(c->g, s, f.spec, f.psi, c->stream));
+    return SNS_OK;
+  }
   {
     Prof pf(c, K_POI_TRI);
     SNS_CUDA(launch_poisson_tri(c->g, f.spec, c->stream));
@@ -848,6 +874,68 @@ static int poisson_rest(Context *c, const StageScalars &s, Fields &f) {
     Prof pf(c, K_POI_BWD);
     SNS_CUDA(launch_poisson_bwd(c->g, s, f.spec, f.psi, c->stream));
   }
+  return SNS_OK;
+}
+
+// Partition-method factors of the Poisson lines (host, once per context) for
+// the parallel tridiagonal form. The form needs itot a multiple of 32 (one
+// segment per lane) and the mean mode's last Thomas pivot to vanish, so that
+// pinning that unknown to zero reproduces the reference's gauge of psi
+// (src/linalg.c:36-38 zeroes the row): true on uniform grids, checked here.
+static int parallel_prepare(Context *c) {
+  if (c->par_ready) return SNS_OK;
+  const int nx = c->nx, ny = c->ny, nh = c->g.nh;
+  if (!parallel_tri_supported(nx, ny))
+    return fail(SNS_ERR_UNSUPPORTED, "parallel tridiagonal form: itot=%d must be a multiple of 32 in [64, 3968]", nx);
+  const double *dxf = c->dxf.data(), *dxc = c->dxc.data();
+  std::vector<double> l_raw(nx), u_raw(nx), a(nx), cc(nx);
+  for (int i = 1; i <= nx; i++) {
+    l_raw[i - 1] = 1. / dxc[i - 1] / dxf[i - 1];  // src/fluid/compute_potential.c:118-119
+    u_raw[i - 1] = 1. / dxc[i] / dxf[i - 1];
+    a[i - 1] = i > 1 ? l_raw[i - 1] : 0.0;
+    cc[i - 1] = i < nx ? u_raw[i - 1] : 0.0;
+  }
+  {
+    // the mean mode's Thomas pivots: only the last one may vanish, and it must
+    std::vector<double> d(nx), inv(nx), up(nx);
+    for (int i = 0; i < nx; i++) d[i] = -l_raw[i] - u_raw[i] + poisson_eigenvalue(c->g.dy, ny, 0);
+    d[0] += l_raw[0];
+    d[nx - 1] += u_raw[nx - 1];
+    factorize(nx, l_raw.data(), d.data(), u_raw.data(), inv.data(), up.data());
+    bool ok = inv[nx - 1] == 0.0;
+    for (int i = 1; i < nx - 1; i++) ok = ok && inv[i] != 0.0;
+    if (!ok)
+      return fail(SNS_ERR_UNSUPPORTED,
+                  "parallel tridiagonal form: the mean mode's last pivot does not vanish on this grid "
+                  "(the reference's gauge of psi cannot be pinned); use the Thomas form");
+  }
+  // per mode: inv, g = a inv, up, v, w (rows interleaved), then the PCR
+  // coefficients; g takes the product by the sub-diagonal off the forward
+  // elimination's dependent chain
+  const size_t base = partition_stride(nx), stride = base + nx;
+  const int m = nx / kPartSeg;
+  std::vector<double> fac(stride * nh), blk(base), lo(nx), hi(nx);
+  for (int x = 0; x < nx; x++) {
+    lo[(size_t)(x % m) * kPartSeg + x / m] = a[x];
+    hi[(size_t)(x % m) * kPartSeg + x / m] = cc[x];
+  }
+  for (int J = 0; J < nh; J++) {
+    partition_factors(nx, a.data(), cc.data(), l_raw.data(), u_raw.data(), poisson_eigenvalue(c->g.dy, ny, J),
+                      J == 0, true, blk.data());
+    double *o = fac.data() + stride * J;
+    std::copy(blk.begin(), blk.begin() + nx, o);                         // inv
+    for (int i = 0; i < nx; i++) o[nx + i] = lo[i] * blk[i];            // g
+    std::copy(blk.begin() + nx, blk.end(), o + 2 * (size_t)nx);         // up v w alpha beta rD
+  }
+  int rc = SNS_OK;
+  if ((rc = upload(c, &c->par.fac, fac)) || (rc = upload(c, &c->par.lo, lo)) || (rc = upload(c, &c->par.hi, hi)))
+    return rc;
+  if ((rc = dev_alloc(c, &c->par.err, (size_t)1))) return rc;
+  SNS_CUDA(cudaMemset(c->par.err, 0, sizeof(unsigned)));
+  if (!c->par_err_host) SNS_CUDA(cudaMallocHost(&c->par_err_host, sizeof(unsigned)));
+  *c->par_err_host = 0;
+  c->par.stride = stride;
+  c->par_ready = true;
   return SNS_OK;
 }
 
@@ -870,8 +958,14 @@ static int fused_prepare(Context *c) {
 }
 
 // after a stream synchronisation: a fused launch whose wait gave up leaves
-// its results undefined; report it, reset the flags and stop fusing
+// its results undefined; report it, reset the flags and stop fusing. A
+// parallel tridiagonal launch whose copy wait gave up left lines unsolved.
 static int fused_check(Context *c) {
+  if (c->par_ready && c->par_err_host && *c->par_err_host) {
+    *c->par_err_host = 0;
+    cudaMemsetAsync(c->par.err, 0, sizeof(unsigned), c->stream);
+    return fail(SNS_ERR_STATE, "parallel tridiagonal launch: a copy wait gave up; results of that step are invalid");
+  }
   if (!c->fused_ready || !c->fz_err_host || *c->fz_err_host == 0) return SNS_OK;
   const unsigned code = *c->fz_err_host;
   *c->fz_err_host = 0;
@@ -884,6 +978,8 @@ static int fused_check(Context *c) {
 static int fused_enqueue_err(Context *c) {
   if (c->fused_ready)
     SNS_CUDA(cudaMemcpyAsync(c->fz_err_host, c->fz.err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+  if (c->par_ready)
+    SNS_CUDA(cudaMemcpyAsync(c->par_err_host, c->par.err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
   return SNS_OK;
 }
 
@@ -893,7 +989,7 @@ static int fused_enqueue_err(Context *c) {
 static int try_fused(Context *c, const StageScalars &s, Fields &f, const double *t_in, double *t_out, double *at,
                        const double *ux_k, const double *uy_k, bool *fused_out) {
   *fused_out = false;
-  if (c->fused) {
+  if (c->fused && c->form == SNS_FORM_EXACT) {
     if (int rc = fused_prepare(c)) return rc;
     cudaError_t e;
     {
@@ -1006,7 +1102,7 @@ static int flush_pending(Context *c) {
     c->ptemp = PendingTemp{};
     {
       Prof pf(c, K_TEMP);
-      SNS_CUDA(launch_temp_update(c->g, pt.s, 0, 0, te->f.t[te->cur], te->f.t[pt.out], te->f.at, nullptr, pt.ux_k,
+      SNS_CUDA(FORM(c, launch_temp_update)(c->g, pt.s, 0, 0, te->f.t[te->cur], te->f.t[pt.out], te->f.at, nullptr, pt.ux_k,
                                   pt.uy_k, c->stream));
     }
     te->cur = pt.out;
@@ -1015,7 +1111,7 @@ static int flush_pending(Context *c) {
     const PendingCorr pc = c->pcorr;
     c->pcorr = PendingCorr{};
     Prof pf(c, K_CORR);
-    SNS_CUDA(launch_correct(c->g, pc.s, fe->f.psi, fe->f.ux, fe->f.uy, c->stream));
+    SNS_CUDA(FORM(c, launch_correct)(c->g, pc.s, fe->f.psi, fe->f.ux, fe->f.uy, c->stream));
   }
   return SNS_OK;
 }
@@ -1309,7 +1405,7 @@ int temperature_update_temp(const param_t *param, const parallel_t *parallel, co
     return fail(SNS_ERR_ARG, "temperature_update_temp: bad argument");
   Context *c = te->ctx;
   if (int rc = flush_pending(c)) return rc;
-  if (c->fused && fe->ctx == c && !param->implicitx && !param->implicity) {
+  if (c->fused && c->form == SNS_FORM_EXACT && fe->ctx == c && !param->implicitx && !param->implicity) {
     // explicit: launched inside the next fluid_compute_potential (it reads the
     // velocity of now, which that call's velocity update leaves in place)
     PendingTemp &pt = c->ptemp;
@@ -1398,7 +1494,7 @@ int fluid_update_pressure(const param_t *param, const parallel_t *parallel, cons
     if (red) SNS_CUDA(cudaMemsetAsync(fe->f.colmax, 0, sizeof(unsigned long long) * (c->nx + 1), c->stream));
     {
       Prof pf(c, K_CORR_PRES);
-      SNS_CUDA(launch_correct_pressure(c->g, s, param->implicitx, param->implicity, fe->f.psi, fe->f.ux, fe->f.uy,
+      SNS_CUDA(FORM(c, launch_correct_pressure)(c->g, s, param->implicitx, param->implicity, fe->f.psi, fe->f.ux, fe->f.uy,
                                        fe->f.p, red ? fe->f.colmax : nullptr, red ? fe->f.uymax : nullptr,
                                        c->stream));
     }
@@ -1407,7 +1503,7 @@ int fluid_update_pressure(const param_t *param, const parallel_t *parallel, cons
   }
   if (int rc = flush_pending(c)) return rc;
   Prof pf(c, K_PRES);
-  SNS_CUDA(launch_pressure(c->g, s, param->implicitx, param->implicity, fe->f.psi, fe->f.p, c->stream));
+  SNS_CUDA(FORM(c, launch_pressure)(c->g, s, param->implicitx, param->implicity, fe->f.psi, fe->f.p, c->stream));
   return SNS_OK;
 }
 
@@ -2061,7 +2157,7 @@ int sns_diagnostics_static(const param_t *param, const fluid_t *fluid, const tem
 static const char *kKindNames[K_NUM_KINDS] = {
     "temperature_update", "velocity_update", "poisson_forward_fft", "poisson_tridiagonal", "poisson_inverse_fft",
     "correct_and_pressure", "correct_velocity", "update_pressure", "max_velocity", "cn_solve_x", "cn_solve_y",
-    "add_increment", "poisson_fused"};
+    "add_increment", "poisson_fused", "poisson_pcr"};
 
 int sns_profile(const fluid_t *fluid, int enable) {
   FluidExt *fe = as_fluid(fluid);
@@ -2101,6 +2197,37 @@ int sns_synchronize(const fluid_t *fluid) {
   if (int rc = fused_enqueue_err(fe->ctx)) return rc;
   SNS_CUDA(cudaStreamSynchronize(fe->ctx->stream));
   return fused_check(fe->ctx);
+}
+
+int sns_set_form(const fluid_t *fluid, int mode) {
+  FluidExt *fe = as_fluid(fluid);
+  if (!fe) return fail(SNS_ERR_ARG, "sns_set_form: bad fluid");
+  if (mode != SNS_FORM_EXACT && mode != SNS_FORM_PARALLEL)
+    return fail(SNS_ERR_ARG, "sns_set_form: unknown mode %d", mode);
+  Context *c = fe->ctx;
+  if (int rc = flush_pending(c)) return rc;
+  if (mode == SNS_FORM_PARALLEL)
+    if (int rc = parallel_prepare(c)) return rc;
+  c->form = mode;
+  return SNS_OK;
+}
+
+int sns_get_form(const fluid_t *fluid) {
+  FluidExt *fe = as_fluid(fluid);
+  return fe ? fe->ctx->form : -1;
+}
+
+int sns_set_wait_limit(const fluid_t *fluid, unsigned polls, int stale) {
+  FluidExt *fe = as_fluid(fluid);
+  if (!fe) return fail(SNS_ERR_ARG, "sns_set_wait_limit: bad fluid");
+  if (int rc = flush_pending(fe->ctx)) return rc;
+  Context *c = fe->ctx;
+  c->fz.spin_limit = polls;
+  c->par.spin_limit = polls ? polls : (1u << 22);
+  // the stale flag arms the next launch of the form in use only
+  c->fz.stale = stale != 0 && c->form == SNS_FORM_EXACT;
+  c->par.stale = stale != 0 && c->form == SNS_FORM_PARALLEL;
+  return SNS_OK;
 }
 
 int sns_set_fused(const fluid_t *fluid, int on) {
@@ -2161,7 +2288,7 @@ static int integrate_impl(const param_t *param, FluidExt *fe, TempExt *te, bool 
         SNS_CUDA(cudaStreamWaitEvent(c->side, c->ev_fwd, 0));
         {
           Prof pf(c, K_TEMP, c->side);
-          SNS_CUDA(launch_temp_update(c->g, s, 0, 0, te->f.t[te->cur], te->f.t[out], te->f.at, nullptr, ux_k, uy_k,
+          SNS_CUDA(FORM(c, launch_temp_update)(c->g, s, 0, 0, te->f.t[te->cur], te->f.t[out], te->f.at, nullptr, ux_k, uy_k,
                                       c->side));
         }
         SNS_CUDA(cudaEventRecord(c->ev_temp, c->side));
@@ -2175,7 +2302,7 @@ static int integrate_impl(const param_t *param, FluidExt *fe, TempExt *te, bool 
     if (red) SNS_CUDA(cudaMemsetAsync(f.colmax, 0, sizeof(unsigned long long) * (c->nx + 1), c->stream));
     {
       Prof pf(c, K_CORR_PRES);
-      SNS_CUDA(launch_correct_pressure(c->g, s, param->implicitx, param->implicity, f.psi, f.ux, f.uy, f.p,
+      SNS_CUDA(FORM(c, launch_correct_pressure)(c->g, s, param->implicitx, param->implicity, f.psi, f.ux, f.uy, f.p,
                                        red ? f.colmax : nullptr, red ? f.uymax : nullptr, c->stream));
     }
     // the next substage reads the new T and overwrites the buffer of u_k

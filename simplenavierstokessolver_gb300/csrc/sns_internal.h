@@ -95,19 +95,7 @@ struct TempFields {
   double *qt;     // increment for the implicit paths
 };
 
-// ---------------------------------------------------------------- launches
-// All return cudaGetLastError() of their launches.
-cudaError_t launch_temp_update(const DevGrid &g, const StageScalars &s, int impx, int impy,
-                               const double *t_in, double *t_out, double *at, double *qt,
-                               const double *ux, const double *uy, cudaStream_t st);
-cudaError_t launch_velocity_update(const DevGrid &g, const StageScalars &s, int impx, int impy,
-                                   const double *ux, const double *uy, const double *p, const double *tforce,
-                                   double *ux_out, double *uy_out, double *aux, double *auy,
-                                   double *qx, double *qy, cudaStream_t st);
-// x-direction Crank-Nicolson solve on q rows, then field += q into out
-// (mode 0: first row divides by d0 (T, uy); mode 1: ux rows 2..nx with a zero row before)
-cudaError_t launch_solve_x(const DevGrid &g, const LineFactors &f, int mode, double *q, cudaStream_t st);
-cudaError_t launch_solve_y(const DevGrid &g, const PeriodicFactors &f, int first_col, double *q, cudaStream_t st);
+// ------------------------------------------------------------ launch types
 // up to three independent fields (temperature, ux, uy) in one launch: their
 // serial sweeps run side by side
 struct SolveXSet {
@@ -122,11 +110,6 @@ struct SolveYSet {
   double *q[3];
   int n;
 };
-cudaError_t launch_solve_x_set(const DevGrid &g, const SolveXSet &s, cudaStream_t st);
-cudaError_t launch_solve_y_set(const DevGrid &g, const SolveYSet &s, cudaStream_t st);
-// out = in + q on the interior (kind 0: T/uy all x; kind 1: ux x >= 1)
-cudaError_t launch_add_increment(const DevGrid &g, int kind, const double *in, const double *q, double *out,
-                                 cudaStream_t st);
 // strided field copies in one launch (host arrays are pinned and read or
 // written in place through their device alias): row y of field k moves
 // width entries from src + y*sstride to dst + y*dstride
@@ -140,15 +123,6 @@ struct XferList {
   XferField f[kXferMax];
   int n, rows;
 };
-cudaError_t launch_xfer(const XferList &L, cudaStream_t st);
-// tempforcex (src/temperature/force.c:17-23) from dense T, written straight
-// into the (itot-1) x jtot host array through its device alias
-cudaError_t launch_tempforce_to_host(const DevGrid &g, const double *t, double *host, cudaStream_t st);
-// running sums of src/statistics/collect.c:10-63 over rows j = 1..jtot of the
-// reference-width arrays (walls included): s = ux1, ux2 [ny][nx+1], then
-// uy1, uy2, temp1, temp2 [ny][nx+2]; t may be null (no temperature sums)
-cudaError_t launch_stats(const DevGrid &g, const double *ux, const double *uy, const double *t, double *s,
-                         cudaStream_t st);
 // fused Poisson solve (+ explicit temperature update): device flag words,
 // sized by fused_layout, zeroed once; epoch advances by one per launch
 struct FusedState {
@@ -156,33 +130,39 @@ struct FusedState {
   unsigned long long *bwd_cnt = nullptr; // [spans]
   unsigned *err = nullptr;               // [1]
   unsigned epoch = 0;
+  unsigned spin_limit = 0;               // polls of a wait before it gives up; 0: the default (~1 s)
+  int stale = 0;                         // test of the bounded waits: the next launch waits for a flag nobody sets
 };
-void fused_layout(const DevGrid &g, int *groups, int *spans);
-// cudaErrorNotSupported when the device cannot hold the cooperative grid for
-// this size; t_out == nullptr: no temperature update in the launch
-cudaError_t launch_poisson_fused(const DevGrid &g, const StageScalars &s, const double *ux, const double *uy,
-                                 double2 *spec, double *psi, const double *t_in, double *t_out, double *at,
-                                 const double *ux_k, const double *uy_k, FusedState &fs, cudaStream_t st);
-cudaError_t launch_poisson_fwd(const DevGrid &g, const StageScalars &s, const double *ux, const double *uy,
-                               double2 *spec, cudaStream_t st);
-cudaError_t launch_poisson_tri(const DevGrid &g, double2 *spec, cudaStream_t st);
-cudaError_t launch_poisson_bwd(const DevGrid &g, const StageScalars &s, const double2 *spec, double *psi,
-                               cudaStream_t st);
-cudaError_t launch_correct(const DevGrid &g, const StageScalars &s, const double *psi, double *ux, double *uy,
+
+// ------------------------------------------------- launches of plain_fp64.cu
+inline namespace exact {
+#include "plain_launch.inc"
+}
+namespace contract {
+#include "plain_launch.inc"
+}
+
+// Partition-method (PCR) form of the Poisson solve (plain_parallel.cu):
+// per-mode factor blocks and the interleaved sub/super diagonals
+struct ParFactors {
+  const double *fac = nullptr;           // [nh][stride]
+  const double *lo = nullptr, *hi = nullptr;  // [nx], rows interleaved
+  size_t stride = 0;
+  unsigned *err = nullptr;               // [1] set when a copy wait gave up
+  unsigned spin_limit = 1u << 22;        // polls of that wait
+  int stale = 0;                         // test of the bounded wait: the next launch issues no copy
+};
+bool parallel_tri_supported(int nx, int ny);
+cudaError_t launch_par_fwd(const DevGrid &g, const StageScalars &s, const double *ux, const double *uy,
+                           double2 *spec, cudaStream_t st);
+cudaError_t launch_par_tri(const DevGrid &g, double2 *spec, const ParFactors &pf, cudaStream_t st);
+cudaError_t launch_par_bwd(const DevGrid &g, const StageScalars &s, const double2 *spec, double *psi,
                            cudaStream_t st);
-cudaError_t launch_pressure(const DevGrid &g, const StageScalars &s, int impx, int impy, const double *psi,
-                            double *p, cudaStream_t st);
-// correct + pressure in one pass; with colmax non-null also the max-|u| reduction for the next dt
-cudaError_t launch_correct_pressure(const DevGrid &g, const StageScalars &s, int impx, int impy,
-                                    const double *psi, double *ux, double *uy, double *p,
-                                    unsigned long long *colmax, unsigned long long *uymax, cudaStream_t st);
-cudaError_t launch_umax(const DevGrid &g, const double *ux, const double *uy, unsigned long long *colmax,
-                        unsigned long long *uymax, cudaStream_t st);
 
 // kernel kinds for the optional per-launch event timing (sns_profile_*)
 enum KernelKind {
   K_TEMP = 0, K_VEL, K_POI_FWD, K_POI_TRI, K_POI_BWD, K_CORR_PRES, K_CORR, K_PRES, K_UMAX, K_SOLVE_X, K_SOLVE_Y,
-  K_ADD_INC, K_POI_FUSED, K_NUM_KINDS
+  K_ADD_INC, K_POI_FUSED, K_POI_PCR, K_NUM_KINDS
 };
 
 // counts kernel launches (process-wide)

@@ -254,6 +254,17 @@ class Case:
     def run(self, nsteps: int):
         N.check(self.lib.sns_run(self.param, self.parallel, self.fluid, self.temperature, nsteps), "sns_run")
 
+    def set_form(self, parallel: bool):
+        """the arithmetic form of the plain path: the reference's operations
+        and order (identical results, the default) or the parallel form
+        (Poisson lines by the partition method with parallel cyclic
+        reduction, fused multiply-adds; within 1e-12 relative L2)"""
+        N.check(self.lib.sns_set_form(self.fluid, N.SNS_FORM_PARALLEL if parallel else N.SNS_FORM_EXACT),
+                "sns_set_form")
+
+    def set_wait_limit(self, polls: int, stale: bool = False):
+        N.check(self.lib.sns_set_wait_limit(self.fluid, polls, int(stale)), "sns_set_wait_limit")
+
     def set_fused(self, on: bool):
         """one cooperative launch per Poisson solve (default) or three kernels"""
         N.check(self.lib.sns_set_fused(self.fluid, int(on)), "sns_set_fused")
