@@ -80,8 +80,18 @@ extern void *sns_batch_stream(const sns_batch *batch);
  * filled by the reference's rules); any pointer may be NULL. Waits. */
 extern int sns_batch_state(sns_batch *batch, int slot, double *ux, double *uy, double *p, double *psi,
                            double *temp);
-/* time, dt of the next step, completed steps, done flag (steps reached). Waits. */
+/* time, dt of the next step, completed steps, done flag (steps reached).
+ * Returns SNS_ERR_NONFINITE (outputs filled) once the case has written a NaN
+ * or infinity to its velocity or pressure (a diverged case; the flag is
+ * sticky). Waits. */
 extern int sns_batch_case_status(sns_batch *batch, int slot, double *time, double *dt, long long *step, int *done);
+/* Bounded wait of the tridiagonal launch (its bulk copies complete on an
+ * mbarrier), no counterpart in the reference: it gives up after `polls`
+ * polls (0: the default, about a second), sets this batch's error word, and
+ * the next sns_batch_synchronize returns SNS_ERR_STATE. stale != 0 makes the
+ * next step issue no copy so that every wait runs out: a test of the error
+ * path that faults nothing. */
+extern int sns_batch_set_wait_limit(sns_batch *batch, unsigned polls, int stale);
 /* number of resident cases; their slots written to slots[0..max) */
 extern int sns_batch_cases(const sns_batch *batch, int *slots, int max);
 /* cells summed over resident unfinished cases (the host knows every case's

@@ -114,6 +114,10 @@ struct temperature_t_ {
 #define SNS_ERR_CUDA 3        /* CUDA launch or runtime error */
 #define SNS_ERR_OOM 4         /* device or host allocation failed */
 #define SNS_ERR_STATE 5       /* call out of order (e.g. object already finalised) */
+/* the state holds NaN or infinity (a diverged run): reported by param_decide_dt
+ * (after deciding dt as the reference would) and by sns_run, which stops
+ * stepping; the batched form reports it per case */
+#define SNS_ERR_NONFINITE 6
 
 /* ----------------------------------------------- reference hot-path entries */
 /* include/fluid.h:15 (src/fluid/init.c:85-92): allocates the structure, its

@@ -20,6 +20,7 @@ SNS_ERR_UNSUPPORTED = 2
 SNS_ERR_CUDA = 3
 SNS_ERR_OOM = 4
 SNS_ERR_STATE = 5
+SNS_ERR_NONFINITE = 6
 
 SNS_FORM_EXACT = 0
 SNS_FORM_PARALLEL = 1
@@ -159,6 +160,7 @@ PROTOTYPES = {
     "sns_batch_remove": (c_int, [c_void_p, c_int]),
     "sns_batch_step": (c_int, [c_void_p, c_int]),
     "sns_batch_synchronize": (c_int, [c_void_p]),
+    "sns_batch_set_wait_limit": (c_int, [c_void_p, ctypes.c_uint, c_int]),
     "sns_batch_stream": (c_void_p, [c_void_p]),
     "sns_batch_state": (c_int, [c_void_p, c_int, _PD, _PD, _PD, _PD, _PD]),
     "sns_batch_case_status": (c_int, [c_void_p, c_int, _PD, _PD, POINTER(c_longlong), POINTER(c_int)]),

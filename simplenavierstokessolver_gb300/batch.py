@@ -134,10 +134,12 @@ class Batch:
         return int(self.lib.sns_batch_active_cells(self.h))
 
     def status(self, slot: int):
-        t, dt, st, done = c_double(), c_double(), c_longlong(), c_int()
-        N.check(self.lib.sns_batch_case_status(self.h, slot, ctypes.byref(t), ctypes.byref(dt), ctypes.byref(st),
-                                               ctypes.byref(done)), "sns_batch_case_status")
-        return {"time": t.value, "dt": dt.value, "step": st.value, "done": bool(done.value)}
+        """time, next dt, step, done; finite is False once the case wrote a
+        NaN or infinity (sns_batch_case_status returns SNS_ERR_NONFINITE)"""
+        return status_of(self.h, slot)
+
+    def set_wait_limit(self, polls: int, stale: bool = False):
+        N.check(self.lib.sns_batch_set_wait_limit(self.h, polls, int(stale)), "sns_batch_set_wait_limit")
 
     def tuning(self) -> dict:
         t = N.Tuning()
@@ -167,6 +169,16 @@ class Batch:
         return out
 
 
+def status_of(batch_handle, slot: int) -> dict:
+    t, dt, st, done = c_double(), c_double(), c_longlong(), c_int()
+    rc = _lib().sns_batch_case_status(batch_handle, slot, ctypes.byref(t), ctypes.byref(dt), ctypes.byref(st),
+                                      ctypes.byref(done))
+    if rc != N.SNS_ERR_NONFINITE:
+        N.check(rc, "sns_batch_case_status")
+    return {"time": t.value, "dt": dt.value, "step": st.value, "done": bool(done.value),
+            "finite": rc != N.SNS_ERR_NONFINITE}
+
+
 def diagnostics_of(batch_handle, slot: int) -> np.ndarray:
     out = np.zeros(11)
     N.check(_lib().sns_batch_diagnostics(batch_handle, slot, _ptr(out)), "sns_batch_diagnostics")
@@ -184,20 +196,25 @@ def state_of(batch_handle, slot: int, desc: Desc):
 def serve(descs: list[Desc], arrivals: list[float], hbm_bytes: int, max_cases: int = 256, chunk_steps: int = 10,
           keep_states: bool = False):
     """Runs sns_serve (continuous batching in real time). Returns admission
-    and completion times (seconds from the start), the busy span and, with
-    keep_states, each request's final fields read just before retirement."""
+    and completion times (seconds from the start), the busy span, whether
+    each request's final state is finite (no NaN or infinity written) and,
+    with keep_states, each request's final fields read just before
+    retirement."""
     n = len(descs)
     arr = (N.CaseDesc * n)(*[d.c() for d in descs])
     at = np.ascontiguousarray(arrivals, dtype=np.float64)
     admit, done = np.zeros(n), np.zeros(n)
+    finite = np.ones(n, dtype=bool)
     busy = c_double()
     states = {}
 
     def on_done(req, bh, slot, user):
-        states[req] = state_of(bh, slot, descs[req])
+        finite[req] = status_of(bh, slot)["finite"]
+        if keep_states:
+            states[req] = state_of(bh, slot, descs[req])
 
-    cb = N.DONE_FN(on_done) if keep_states else None
+    cb = N.DONE_FN(on_done)
     rc = _lib().sns_serve(arr, _ptr(at), n, hbm_bytes, max_cases, chunk_steps, _ptr(admit), _ptr(done),
-                          ctypes.byref(busy), ctypes.cast(cb, ctypes.c_void_p) if cb else None, None)
+                          ctypes.byref(busy), ctypes.cast(cb, ctypes.c_void_p), None)
     N.check(rc, "sns_serve")
-    return {"admit": admit, "done": done, "busy_s": busy.value, "states": states}
+    return {"admit": admit, "done": done, "busy_s": busy.value, "finite": finite, "states": states}

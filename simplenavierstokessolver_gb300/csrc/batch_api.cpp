@@ -203,6 +203,11 @@ struct sns_batch {
   double *diag = nullptr;  // block partials of sns_batch_diagnostics
   size_t diag_words = 0;
   sns_batch_tuning tune{kBTileX, kBTileY, kBModesPerBlock, 0};
+  // this batch's error word: a tridiagonal bulk-copy wait gave up
+  unsigned *d_err = nullptr;
+  unsigned *h_err = nullptr;  // pinned
+  unsigned tri_spin = 1u << 22;  // polls of that wait
+  int tri_stale = 0;             // test of the error path: the next step issues no copy
   std::mutex mu;
 };
 
@@ -331,7 +336,9 @@ static int rebuild(sns_batch *b) {
     if ((err = launch_batch_fwd(b->d_cases, b->d_cols, b->ncols, rk, b->fft_smem, b->fft_threads, b->stream)) !=
         cudaSuccess)
       break;
-    if ((err = launch_batch_tri(b->d_cases, b->d_modes, b->nmodes, mpb, nmax, b->stream)) != cudaSuccess) break;
+    if ((err = launch_batch_tri(b->d_cases, b->d_modes, b->nmodes, mpb, nmax, b->d_err, b->tri_spin,
+                                rk == 0 ? b->tri_stale : 0, b->stream)) != cudaSuccess)
+      break;
     if ((err = launch_batch_bwd(b->d_cases, b->d_cols, b->ncols, b->fft_smem, b->fft_threads, b->stream)) !=
         cudaSuccess)
       break;
@@ -371,6 +378,9 @@ sns_batch *sns_batch_create(size_t hbm_bytes, int max_cases) {
   if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
       batch_kernels_init() != cudaSuccess || cudaMalloc((void **)&b->arena, hbm_bytes) != cudaSuccess ||
       cudaMalloc((void **)&b->d_cases, sizeof(BCase) * max_cases) != cudaSuccess ||
+      cudaMalloc((void **)&b->d_err, sizeof(unsigned)) != cudaSuccess ||
+      cudaMemset(b->d_err, 0, sizeof(unsigned)) != cudaSuccess ||
+      cudaMallocHost((void **)&b->h_err, sizeof(unsigned)) != cudaSuccess ||
       cudaMemcpy(b->d_cases, b->table.data(), sizeof(BCase) * max_cases, cudaMemcpyHostToDevice) != cudaSuccess) {
     bfail(SNS_ERR_OOM, "sns_batch_create: %s", cudaGetErrorString(cudaGetLastError()));
     sns_batch_destroy(b);
@@ -391,6 +401,8 @@ int sns_batch_destroy(sns_batch *b) {
   cudaFree(b->d_tiles);
   cudaFree(b->d_cols);
   cudaFree(b->d_modes);
+  cudaFree(b->d_err);
+  if (b->h_err) cudaFreeHost(b->h_err);
   if (b->staging) cudaFreeHost(b->staging);
   cudaFree(b->diag);
   if (b->stream) cudaStreamDestroy(b->stream);
@@ -750,6 +762,10 @@ int sns_batch_step(sns_batch *b, int nsteps) {
     if (b->ntiles == 0) break;
     BCUDA(cudaGraphLaunch(b->exec, b->stream));
     count_launches(b->graph_launches);
+    if (b->tri_stale) {  // a test's stale wait applies to one step
+      b->tri_stale = 0;
+      b->dirty = true;
+    }
     bool finished_one = false;
     for (CaseHost &h : b->hc) {
       if (!h.used || (h.d.steps > 0 && h.steps_done >= h.d.steps)) continue;
@@ -874,10 +890,24 @@ int sns_batch_autotune(sns_batch *b, int steps, sns_batch_tuning *chosen, double
 
 int sns_batch_synchronize(sns_batch *b) {
   if (!b) return bfail(SNS_ERR_ARG, "NULL batch");
+  // this batch's own error word, read in stream order
+  BCUDA(cudaMemcpyAsync(b->h_err, b->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, b->stream));
   BCUDA(cudaStreamSynchronize(b->stream));
-  if (unsigned e = batch_error_take())
+  if (const unsigned e = *b->h_err) {
+    *b->h_err = 0;
+    BCUDA(cudaMemsetAsync(b->d_err, 0, sizeof(unsigned), b->stream));
     return bfail(SNS_ERR_STATE, "batched tridiagonal solve: a bulk-copy wait gave up (code %u); results are invalid",
                  e);
+  }
+  return SNS_OK;
+}
+
+int sns_batch_set_wait_limit(sns_batch *b, unsigned polls, int stale) {
+  if (!b) return bfail(SNS_ERR_ARG, "NULL batch");
+  std::lock_guard<std::mutex> lk(b->mu);
+  b->tri_spin = polls ? polls : (1u << 22);
+  b->tri_stale = stale != 0;
+  b->dirty = true;  // the step graph carries both as launch parameters
   return SNS_OK;
 }
 
@@ -909,6 +939,8 @@ int sns_batch_case_status(sns_batch *b, int slot, double *time, double *dt, long
   if (dt) *dt = t.dt;
   if (step) *step = t.step;
   if (done) *done = t.done;
+  if (t.nonfinite)
+    return bfail(SNS_ERR_NONFINITE, "case in slot %d holds NaN or infinity (step %lld)", slot, t.step);
   return SNS_OK;
 }
 
@@ -1012,7 +1044,8 @@ extern "C" int sns_batch_checkpoint(sns_batch *b, int slot, const char *dirname)
   double time = 0.0, dt = 0.0;
   long long step = 0;
   int done = 0;
-  if (int rc = sns_batch_case_status(b, slot, &time, &dt, &step, &done)) return rc;
+  // a diverged case is saved as it is (the reference's save() writes NaN too)
+  if (int rc = sns_batch_case_status(b, slot, &time, &dt, &step, &done); rc && rc != SNS_ERR_NONFINITE) return rc;
   std::vector<double> xf(nx + 1), xc(nx + 2), dxf(nx), dxc(nx + 1), yf(ny + 1), yc(ny);
   double dy;
   make_grid(nx, ny, 1.0, d.ly, d.stretch, xf.data(), xc.data(), dxf.data(), dxc.data(), yf.data(), yc.data(), &dy);

@@ -447,14 +447,14 @@ __global__ void __launch_bounds__(256) k_b_bwd(const BCase *__restrict__ cases, 
 // asynchronous copies (the TMA engine, completion on an mbarrier), solves
 // there, and writes the line back with coalesced stores: the per-lane
 // segment sweeps then read shared memory instead of scattered global lines.
-__device__ unsigned g_tri_err;  // nonzero: a bulk-copy wait gave up (read and cleared by the host)
-
-constexpr unsigned kTriWaitSpins = 1u << 22;
+// polls of the wait that lets a warp's copies land after its first wait gave
+// up, so that no copy into the warp's shared memory outlives the warp
+constexpr unsigned kTriDrainSpins = 1u << 22;
 
 __device__ __forceinline__ unsigned smem_addr(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 
-__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
-  for (unsigned k = 0; k < kTriWaitSpins; ++k) {
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, unsigned spins) {
+  for (unsigned k = 0; k < spins; ++k) {
     unsigned ok;
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
@@ -467,7 +467,8 @@ __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity) {
 }
 
 __global__ void __launch_bounds__(32 * kBModesPerBlockMax) k_b_tri(const BCase *__restrict__ cases,
-                                                               const BModes *__restrict__ items, int nmax) {
+                                                               const BModes *__restrict__ items, int nmax,
+                                                               unsigned *err, unsigned spin, int stale) {
   extern __shared__ __align__(128) unsigned char tri_sm[];
   const BModes it = items[blockIdx.x];
   const BCase &C = cases[it.c];
@@ -489,6 +490,9 @@ __global__ void __launch_bounds__(32 * kBModesPerBlockMax) k_b_tri(const BCase *
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b), "r"(line_bytes + fac_bytes)
                  : "memory");
+  }
+  if (lane == 0 && !stale) {
+    const unsigned b = smem_addr(bar);
     asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                      smem_addr(line)),
                  "l"(__cvta_generic_to_global(gline)), "r"(line_bytes), "r"(b)
@@ -499,9 +503,12 @@ __global__ void __launch_bounds__(32 * kBModesPerBlockMax) k_b_tri(const BCase *
                  : "memory");
   }
   __syncwarp();
-  if (!mbar_wait(smem_addr(bar), 0)) {
-    if (lane == 0) atomicOr(&g_tri_err, 1u);
-    return;  // this line is left unsolved; the host reports the error
+  if (!mbar_wait(smem_addr(bar), 0, spin)) {
+    if (lane == 0) atomicOr(err, 1u);
+    // this line is left unsolved and the host reports the error, once the
+    // copies issued into this warp's shared memory have landed
+    if (!stale) mbar_wait(smem_addr(bar), 0, kTriDrainSpins);
+    return;
   }
   const double *inv = f, *up = f + n, *vv = f + 2 * n, *ww = f + 3 * n;
   const double *alpha = f + 4 * n, *beta = alpha + kPcrLevels * kSeg, *rD = beta + kPcrLevels * kSeg;
@@ -578,6 +585,7 @@ __global__ void __launch_bounds__(kBTileXMax) k_b_corr(BCase *__restrict__ cases
   const int x = tl.x0 + threadIdx.x;
   const bool live = x < nx;
   float mx = 0.f, my = 0.f;
+  bool nf = false;  // a NaN or infinity among the values written
   if (live) {
     const int y0 = tl.y0, y1 = min(y0 + rows, ny);
     const int pu = C.par ^ (rk & 1) ^ 1;
@@ -610,6 +618,7 @@ __global__ void __launch_bounds__(kBTileXMax) k_b_corr(BCase *__restrict__ cases
         ux[r] = u;
         uxl[r] = ul;
         mx = fmaxf(mx, fabsf(u) * rxc);
+        nf |= (__float_as_uint(u) & 0x7f800000u) == 0x7f800000u;
       }
       float v, vlo;
       const double dv = -((sc - sm) * gy);  // :31-37
@@ -623,10 +632,15 @@ __global__ void __launch_bounds__(kBTileXMax) k_b_corr(BCase *__restrict__ cases
       uy[r] = v;
       uyl[r] = vlo;
       my = fmaxf(my, fabsf(v) * rdyf);
-      p[r] += sc;  // src/fluid/update_pressure.c:26-31
+      const double pv = p[r] + sc;  // src/fluid/update_pressure.c:26-31
+      p[r] = pv;
+      nf |= ((__float_as_uint(v) & 0x7f800000u) == 0x7f800000u) |
+            ((__double2hiint(pv) & 0x7ff00000) == 0x7ff00000);
       sm = sc;
     }
   }
+  // a NaN or infinity written: the case is flagged (sticky) for the host
+  if (__any_sync(0xffffffffu, nf) && (threadIdx.x & 31) == 0) atomicOr(&C.nonfinite, 1);
   if (rk == 2) {  // max |u|/dx for the next step's dt (src/param/decide_dt.c:35-50)
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
@@ -716,17 +730,11 @@ size_t batch_tri_smem(int nmax, int modes_per_block) {
 }
 
 cudaError_t launch_batch_tri(const BCase *cases, const BModes *modes, int nmodes, int modes_per_block, int nmax,
-                             cudaStream_t st) {
+                             unsigned *err, unsigned spin, int stale, cudaStream_t st) {
   if (nmodes == 0) return cudaSuccess;
-  k_b_tri<<<nmodes, 32 * modes_per_block, batch_tri_smem(nmax, modes_per_block), st>>>(cases, modes, nmax);
+  k_b_tri<<<nmodes, 32 * modes_per_block, batch_tri_smem(nmax, modes_per_block), st>>>(cases, modes, nmax, err, spin,
+                                                                                      stale);
   return cudaGetLastError();
-}
-
-unsigned batch_error_take() {
-  unsigned v = 0, z = 0;
-  if (cudaMemcpyFromSymbol(&v, g_tri_err, sizeof v) != cudaSuccess) return 0xffffffffu;
-  if (v) cudaMemcpyToSymbol(g_tri_err, &z, sizeof z);
-  return v;
 }
 
 cudaError_t launch_batch_corr(const BCase *cases, const BTile *tiles, int ntiles, int rk, int tile_x, int rows,

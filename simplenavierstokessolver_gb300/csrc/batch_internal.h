@@ -58,6 +58,7 @@ struct BCase {
   double time, dt;
   double adt[3], bdt[3], gdt[3], rgdt[3];
   unsigned int umax[2];            // float bits of max |ux|/DXC and max |uy|/dy (next dt)
+  int nonfinite;                   // sticky: a NaN or infinity was written to ux, uy or p
 };
 
 struct BTile {
@@ -85,10 +86,11 @@ cudaError_t launch_batch_fwd(const BCase *cases, const BCols *cols, int ncols, i
                              cudaStream_t st);
 // shared memory of the tridiagonal launch for lines up to nmax long
 size_t batch_tri_smem(int nmax, int modes_per_block);
+// err: the batch's error word, set when a bulk-copy wait gave up after
+// `spin` polls; stale: issue no copy, so that every wait runs out (a test of
+// the error path)
 cudaError_t launch_batch_tri(const BCase *cases, const BModes *modes, int nmodes, int modes_per_block, int nmax,
-                             cudaStream_t st);
-// the tridiagonal kernels' error word (a bulk-copy wait gave up), cleared on read
-unsigned batch_error_take();
+                             unsigned *err, unsigned spin, int stale, cudaStream_t st);
 cudaError_t launch_batch_bwd(const BCase *cases, const BCols *cols, int ncols, size_t smem, int threads,
                              cudaStream_t st);
 cudaError_t launch_batch_corr(const BCase *cases, const BTile *tiles, int ntiles, int rk, int tile_x, int rows,

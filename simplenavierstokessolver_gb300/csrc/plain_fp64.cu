@@ -1146,10 +1146,15 @@ struct CorrArgs {
 
 __device__ __forceinline__ unsigned long long abs_bits(double v) {
   // |v| as an order-preserving key; NaN counts as 0 (fmax(NaN, small) = small
-  // in src/param/decide_dt.c:147,155). Integer operations only: an FP64
+  // in src/param/decide_dt.c:38,46). Integer operations only: an FP64
   // compare would occupy the (slow) FP64 pipe.
   const unsigned long long b = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
   return b > 0x7ff0000000000000ull ? 0ull : b;
+}
+
+// NaN or infinity: exponent field all ones (integer test, off the FP64 pipe)
+__device__ __forceinline__ bool nonfinite(double v) {
+  return (__double2hiint(v) & 0x7ff00000) == 0x7ff00000;
 }
 
 constexpr int kCorrRows = 4;  // rows per thread in the (memory-latency bound) correction kernels
@@ -1171,6 +1176,7 @@ __global__ void __launch_bounds__(128) k_corr(const CorrArgs a) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const bool live = x < nx;
   unsigned long long mx = 0ull, my = 0ull;
+  bool nf = false;  // a NaN or infinity among the values written
   if (live) {
     const int y0 = blockIdx.y * kCorrRows;
     int y1 = min(y0 + kCorrRows, ny);
@@ -1224,10 +1230,13 @@ __global__ void __launch_bounds__(128) k_corr(const CorrArgs a) {
           if (!left) {
             a.ux[r] = un[k];
             mx = max(mx, abs_bits(un[k]));
+            nf |= nonfinite(un[k]);
           }
           a.uy[r] = vn[k];
           my = max(my, abs_bits(vn[k]));
-          a.p[r] = pp[k] + ps[k];
+          const double pv = pp[k] + ps[k];
+          a.p[r] = pv;
+          nf |= nonfinite(vn[k]) | nonfinite(pv);
         }
         y1 = y0;  // done: skip the row loop below
       }
@@ -1241,10 +1250,12 @@ __global__ void __launch_bounds__(128) k_corr(const CorrArgs a) {
           const double u = a.ux[r] - ((gdt * (sc - sl)) * dxi);
           a.ux[r] = u;
           mx = max(mx, abs_bits(u));
+          nf |= nonfinite(u);
         }
         const double v = a.uy[r] - dv<RCP>(gdt * (sc - sm), dy, rdy);
         a.uy[r] = v;
         my = max(my, abs_bits(v));
+        nf |= nonfinite(v);
       }
       if (PRES) {
         double pv = a.p[r] + sc;
@@ -1261,6 +1272,7 @@ __global__ void __launch_bounds__(128) k_corr(const CorrArgs a) {
           pv = pv + a.s.pcorr * dv<RCP>(gp - gm, dy, rdy);
         }
         a.p[r] = pv;
+        nf |= nonfinite(pv);
       }
       sm = sc;
     }
@@ -1269,6 +1281,8 @@ __global__ void __launch_bounds__(128) k_corr(const CorrArgs a) {
     if (live && x >= 1) atomicMax(a.colmax + x, mx);
     my = warp_max_u64(my);
     if ((threadIdx.x & 31) == 0) atomicMax(a.uymax, my);
+    // word 0 of the column maxima (no ux column 0 exists): non-finite state
+    if (__any_sync(0xffffffffu, nf) && (threadIdx.x & 31) == 0) atomicOr(a.colmax, 1ull);
   }
 }
 
@@ -1276,18 +1290,25 @@ __global__ void __launch_bounds__(128) k_umax(int nx, int ny, const double *ux, 
                                               unsigned long long *colmax, unsigned long long *uymax) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long mx = 0ull, my = 0ull;
+  bool nf = false;
   if (x < nx) {
     const int y0 = blockIdx.y * kRows;
     const int y1 = min(y0 + kRows, ny);
     for (int y = y0; y < y1; ++y) {
       const size_t r = (size_t)y * nx + x;
-      if (x >= 1) mx = max(mx, abs_bits(ux[r]));
-      my = max(my, abs_bits(uy[r]));
+      const double u = ux[r], v = uy[r];
+      if (x >= 1) {
+        mx = max(mx, abs_bits(u));
+        nf |= nonfinite(u);
+      }
+      my = max(my, abs_bits(v));
+      nf |= nonfinite(v);
     }
     if (x >= 1) atomicMax(colmax + x, mx);
   }
   my = warp_max_u64(my);
   if ((threadIdx.x & 31) == 0) atomicMax(uymax, my);
+  if (__any_sync(0xffffffffu, nf) && (threadIdx.x & 31) == 0) atomicOr(colmax, 1ull);
 }
 
 dim3 march_grid(const DevGrid &g, int rows = kRows) {

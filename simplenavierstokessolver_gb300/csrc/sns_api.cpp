@@ -1070,6 +1070,16 @@ static void finish_decide_dt(param_t *param, const Context *c) {
   param->dt = dt;
 }
 
+// word 0 of the reduction copied to the host: a NaN or infinity in ux, uy
+// or p (set by the reduction kernels). The reference has no such check (its
+// dt rule ignores NaN, src/param/decide_dt.c:38,46): the dt is decided as
+// it would be, and the caller learns of the divergence from the status.
+static int nonfinite_check(const Context *c, const param_t *param) {
+  if (c->red_host[0] == 0) return SNS_OK;
+  return fail(SNS_ERR_NONFINITE, "the velocity or pressure holds NaN or infinity (step %d, time %g)",
+              param ? param->step : -1, param ? param->time : 0.0);
+}
+
 static int reduce_to_host(Context *c, Fields &f, bool launch) {
   // copied to the host at the end of the call that computed it
   if (!launch && c->red_host_version == c->version) return SNS_OK;
@@ -1592,7 +1602,7 @@ int param_decide_dt(param_t *param, const parallel_t *parallel, const fluid_t *f
   if (int rc = reduce_to_host(c, fe->f, c->red_version != c->version)) return rc;
   c->red_version = c->version;
   finish_decide_dt(param, fe->ctx);
-  return SNS_OK;
+  return nonfinite_check(c, param);
 }
 
 // Device -> host. state_only: ux, uy, p and temp alone, the whole input and
@@ -2337,6 +2347,7 @@ int sns_run(param_t *param, const parallel_t *parallel, fluid_t *fluid, temperat
   bool have_reduction = c->red_version == c->version;
   for (int s = 0; s < nsteps; s++) {
     if (int rc = reduce_to_host(c, fe->f, !have_reduction)) return rc;
+    if (int rc = nonfinite_check(c, param)) return rc;  // stop stepping a diverged state
     finish_decide_dt(param, c);
     c->version++;
     if (int rc = integrate_impl(param, fe, te, true)) return rc;
@@ -2357,6 +2368,7 @@ int sns_run(param_t *param, const parallel_t *parallel, fluid_t *fluid, temperat
   if (nsteps > 0) {
     if (int rc = fused_check(c)) return rc;
     c->red_host_version = c->red_version;
+    return nonfinite_check(c, param);
   }
   return SNS_OK;
 }
