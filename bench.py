@@ -348,64 +348,143 @@ def hbm_roofline(cell_steps_per_s: float, compensated: bool) -> dict:
             "note": "algorithmic bytes of the whole step over its event time; the FP64 DFTs bound the step"}
 
 
-def large_instance(args, torch, nx=2048, ny=4096, Ra=1e10, steps=10):
-    """the 2048 x 4096, Ra 1e10 instance: plain FP64 (sns_run, treatment by
-    param_decide_dt with the fixed cost table) and the FP32-stencil form, per
-    step with CUDA events after warm-up; the plain path's per-kernel times"""
+def large_instance(args, torch, nx=2048, ny=4096, Ra=1e10, steps=500, acc_steps=200):
+    """The 2048 x 4096, Ra 1e10 instance.
+
+    Plain FP64 in both arithmetic forms: `steps` steps of sns_run (treatment
+    by param_decide_dt with the fixed cost table: Crank-Nicolson in x and y
+    here), a CUDA event pair around every step on the solver's stream (each
+    sns_run call ends with a host synchronisation, so an interval holds the
+    step's device work and any host gap inside it), per-kernel times from a
+    profiled pass. The FP32 and compensated batched forms integrate
+    explicitly (their dt is the explicit limit), so beside cell-steps/s every
+    leg reports simulated time per wall second. Accuracy of the two batched
+    forms: `acc_steps` steps against the plain FP64 path made to take the
+    same explicit steps (the batch's dt sequence replayed)."""
     import ctypes
+
+    import numpy as np
 
     from simplenavierstokessolver_gb300 import Case
     from simplenavierstokessolver_gb300.batch import Batch, Desc
 
     cells = nx * ny
     out = {"workload": f"rayleigh_benard_{nx}x{ny}_Ra{Ra:.0e}_Pr1", "steps": steps}
-    with Case(nx, ny, ly=2.0, Ra=Ra, Pr=1.0) as c:
-        lib = c.lib
-        stream = torch.cuda.ExternalStream(c.stream())
-        c.run(3)
-        c.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        c.run(steps)
-        e1.record(stream)
-        c.synchronize()
-        ms = e0.elapsed_time(e1)
-        d = c.get_dt()
-        lib.sns_profile(c.fluid, 1)
-        c.run(2)
-        c.synchronize()
-        kms = (ctypes.c_double * 32)()
-        kcnt = (ctypes.c_longlong * 32)()
-        n = lib.sns_profile_read(c.fluid, kms, kcnt, 32)
-        lib.sns_profile(c.fluid, 0)
-        kernels = {lib.sns_profile_kind_name(k).decode(): round(1e3 * kms[k] / kcnt[k], 1) for k in range(n) if kcnt[k]}
     peak, _ = load_peaks()
-    kgbs = {}
-    for k, us in kernels.items():
-        bpc = IMPLICIT_MODEL.get(k, KERNEL_MODEL.get(k, (None,))[0])
-        if bpc and us > 0:
-            gbs = bpc * cells / (us * 1e-6) / 1e9
-            kgbs[k] = {"bytes_per_cell": bpc, "achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4)}
-    out["plain_fp64"] = {"value": cells * steps / (ms * 1e-3), "ms_per_step": ms / steps,
-                         "scheme": f"implicit x {d['implicitx']}, implicit y {d['implicity']}",
-                         "kernel_avg_us": kernels, "kernel_hbm": kgbs, "hbm_peak_gbs": peak}
-    with Batch(16 << 30) as b:
-        b.add(Desc(nx, ny, ly=2.0, Ra=Ra, Pr=1.0))
-        stream = torch.cuda.ExternalStream(b.stream())
-        b.step(3)
-        shapes, _ = b.autotune(steps=3)
-        b.step(2)
-        b.synchronize()
-        e0.record(stream)
-        b.step(steps)
-        e1.record(stream)
-        b.synchronize()
-        ms = e0.elapsed_time(e1)
-    v32 = cells * steps / (ms * 1e-3)
-    out["fp32_stencil"] = {"value": v32, "ms_per_step": ms / steps,
-                           "scheme": "explicit x / explicit y (batched form)", "autotuned_shapes": shapes,
-                           "hbm_roofline": hbm_roofline(v32, False)}
+    for form in ("exact", "parallel"):
+        with Case(nx, ny, ly=2.0, Ra=Ra, Pr=1.0) as c:
+            lib = c.lib
+            c.set_form(form == "parallel")
+            stream = torch.cuda.ExternalStream(c.stream())
+            c.run(3)
+            c.synchronize()
+            t0 = c.get_dt()["time"]
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+            schemes = []
+            for a, b in ev:
+                a.record(stream)
+                c.run(1)
+                b.record(stream)
+                dd = c.get_dt()
+                schemes.append((dd["implicitx"], dd["implicity"]))
+            c.synchronize()
+            per = np.array([a.elapsed_time(b) for a, b in ev])
+            imp = np.array([x or y for x, y in schemes])
+            ms = float(per.sum())
+            d = c.get_dt()
+            sim = d["time"] - t0
+            lib.sns_profile(c.fluid, 1)
+            c.run(2)
+            c.synchronize()
+            kms = (ctypes.c_double * 32)()
+            kcnt = (ctypes.c_longlong * 32)()
+            n = lib.sns_profile_read(c.fluid, kms, kcnt, 32)
+            lib.sns_profile(c.fluid, 0)
+            kernels = {lib.sns_profile_kind_name(k).decode(): round(1e3 * kms[k] / kcnt[k], 1)
+                       for k in range(n) if kcnt[k]}
+        kgbs = {}
+        for k, us in kernels.items():
+            bpc = IMPLICIT_MODEL.get(k, KERNEL_MODEL.get(k, (None,))[0])
+            if bpc and us > 0:
+                gbs = bpc * cells / (us * 1e-6) / 1e9
+                kgbs[k] = {"bytes_per_cell": bpc, "achieved_gbs": round(gbs, 1), "frac": round(gbs / peak, 4)}
+        out[f"plain_fp64_{form}"] = {
+            "value": cells * steps / (ms * 1e-3), "ms_per_step": ms / steps,
+            "ms_step_median": float(np.median(per)), "ms_step_min": float(per.min()), "ms_step_max": float(per.max()),
+            "simulated_time_per_s": sim / (ms * 1e-3), "simulated_time": sim,
+            "scheme": "param_decide_dt per step with the cost table (1, 2, 2, 3): Crank-Nicolson in x and y "
+                      "while the explicit diffusive limit is the tighter one, explicit once the flow is fast",
+            "implicit_steps": int(imp.sum()), "explicit_steps": int((~imp).sum()),
+            "ms_step_implicit_median": float(np.median(per[imp])) if imp.any() else None,
+            "ms_step_explicit_median": float(np.median(per[~imp])) if (~imp).any() else None,
+            "kernel_avg_us": kernels, "kernel_hbm": kgbs, "hbm_peak_gbs": peak}
+    for name, comp in (("fp32_stencil", False), ("fp32_compensated", True)):
+        with Batch(16 << 30) as b:
+            s = b.add(Desc(nx, ny, ly=2.0, Ra=Ra, Pr=1.0, compensated=comp))
+            stream = torch.cuda.ExternalStream(b.stream())
+            b.step(3)
+            shapes, _ = b.autotune(steps=3)
+            b.step(2)
+            b.synchronize()
+            t0 = b.status(s)["time"]
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            b.step(steps)
+            e1.record(stream)
+            b.synchronize()
+            ms = e0.elapsed_time(e1)
+            sim = b.status(s)["time"] - t0
+        v32 = cells * steps / (ms * 1e-3)
+        out[name] = {"value": v32, "ms_per_step": ms / steps, "simulated_time_per_s": sim / (ms * 1e-3),
+                     "scheme": "explicit x / explicit y (batched form)", "autotuned_shapes": shapes,
+                     "hbm_roofline": hbm_roofline(v32, comp)}
+        if acc_steps > 0:
+            out[name]["accuracy_vs_fp64"] = batched_accuracy(nx, ny, Ra, 1.0, acc_steps, comp)
     return out
+
+
+def batched_accuracy(nx, ny, Ra, Pr, nsteps, compensated):
+    from simplenavierstokessolver_gb300.batch import Desc
+
+    return batched_accuracy_desc(Desc(nx, ny, ly=2.0, Ra=Ra, Pr=Pr, compensated=compensated), nsteps)
+
+
+def batched_accuracy_desc(desc, nsteps):
+    """relative L2 per field (p modulo its mean) of a batched-form run of
+    `desc` against the plain FP64 path (exact form) taking the same explicit
+    steps from the same initial state: the batch's dt sequence replayed"""
+    import dataclasses
+
+    import numpy as np
+
+    from simplenavierstokessolver_gb300 import Case
+    from simplenavierstokessolver_gb300.batch import Batch, initial_temperature
+
+    desc = dataclasses.replace(desc, steps=0)
+    dts = []
+    with Batch(16 << 30) as b:
+        s = b.add(desc)
+        for _ in range(nsteps):
+            dts.append(b.status(s)["dt"])
+            b.step(1)
+        got = b.state(s)
+        finite = b.status(s)["finite"]
+    with Case(desc.itot, desc.jtot, ly=desc.ly, stretch=desc.stretch, Ra=desc.Ra, Pr=desc.Pr) as c:
+        st = c.get_state()
+        c.set_state(st["ux"], st["uy"], st["p"], initial_temperature(desc))
+        for dt in dts:
+            c.set_dt(dt, 0, 0)
+            c.integrate()
+        c.synchronize()
+        ref = c.get_state()
+    err = {}
+    for k in ("ux", "uy", "temp", "p"):
+        a, r = got[k][1:-1, 1:-1], ref[k][1:-1, 1:-1]
+        if k == "p":
+            a, r = a - a.mean(), r - r.mean()
+        err[k] = float(np.linalg.norm(a - r) / np.linalg.norm(r))
+    return {"steps": nsteps, "time": float(sum(dts)), "rel_l2": err, "finite": bool(finite),
+            "dt": "explicit dt of the batched run, replayed in the FP64 run"}
 
 
 def fp32_accuracy(args, compensated=False):
@@ -611,22 +690,44 @@ def ensemble_accuracy(args, compensated=False):
 
 
 def serving(args):
+    """sns_serve on a Poisson stream of requests: time to completion and queue
+    wait percentiles, aggregate cell-steps/s over the busy span, the number of
+    requests whose final state holds a NaN or infinity, and for a seeded
+    sample of requests (the cheapest few) the relative L2 error of the served
+    result against the plain FP64 path taking the same explicit steps (a
+    request's arithmetic reads only its own data, so its result served alone
+    equals its result in the mix: tests/test_gpu_batch.py)"""
+    import dataclasses
+
     import numpy as np
 
     from simplenavierstokessolver_gb300.batch import serve
     from simplenavierstokessolver_gb300.workloads import serving_stream
 
     descs, arrivals = serving_stream(args.serve_rate, args.serve_seconds)
+    descs = [dataclasses.replace(d, compensated=args.serve_compensated) for d in descs]
     r = serve(descs, arrivals, hbm_bytes=args.serve_hbm << 20, max_cases=256, chunk_steps=args.serve_chunk)
-    ttc = r["done"] - np.asarray(arrivals)
+    arr = np.asarray(arrivals)
+    ttc = r["done"] - arr
+    wait = r["admit"] - arr
     work = sum(d.itot * d.jtot * d.steps for d in descs)
-    return {"requests": len(descs), "rate_per_s": args.serve_rate, "arrival_window_s": args.serve_seconds,
-            "p50_s": float(np.percentile(ttc, 50)), "p99_s": float(np.percentile(ttc, 99)),
-            "mean_queue_wait_s": float(np.mean(r["admit"] - np.asarray(arrivals))),
-            "value": work / r["busy_s"], "unit": "cell-steps/s", "busy_s": r["busy_s"],
-            "hbm_arena_bytes": args.serve_hbm << 20, "chunk_steps": args.serve_chunk,
-            "workload": "Poisson arrivals; nx in {64,128,256,512}, ny=2nx, log10 Ra in [6,10], Pr in [0.7,7], "
-                        "steps in {200..2000}"}
+    out = {"requests": len(descs), "rate_per_s": args.serve_rate, "arrival_window_s": args.serve_seconds,
+           "form": "compensated (float-float stencils)" if args.serve_compensated else "FP32 stencils",
+           "p50_s": float(np.percentile(ttc, 50)), "p99_s": float(np.percentile(ttc, 99)),
+           "queue_wait_p50_s": float(np.percentile(wait, 50)), "queue_wait_p99_s": float(np.percentile(wait, 99)),
+           "mean_queue_wait_s": float(np.mean(wait)),
+           "value": work / r["busy_s"], "unit": "cell-steps/s", "busy_s": r["busy_s"],
+           "nonfinite_requests": int((~r["finite"]).sum()),
+           "hbm_arena_bytes": args.serve_hbm << 20, "chunk_steps": args.serve_chunk,
+           "workload": "Poisson arrivals; nx in {64,128,256,512}, ny=2nx, log10 Ra in [6,10], Pr in [0.7,7], "
+                       "steps in {200..2000}"}
+    if args.serve_acc_sample > 0:
+        order = sorted(range(len(descs)), key=lambda k: descs[k].itot * descs[k].jtot * descs[k].steps)
+        sample = order[:args.serve_acc_sample]
+        out["accuracy_sample"] = [
+            {"request": k, "nx": descs[k].itot, "Ra": descs[k].Ra, "Pr": descs[k].Pr, "steps": descs[k].steps,
+             **batched_accuracy_desc(descs[k], descs[k].steps)} for k in sample]
+    return out
 
 
 # ----------------------------------------------------------------- GPU arm
@@ -641,6 +742,13 @@ def gpu_arm(args, world, rank, local):
     from simplenavierstokessolver_gb300 import _native as N
 
     lib = N.lib()
+    if args.large_only or args.serving_only:
+        # one leg alone, for its own measurement runs (not a bench line)
+        part = large_instance(args, torch, steps=args.large_steps, acc_steps=args.large_acc_steps) \
+            if args.large_only else serving(args)
+        if rank == 0:
+            print(json.dumps({"leg": "large_instance" if args.large_only else "serving", **part}))
+        return 0
     case = Case(args.nx, args.ny, ly=2.0, Ra=args.Ra, Pr=args.Pr)
     # the headline's arithmetic form: the parallel form (within 1e-12 of the
     # oracle after the stated step counts) where the grid supports it
@@ -856,7 +964,8 @@ def gpu_arm(args, world, rank, local):
         extra["fp32_compensated"] = comp
         extra["serving"] = serving(args)
         if args.large_steps > 0:
-            extra["large_instance"] = large_instance(args, torch, steps=args.large_steps)
+            extra["large_instance"] = large_instance(args, torch, steps=args.large_steps,
+                                                     acc_steps=args.large_acc_steps)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -899,16 +1008,24 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--plain-only", action="store_true", help="skip the FP32-stencil, ensemble and serving parts")
+    ap.add_argument("--large-only", action="store_true", help="run the 2048x4096 leg alone")
+    ap.add_argument("--serving-only", action="store_true", help="run the serving leg alone")
     ap.add_argument("--form", default="parallel", choices=["parallel", "exact"],
                     help="arithmetic form of the headline plain FP64 step (sns_set_form)")
     ap.add_argument("--acc-steps", type=int, default=2000, help="steps of the FP32-vs-FP64 accuracy run")
     ap.add_argument("--ens-steps", type=int, default=50)
     ap.add_argument("--ens-acc-steps", type=int, default=500, help="steps of the ensemble FP32-vs-FP64 accuracy run")
-    ap.add_argument("--large-steps", type=int, default=10, help="timed steps of the 2048x4096 Ra=1e10 instance")
+    ap.add_argument("--large-steps", type=int, default=500, help="timed steps of the 2048x4096 Ra=1e10 instance")
+    ap.add_argument("--large-acc-steps", type=int, default=200,
+                    help="steps of the batched forms' accuracy run at 2048x4096 (0: skip)")
     ap.add_argument("--serve-rate", type=float, default=6.0)
     ap.add_argument("--serve-seconds", type=float, default=12.0)
     ap.add_argument("--serve-hbm", type=int, default=2048, help="serving arena in MiB")
     ap.add_argument("--serve-chunk", type=int, default=10)
+    ap.add_argument("--serve-compensated", type=int, default=1,
+                    help="requests in the compensated (float-float) form (1) or FP32 (0)")
+    ap.add_argument("--serve-acc-sample", type=int, default=3,
+                    help="served requests checked against the FP64 path (the cheapest ones)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -239,9 +239,11 @@ extern int sns_diagnostics(const param_t *param, const fluid_t *fluid, const tem
  * are summed on the device with the same compensated sums in the same order,
  * so out[] equals sns_diagnostics's bit for bit. A grid needing more than
  * 4096 partials, ceil((itot+1)/64) * ceil(jtot/16) > 4096 (1024 x 2048
- * fits, 1024 x 4096 does not), returns SNS_ERR_UNSUPPORTED with a message. The first call on
- * a device looks the scratch up (cudaGetSymbolAddress, with the case's device
- * current); make it before any stream capture. Nothing in the scratch needs
+ * fits, 1024 x 4096 does not), returns SNS_ERR_UNSUPPORTED with a message. Every call
+ * looks the scratch up (cudaGetSymbolAddress, with the case's device current;
+ * cheap once the module is loaded, and never stale after a device reset); the
+ * first call on a device may load the module, so make it before any stream
+ * capture. sns_allocations() does not move across a call. Nothing in the scratch needs
  * to start at zero. There is one scratch per device: calls that overlap on
  * one device (several threads, several cases) race on it; serialise them.
  * Blocks until done. */
@@ -381,6 +383,10 @@ extern int sns_fp64_issue_rate(double out[2]);
 extern const char *sns_last_error(void);
 /* number of kernel launches issued by this process so far */
 extern long long sns_kernel_launches(void);
+/* number of device and pinned host allocations (cudaMalloc, cudaHostAlloc)
+ * the library has made in this process so far; no counterpart in the
+ * reference. Steady-state stepping and sns_diagnostics_static make none. */
+extern long long sns_allocations(void);
 /* struct layout as compiled into the library, for binding checks: writes up to
  * n values -- sizeof(param_t), offsetof(param_t, itot / dy / rkcoefs / time /
  * dt / step / expimp_wtimes / timemax / log / stat), sizeof(parallel_t),

@@ -127,6 +127,7 @@ PROTOTYPES = {
     "sns_run": (c_int, [PP, PL, PF, PT, c_int]),
     "sns_last_error": (c_char_p, []),
     "sns_kernel_launches": (c_longlong, []),
+    "sns_allocations": (c_longlong, []),
     "sns_abi_layout": (c_int, [POINTER(c_size_t), c_int]),
     "sns_diagnostics": (c_int, [PP, PF, PT, _PD]),
     "sns_diagnostics_static": (c_int, [PP, PF, PT, _PD]),

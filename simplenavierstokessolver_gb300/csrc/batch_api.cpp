@@ -247,7 +247,7 @@ static int ensure_device_list(T **ptr, size_t *cap, size_t need) {
   if (*ptr) cudaFree(*ptr);
   *ptr = nullptr;
   const size_t n = std::max<size_t>(need, 2 * *cap);
-  BCUDA(cudaMalloc((void **)ptr, sizeof(T) * n));
+  BCUDA(counted_malloc((void **)ptr, sizeof(T) * n));
   *cap = n;
   return SNS_OK;
 }
@@ -376,11 +376,11 @@ sns_batch *sns_batch_create(size_t hbm_bytes, int max_cases) {
     t.done = 1;  // empty slots are skipped by every kernel
   }
   if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      batch_kernels_init() != cudaSuccess || cudaMalloc((void **)&b->arena, hbm_bytes) != cudaSuccess ||
-      cudaMalloc((void **)&b->d_cases, sizeof(BCase) * max_cases) != cudaSuccess ||
-      cudaMalloc((void **)&b->d_err, sizeof(unsigned)) != cudaSuccess ||
+      batch_kernels_init() != cudaSuccess || counted_malloc((void **)&b->arena, hbm_bytes) != cudaSuccess ||
+      counted_malloc((void **)&b->d_cases, sizeof(BCase) * max_cases) != cudaSuccess ||
+      counted_malloc((void **)&b->d_err, sizeof(unsigned)) != cudaSuccess ||
       cudaMemset(b->d_err, 0, sizeof(unsigned)) != cudaSuccess ||
-      cudaMallocHost((void **)&b->h_err, sizeof(unsigned)) != cudaSuccess ||
+      counted_malloc_host((void **)&b->h_err, sizeof(unsigned)) != cudaSuccess ||
       cudaMemcpy(b->d_cases, b->table.data(), sizeof(BCase) * max_cases, cudaMemcpyHostToDevice) != cudaSuccess) {
     bfail(SNS_ERR_OOM, "sns_batch_create: %s", cudaGetErrorString(cudaGetLastError()));
     sns_batch_destroy(b);
@@ -814,8 +814,8 @@ int sns_batch_autotune(sns_batch *b, int steps, sns_batch_tuning *chosen, double
   if (!any) return bfail(SNS_ERR_STATE, "sns_batch_autotune: no active case to tune on");
   char *save = nullptr;
   BCase *save_table = nullptr;
-  if (cudaMalloc((void **)&save, std::max<size_t>(high, 1)) != cudaSuccess ||
-      cudaMalloc((void **)&save_table, sizeof(BCase) * b->max_cases) != cudaSuccess) {
+  if (counted_malloc((void **)&save, std::max<size_t>(high, 1)) != cudaSuccess ||
+      counted_malloc((void **)&save_table, sizeof(BCase) * b->max_cases) != cudaSuccess) {
     cudaGetLastError();
     if (save) cudaFree(save);
     return bfail(SNS_ERR_OOM, "sns_batch_autotune: %zu bytes for the state snapshot are not available", high);
@@ -955,7 +955,7 @@ int sns_batch_state(sns_batch *b, int slot, double *ux, double *uy, double *p, d
   if (b->staging_bytes < sizeof(double) * cells) {
     if (b->staging) cudaFreeHost(b->staging);
     b->staging = nullptr;
-    BCUDA(cudaMallocHost((void **)&b->staging, sizeof(double) * cells));
+    BCUDA(counted_malloc_host((void **)&b->staging, sizeof(double) * cells));
     b->staging_bytes = sizeof(double) * cells;
   }
   const int cur = t.par;
@@ -1096,7 +1096,7 @@ int sns_batch_diagnostics(sns_batch *b, int slot, double out[11]) {
   if (b->diag_words < words) {
     cudaFree(b->diag);
     b->diag = nullptr;
-    BCUDA(cudaMalloc((void **)&b->diag, sizeof(double) * words));
+    BCUDA(counted_malloc((void **)&b->diag, sizeof(double) * words));
     b->diag_words = words;
   }
   const sns_case_desc &d = b->hc[slot].d;

@@ -98,6 +98,23 @@ cudaError_t launch_batch_corr(const BCase *cases, const BTile *tiles, int ntiles
 cudaError_t launch_batch_dt(BCase *cases, int ncases, const double *rk_a, const double *rk_b, cudaStream_t st);
 
 void count_launches(long long n);
+// counts the device and pinned host allocations the library makes (process-wide)
+void count_allocation();
+#ifndef SNS_COUNTED_ALLOC
+#define SNS_COUNTED_ALLOC
+template <typename T>
+inline cudaError_t counted_malloc(T **p, size_t bytes) {
+  const cudaError_t e = cudaMalloc(reinterpret_cast<void **>(p), bytes);
+  if (e == cudaSuccess) count_allocation();
+  return e;
+}
+template <typename T>
+inline cudaError_t counted_malloc_host(T **p, size_t bytes, unsigned flags = cudaHostAllocDefault) {
+  const cudaError_t e = cudaHostAlloc(reinterpret_cast<void **>(p), bytes, flags);
+  if (e == cudaSuccess) count_allocation();
+  return e;
+}
+#endif
 // sets the message returned by sns_last_error() on this thread
 void record_error(const char *msg);
 

@@ -213,10 +213,6 @@ namespace {
 constexpr size_t kDiagStaticWords = (size_t)kDiagStaticBlocks * (2 * kDiagSums + 1);
 static __device__ __align__(256) double g_diag_scratch[kDiagStaticWords + 16];
 
-constexpr int kMaxDevices = 64;
-static double *g_scratch_ptr[kMaxDevices];
-static std::mutex g_scratch_mu;
-
 // the same compensated sums in the same order as diag_finish, one thread per
 // sum, so the results equal those of sns_diagnostics bit for bit
 __global__ void __launch_bounds__(32) k_diag_finish(const double *partials, int nblocks, double ly, double *out) {
@@ -252,22 +248,17 @@ __global__ void __launch_bounds__(32) k_diag_finish(const double *partials, int 
   }
 }
 
-// set-up, once per device, with that device current: the scratch's address.
-// The first call on a device makes it (and may load the module); make that
-// first call before any stream capture.
+// The scratch's device address, looked up on every call with the caller's
+// device current: an address kept from an earlier call could belong to a
+// context that no longer exists (after cudaDeviceReset the module is loaded
+// again, possibly elsewhere). The lookup is cheap once the module is loaded;
+// the first call on a device may load it, so make that call before any
+// stream capture.
 cudaError_t scratch_for_current_device(double **ptr) {
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_diag_scratch);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (!g_scratch_ptr[dev]) {
-    void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_diag_scratch);
-    if (e != cudaSuccess) return e;
-    g_scratch_ptr[dev] = static_cast<double *>(p);
-  }
-  *ptr = g_scratch_ptr[dev];
+  *ptr = static_cast<double *>(p);
   return cudaSuccess;
 }
 

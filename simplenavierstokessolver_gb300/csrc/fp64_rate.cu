@@ -64,7 +64,7 @@ extern "C" int sns_fp64_issue_rate(double out[2]) {
     rc = SNS_ERR_CUDA;
     return false;
   };
-  if (ok(cudaMalloc(&buf, sizeof(double) * (size_t)blocks * kRateThreads)) &&
+  if (ok(counted_malloc(&buf, sizeof(double) * (size_t)blocks * kRateThreads)) &&
       ok(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) && ok(cudaEventCreate(&e0)) &&
       ok(cudaEventCreate(&e1))) {
     for (int op = 0; op < 2 && rc == SNS_OK; ++op) {

@@ -1465,18 +1465,40 @@ cudaError_t launch_stats(const DevGrid &g, const double *ux, const double *uy, c
 }
 
 // --------------------------------------------------------- host transfers
-__global__ void __launch_bounds__(256) k_xfer(const XferList L) {
+// Strided field copies between pinned host arrays (read or written in place
+// through their device alias, over the host link) and dense device fields.
+// The link's latency is long, so each thread keeps kXferRows loads in flight
+// (one column of kXferRows rows) before it stores them; blocks walk row
+// groups of one field (blockIdx.y).
+constexpr int kXferRows = 8;
+constexpr int kXferThreads = 256;
+
+__global__ void __launch_bounds__(kXferThreads) k_xfer(const XferList L) {
   const XferField f = L.f[blockIdx.y];
-  const size_t total = (size_t)L.rows * f.width;
-  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x) {
-    const int y = (int)(k / f.width), x = (int)(k - (size_t)y * f.width);
-    f.dst[(size_t)y * f.dstride + x] = f.src[(size_t)y * f.sstride + x];
+  const int groups = (L.rows + kXferRows - 1) / kXferRows;
+  for (int gi = blockIdx.x; gi < groups; gi += gridDim.x) {
+    const int y0 = gi * kXferRows;
+    const int ny = min(kXferRows, L.rows - y0);
+    for (int x = threadIdx.x; x < f.width; x += kXferThreads) {
+      double v[kXferRows];
+#pragma unroll
+      for (int r = 0; r < kXferRows; ++r)
+        if (r < ny) v[r] = __ldcs(f.src + (size_t)(y0 + r) * f.sstride + x);
+#pragma unroll
+      for (int r = 0; r < kXferRows; ++r)
+        if (r < ny) __stcs(f.dst + (size_t)(y0 + r) * f.dstride + x, v[r]);
+    }
   }
 }
 
 cudaError_t launch_xfer(const XferList &L, cudaStream_t st) {
   if (L.n <= 0) return cudaSuccess;
-  k_xfer<<<dim3(2 * 152 / L.n + 1, L.n), 256, 0, st>>>(L);
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int groups = (L.rows + kXferRows - 1) / kXferRows;
+  // about four blocks per SM over all fields
+  const int per_field = std::max(1, std::min(groups, 4 * sms / L.n));
+  k_xfer<<<dim3(per_field, L.n), kXferThreads, 0, st>>>(L);
   count_launches(1);
   return cudaGetLastError();
 }

@@ -32,6 +32,8 @@ namespace sns {
 
 static std::atomic<long long> g_launches{0};
 void count_launches(long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+static std::atomic<long long> g_allocs{0};
+void count_allocation() { g_allocs.fetch_add(1, std::memory_order_relaxed); }
 
 static thread_local std::string g_error;
 
@@ -85,6 +87,8 @@ struct PendingCorr {
   StageScalars s{};
 };
 
+constexpr int kFacSlots = 8;  // factor upload slots: more than one substage's uploads
+
 struct Context {
   const param_t *param = nullptr;
   int refs = 0;
@@ -97,9 +101,16 @@ struct Context {
   std::vector<double> dxf, dxc;  // host copies of the reference arrays (0-based)
   double *staging = nullptr;     // pinned, nx*ny doubles
   unsigned long long *red_host = nullptr;  // pinned, nx+1 words
-  // factors for the implicit solves: device buffer + host mirror
+  // factors for the implicit solves: device buffer, and a ring of pinned host
+  // staging slots so that the uploads are asynchronous; a slot is rewritten
+  // only after its previous upload completed (fac_ev)
   double *fac = nullptr;
   size_t fac_words = 0;
+  double *fac_host = nullptr;  // [kFacSlots][fac_words], pinned
+  cudaEvent_t fac_ev[kFacSlots] = {};
+  unsigned fac_next = 0;        // next slot of the ring
+  int fac_slot = 0;             // the slot being filled
+  double *fac_stage = nullptr;  // its host words
   double *diag = nullptr;  // block partials of sns_diagnostics
   // fused Poisson (+ temperature) launches: flag words, on unless disabled
   // or unsupported for this size
@@ -218,7 +229,7 @@ static TempExt *as_temp(const temperature_t *t) {
 template <typename T>
 static int dev_alloc(Context *c, T **p, size_t count) {
   void *ptr = nullptr;
-  cudaError_t e = cudaMalloc(&ptr, std::max<size_t>(count, 1) * sizeof(T));
+  cudaError_t e = counted_malloc(&ptr, std::max<size_t>(count, 1) * sizeof(T));
   if (e != cudaSuccess) return fail(SNS_ERR_OOM, "cudaMalloc(%zu bytes): %s", count * sizeof(T), cudaGetErrorString(e));
   c->allocs.push_back(ptr);
   *p = static_cast<T *>(ptr);
@@ -249,6 +260,9 @@ static void destroy_context(Context *c) {
   if (c->red_host) cudaFreeHost(c->red_host);
   if (c->fz_err_host) cudaFreeHost(c->fz_err_host);
   if (c->par_err_host) cudaFreeHost(c->par_err_host);
+  if (c->fac_host) cudaFreeHost(c->fac_host);
+  for (cudaEvent_t e : c->fac_ev)
+    if (e) cudaEventDestroy(e);
   if (c->ev_fwd) cudaEventDestroy(c->ev_fwd);
   if (c->ev_temp) cudaEventDestroy(c->ev_temp);
   if (c->side) cudaStreamDestroy(c->side);
@@ -344,8 +358,8 @@ static int build_context(Context *c, const param_t *param) {
   const std::vector<double> tw = twiddle_table(ny);
   if ((rc = upload(c, &g.tw, tw))) return rc;
   fft_layout(ny, &g.fft_nst, &g.fft_first2);
-  SNS_CUDA(cudaMallocHost(&c->staging, sizeof(double) * (size_t)nx * ny));
-  SNS_CUDA(cudaMallocHost(&c->red_host, sizeof(unsigned long long) * (size_t)(nx + 1)));
+  SNS_CUDA(counted_malloc_host(&c->staging, sizeof(double) * (size_t)nx * ny));
+  SNS_CUDA(counted_malloc_host(&c->red_host, sizeof(unsigned long long) * (size_t)(nx + 1)));
   return SNS_OK;
 }
 
@@ -507,10 +521,26 @@ static bool xfer_src(XferList &L, int nx, double *dev, const double *host, int i
   return true;
 }
 
+// one entry of a device -> host transfer list, as download / download_src lay it out
+static bool xfer_field_down(XferList &L, int nx, const double *dev, double *host, int width, int off, int first_x) {
+  double *a = dev_alias(host);
+  if (!a || L.n >= kXferMax) return false;
+  L.f[L.n++] = XferField{dev + first_x, a + width + off + first_x, nx, width, nx - first_x};
+  return true;
+}
+
+static bool xfer_src_down(XferList &L, int nx, const double *dev, double *host, int is_ux) {
+  double *a = dev_alias(host);
+  if (!a || L.n >= kXferMax) return false;
+  const int w = is_ux ? nx - 1 : nx, x0 = is_ux ? 1 : 0;
+  L.f[L.n++] = XferField{dev + x0, a, nx, w, w};
+  return true;
+}
+
 // pinned, zeroed host array (nullptr on failure)
 static double *host_array(size_t n) {
   void *p = nullptr;
-  if (cudaHostAlloc(&p, std::max<size_t>(n, 1) * sizeof(double), cudaHostAllocDefault) != cudaSuccess) return nullptr;
+  if (counted_malloc_host(&p, std::max<size_t>(n, 1) * sizeof(double)) != cudaSuccess) return nullptr;
   std::memset(p, 0, std::max<size_t>(n, 1) * sizeof(double));
   return static_cast<double *>(p);
 }
@@ -634,14 +664,22 @@ static void y_system(const param_t *param, int rk, int is_temp, HostFactors &sub
   den = (d[n - 1] + u[n - 1] * q1[0] + l[n - 1] * q1[n - 2]);
 }
 
+// copies n doubles at word offset `off` of the substage's pinned staging slot
+// into the device factor buffer (stream-ordered, asynchronous)
+static int stage_upload(Context *c, size_t off, const double *src, size_t n) {
+  std::memcpy(c->fac_stage + off, src, n * sizeof(double));
+  SNS_CUDA(cudaMemcpyAsync(c->fac + off, c->fac_stage + off, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  return SNS_OK;
+}
+
 // copies factor arrays into the context's device buffer at word offset `off`
 static int push_factors(Context *c, const HostFactors &hf, size_t off, LineFactors &lf) {
   const size_t n = hf.l.size();
-  std::vector<double> buf(3 * n, 0.0);
-  std::memcpy(&buf[0], hf.l.data(), n * sizeof(double));
-  std::memcpy(&buf[n], hf.inv.data(), n * sizeof(double));  // 0 marks |pivot| < DBL_EPSILON rows
-  std::memcpy(&buf[2 * n], hf.up.data(), n * sizeof(double));
-  SNS_CUDA(cudaMemcpyAsync(c->fac + off, buf.data(), buf.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  double *st = c->fac_stage + off;
+  std::memcpy(st, hf.l.data(), n * sizeof(double));
+  std::memcpy(st + n, hf.inv.data(), n * sizeof(double));  // 0 marks |pivot| < DBL_EPSILON rows
+  std::memcpy(st + 2 * n, hf.up.data(), n * sizeof(double));
+  SNS_CUDA(cudaMemcpyAsync(c->fac + off, st, 3 * n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   lf.n = (int)n;
   lf.l = c->fac + off;
   lf.inv = c->fac + off + n;
@@ -660,7 +698,27 @@ static int ensure_factor_buffer(Context *c) {
   const size_t need = std::max(4 * (size_t)(c->nx + 1) + 5 * (size_t)c->ny, yset_off(c, 2)) + 16;
   if (c->fac_words >= need) return SNS_OK;
   if (int rc = dev_alloc(c, &c->fac, need)) return rc;
+  if (c->fac_host) cudaFreeHost(c->fac_host);
+  c->fac_host = nullptr;
+  SNS_CUDA(counted_malloc_host(&c->fac_host, kFacSlots * need * sizeof(double)));
+  for (cudaEvent_t &e : c->fac_ev)
+    if (!e) SNS_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   c->fac_words = need;
+  return SNS_OK;
+}
+
+// the next pinned staging slot of the ring, once its previous upload ran (in
+// steady state long done: the ring spans more than a substage's uploads)
+static int begin_factor_uploads(Context *c) {
+  if (int rc = ensure_factor_buffer(c)) return rc;
+  c->fac_slot = (int)(c->fac_next++ % kFacSlots);
+  SNS_CUDA(cudaEventSynchronize(c->fac_ev[c->fac_slot]));
+  c->fac_stage = c->fac_host + (size_t)c->fac_slot * c->fac_words;
+  return SNS_OK;
+}
+
+static int end_factor_uploads(Context *c) {
+  SNS_CUDA(cudaEventRecord(c->fac_ev[c->fac_slot], c->stream));
   return SNS_OK;
 }
 
@@ -668,7 +726,9 @@ static int implicit_x(Context *c, const param_t *param, int rk, int kind, double
   HostFactors hf;
   x_system(param, rk, kind, hf);
   LineFactors lf{};
+  if (int rc = begin_factor_uploads(c)) return rc;
   if (int rc = push_factors(c, hf, 0, lf)) return rc;
+  if (int rc = end_factor_uploads(c)) return rc;
   Prof pf(c, K_SOLVE_X);
   SNS_CUDA(FORM(c, launch_solve_x)(c->g, lf, kind == 1 ? 1 : 0, q, c->stream));
   return SNS_OK;
@@ -680,9 +740,11 @@ static int implicit_y(Context *c, const param_t *param, int rk, int is_temp, int
   PeriodicFactors pf{};
   y_system(param, rk, is_temp, sub, q1, pf.l_last, pf.u_last, pf.den);
   const size_t off = 4 * (size_t)(c->nx + 1);
+  if (int rc = begin_factor_uploads(c)) return rc;
   if (int rc = push_factors(c, sub, off, pf.sub)) return rc;
   const size_t qoff = off + 4 * sub.l.size();
-  SNS_CUDA(cudaMemcpyAsync(c->fac + qoff, q1.data(), q1.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  if (int rc = stage_upload(c, qoff, q1.data(), q1.size())) return rc;
+  if (int rc = end_factor_uploads(c)) return rc;
   pf.q1 = c->fac + qoff;
   Prof pr(c, K_SOLVE_Y);
   SNS_CUDA(FORM(c, launch_solve_y)(c->g, pf, first_col, q, c->stream));
@@ -791,6 +853,8 @@ static int implicit_updates(const param_t *param, int rk, FluidExt *fe, TempExt 
   // fields: temperature (if coupled), ux, uy
   const int kinds[3] = {0, 1, 2};
   double *qs[3] = {with_t ? te->f.qt : nullptr, f.qx, f.qy};
+  if (impx || impy)
+    if (int rc = begin_factor_uploads(c)) return rc;
   if (impx) {
     SolveXSet set{};
     for (int k = with_t ? 0 : 1; k < 3; k++) {
@@ -814,8 +878,7 @@ static int implicit_updates(const param_t *param, int rk, FluidExt *fe, TempExt 
       const size_t off = yset_off(c, sys);
       if (int rc = push_factors(c, sub, off, pf.sub)) return rc;
       const size_t qoff = off + 3 * sub.l.size();
-      SNS_CUDA(cudaMemcpyAsync(c->fac + qoff, q1.data(), q1.size() * sizeof(double), cudaMemcpyHostToDevice,
-                               c->stream));
+      if (int rc = stage_upload(c, qoff, q1.data(), q1.size())) return rc;
       pf.q1 = c->fac + qoff;
       if (sys == 0) {
         set.f[set.n] = pf;
@@ -833,6 +896,8 @@ static int implicit_updates(const param_t *param, int rk, FluidExt *fe, TempExt 
     Prof pr(c, K_SOLVE_Y);
     SNS_CUDA(FORM(c, launch_solve_y_set)(c->g, set, c->stream));
   }
+  if (impx || impy)
+    if (int rc = end_factor_uploads(c)) return rc;
   {
     Prof pf(c, K_ADD_INC);
     if (with_t) SNS_CUDA(launch_add_increment(c->g, 0, te->f.t[te->cur], te->f.qt, te->f.t[out], c->stream));
@@ -932,7 +997,7 @@ static int parallel_prepare(Context *c) {
     return rc;
   if ((rc = dev_alloc(c, &c->par.err, (size_t)1))) return rc;
   SNS_CUDA(cudaMemset(c->par.err, 0, sizeof(unsigned)));
-  if (!c->par_err_host) SNS_CUDA(cudaMallocHost(&c->par_err_host, sizeof(unsigned)));
+  if (!c->par_err_host) SNS_CUDA(counted_malloc_host(&c->par_err_host, sizeof(unsigned)));
   *c->par_err_host = 0;
   c->par.stride = stride;
   c->par_ready = true;
@@ -950,7 +1015,7 @@ static int fused_prepare(Context *c) {
   SNS_CUDA(cudaMemsetAsync(c->fz.fwd_done, 0, sizeof(unsigned) * groups, c->stream));
   SNS_CUDA(cudaMemsetAsync(c->fz.bwd_cnt, 0, sizeof(unsigned long long) * spans, c->stream));
   SNS_CUDA(cudaMemsetAsync(c->fz.err, 0, sizeof(unsigned), c->stream));
-  if (!c->fz_err_host) SNS_CUDA(cudaMallocHost(&c->fz_err_host, sizeof(unsigned)));
+  if (!c->fz_err_host) SNS_CUDA(counted_malloc_host(&c->fz_err_host, sizeof(unsigned)));
   *c->fz_err_host = 0;
   c->fz.epoch = 0;
   c->fused_ready = true;
@@ -1141,6 +1206,7 @@ extern "C" {
 
 const char *sns_last_error(void) { return g_error.c_str(); }
 long long sns_kernel_launches(void) { return g_launches.load(); }
+long long sns_allocations(void) { return g_allocs.load(); }
 
 int sns_abi_layout(size_t *out, int n) {
   const size_t v[] = {sizeof(param_t),          offsetof(param_t, itot),    offsetof(param_t, dy),
@@ -1620,9 +1686,31 @@ static int sync_to_host_impl(const param_t *param, fluid_t *fluid, temperature_t
   if (fluid && !(fe = as_fluid(fluid))) return fail(SNS_ERR_ARG, "%s: foreign fluid_t", fn);
   if (temperature && !(te = as_temp(temperature))) return fail(SNS_ERR_ARG, "%s: foreign temperature_t", fn);
   // every copy is enqueued before one wait (a wait between the fluid and the
-  // temperature copies left the link idle meanwhile)
+  // temperature copies left the link idle meanwhile). Pinned host arrays are
+  // written in place by one copy kernel for all fields (strided 2D DMA of
+  // ~4 KB rows runs well below the link rate); others go through 2D DMA.
   int rc = SNS_OK;
+  const bool same = fe && te && fe->ctx == te->ctx;
+  XferList L{};
+  L.rows = ny;
+  bool direct = true;
   if (fe) {
+    fluid_t &h = fe->pub;
+    direct = xfer_field_down(L, nx, fe->f.ux, h.ux, nx + 1, 0, 1) && xfer_field_down(L, nx, fe->f.uy, h.uy, nx + 2, 1, 0) &&
+             xfer_field_down(L, nx, fe->f.p, h.p, nx + 2, 1, 0);
+    if (!state_only)
+      direct = direct && xfer_field_down(L, nx, fe->f.psi, h.psi, nx + 2, 1, 0) &&
+               xfer_src_down(L, nx, fe->f.aux, h.srcuxa, 1) && xfer_src_down(L, nx, fe->f.auy, h.srcuya, 0);
+  }
+  if (te) {
+    temperature_t &h = te->pub;
+    direct = direct && xfer_field_down(L, nx, te->f.t[te->cur], h.temp, nx + 2, 1, 0) &&
+             (state_only || xfer_src_down(L, nx, te->f.at, h.srctempa, 0));
+  }
+  direct = direct && (same || !fe || !te);
+  if (direct) {
+    if (L.n > 0) SNS_CUDA(launch_xfer(L, (fe ? fe->ctx : te->ctx)->stream));
+  } else if (fe) {
     Context *c = fe->ctx;
     fluid_t &h = fe->pub;
     if ((rc = download(c, fe->f.ux, h.ux, nx + 1, 0, 1)) || (rc = download(c, fe->f.uy, h.uy, nx + 2, 1, 0)) ||
@@ -1638,8 +1726,8 @@ static int sync_to_host_impl(const param_t *param, fluid_t *fluid, temperature_t
   if (te) {
     Context *c = te->ctx;
     temperature_t &h = te->pub;
-    if ((rc = download(c, te->f.t[te->cur], h.temp, nx + 2, 1, 0)) ||
-        (!state_only && (rc = download_src(c, te->f.at, h.srctempa, 0))))
+    if (!direct && ((rc = download(c, te->f.t[te->cur], h.temp, nx + 2, 1, 0)) ||
+                    (!state_only && (rc = download_src(c, te->f.at, h.srctempa, 0)))))
       return rc;
     snap = state_only ? -1 : te->snap;
     tf_alias = snap >= 0 ? dev_alias(h.tempforcex) : nullptr;
@@ -1855,11 +1943,18 @@ int sns_checkpoint(const param_t *param, const fluid_t *fluid, const temperature
   Context *c = fe->ctx;
   if (int rc = flush_pending(c)) return rc;
   if (c->ck_thread.joinable()) c->ck_thread.join();  // one checkpoint in flight per solver
+  if (c->ck_status != SNS_OK) {
+    // the previous checkpoint failed and nobody collected its error: report
+    // it now (once) instead of starting a new snapshot over it
+    const int rc = c->ck_status;
+    c->ck_status = SNS_OK;
+    return fail(rc, "sns_checkpoint: the previous checkpoint failed: %s", c->ck_error.c_str());
+  }
   const int nx = c->nx, ny = c->ny;
   const size_t cells = (size_t)nx * ny;
   if (!c->ck_dev) {
     if (int rc = dev_alloc(c, &c->ck_dev, 4 * cells)) return rc;
-    SNS_CUDA(cudaMallocHost(&c->ck_host, sizeof(double) * 4 * cells));
+    SNS_CUDA(counted_malloc_host(&c->ck_host, sizeof(double) * 4 * cells));
     SNS_CUDA(cudaStreamCreateWithFlags(&c->ck_stream, cudaStreamNonBlocking));
     SNS_CUDA(cudaEventCreateWithFlags(&c->ck_snap, cudaEventDisableTiming));
     SNS_CUDA(cudaEventCreateWithFlags(&c->ck_done, cudaEventDisableTiming));
@@ -1938,7 +2033,11 @@ int sns_checkpoint_wait(const fluid_t *fluid) {
   if (!fe) return fail(SNS_ERR_ARG, "sns_checkpoint_wait: bad argument");
   Context *c = fe->ctx;
   if (c->ck_thread.joinable()) c->ck_thread.join();
-  if (c->ck_status != SNS_OK) return fail(c->ck_status, "sns_checkpoint: %s", c->ck_error.c_str());
+  if (c->ck_status != SNS_OK) {
+    const int rc = c->ck_status;
+    c->ck_status = SNS_OK;  // reported once
+    return fail(rc, "sns_checkpoint: %s", c->ck_error.c_str());
+  }
   return SNS_OK;
 }
 
@@ -2059,7 +2158,7 @@ int statistics_collect(param_t *param, const parallel_t *parallel, const fluid_t
   if (!e->dev) {
     e->ctx = c;
     void *p = nullptr;
-    cudaError_t err = cudaMalloc(&p, sizeof(double) * words);
+    cudaError_t err = counted_malloc(&p, sizeof(double) * words);
     if (err != cudaSuccess) return fail(SNS_ERR_OOM, "statistics_collect: cudaMalloc: %s", cudaGetErrorString(err));
     e->dev = static_cast<double *>(p);
     SNS_CUDA(cudaMemsetAsync(e->dev, 0, sizeof(double) * words, c->stream));

@@ -93,3 +93,22 @@ def test_statistics_equal_the_reference_output(tmp_path):
         assert st.num == steps
         st.output_to(str(tmp_path / "stat"))
     same_files(tmp_path / "stat", os.path.join(HERE, "golden", "stat_rb_uniform_32x64"))
+
+
+def test_failed_checkpoint_is_reported_by_the_next_one(tmp_path):
+    """a checkpoint whose writer fails (its directory cannot be created: a
+    file stands in the path) is reported by the next sns_checkpoint, once;
+    the call after that writes normally"""
+    from simplenavierstokessolver_gb300 import SnsError
+
+    blocker = tmp_path / "not_a_dir"
+    blocker.write_text("a file where the checkpoint directory would go")
+    c, steps = golden_case()
+    with c:
+        c.run(steps)
+        c.checkpoint(str(blocker / "ck"))  # enqueued; the writer thread fails later
+        with pytest.raises(SnsError):
+            c.checkpoint(str(tmp_path / "good"))
+        c.checkpoint(str(tmp_path / "good"))
+        c.checkpoint_wait()
+    same_files(tmp_path / "good", GOLD)

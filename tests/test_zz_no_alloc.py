@@ -1,9 +1,16 @@
 """sns_diagnostics_static: the allocation-free diagnostics entry point.
 
+Some callers of this library cannot allocate: a thread that samples a run
+while its kernels are in flight (cudaMalloc and cudaFree may synchronise the
+device and stall the solver) and a process whose device memory is committed
+to a batch arena (an allocation there fails). This entry point serves them
+from a fixed scratch array in the library.
+
 Called through the C ABI and compared with sns_diagnostics on the same device
-state, twice in a row (the second call reuses the static scratch the first one
-looked up). The two entry points run the same compensated sums in the same
-order, so the tolerance below is far above what they may differ by.
+state, two calls in a row and once more after the state moved on: the two
+entry points run the same compensated sums in the same order, so their
+results are equal bit for bit. The library's allocation counter
+(sns_allocations) must not move across the calls.
 """
 import ctypes
 
@@ -11,8 +18,6 @@ import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
-
-RTOL = 1e-14
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -40,16 +45,20 @@ def test_static_scratch_matches_the_allocating_entry_point(cfg):
 
     with Case(**cfg) as c:
         c.run(20)
-        ref = _call(c, "sns_diagnostics")
+        ref = _call(c, "sns_diagnostics")  # its first call allocates its partials
+        allocs = c.lib.sns_allocations()
         first = _call(c, "sns_diagnostics_static")
         second = _call(c, "sns_diagnostics_static")
+        assert c.lib.sns_allocations() == allocs, "sns_diagnostics_static allocated"
         c.run(3)  # the state moves on: the scratch holds nothing stale
         ref2 = _call(c, "sns_diagnostics")
+        allocs = c.lib.sns_allocations()
         third = _call(c, "sns_diagnostics_static")
+        assert c.lib.sns_allocations() == allocs, "sns_diagnostics_static allocated"
     assert np.all(np.isfinite(ref)) and ref[8] > 1.0
     for got in (first, second):
-        np.testing.assert_allclose(got, ref, rtol=RTOL, atol=0.0)
-    np.testing.assert_allclose(third, ref2, rtol=RTOL, atol=0.0)
+        assert np.array_equal(got, ref), (got, ref)
+    assert np.array_equal(third, ref2), (third, ref2)
 
 
 def test_grids_beyond_the_scratch_are_rejected():
