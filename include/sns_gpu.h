@@ -341,7 +341,7 @@ extern int sns_set_fused(const fluid_t *fluid, int on);
  * multiply-adds (fewer FP64 instructions, shorter Crank-Nicolson chains).
  * Results differ from the reference's by rounding, held to 1e-12 relative L2
  * per field after the stated step counts. Needs itot a multiple of 32 in
- * [64, 3968] and a grid on which the mean mode's last Thomas pivot vanishes
+ * [64, 14048] and a grid on which the mean mode's last Thomas pivot vanishes
  * (uniform grids), otherwise SNS_ERR_UNSUPPORTED and the form is unchanged.
  * The first switch to it computes the factors (host, O(itot * jtot)) and
  * allocates them on the device. */

@@ -33,7 +33,7 @@
 namespace sns {
 namespace {
 
-constexpr int kParWarpsMax = 4;  // mode lines per block of the PCR kernel
+constexpr int kParWarpsMax = 8;  // mode lines per block of the PCR kernel
 constexpr size_t kParSmemMax = 220 * 1024;
 
 struct ParArgs {
@@ -136,23 +136,31 @@ __device__ __forceinline__ bool mbar_try(unsigned bar, unsigned parity) {
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 
+// rows per chunk of the segment sweeps: the next chunk's factors are loaded
+// while the current chunk is eliminated, off the dependent chain
+constexpr int kParChunk = 8;
+
 // src/fluid/compute_potential.c:109-136 by the partition method: one warp per
-// mode line. The warp's lane 0 moves the line (16 nx bytes) and its factor
-// block into shared memory with two bulk asynchronous copies (completion on
-// an mbarrier, bounded wait), the warp solves there and writes the line back
-// with coalesced stores. Real and imaginary parts see the same real matrix.
+// mode line. The warp's lane 0 moves the line (16 nx bytes) into shared
+// memory with a bulk asynchronous copy (completion on an mbarrier, bounded
+// wait), STAGED: also the mode's factor block; otherwise the factors are read
+// from global memory, coalesced by the interleaved row order, a chunk ahead.
+// The warp solves in shared memory and writes the line back with coalesced
+// stores. Real and imaginary parts see the same real matrix.
+template <bool STAGED>
 __global__ void __launch_bounds__(32 * kParWarpsMax) k_par_tri(const ParTriArgs a) {
   extern __shared__ __align__(128) unsigned char sm[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int J = blockIdx.x * (blockDim.x >> 5) + w;
   if (J >= a.nh) return;  // the whole warp
   const int n = a.nx, m = a.m;
-  const size_t per_warp = 16 * (size_t)n + 8 * a.stride;
+  const size_t per_warp = 16 * (size_t)n + (STAGED ? 8 * a.stride : 0);
   double2 *line = reinterpret_cast<double2 *>(sm + 128 + (size_t)w * per_warp);
-  double *f = reinterpret_cast<double *>(line + n);
+  double *fs = reinterpret_cast<double *>(line + n);
   double2 *gline = a.spec + (size_t)J * n;
+  const double *gfac = a.fac + (size_t)J * a.stride;
   const unsigned bar = smem_u32(reinterpret_cast<unsigned long long *>(sm) + w);
-  const unsigned line_bytes = 16u * (unsigned)n, fac_bytes = 8u * (unsigned)a.stride;
+  const unsigned line_bytes = 16u * (unsigned)n, fac_bytes = STAGED ? 8u * (unsigned)a.stride : 0u;
   if (lane == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -164,10 +172,32 @@ __global__ void __launch_bounds__(32 * kParWarpsMax) k_par_tri(const ParTriArgs 
                      smem_u32(line)),
                  "l"(__cvta_generic_to_global(gline)), "r"(line_bytes), "r"(bar)
                  : "memory");
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(f)),
-                 "l"(__cvta_generic_to_global(a.fac + (size_t)J * a.stride)), "r"(fac_bytes), "r"(bar)
-                 : "memory");
+    if (STAGED)
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                       smem_u32(fs)),
+                   "l"(__cvta_generic_to_global(gfac)), "r"(fac_bytes), "r"(bar)
+                   : "memory");
+  }
+  const double *f = STAGED ? fs : gfac;
+  auto ld = [&](const double *p) -> double {
+    if constexpr (STAGED) {
+      return *p;
+    } else {
+      return __ldg(p);
+    }
+  };
+  const double *inv = f, *gg = f + n, *up = f + 2 * n, *vv = f + 3 * n, *ww = f + 4 * n;
+  const double *alpha = f + 5 * n, *beta = alpha + kPartLevels * kPartSeg, *rD = beta + kPartLevels * kPartSeg;
+  // global form: the first chunk's factors while the copy lands
+  double ci[kParChunk], cg[kParChunk];
+  const double inv0 = STAGED ? 0.0 : ld(inv + lane);
+  if constexpr (!STAGED) {
+#pragma unroll
+    for (int k = 0; k < kParChunk; ++k) {
+      const int r = 1 + k, i = r * kPartSeg + lane;
+      ci[k] = r < m - 1 ? ld(inv + i) : 0.0;
+      cg[k] = r < m - 1 ? ld(gg + i) : 0.0;
+    }
   }
   __syncwarp();
   bool done = false;
@@ -181,36 +211,79 @@ __global__ void __launch_bounds__(32 * kParWarpsMax) k_par_tri(const ParTriArgs 
       }
     return;
   }
-  const double *inv = f, *gg = f + n, *up = f + 2 * n, *vv = f + 3 * n, *ww = f + 4 * n;
-  const double *alpha = f + 5 * n, *beta = alpha + kPartLevels * kPartSeg, *rD = beta + kPartLevels * kPartSeg;
+  if constexpr (STAGED) {
+#pragma unroll
+    for (int k = 0; k < kParChunk; ++k) {
+      const int r = 1 + k, i = r * kPartSeg + lane;
+      ci[k] = r < m - 1 ? ld(inv + i) : 0.0;
+      cg[k] = r < m - 1 ? ld(gg + i) : 0.0;
+    }
+  }
   // 1) the segment's interior rows r = 0 .. m-2 (line index r*32 + lane)
   //    with zero boundary values: forward elimination and back substitution.
   //    y_r = inv_r q_r - g_r y_{r-1} with g_r = a_r inv_r: one FMA per row on
   //    the dependent chain, the product inv_r q_r off it
   double2 y = line[lane];
-  y.x *= inv[lane];
-  y.y *= inv[lane];
+  {
+    const double i0 = STAGED ? ld(inv + lane) : inv0;
+    y.x *= i0;
+    y.y *= i0;
+  }
   line[lane] = y;
-#pragma unroll 4
-  for (int r = 1; r < m - 1; ++r) {
-    const int i = r * kPartSeg + lane;
-    double2 q = line[i];
-    const double iv = inv[i], g = gg[i];
-    q.x = fma(-g, y.x, iv * q.x);
-    q.y = fma(-g, y.y, iv * q.y);
-    line[i] = q;
-    y = q;
+#pragma unroll 1
+  for (int b = 1; b < m - 1; b += kParChunk) {
+    double ni[kParChunk], ng[kParChunk];
+#pragma unroll
+    for (int k = 0; k < kParChunk; ++k) {
+      const int r = b + kParChunk + k, i = r * kPartSeg + lane;
+      ni[k] = r < m - 1 ? ld(inv + i) : 0.0;
+      ng[k] = r < m - 1 ? ld(gg + i) : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < kParChunk; ++k) {
+      const int r = b + k, i = r * kPartSeg + lane;
+      if (r < m - 1) {
+        double2 q = line[i];
+        q.x = fma(-cg[k], y.x, ci[k] * q.x);
+        q.y = fma(-cg[k], y.y, ci[k] * q.y);
+        line[i] = q;
+        y = q;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kParChunk; ++k) {
+      ci[k] = ni[k];
+      cg[k] = ng[k];
+    }
   }
   const double2 ylast = y;  // row m-2
-#pragma unroll 4
-  for (int r = m - 3; r >= 0; --r) {
-    const int i = r * kPartSeg + lane;
-    double2 q = line[i];
-    const double u = up[i];
-    q.x = fma(-u, y.x, q.x);
-    q.y = fma(-u, y.y, q.y);
-    line[i] = q;
-    y = q;
+  double cu[kParChunk];
+#pragma unroll
+  for (int k = 0; k < kParChunk; ++k) {
+    const int r = m - 3 - k;
+    cu[k] = r >= 0 ? ld(up + r * kPartSeg + lane) : 0.0;
+  }
+#pragma unroll 1
+  for (int b = m - 3; b >= 0; b -= kParChunk) {
+    double nu[kParChunk];
+#pragma unroll
+    for (int k = 0; k < kParChunk; ++k) {
+      const int r = b - kParChunk - k;
+      nu[k] = r >= 0 ? ld(up + r * kPartSeg + lane) : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < kParChunk; ++k) {
+      const int r = b - k, i = r * kPartSeg + lane;
+      if (r >= 0) {
+        double2 q = line[i];
+        q.x = fma(-cu[k], y.x, q.x);
+        q.y = fma(-cu[k], y.y, q.y);
+        line[i] = q;
+        y = q;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kParChunk; ++k) cu[k] = nu[k];
   }
   // y: the first interior value (row 0). 2) right-hand side of the interface
   // row e: r_e - a_e y_{e-1} - c_e y'_0 (y'_0 of the next segment)
@@ -231,24 +304,37 @@ __global__ void __launch_bounds__(32 * kParWarpsMax) k_par_tri(const ParTriArgs 
     const int d = 1 << lev;
     const double mx = __shfl_up_sync(0xffffffffu, Rx, d), my = __shfl_up_sync(0xffffffffu, Ry, d);
     const double px = __shfl_down_sync(0xffffffffu, Rx, d), py = __shfl_down_sync(0xffffffffu, Ry, d);
-    const double al = alpha[lev * kPartSeg + lane], be = beta[lev * kPartSeg + lane];
+    const double al = ld(alpha + lev * kPartSeg + lane), be = ld(beta + lev * kPartSeg + lane);
     const double lmx = lane >= d ? mx : 0.0, lmy = lane >= d ? my : 0.0;
     const double lpx = lane + d < kPartSeg ? px : 0.0, lpy = lane + d < kPartSeg ? py : 0.0;
     Rx = fma(be, lpx, fma(al, lmx, Rx));
     Ry = fma(be, lpy, fma(al, lmy, Ry));
   }
-  const double xe_x = Rx * rD[lane], xe_y = Ry * rD[lane];
+  const double rd = ld(rD + lane);
+  const double xe_x = Rx * rd, xe_y = Ry * rd;
   line[ie] = make_double2(xe_x, xe_y);
   // 4) interiors from the spikes: x_i = y_i + v_i x_{e(k-1)} + w_i x_{e(k)}
   const double xl_x = __shfl_up_sync(0xffffffffu, xe_x, 1), xl_y = __shfl_up_sync(0xffffffffu, xe_y, 1);
   const double lx = lane > 0 ? xl_x : 0.0, ly = lane > 0 ? xl_y : 0.0;
-#pragma unroll 4
-  for (int r = 0; r < m - 1; ++r) {
-    const int i = r * kPartSeg + lane;
-    double2 q = line[i];
-    q.x = fma(ww[i], xe_x, fma(vv[i], lx, q.x));
-    q.y = fma(ww[i], xe_y, fma(vv[i], ly, q.y));
-    line[i] = q;
+#pragma unroll 1
+  for (int b = 0; b < m - 1; b += kParChunk) {
+    double cv[kParChunk], cw[kParChunk];
+#pragma unroll
+    for (int k = 0; k < kParChunk; ++k) {
+      const int r = b + k, i = r * kPartSeg + lane;
+      cv[k] = r < m - 1 ? ld(vv + i) : 0.0;
+      cw[k] = r < m - 1 ? ld(ww + i) : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < kParChunk; ++k) {
+      const int r = b + k, i = r * kPartSeg + lane;
+      if (r < m - 1) {
+        double2 q = line[i];
+        q.x = fma(cw[k], xe_x, fma(cv[k], lx, q.x));
+        q.y = fma(cw[k], xe_y, fma(cv[k], ly, q.y));
+        line[i] = q;
+      }
+    }
   }
   __syncwarp();
   for (int i = lane; i < n; i += 32) gline[i] = line[i];
@@ -266,16 +352,24 @@ int par_threads(const DevGrid &g, int cols) {
   return b <= 64 ? 64 : b >= 256 ? 256 : (b + 31) / 32 * 32;
 }
 
-int par_warps(int nx, size_t stride) {
-  const size_t per_warp = 16 * (size_t)nx + 8 * stride;
-  int w = (int)std::min<size_t>(kParWarpsMax, (kParSmemMax - 128) / per_warp);
-  return std::max(w, 0);
+// mode lines per block: enough blocks to spread over the SMs twice, and at
+// least two blocks per SM where the lines' shared memory allows it
+int par_warps(int nx, size_t per_warp, int nh) {
+  const size_t room = 2 * per_warp + 256 <= kParSmemMax ? kParSmemMax / 2 - 128 : kParSmemMax - 128;
+  const int by_smem = (int)std::min<size_t>(kParWarpsMax, room / per_warp);
+  const int spread = (nh + 2 * 152 - 1) / (2 * 152);
+  return std::max(0, std::min(by_smem, std::max(1, spread)));
 }
+
+// the factor block goes to shared memory along with the line when both fit
+// twice per SM (lines up to itot 1024: the copy engine brings them in one
+// go); longer lines read their factors from global memory a chunk ahead
+bool par_staged(int nx, size_t stride) { return 2 * (16 * (size_t)nx + 8 * stride) + 256 <= kParSmemMax; }
 
 }  // namespace
 
 bool parallel_tri_supported(int nx, int ny) {
-  return nx >= 2 * kPartSeg && nx % kPartSeg == 0 && ny >= 4 && par_warps(nx, partition_stride(nx) + nx) >= 1;
+  return nx >= 2 * kPartSeg && nx % kPartSeg == 0 && ny >= 4 && 16 * (size_t)nx + 128 <= kParSmemMax;
 }
 
 cudaError_t launch_par_fwd(const DevGrid &g, const StageScalars &s, const double *ux, const double *uy,
@@ -296,15 +390,22 @@ cudaError_t launch_par_fwd(const DevGrid &g, const StageScalars &s, const double
 cudaError_t launch_par_tri(const DevGrid &g, double2 *spec, const ParFactors &pf, cudaStream_t st) {
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_par_tri, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kParSmemMax);
+    cudaFuncSetAttribute(k_par_tri<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kParSmemMax);
+    cudaFuncSetAttribute(k_par_tri<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kParSmemMax);
     attr = true;
   }
-  const int wpb = par_warps(g.nx, pf.stride);
+  const bool staged = par_staged(g.nx, pf.stride);
+  const size_t per_warp = 16 * (size_t)g.nx + (staged ? 8 * pf.stride : 0);
+  const int wpb = par_warps(g.nx, per_warp, g.nh);
   if (wpb < 1) return cudaErrorInvalidValue;
   const ParTriArgs a{spec,  pf.fac, pf.lo, pf.hi, pf.stride, g.nx, g.nh, g.nx / kPartSeg, pf.err, pf.spin_limit,
                      pf.stale};
-  const size_t smem = 128 + (size_t)wpb * (16 * (size_t)g.nx + 8 * pf.stride);
-  k_par_tri<<<(g.nh + wpb - 1) / wpb, 32 * wpb, smem, st>>>(a);
+  const size_t smem = 128 + (size_t)wpb * per_warp;
+  if (staged) {
+    k_par_tri<true><<<(g.nh + wpb - 1) / wpb, 32 * wpb, smem, st>>>(a);
+  } else {
+    k_par_tri<false><<<(g.nh + wpb - 1) / wpb, 32 * wpb, smem, st>>>(a);
+  }
   count_launches(1);
   return cudaGetLastError();
 }

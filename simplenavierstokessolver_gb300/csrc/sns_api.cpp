@@ -951,7 +951,7 @@ static int parallel_prepare(Context *c) {
   if (c->par_ready) return SNS_OK;
   const int nx = c->nx, ny = c->ny, nh = c->g.nh;
   if (!parallel_tri_supported(nx, ny))
-    return fail(SNS_ERR_UNSUPPORTED, "parallel tridiagonal form: itot=%d must be a multiple of 32 in [64, 3968]", nx);
+    return fail(SNS_ERR_UNSUPPORTED, "parallel tridiagonal form: itot=%d must be a multiple of 32 in [64, 14048]", nx);
   const double *dxf = c->dxf.data(), *dxc = c->dxc.data();
   std::vector<double> l_raw(nx), u_raw(nx), a(nx), cc(nx);
   for (int i = 1; i <= nx; i++) {

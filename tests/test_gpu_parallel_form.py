@@ -48,10 +48,15 @@ def _errors(c, o):
     return {k: rel_l2(g[k], r[k]) for k in STATE}
 
 
-def test_poisson_solve_alone_matches_oracle():
+@pytest.mark.parametrize("nx,ny", [(256, 128), (64, 32), (2048, 64)], ids=["256x128", "64x32", "2048x64"])
+def test_poisson_solve_alone_matches_oracle(nx, ny):
     """one fluid_compute_potential on a seeded divergent velocity: psi
-    within round-off of the Thomas solution"""
-    cfg = Config(256, 128, ly=1.0, Ra=1e7, Pr=1.0)
+    within round-off of the Thomas solution (segments of 8, 2 and 64 rows;
+    itot 2048 reads its factors from global memory, the others stage them
+    in shared memory). The mean mode's line is the Neumann Laplacian, whose
+    condition number grows as itot^2: two solution methods differ by that
+    times the rounding, hence the bound (an indexing fault is O(1))."""
+    cfg = Config(nx, ny, ly=1.0, Ra=1e7, Pr=1.0)
     rng = np.random.default_rng(3)
     su, sc = (cfg.jtot + 2, cfg.itot + 1), (cfg.jtot + 2, cfg.itot + 2)
     state = (0.1 * rng.uniform(-1, 1, su), 0.1 * rng.uniform(-1, 1, sc), np.zeros(sc), rng.uniform(-0.5, 0.5, sc))
@@ -67,7 +72,7 @@ def test_poisson_solve_alone_matches_oracle():
             c.fluid_compute_potential(rk)
             o.call("fluid_compute_potential", rk)
             err = rel_l2(c.get_state()["psi"][1:-1, 1:-1], o.get_state()["psi"][1:-1, 1:-1])
-            assert err < 1e-13, (rk, err)
+            assert err < 1e-10, (rk, err)
 
 
 @pytest.mark.parametrize("nx,ny,Ra,steps", [(128, 256, 1e8, 1000), (512, 1024, 1e9, 2000)],
