@@ -559,11 +559,26 @@ def ensemble_throughput(args, torch, compensated=False):
         ms_default = timed()
         tuned_shapes, _ = b.autotune(steps=5)
         ms_b = timed()
+        # A/B: one persistent cooperative launch per substage (same shapes,
+        # same results) against the step graph of per-phase launches
+        persistent = None
+        try:
+            b.set_persistent(True)
+            b.step(args.warmup)
+            b.synchronize()
+            ms_p = timed()
+            persistent = {"value": cells * args.ens_steps / (ms_p * 1e-3), "vs_graph_of_phases": ms_b / ms_p,
+                          "launches_per_step": 4}
+        except Exception as err:  # noqa: BLE001 -- reported; the per-phase form stands
+            persistent = {"unavailable": str(err)}
+        finally:
+            b.set_persistent(False)
     batched = cells * args.ens_steps / (ms_b * 1e-3)
     batched_default = cells * args.ens_steps / (ms_default * 1e-3)
     if compensated:
         return {"cases": len(descs), "cells": cells, "batched_compensated": batched,
                 "batched_default_shapes": batched_default, "autotuned_shapes": tuned_shapes,
+                "persistent_substage": persistent,
                 "unit": "cell-steps/s", "batched_steps": args.ens_steps,
                 "hbm_roofline": hbm_roofline(batched, True)}
     plain_steps = max(2, args.ens_steps // 5)
@@ -580,28 +595,35 @@ def ensemble_throughput(args, torch, compensated=False):
     # stream with its first CFL dt kept fixed (no per-step host decision), the
     # Poisson solve as three kernels (the fused launch takes the whole GPU),
     # steps issued round-robin so that the cases' kernels overlap
-    cases = [Case(d.itot, d.jtot, ly=d.ly, Ra=d.Ra, Pr=d.Pr) for d in descs]
-    try:
-        for c in cases:
-            c.set_fused(False)
-            c.param_decide_dt()
-            c.integrate()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(plain_steps):
+    def concurrent(parallel_form):
+        cases = [Case(d.itot, d.jtot, ly=d.ly, Ra=d.Ra, Pr=d.Pr) for d in descs]
+        try:
             for c in cases:
+                c.set_fused(False)
+                c.set_form(parallel_form)
+                c.param_decide_dt()
                 c.integrate()
-        for c in cases:
-            c.synchronize()
-        conc_s = time.perf_counter() - t0
-    finally:
-        for c in cases:
-            c.close()
-    plain_concurrent = cells * plain_steps / conc_s
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(plain_steps):
+                for c in cases:
+                    c.integrate()
+            for c in cases:
+                c.synchronize()
+            return cells * plain_steps / (time.perf_counter() - t0)
+        finally:
+            for c in cases:
+                c.close()
+
+    plain_concurrent_exact = concurrent(False)
+    plain_concurrent_parallel = concurrent(True)
+    plain_concurrent = max(plain_concurrent_exact, plain_concurrent_parallel)
     return {"cases": len(descs), "cells": cells, "batched_fp32_stencil": batched,
             "batched_default_shapes": batched_default, "default_shapes": default_shapes,
-            "autotuned_shapes": tuned_shapes, "plain_fp64_one_by_one": plain,
+            "autotuned_shapes": tuned_shapes, "persistent_substage": persistent, "plain_fp64_one_by_one": plain,
             "plain_fp64_concurrent_streams": plain_concurrent,
+            "plain_fp64_concurrent_streams_exact_form": plain_concurrent_exact,
+            "plain_fp64_concurrent_streams_parallel_form": plain_concurrent_parallel,
             "ratio_vs_concurrent": batched / plain_concurrent,
             "ratio": batched / plain, "unit": "cell-steps/s", "batched_steps": args.ens_steps,
             "hbm_roofline": hbm_roofline(batched, False),
@@ -915,22 +937,40 @@ def gpu_arm(args, world, rank, local):
     h2d_full = sum(host[k].size * 8 for k in ("ux", "uy", "p", "psi", "temp", "srcuxa", "srcuya", "srctempa"))
     d2h_full = h2d_full + host["tempforcex"].size * 8
 
+    breakdown = {}
+
     def e2e_rate(step, state_only):
         up = case.sync_state_to_device if state_only else case.sync_to_device
         down = case.sync_state_to_host if state_only else case.sync_to_host
         torch.cuda.synchronize()
         barrier(world)
+        t = [0.0, 0.0, 0.0]
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
+            a = time.perf_counter()
             up()
+            b = time.perf_counter()
             step()
+            c = time.perf_counter()
             down()
-        return cells * e2e_steps * world / max_over_ranks(time.perf_counter() - t0, world)
+            d = time.perf_counter()
+            t[0] += b - a
+            t[1] += c - b
+            t[2] += d - c
+        total = time.perf_counter() - t0
+        breakdown[(state_only, step)] = {"to_device_ms": 1e3 * t[0] / e2e_steps, "step_ms": 1e3 * t[1] / e2e_steps,
+                                         "to_host_ms": 1e3 * t[2] / e2e_steps}
+        return cells * e2e_steps * world / max_over_ranks(total, world)
 
-    e2e_full = e2e_rate(lambda: case.run(1), False)
+    run1 = lambda: case.run(1)  # noqa: E731
+    e2e_full = e2e_rate(run1, False)
     e2e_calls = e2e_rate(lambda: case.run_calls(1), False)
-    e2e = {"value": e2e_rate(lambda: case.run(1), True), "unit": "cell-steps/s", "h2d_bytes_per_step": state_bytes,
+    e2e_value = e2e_rate(run1, True)
+    e2e = {"value": e2e_value, "unit": "cell-steps/s", "h2d_bytes_per_step": state_bytes,
            "d2h_bytes_per_step": state_bytes, "steps": e2e_steps,
+           "breakdown_host_wall": breakdown[(True, run1)],
+           "link_gbs": {"to_device": state_bytes / (breakdown[(True, run1)]["to_device_ms"] * 1e-3) / 1e9,
+                        "to_host": state_bytes / (breakdown[(True, run1)]["to_host_ms"] * 1e-3) / 1e9},
            "path": "sns_sync_state_to_device + sns_run(1) (param_decide_dt + 3 fused substages) "
                    "+ sns_sync_state_to_host",
            "all_host_arrays": {"value": e2e_full, "unit": "cell-steps/s", "h2d_bytes_per_step": h2d_full,

@@ -92,6 +92,17 @@ extern int sns_batch_case_status(sns_batch *batch, int slot, double *time, doubl
  * next step issue no copy so that every wait runs out: a test of the error
  * path that faults nothing. */
 extern int sns_batch_set_wait_limit(sns_batch *batch, unsigned polls, int stale);
+/* One persistent cooperative launch per RK substage (on != 0) instead of
+ * five per-phase launches; no counterpart in the reference. The launch's
+ * blocks are all resident, walk each phase's work list (stencil tiles,
+ * column groups, mode lines, correction tiles) and meet at a grid barrier
+ * between phases (a bounded wait: a barrier that gives up makes the next
+ * sns_batch_synchronize return SNS_ERR_STATE). The arithmetic per work item
+ * is the per-phase kernels', so results are identical either way; the step
+ * graph holds 4 launches instead of 16. Default off: measured against the
+ * per-phase launches on the 64-case ensemble (bench key
+ * ensemble_64.persistent_substage). */
+extern int sns_batch_set_persistent(sns_batch *batch, int on);
 /* number of resident cases; their slots written to slots[0..max) */
 extern int sns_batch_cases(const sns_batch *batch, int *slots, int max);
 /* cells summed over resident unfinished cases (the host knows every case's

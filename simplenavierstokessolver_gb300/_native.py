@@ -162,6 +162,7 @@ PROTOTYPES = {
     "sns_batch_step": (c_int, [c_void_p, c_int]),
     "sns_batch_synchronize": (c_int, [c_void_p]),
     "sns_batch_set_wait_limit": (c_int, [c_void_p, ctypes.c_uint, c_int]),
+    "sns_batch_set_persistent": (c_int, [c_void_p, c_int]),
     "sns_batch_stream": (c_void_p, [c_void_p]),
     "sns_batch_state": (c_int, [c_void_p, c_int, _PD, _PD, _PD, _PD, _PD]),
     "sns_batch_case_status": (c_int, [c_void_p, c_int, _PD, _PD, POINTER(c_longlong), POINTER(c_int)]),

@@ -138,6 +138,10 @@ class Batch:
         NaN or infinity (sns_batch_case_status returns SNS_ERR_NONFINITE)"""
         return status_of(self.h, slot)
 
+    def set_persistent(self, on: bool):
+        """one persistent cooperative launch per substage (identical results)"""
+        N.check(self.lib.sns_batch_set_persistent(self.h, int(on)), "sns_batch_set_persistent")
+
     def set_wait_limit(self, polls: int, stale: bool = False):
         N.check(self.lib.sns_batch_set_wait_limit(self.h, polls, int(stale)), "sns_batch_set_wait_limit")
 

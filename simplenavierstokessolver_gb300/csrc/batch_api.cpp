@@ -208,6 +208,10 @@ struct sns_batch {
   unsigned *h_err = nullptr;  // pinned
   unsigned tri_spin = 1u << 22;  // polls of that wait
   int tri_stale = 0;             // test of the error path: the next step issues no copy
+  // one persistent cooperative launch per substage instead of five per-phase
+  // launches (sns_batch_set_persistent): barrier words
+  bool persistent = false;
+  unsigned *d_bar = nullptr;  // [2] arrival count, generation
   std::mutex mu;
 };
 
@@ -278,6 +282,7 @@ static int rebuild(sns_batch *b) {
     if (h.used && !(h.d.steps > 0 && h.steps_done >= h.d.steps)) nmax = std::max(nmax, h.d.itot);
   int mpb = b->tune.modes_per_block;
   while (mpb > 1 && batch_tri_smem(nmax, mpb) > 200 * 1024) mpb /= 2;
+  if (b->persistent) mpb = std::min(mpb, 4);  // the persistent launch's four line slots per block
   for (int c = 0; c < b->max_cases; c++) {
     const CaseHost &h = b->hc[c];
     if (!h.used) continue;
@@ -326,10 +331,25 @@ static int rebuild(sns_batch *b) {
     b->graph = nullptr;
   }
   BCUDA(cudaStreamSynchronize(b->stream));
+  // persistent form: its shared memory and grid (every block resident)
+  size_t sub_smem = 0;
+  int sub_blocks = 0;
+  if (b->persistent) {
+    if (256 % tx)
+      return bfail(SNS_ERR_UNSUPPORTED, "persistent batch step: tile width %d does not divide 256", tx);
+    sub_smem = batch_substage_smem(b->fft_smem, nmax, mpb);
+    sub_blocks = batch_substage_blocks(sub_smem);
+    if (sub_blocks <= 0) return bfail(SNS_ERR_UNSUPPORTED, "persistent batch step: no cooperative grid fits");
+    b->graph_launches = 3 + 1;
+  }
   // one time step: three substages of five phases, then the per-case dt update
   BCUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   cudaError_t err = cudaSuccess;
-  for (int rk = 0; rk < 3 && err == cudaSuccess; rk++) {
+  for (int rk = 0; rk < 3 && err == cudaSuccess && b->persistent; rk++)
+    err = launch_batch_substage(b->d_cases, b->d_tiles, b->ntiles, b->ntiles_x2, b->d_cols, b->ncols, b->d_modes,
+                                b->nmodes, rk, tx, ty, mpb, nmax, sub_smem, b->d_err, b->tri_spin, b->d_bar,
+                                sub_blocks, b->stream);
+  for (int rk = 0; rk < 3 && err == cudaSuccess && !b->persistent; rk++) {
     if ((err = launch_batch_stencil(b->d_cases, b->d_tiles, b->ntiles, b->ntiles_x2, rk, tx, ty, b->stream)) !=
         cudaSuccess)
       break;
@@ -380,6 +400,8 @@ sns_batch *sns_batch_create(size_t hbm_bytes, int max_cases) {
       counted_malloc((void **)&b->d_cases, sizeof(BCase) * max_cases) != cudaSuccess ||
       counted_malloc((void **)&b->d_err, sizeof(unsigned)) != cudaSuccess ||
       cudaMemset(b->d_err, 0, sizeof(unsigned)) != cudaSuccess ||
+      counted_malloc((void **)&b->d_bar, 2 * sizeof(unsigned)) != cudaSuccess ||
+      cudaMemset(b->d_bar, 0, 2 * sizeof(unsigned)) != cudaSuccess ||
       counted_malloc_host((void **)&b->h_err, sizeof(unsigned)) != cudaSuccess ||
       cudaMemcpy(b->d_cases, b->table.data(), sizeof(BCase) * max_cases, cudaMemcpyHostToDevice) != cudaSuccess) {
     bfail(SNS_ERR_OOM, "sns_batch_create: %s", cudaGetErrorString(cudaGetLastError()));
@@ -402,6 +424,7 @@ int sns_batch_destroy(sns_batch *b) {
   cudaFree(b->d_cols);
   cudaFree(b->d_modes);
   cudaFree(b->d_err);
+  cudaFree(b->d_bar);
   if (b->h_err) cudaFreeHost(b->h_err);
   if (b->staging) cudaFreeHost(b->staging);
   cudaFree(b->diag);
@@ -896,9 +919,20 @@ int sns_batch_synchronize(sns_batch *b) {
   if (const unsigned e = *b->h_err) {
     *b->h_err = 0;
     BCUDA(cudaMemsetAsync(b->d_err, 0, sizeof(unsigned), b->stream));
-    return bfail(SNS_ERR_STATE, "batched tridiagonal solve: a bulk-copy wait gave up (code %u); results are invalid",
+    BCUDA(cudaMemsetAsync(b->d_bar, 0, 2 * sizeof(unsigned), b->stream));  // a barrier that gave up
+    return bfail(SNS_ERR_STATE,
+                 "batched step: a bounded wait gave up (code %u: 1 a tridiagonal bulk copy, 2 a persistent launch's "
+                 "grid barrier); results are invalid",
                  e);
   }
+  return SNS_OK;
+}
+
+int sns_batch_set_persistent(sns_batch *b, int on) {
+  if (!b) return bfail(SNS_ERR_ARG, "NULL batch");
+  std::lock_guard<std::mutex> lk(b->mu);
+  b->persistent = on != 0;
+  b->dirty = true;
   return SNS_OK;
 }
 

@@ -20,6 +20,7 @@
 // reduction across lanes (precomputed multipliers), and the interiors are
 // recovered from the precomputed spike vectors. The critical path is
 // nx/32 + 5 steps instead of nx.
+#include <algorithm>
 #include <cstdint>
 
 #include "batch_internal.h"
@@ -237,15 +238,9 @@ __global__ void __launch_bounds__(kBTileXMax) k_b_stencil_x2(const BCase *__rest
   stencil_x2(C, x, tile.y0, min(tile.y0 + rows, C.ny), rk);
 }
 
-__global__ void __launch_bounds__(kBTileXMax) k_b_stencil(const BCase *__restrict__ cases,
-                                                         const BTile *__restrict__ tiles, int rk, int rows) {
-  const BTile tile = tiles[blockIdx.x];
-  const BCase &C = cases[tile.c];
-  if (C.done) return;
+// the FP32 stencil of column x, rows y0 .. y1-1 (one thread)
+__device__ __forceinline__ void stencil_fp32(const BCase &C, int x, int y0, int y1, int rk) {
   const int nx = C.nx, ny = C.ny;
-  const int x = tile.x0 + threadIdx.x;
-  if (x >= nx) return;
-  const int y0 = tile.y0, y1 = min(y0 + rows, ny);
   const int pin = C.par ^ (rk & 1), pout = pin ^ 1;
   const float *__restrict__ ux = C.ux[pin];
   const float *__restrict__ uy = C.uy[pin];
@@ -363,16 +358,22 @@ __global__ void __launch_bounds__(kBTileXMax) k_b_stencil(const BCase *__restric
   }
 }
 
+__global__ void __launch_bounds__(kBTileXMax) k_b_stencil(const BCase *__restrict__ cases,
+                                                         const BTile *__restrict__ tiles, int rk, int rows) {
+  const BTile tile = tiles[blockIdx.x];
+  const BCase &C = cases[tile.c];
+  if (C.done) return;
+  const int x = tile.x0 + threadIdx.x;
+  if (x >= C.nx) return;
+  stencil_fp32(C, x, tile.y0, min(tile.y0 + rows, C.ny), rk);
+}
+
 // ------------------------------------------------------------------- Poisson
 // FP64 divergence of the FP32 predicted velocity (src/fluid/compute_potential.c:74-86)
 // and the forward real DFT along y of `fcols` columns.
-__global__ void __launch_bounds__(256) k_b_fwd(const BCase *__restrict__ cases, const BCols *__restrict__ cols,
-                                               int rk) {
-  extern __shared__ double2 zs[];
-  const BCols it = cols[blockIdx.x];
-  const BCase &C = cases[it.c];
-  if (C.done) return;
-  const int nx = C.nx, ny = C.ny, M = ny / 2, nc = C.fcols, x0 = it.x0;
+// the block's column group x0 .. x0+fcols-1 (every thread of the block)
+__device__ __forceinline__ void fwd_cols(const BCase &C, int x0, int rk, double2 *zs) {
+  const int nx = C.nx, ny = C.ny, M = ny / 2, nc = C.fcols;
   const int pu = C.par ^ (rk & 1) ^ 1;
   const float *__restrict__ ux = C.ux[pu];
   const float *__restrict__ uy = C.uy[pu];
@@ -411,13 +412,18 @@ __global__ void __launch_bounds__(256) k_b_fwd(const BCase *__restrict__ cases, 
   }
 }
 
-// inverse DFT and 1/jtot (src/fluid/compute_potential.c:146-157)
-__global__ void __launch_bounds__(256) k_b_bwd(const BCase *__restrict__ cases, const BCols *__restrict__ cols) {
+__global__ void __launch_bounds__(256) k_b_fwd(const BCase *__restrict__ cases, const BCols *__restrict__ cols,
+                                               int rk) {
   extern __shared__ double2 zs[];
   const BCols it = cols[blockIdx.x];
   const BCase &C = cases[it.c];
   if (C.done) return;
-  const int nx = C.nx, ny = C.ny, M = ny / 2, nc = C.fcols, x0 = it.x0;
+  fwd_cols(C, it.x0, rk, zs);
+}
+
+// inverse DFT and 1/jtot (src/fluid/compute_potential.c:146-157)
+__device__ __forceinline__ void bwd_cols(const BCase &C, int x0, double2 *zs) {
+  const int nx = C.nx, ny = C.ny, M = ny / 2, nc = C.fcols;
   const double2 *tw = reinterpret_cast<const double2 *>(C.tw);
   const int half = M / 2 + 1;
   for (int e = threadIdx.x; e < nc * half; e += blockDim.x) {
@@ -438,6 +444,14 @@ __global__ void __launch_bounds__(256) k_b_bwd(const BCase *__restrict__ cases, 
     const int c = e % nc, y = e / nc, x = x0 + c;
     if (x < nx) C.psi[(size_t)y * nx + x] = zd[2 * (c * M + (y >> 1)) + (y & 1)] * rny;
   }
+}
+
+__global__ void __launch_bounds__(256) k_b_bwd(const BCase *__restrict__ cases, const BCols *__restrict__ cols) {
+  extern __shared__ double2 zs[];
+  const BCols it = cols[blockIdx.x];
+  const BCase &C = cases[it.c];
+  if (C.done) return;
+  bwd_cols(C, it.x0, zs);
 }
 
 // Partition-method solve of the mode lines J = j0 .. j0+w-1 (one warp each).
@@ -466,16 +480,10 @@ __device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, unsigne
   return false;
 }
 
-__global__ void __launch_bounds__(32 * kBModesPerBlockMax) k_b_tri(const BCase *__restrict__ cases,
-                                                               const BModes *__restrict__ items, int nmax,
-                                                               unsigned *err, unsigned spin, int stale) {
-  extern __shared__ __align__(128) unsigned char tri_sm[];
-  const BModes it = items[blockIdx.x];
-  const BCase &C = cases[it.c];
-  if (C.done) return;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int J = it.j0 + w;
-  if (J >= C.nh) return;  // the whole warp
+// mode line J of case C by warp w of the block (its shared memory slot w)
+__device__ __forceinline__ void tri_line(const BCase &C, int J, int w, unsigned char *tri_sm, int nmax, unsigned *err,
+                                         unsigned spin, int stale) {
+  const int lane = threadIdx.x & 31;
   const int n = C.nx, m = C.seg;
   const int s = lane * m, e = s + m - 1;
   double2 *gline = C.spec + (size_t)J * n;
@@ -484,7 +492,11 @@ __global__ void __launch_bounds__(32 * kBModesPerBlockMax) k_b_tri(const BCase *
   double *f = reinterpret_cast<double *>(line + nmax);
   unsigned long long *bar = reinterpret_cast<unsigned long long *>(tri_sm) + w;
   const unsigned line_bytes = 16u * (unsigned)n, fac_bytes = 8u * (unsigned)C.pstride;
+  __syncwarp();
   if (lane == 0) {
+    // the slot's earlier generic reads and writes (a previous line, another
+    // phase of a persistent launch) before the bulk copies write it
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     const unsigned b = smem_addr(bar);
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -573,16 +585,28 @@ __global__ void __launch_bounds__(32 * kBModesPerBlockMax) k_b_tri(const BCase *
   }
   __syncwarp();
   for (int i = lane; i < n; i += 32) gline[i] = line[i];
+  __syncwarp();  // the slot may take the next line
+}
+
+__global__ void __launch_bounds__(32 * kBModesPerBlockMax) k_b_tri(const BCase *__restrict__ cases,
+                                                               const BModes *__restrict__ items, int nmax,
+                                                               unsigned *err, unsigned spin, int stale) {
+  extern __shared__ __align__(128) unsigned char tri_sm[];
+  const BModes it = items[blockIdx.x];
+  const BCase &C = cases[it.c];
+  if (C.done) return;
+  const int w = threadIdx.x >> 5;
+  const int J = it.j0 + w;
+  if (J >= C.nh) return;  // the whole warp
+  tri_line(C, J, w, tri_sm, nmax, err, spin, stale);
 }
 
 // ---------------------------------------------------- correction and pressure
-__global__ void __launch_bounds__(kBTileXMax) k_b_corr(BCase *__restrict__ cases, const BTile *__restrict__ tiles,
-                                                      int rk, int rows) {
-  const BTile tl = tiles[blockIdx.x];
-  BCase &C = cases[tl.c];
-  if (C.done) return;
+// correction and pressure of column tl.x0 + tx (tx < tile width); every lane
+// of the warp calls it for the same tile (warp reductions at the end)
+__device__ __forceinline__ void corr_col(BCase &C, const BTile tl, int tx, int rk, int rows) {
   const int nx = C.nx, ny = C.ny;
-  const int x = tl.x0 + threadIdx.x;
+  const int x = tl.x0 + tx;
   const bool live = x < nx;
   float mx = 0.f, my = 0.f;
   bool nf = false;  // a NaN or infinity among the values written
@@ -650,6 +674,131 @@ __global__ void __launch_bounds__(kBTileXMax) k_b_corr(BCase *__restrict__ cases
     if ((threadIdx.x & 31) == 0) {
       atomicMax(&C.umax[0], __float_as_uint(mx));
       atomicMax(&C.umax[1], __float_as_uint(my));
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kBTileXMax) k_b_corr(BCase *__restrict__ cases, const BTile *__restrict__ tiles,
+                                                      int rk, int rows) {
+  const BTile tl = tiles[blockIdx.x];
+  BCase &C = cases[tl.c];
+  if (C.done) return;
+  corr_col(C, tl, threadIdx.x, rk, rows);
+}
+
+// ---------------------------------------------- one persistent launch per substage
+// The five phases of a substage (stencils, forward DFT, tridiagonal, inverse
+// DFT, correction) in one cooperative launch: every block of the grid is
+// resident, walks each phase's work list with a grid stride, and the grid
+// meets at a barrier between phases. The arithmetic per work item is that of
+// the per-phase kernels above (the same device functions), so the results are
+// the same bits. The barrier is a counter and a generation word in global
+// memory; its wait is bounded: a block that gives up sets *err and goes on,
+// so a launch always ends (the host then reports SNS_ERR_STATE).
+constexpr unsigned kGridWaitSpins = 1u << 24;
+// warps of a block that take mode lines in the tridiagonal phase: shared
+// memory for four line slots leaves room for two blocks per SM
+constexpr int kSubTriWarps = 4;
+
+__device__ void grid_barrier(unsigned *count, unsigned *gen, unsigned *err) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned g = *reinterpret_cast<volatile unsigned *>(gen);
+    __threadfence();
+    if (atomicAdd(count, 1u) == gridDim.x - 1) {
+      atomicExch(count, 0u);
+      __threadfence();
+      atomicAdd(gen, 1u);
+    } else {
+      unsigned k = 0;
+      while (*reinterpret_cast<volatile unsigned *>(gen) == g && ++k < kGridWaitSpins) {
+      }
+      if (k >= kGridWaitSpins) atomicOr(err, 2u);
+    }
+    __threadfence();
+  }
+  __syncthreads();
+}
+
+struct SubstageArgs {
+  BCase *cases;
+  const BTile *tiles;
+  const BCols *cols;
+  const BModes *modes;
+  int ntiles, ntiles_x2, ncols, nmodes;
+  int rk, tile_x, rows, mpb, nmax;
+  unsigned *err;
+  unsigned spin;
+  unsigned *bar;  // [2]: arrival count, generation
+};
+
+__global__ void __launch_bounds__(256, 2) k_b_substage(const SubstageArgs a) {
+  extern __shared__ __align__(128) unsigned char sm[];
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  // 1) stencils: nthr / tile_x tiles per block at a time (FP32 tiles first,
+  //    then compensated ones)
+  {
+    const int per = nthr / a.tile_x;
+    for (int t0 = blockIdx.x * per; t0 < a.ntiles; t0 += gridDim.x * per) {
+      const int t = t0 + tid / a.tile_x;
+      if (t < a.ntiles) {
+        const BTile tile = a.tiles[t];
+        const BCase &C = a.cases[tile.c];
+        const int x = tile.x0 + tid % a.tile_x;
+        if (!C.done && x < C.nx) {
+          const int y1 = min(tile.y0 + a.rows, C.ny);
+          if (t >= a.ntiles - a.ntiles_x2) {
+            stencil_x2(C, x, tile.y0, y1, a.rk);
+          } else {
+            stencil_fp32(C, x, tile.y0, y1, a.rk);
+          }
+        }
+      }
+    }
+  }
+  grid_barrier(a.bar, a.bar + 1, a.err);
+  // 2) forward DFTs: one column group per block at a time
+  double2 *zs = reinterpret_cast<double2 *>(sm);
+  for (int i = blockIdx.x; i < a.ncols; i += gridDim.x) {
+    const BCols it = a.cols[i];
+    const BCase &C = a.cases[it.c];
+    if (!C.done) fwd_cols(C, it.x0, a.rk, zs);
+    __syncthreads();
+  }
+  grid_barrier(a.bar, a.bar + 1, a.err);
+  // 3) tridiagonal: warps of the block take mode lines (mpb per work item)
+  {
+    const int w = tid >> 5;
+    const int ipb = max(1, kSubTriWarps / a.mpb);
+    for (int b0 = blockIdx.x * ipb; b0 < a.nmodes; b0 += gridDim.x * ipb) {
+      const int item = b0 + w / a.mpb;
+      if (w < ipb * a.mpb && item < a.nmodes) {
+        const BModes it = a.modes[item];
+        const BCase &C = a.cases[it.c];
+        const int J = it.j0 + w % a.mpb;
+        if (!C.done && J < C.nh) tri_line(C, J, w, sm, a.nmax, a.err, a.spin, 0);
+      }
+    }
+  }
+  grid_barrier(a.bar, a.bar + 1, a.err);
+  // 4) inverse DFTs
+  for (int i = blockIdx.x; i < a.ncols; i += gridDim.x) {
+    const BCols it = a.cols[i];
+    const BCase &C = a.cases[it.c];
+    if (!C.done) bwd_cols(C, it.x0, zs);
+    __syncthreads();
+  }
+  grid_barrier(a.bar, a.bar + 1, a.err);
+  // 5) correction and pressure: whole warps per tile (tile_x is a multiple of 32)
+  {
+    const int per = nthr / a.tile_x;
+    for (int t0 = blockIdx.x * per; t0 < a.ntiles; t0 += gridDim.x * per) {
+      const int t = t0 + tid / a.tile_x;
+      if (t < a.ntiles) {
+        const BTile tile = a.tiles[t];
+        BCase &C = a.cases[tile.c];
+        if (!C.done) corr_col(C, tile, tid % a.tile_x, a.rk, a.rows);
+      }
     }
   }
 }
@@ -735,6 +884,34 @@ cudaError_t launch_batch_tri(const BCase *cases, const BModes *modes, int nmodes
   k_b_tri<<<nmodes, 32 * modes_per_block, batch_tri_smem(nmax, modes_per_block), st>>>(cases, modes, nmax, err, spin,
                                                                                       stale);
   return cudaGetLastError();
+}
+
+// shared memory of the persistent substage launch: the larger of the FFT
+// phases' column groups and the tridiagonal phase's line slots
+size_t batch_substage_smem(size_t fft_smem, int nmax, int mpb) {
+  const int slots = std::max(1, kSubTriWarps / mpb) * mpb;
+  return std::max(fft_smem, 128 + (size_t)slots * (48 * (size_t)nmax + 8 * (2 * kPcrLevels * kSeg + kSeg)));
+}
+
+cudaError_t launch_batch_substage(BCase *cases, const BTile *tiles, int ntiles, int ntiles_x2, const BCols *cols,
+                                  int ncols, const BModes *modes, int nmodes, int rk, int tile_x, int rows, int mpb,
+                                  int nmax, size_t smem, unsigned *err, unsigned spin, unsigned *bar, int blocks,
+                                  cudaStream_t st) {
+  SubstageArgs a{cases, tiles, cols, modes, ntiles, ntiles_x2, ncols, nmodes, rk, tile_x, rows, mpb, nmax,
+                 err, spin, bar};
+  void *args[] = {&a};
+  return cudaLaunchCooperativeKernel((const void *)k_b_substage, dim3(blocks), dim3(256), args, smem, st);
+}
+
+int batch_substage_blocks(size_t smem) {
+  int dev = 0, sms = 0, per = 0, coop = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) ||
+      cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) || !coop)
+    return 0;
+  if (cudaFuncSetAttribute(k_b_substage, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024) != cudaSuccess)
+    return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_b_substage, 256, smem) != cudaSuccess) return 0;
+  return per * sms;
 }
 
 cudaError_t launch_batch_corr(const BCase *cases, const BTile *tiles, int ntiles, int rk, int tile_x, int rows,

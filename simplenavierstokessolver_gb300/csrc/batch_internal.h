@@ -93,6 +93,14 @@ cudaError_t launch_batch_tri(const BCase *cases, const BModes *modes, int nmodes
                              unsigned *err, unsigned spin, int stale, cudaStream_t st);
 cudaError_t launch_batch_bwd(const BCase *cases, const BCols *cols, int ncols, size_t smem, int threads,
                              cudaStream_t st);
+// the five phases of substage rk in one persistent cooperative launch of
+// `blocks` blocks of 256 threads (batch_substage_blocks: every block resident)
+size_t batch_substage_smem(size_t fft_smem, int nmax, int mpb);
+int batch_substage_blocks(size_t smem);
+cudaError_t launch_batch_substage(BCase *cases, const BTile *tiles, int ntiles, int ntiles_x2, const BCols *cols,
+                                  int ncols, const BModes *modes, int nmodes, int rk, int tile_x, int rows, int mpb,
+                                  int nmax, size_t smem, unsigned *err, unsigned spin, unsigned *bar, int blocks,
+                                  cudaStream_t st);
 cudaError_t launch_batch_corr(const BCase *cases, const BTile *tiles, int ntiles, int rk, int tile_x, int rows,
                               cudaStream_t st);
 cudaError_t launch_batch_dt(BCase *cases, int ncases, const double *rk_a, const double *rk_b, cudaStream_t st);

@@ -370,3 +370,34 @@ def test_restart_from_a_plain_checkpoint(tmp_path):
     for k in ("ux", "uy", "temp"):  # FP64 values held as compensated FP32 pairs: ~2^-48 relative
         assert np.abs(got[k] - ref[k])[1:-1, 1:-1].max() <= 1e-13 * max(np.abs(ref[k]).max(), 1.0), k
     assert np.array_equal(got["p"][1:-1, 1:-1], ref["p"][1:-1, 1:-1])
+
+
+@pytest.mark.parametrize("shape", [dict(tile_x=64, tile_rows=8, modes_per_block=4, fcols_shift=0),
+                                   dict(tile_x=128, tile_rows=4, modes_per_block=2, fcols_shift=-1)],
+                         ids=["64x8_mpb4", "128x4_mpb2"])
+def test_persistent_substage_launch_gives_identical_results(shape):
+    """one persistent cooperative launch per substage (its blocks walk every
+    phase's work list, a grid barrier between phases) against the graph of
+    per-phase launches: the same device functions per work item, so the
+    same bits, for FP32 and compensated cases of several sizes"""
+    from simplenavierstokessolver_gb300.batch import Batch, Desc
+
+    descs = [Desc(64, 128, Ra=3e6, Pr=0.7, seed=1), Desc(128, 256, Ra=1e8, Pr=5.0, seed=2),
+             Desc(96, 64, ly=0.5, Ra=1e5, Pr=2.0, seed=3, stretch=4),
+             Desc(64, 64, ly=1.0, Ra=1e6, Pr=1.0, seed=4, compensated=True)]
+    results = []
+    for persistent in (False, True):
+        with Batch(1 << 30) as b:
+            slots = [b.add(d) for d in descs]
+            b.set_tuning(**shape)
+            b.set_persistent(persistent)
+            b.step(9)
+            b.synchronize()
+            results.append([b.state(s) for s in slots])
+            if persistent:
+                b.set_persistent(False)  # and back: the per-phase form continues
+                b.step(1)
+                b.synchronize()
+    for a, m in zip(results[0], results[1]):
+        for k in a:
+            assert np.array_equal(a[k], m[k]), k
