@@ -98,8 +98,9 @@ extern int sns_batch_set_wait_limit(sns_batch *batch, unsigned polls, int stale)
  * column groups, mode lines, correction tiles) and meet at a grid barrier
  * between phases (a bounded wait: a barrier that gives up makes the next
  * sns_batch_synchronize return SNS_ERR_STATE). The arithmetic per work item
- * is the per-phase kernels', so results are identical either way; the step
- * graph holds 4 launches instead of 16. Default off: measured against the
+ * is the per-phase kernels' (the same device functions; the compiler may
+ * pair multiply-adds differently, so FP32 results agree to their rounding);
+ * the step graph holds 4 launches instead of 16. Default off: measured against the
  * per-phase launches on the 64-case ensemble (bench key
  * ensemble_64.persistent_substage). */
 extern int sns_batch_set_persistent(sns_batch *batch, int on);

@@ -139,7 +139,7 @@ class Batch:
         return status_of(self.h, slot)
 
     def set_persistent(self, on: bool):
-        """one persistent cooperative launch per substage (identical results)"""
+        """one persistent cooperative launch per substage (the same arithmetic)"""
         N.check(self.lib.sns_batch_set_persistent(self.h, int(on)), "sns_batch_set_persistent")
 
     def set_wait_limit(self, polls: int, stale: bool = False):

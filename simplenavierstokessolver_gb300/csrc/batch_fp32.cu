@@ -691,8 +691,9 @@ __global__ void __launch_bounds__(kBTileXMax) k_b_corr(BCase *__restrict__ cases
 // DFT, correction) in one cooperative launch: every block of the grid is
 // resident, walks each phase's work list with a grid stride, and the grid
 // meets at a barrier between phases. The arithmetic per work item is that of
-// the per-phase kernels above (the same device functions), so the results are
-// the same bits. The barrier is a counter and a generation word in global
+// the per-phase kernels above (the same device functions; with contraction
+// on, the compiler may pair multiply-adds differently in this kernel, so FP32
+// results agree to their rounding, not bit for bit). The barrier is a counter and a generation word in global
 // memory; its wait is bounded: a block that gives up sets *err and goes on,
 // so a launch always ends (the host then reports SNS_ERR_STATE).
 constexpr unsigned kGridWaitSpins = 1u << 24;
