@@ -1503,6 +1503,102 @@ cudaError_t launch_xfer(const XferList &L, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// One entry (row j in 0..ny+1, column c in 0..W-1) of a reference-layout
+// array from the dense device field, boundary rules included; false for the
+// temperature's corners, which the reference's rules never write.
+__device__ __forceinline__ bool lin_entry(const LinField &f, int nx, int ny, int j, int c, double &v) {
+  const int jj = j == 0 ? ny : (j == ny + 1 ? 1 : j);  // periodic halo rows
+  const double *row = f.dev + (size_t)(jj - 1) * nx;
+  switch (f.kind) {
+    case LIN_UX:  // c = i - 1; walls i = 1 and i = itot+1 hold 0
+      v = (c == 0 || c == nx) ? 0.0 : row[c];
+      return true;
+    case LIN_UY:  // c = i; walls i = 0 and i = itot+1 hold 0
+      v = (c == 0 || c == nx + 1) ? 0.0 : row[c - 1];
+      return true;
+    case LIN_P:  // Neumann: p(0) = p(1), p(itot+1) = p(itot), halo rows included
+      v = row[min(max(c, 1), nx) - 1];
+      return true;
+    default:  // temperature: wall values on rows 1..jtot only
+      if (c == 0 || c == nx + 1) {
+        if (j == 0 || j == ny + 1) return false;
+        v = c == 0 ? kTempXm : kTempXp;
+        return true;
+      }
+      v = row[c - 1];
+      return true;
+  }
+}
+
+constexpr int kLinPairs = 4;  // 16-byte pairs in flight per thread
+
+__global__ void __launch_bounds__(256) k_lin(const LinList L, int to_host) {
+  const LinField f = L.f[blockIdx.y];
+  const int nx = L.nx, ny = L.ny, W = f.W;
+  const size_t pairs = (size_t)(ny + 2) * W / 2;  // (ny + 2) is even
+  const size_t stride = (size_t)gridDim.x * blockDim.x * kLinPairs;
+  double2 *host2 = reinterpret_cast<double2 *>(f.host);
+  for (size_t base = (size_t)blockIdx.x * blockDim.x * kLinPairs + threadIdx.x; base < pairs; base += stride) {
+    if (to_host) {
+#pragma unroll
+      for (int k = 0; k < kLinPairs; ++k) {
+        const size_t t = base + (size_t)k * blockDim.x;
+        if (t >= pairs) break;
+        const size_t e = 2 * t;
+        const int j0 = (int)(e / W), c0 = (int)(e - (size_t)j0 * W);
+        const int j1 = c0 + 1 == W ? j0 + 1 : j0, c1 = c0 + 1 == W ? 0 : c0 + 1;
+        double v0, v1;
+        const bool w0 = lin_entry(f, nx, ny, j0, c0, v0), w1 = lin_entry(f, nx, ny, j1, c1, v1);
+        if (w0 && w1) {
+          __stcs(host2 + t, make_double2(v0, v1));
+        } else {
+          if (w0) f.host[e] = v0;
+          if (w1) f.host[e + 1] = v1;
+        }
+      }
+    } else {
+      double2 v[kLinPairs];
+#pragma unroll
+      for (int k = 0; k < kLinPairs; ++k) {
+        const size_t t = base + (size_t)k * blockDim.x;
+        if (t < pairs) v[k] = __ldcs(host2 + t);
+      }
+#pragma unroll
+      for (int k = 0; k < kLinPairs; ++k) {
+        const size_t t = base + (size_t)k * blockDim.x;
+        if (t >= pairs) break;
+        const double vv[2] = {v[k].x, v[k].y};
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const size_t e = 2 * t + h;
+          const int j = (int)(e / W), c = (int)(e - (size_t)j * W);
+          if (j < 1 || j > ny) continue;
+          // interior columns: ux c = 1..itot-1 (device x = c; x = 0 is the
+          // wall i = 1, kept at 0), the others c = 1..itot (x = c - 1)
+          if (f.kind == LIN_UX) {
+            if (c >= 1 && c <= nx - 1) f.dev[(size_t)(j - 1) * nx + c] = vv[h];
+          } else if (c >= 1 && c <= nx) {
+            f.dev[(size_t)(j - 1) * nx + c - 1] = vv[h];
+          }
+        }
+      }
+    }
+  }
+}
+
+cudaError_t launch_lin(const LinList &L, int to_host, cudaStream_t st) {
+  if (L.n <= 0) return cudaSuccess;
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  size_t most = 0;
+  for (int k = 0; k < L.n; ++k) most = std::max(most, (size_t)(L.ny + 2) * L.f[k].W / 2);
+  const size_t per_block = 256 * (size_t)kLinPairs;
+  const int blocks = (int)std::max<size_t>(1, std::min<size_t>((most + per_block - 1) / per_block, 4 * sms / L.n));
+  k_lin<<<dim3(blocks, L.n), 256, 0, st>>>(L, to_host);
+  count_launches(1);
+  return cudaGetLastError();
+}
+
 // TEMPFORCEX(i, j) = 0.5*TEMP(i-1, j) + 0.5*TEMP(i, j), i = 2..itot
 __global__ void __launch_bounds__(256) k_tempforce(int nx, int ny, const double *t, double *out) {
   const size_t w = (size_t)nx - 1, total = w * ny;

@@ -505,14 +505,7 @@ static double *dev_alias(const double *h) {
   return static_cast<double *>(d);
 }
 
-// one entry of a host -> device transfer list, as upload_field / upload_src lay it out
-static bool xfer_field(XferList &L, int nx, double *dev, const double *host, int width, int off, int first_x) {
-  const double *a = dev_alias(host);
-  if (!a || L.n >= kXferMax) return false;
-  L.f[L.n++] = XferField{a + width + off + first_x, dev + first_x, width, nx, nx - first_x};
-  return true;
-}
-
+// one entry of a host -> device transfer list, as upload_src lays it out
 static bool xfer_src(XferList &L, int nx, double *dev, const double *host, int is_ux) {
   const double *a = dev_alias(host);
   if (!a || L.n >= kXferMax) return false;
@@ -521,19 +514,21 @@ static bool xfer_src(XferList &L, int nx, double *dev, const double *host, int i
   return true;
 }
 
-// one entry of a device -> host transfer list, as download / download_src lay it out
-static bool xfer_field_down(XferList &L, int nx, const double *dev, double *host, int width, int off, int first_x) {
-  double *a = dev_alias(host);
-  if (!a || L.n >= kXferMax) return false;
-  L.f[L.n++] = XferField{dev + first_x, a + width + off + first_x, nx, width, nx - first_x};
-  return true;
-}
-
+// one entry of a device -> host transfer list, as download_src lays it out
 static bool xfer_src_down(XferList &L, int nx, const double *dev, double *host, int is_ux) {
   double *a = dev_alias(host);
   if (!a || L.n >= kXferMax) return false;
   const int w = is_ux ? nx - 1 : nx, x0 = is_ux ? 1 : 0;
   L.f[L.n++] = XferField{dev + x0, a, nx, w, w};
+  return true;
+}
+
+// a reference-layout host array moved whole by the linear copy kernel: needs
+// the array pinned (a device alias) and 16-byte aligned
+static bool lin_field(LinList &L, double *dev, double *host, int W, int kind) {
+  double *a = dev_alias(host);
+  if (!a || (reinterpret_cast<uintptr_t>(a) & 15u) || L.n >= kXferMax) return false;
+  L.f[L.n++] = LinField{a, dev, W, kind};
   return true;
 }
 
@@ -1687,29 +1682,36 @@ static int sync_to_host_impl(const param_t *param, fluid_t *fluid, temperature_t
   if (temperature && !(te = as_temp(temperature))) return fail(SNS_ERR_ARG, "%s: foreign temperature_t", fn);
   // every copy is enqueued before one wait (a wait between the fluid and the
   // temperature copies left the link idle meanwhile). Pinned host arrays are
-  // written in place by one copy kernel for all fields (strided 2D DMA of
-  // ~4 KB rows runs well below the link rate); others go through 2D DMA.
+  // written in place by copy kernels: the reference-layout fields whole, in
+  // one linear pass of aligned 16-byte pairs with their halo and wall values
+  // (full cache lines on the link), the sources row by row; arrays that are
+  // not pinned go through 2D DMA.
   int rc = SNS_OK;
   const bool same = fe && te && fe->ctx == te->ctx;
+  LinList F{};
+  F.nx = nx;
+  F.ny = ny;
   XferList L{};
   L.rows = ny;
   bool direct = true;
   if (fe) {
     fluid_t &h = fe->pub;
-    direct = xfer_field_down(L, nx, fe->f.ux, h.ux, nx + 1, 0, 1) && xfer_field_down(L, nx, fe->f.uy, h.uy, nx + 2, 1, 0) &&
-             xfer_field_down(L, nx, fe->f.p, h.p, nx + 2, 1, 0);
+    direct = lin_field(F, fe->f.ux, h.ux, nx + 1, LIN_UX) && lin_field(F, fe->f.uy, h.uy, nx + 2, LIN_UY) &&
+             lin_field(F, fe->f.p, h.p, nx + 2, LIN_P);
     if (!state_only)
-      direct = direct && xfer_field_down(L, nx, fe->f.psi, h.psi, nx + 2, 1, 0) &&
+      direct = direct && lin_field(F, fe->f.psi, h.psi, nx + 2, LIN_P) &&
                xfer_src_down(L, nx, fe->f.aux, h.srcuxa, 1) && xfer_src_down(L, nx, fe->f.auy, h.srcuya, 0);
   }
   if (te) {
     temperature_t &h = te->pub;
-    direct = direct && xfer_field_down(L, nx, te->f.t[te->cur], h.temp, nx + 2, 1, 0) &&
+    direct = direct && lin_field(F, te->f.t[te->cur], h.temp, nx + 2, LIN_T) &&
              (state_only || xfer_src_down(L, nx, te->f.at, h.srctempa, 0));
   }
   direct = direct && (same || !fe || !te);
   if (direct) {
-    if (L.n > 0) SNS_CUDA(launch_xfer(L, (fe ? fe->ctx : te->ctx)->stream));
+    cudaStream_t st = (fe ? fe->ctx : te->ctx)->stream;
+    if (F.n > 0) SNS_CUDA(launch_lin(F, 1, st));
+    if (L.n > 0) SNS_CUDA(launch_xfer(L, st));
   } else if (fe) {
     Context *c = fe->ctx;
     fluid_t &h = fe->pub;
@@ -1739,7 +1741,8 @@ static int sync_to_host_impl(const param_t *param, fluid_t *fluid, temperature_t
   }
   if (fe) SNS_CUDA(cudaStreamSynchronize(fe->ctx->stream));
   if (te && (!fe || te->ctx != fe->ctx)) SNS_CUDA(cudaStreamSynchronize(te->ctx->stream));
-  if (fe) {
+  // the copy kernels wrote the halo and wall values; DMA copies leave them to the host
+  if (fe && !direct) {
     fluid_t &h = fe->pub;
     host_bc_ux(nx, ny, h.ux);
     host_bc_uy(nx, ny, h.uy);
@@ -1749,7 +1752,7 @@ static int sync_to_host_impl(const param_t *param, fluid_t *fluid, temperature_t
   if (te) {
     Context *c = te->ctx;
     temperature_t &h = te->pub;
-    host_bc_temp(nx, ny, h.temp);
+    if (!direct) host_bc_temp(nx, ny, h.temp);
     if (snap >= 0 && !tf_alias) {
       // tempforcex (src/temperature/force.c:17-23) from the snapshot buffer
       for (int j = 1; j <= ny; j++)
@@ -1788,26 +1791,34 @@ static int sync_to_device_impl(const param_t *param, fluid_t *fluid, temperature
   Context *c = fe ? fe->ctx : te ? te->ctx : nullptr;
   if (!c) return SNS_OK;
   c->version++;
+  // pinned host arrays are read in place by copy kernels: the
+  // reference-layout fields whole, in one linear pass of aligned 16-byte
+  // pairs (full cache lines on the link; only the interior is kept), the
+  // sources row by row
+  LinList F{};
+  F.nx = nx;
+  F.ny = c->ny;
   XferList L{};
   L.rows = c->ny;
   bool direct = true;
   if (fe) {
     const fluid_t &h = fe->pub;
-    direct = xfer_field(L, nx, fe->f.ux, h.ux, nx + 1, 0, 1) && xfer_field(L, nx, fe->f.uy, h.uy, nx + 2, 1, 0) &&
-             xfer_field(L, nx, fe->f.p, h.p, nx + 2, 1, 0);
+    direct = lin_field(F, fe->f.ux, h.ux, nx + 1, LIN_UX) && lin_field(F, fe->f.uy, h.uy, nx + 2, LIN_UY) &&
+             lin_field(F, fe->f.p, h.p, nx + 2, LIN_P);
     if (!state_only)
-      direct = direct && xfer_field(L, nx, fe->f.psi, h.psi, nx + 2, 1, 0) &&
+      direct = direct && lin_field(F, fe->f.psi, h.psi, nx + 2, LIN_P) &&
                xfer_src(L, nx, fe->f.aux, h.srcuxa, 1) && xfer_src(L, nx, fe->f.auy, h.srcuya, 0);
   }
   if (te) {
     te->cur = 0;
     te->snap = -2;
     const temperature_t &h = te->pub;
-    direct = direct && xfer_field(L, nx, te->f.t[0], h.temp, nx + 2, 1, 0) &&
+    direct = direct && lin_field(F, te->f.t[0], h.temp, nx + 2, LIN_T) &&
              (state_only || xfer_src(L, nx, te->f.at, h.srctempa, 0));
   }
   if (direct) {
-    SNS_CUDA(launch_xfer(L, c->stream));
+    if (F.n > 0) SNS_CUDA(launch_lin(F, 0, c->stream));
+    if (L.n > 0) SNS_CUDA(launch_xfer(L, c->stream));
   } else {
     int rc = SNS_OK;
     if (fe) {

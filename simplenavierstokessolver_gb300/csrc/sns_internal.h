@@ -123,6 +123,27 @@ struct XferList {
   XferField f[kXferMax];
   int n, rows;
 };
+// Whole reference-layout host arrays moved in one linear pass (pinned host
+// memory read or written in place through its device alias, 16-byte pairs of
+// elements, full cache lines on the link): `host` holds (ny+2) rows of W
+// entries, `dev` the dense ny x nx field. To the host every entry is written:
+// the interior from the device, halo rows and wall columns by the reference's
+// boundary rules of the field's kind (src/fluid/boundary_conditions.c:6-55,
+// src/temperature/boundary_conditions.c:6-21; the temperature's four corners,
+// which those rules leave alone, are not written). To the device only the
+// interior is read.
+enum LinKind { LIN_UX = 0, LIN_UY = 1, LIN_P = 2, LIN_T = 3 };
+struct LinField {
+  double *host;
+  double *dev;
+  int W;     // nx+1 (ux) or nx+2
+  int kind;  // LinKind
+};
+struct LinList {
+  LinField f[kXferMax];
+  int n, nx, ny;
+};
+
 // fused Poisson solve (+ explicit temperature update): device flag words,
 // sized by fused_layout, zeroed once; epoch advances by one per launch
 struct FusedState {
