@@ -66,6 +66,8 @@ KERNEL_MODEL = {
 
 
 # DRAM bytes (read + write) per launch from ncu captures of the default
+# workload; the parallel form's velocity update reads 16.8-25.2 MB per launch
+# (profiles/plain_parallel_fp64_counts_512x1024.md), as the exact form's does
 # workload (profiles/plain_fp64_fused_512x1024_ncu.md for the fused launch and
 # the velocity update, the three-kernel form's from an earlier capture of the
 # same size); keyed by kernel and size
@@ -79,6 +81,13 @@ PROFILED_TRAFFIC = {
     ("correct_and_pressure", 512, 1024): 16805376,
 }
 
+
+# FP64 instructions per cell of the parallel form's kernels on a uniform
+# power-of-two grid (DADD + DMUL + DFMA thread instructions counted by ncu at
+# 512 x 1024: profiles/plain_parallel_fp64_counts_512x1024.md; the DFT
+# counts grow with log2(jtot))
+PARALLEL_FP64_OPS = {"velocity_update": 47.5, "temperature_update": 17.0, "poisson_forward_fft": 23.5,
+                     "poisson_pcr": 5.4, "poisson_inverse_fft": 19.0, "correct_and_pressure": 9.0}
 
 # algorithmic DRAM bytes per cell of the plain path's implicit-scheme
 # launches (2048 x 4096 at Ra 1e10): each Crank-Nicolson launch solves the
@@ -848,6 +857,9 @@ def gpu_arm(args, world, rank, local):
         opc = fft_ops_per_cell(args.ny, False)
     if dom == "poisson_fused":
         opc = fft_ops_per_cell(args.ny, True) + fft_ops_per_cell(args.ny, False) + 5.0 + 27.0
+    measured_ops = form == "parallel" and (args.nx, args.ny) == (512, 1024) and dom in PARALLEL_FP64_OPS
+    if measured_ops:
+        opc = PARALLEL_FP64_OPS[dom]
     avg_s = kernels[dom]["avg_us"] * 1e-6
     achieved = bpc * cells / avg_s / 1e9 if bpc else None
     roofline = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -861,7 +873,9 @@ def gpu_arm(args, world, rank, local):
         ach = opc * cells / avg_s / 1e9
         fp64 = {"kernel": dom, "achieved": ach, "peak": fp64_peak, "unit": "Gop/s (FP64 instructions)",
                 "frac": ach / fp64_peak, "ops_per_cell": opc, "peak_source": fp64_source,
-                "ops_counted_for": "the exact form (the parallel form's contracted kernels issue fewer)"}
+                "ops_source": ("ncu instruction counts of the parallel form's kernel at 512x1024 "
+                               "(profiles/plain_parallel_fp64_counts_512x1024.md)") if measured_ops
+                else "counted from the exact form's kernels"}
     # the whole explicit step against the FP64 issue rate: FP64 operations per
     # cell-step from the kernels' counts (3 substages of temperature, velocity,
     # forward DFT, sweep, inverse DFT and correction)
@@ -870,6 +884,8 @@ def gpu_arm(args, world, rank, local):
     ops_step = 3 * (KERNEL_MODEL["temperature_update"][1] + KERNEL_MODEL[vel_model][1] +
                     fft_ops_per_cell(args.ny, True) + KERNEL_MODEL["poisson_tridiagonal"][1] +
                     fft_ops_per_cell(args.ny, False) + KERNEL_MODEL["correct_and_pressure"][1])
+    if form == "parallel" and (args.nx, args.ny) == (512, 1024):
+        ops_step = 3 * sum(PARALLEL_FP64_OPS.values())
     step_fp64 = {"form": form, "ops_per_cell_step": ops_step, "achieved": value * ops_step / 1e9, "peak": fp64_peak,
                  "unit": "Gop/s (FP64 instructions)", "frac": value * ops_step / 1e9 / fp64_peak,
                  "peak_source": fp64_source}
