@@ -1838,7 +1838,23 @@ static int sync_to_device_impl(const param_t *param, fluid_t *fluid, temperature
         return rc;
     }
   }
+  // the new velocity's max-|u| reduction and its copy to the host inside this
+  // call's wait: the next param_decide_dt / sns_run decides dt without a
+  // launch and a round trip of its own
+  if (fe) {
+    SNS_CUDA(cudaMemsetAsync(fe->f.colmax, 0, sizeof(unsigned long long) * (c->nx + 1), c->stream));
+    {
+      Prof pf(c, K_UMAX);
+      SNS_CUDA(launch_umax(c->g, fe->f.ux, fe->f.uy, fe->f.colmax, fe->f.uymax, c->stream));
+    }
+    SNS_CUDA(cudaMemcpyAsync(c->red_host, fe->f.colmax, sizeof(unsigned long long) * (c->nx + 1),
+                             cudaMemcpyDeviceToHost, c->stream));
+  }
   SNS_CUDA(cudaStreamSynchronize(c->stream));
+  if (fe) {
+    c->red_version = c->version;
+    c->red_host_version = c->version;
+  }
   return SNS_OK;
 }
 
