@@ -42,26 +42,26 @@ struct ParArgs {
   const double *ux, *uy;
   double2 *spec;  // [nh][nx], interleaved rows
   double *psi;
-  int cols;       // line positions per block of the DFT kernels
+  int cols;       // adjacent x columns per block of the DFT kernels
   int m;          // rows per segment, nx / 32
 };
 
-// x of line position p (p = (x % m) * 32 + x / m)
-__device__ __forceinline__ int par_x(int p, int m) { return (p % kPartSeg) * m + p / kPartSeg; }
+// line position of column x (rows of a mode line interleaved by segment)
+__device__ __forceinline__ int par_p(int x, int m) { return (x % m) * kPartSeg + x / m; }
 
 // src/fluid/compute_potential.c:69-92: (div u*)/(gamma dt) and its real DFT
-// along y, for the columns at line positions p0 .. p0+cols-1
+// along y, for the adjacent columns x0 .. x0+cols-1 (coalesced reads of the
+// velocity); each column's spectrum goes to its line position
 __global__ void __launch_bounds__(256) k_par_fwd(const ParArgs a) {
   extern __shared__ double2 z[];
   const int nx = a.g.nx, ny = a.g.ny, M = ny / 2, C = a.cols;
-  const int p0 = blockIdx.x * C;
+  const int x0 = blockIdx.x * C;
   double *zd = reinterpret_cast<double *>(z);
   const double rdy = a.g.rdy, rgdt = a.s.rgdt;
   for (int e = threadIdx.x; e < C * ny; e += blockDim.x) {
-    const int c = e % C, y = e / C, p = p0 + c;
+    const int c = e % C, y = e / C, x = x0 + c;
     double d = 0.0;
-    if (p < nx) {
-      const int x = par_x(p, a.m);
+    if (x < nx) {
       const size_t r = (size_t)y * nx + x;
       const double uxm = a.ux[r];
       const double uxp = x == nx - 1 ? 0.0 : a.ux[r + 1];
@@ -76,8 +76,8 @@ __global__ void __launch_bounds__(256) k_par_fwd(const ParArgs a) {
   fft::fft_stages<true>(z, C, M, ny, a.g.fft_nst, a.g.fft_first2, tw);
   const int half = M / 2 + 1;
   for (int e = threadIdx.x; e < C * half; e += blockDim.x) {
-    const int c = e % C, k = e / C, p = p0 + c;
-    if (p < nx) fft::rfft_post(z + c * M, a.spec + p, M, k, tw, (size_t)nx);
+    const int c = e % C, k = e / C, x = x0 + c;
+    if (x < nx) fft::rfft_post(z + c * M, a.spec + par_p(x, a.m), M, k, tw, (size_t)nx);
   }
 }
 
@@ -85,26 +85,26 @@ __global__ void __launch_bounds__(256) k_par_fwd(const ParArgs a) {
 __global__ void __launch_bounds__(256) k_par_bwd(const ParArgs a) {
   extern __shared__ double2 z[];
   const int nx = a.g.nx, ny = a.g.ny, M = ny / 2, C = a.cols;
-  const int p0 = blockIdx.x * C;
+  const int x0 = blockIdx.x * C;
   const double2 *tw = reinterpret_cast<const double2 *>(a.g.tw);
   const int half = M / 2 + 1;
   for (int e = threadIdx.x; e < C * half; e += blockDim.x) {
-    const int c = e % C, k = e / C, p = p0 + c;
+    const int c = e % C, k = e / C, x = x0 + c;
     double2 *zc = z + c * M;
-    if (p >= nx) {
+    if (x >= nx) {
       zc[fft::fft_slot(k, M, a.g.fft_nst, a.g.fft_first2)] = make_double2(0.0, 0.0);
       if (k > 0) zc[fft::fft_slot(M - k, M, a.g.fft_nst, a.g.fft_first2)] = make_double2(0.0, 0.0);
       continue;
     }
-    fft::rfft_pre(a.spec + p, zc, M, k, tw, a.g.fft_nst, a.g.fft_first2, (size_t)nx);
+    fft::rfft_pre(a.spec + par_p(x, a.m), zc, M, k, tw, a.g.fft_nst, a.g.fft_first2, (size_t)nx);
   }
   __syncthreads();
   fft::fft_stages<false>(z, C, M, ny, a.g.fft_nst, a.g.fft_first2, tw);
   const double *zd = reinterpret_cast<const double *>(z);
   for (int e = threadIdx.x; e < C * ny; e += blockDim.x) {
-    const int c = e % C, y = e / C, p = p0 + c;
-    if (p >= nx) continue;
-    a.psi[(size_t)y * nx + par_x(p, a.m)] = zd[2 * (c * M + (y >> 1)) + (y & 1)] * a.s.rny;
+    const int c = e % C, y = e / C, x = x0 + c;
+    if (x >= nx) continue;
+    a.psi[(size_t)y * nx + x] = zd[2 * (c * M + (y >> 1)) + (y & 1)] * a.s.rny;
   }
 }
 
@@ -340,10 +340,12 @@ __global__ void __launch_bounds__(32 * kParWarpsMax) k_par_tri(const ParTriArgs 
   for (int i = lane; i < n; i += 32) gline[i] = line[i];
 }
 
+// adjacent columns per block of the DFT kernels: kParCols (whole 32-byte
+// sectors of the velocity rows at 4) where the shared memory allows it
+constexpr int kParCols = 4;
 int par_cols(const DevGrid &g) {
-  // enough blocks to cover the SMs at least twice, at most 64 KiB of shared memory each
-  int c = 1;
-  while (c < 16 && (size_t)(2 * c) * g.ny * sizeof(double) <= 65536 && g.nx / (2 * c) >= 304) c *= 2;
+  int c = kParCols;
+  while (c > 1 && (size_t)c * g.ny * sizeof(double) > 128 * 1024) c /= 2;
   return c;
 }
 

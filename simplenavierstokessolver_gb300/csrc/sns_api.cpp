@@ -275,8 +275,13 @@ static int build_context(Context *c, const param_t *param) {
   c->param = param;
   c->nx = nx;
   c->ny = ny;
-  SNS_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-  SNS_CUDA(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+  // the side stream carries the temperature update beside the Poisson
+  // kernels (off the critical path); the main stream's blocks are scheduled
+  // first when both have work waiting
+  int prio_least = 0, prio_greatest = 0;
+  SNS_CUDA(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest));
+  SNS_CUDA(cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, prio_greatest));
+  SNS_CUDA(cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, prio_least));
   SNS_CUDA(cudaEventCreateWithFlags(&c->ev_fwd, cudaEventDisableTiming));
   SNS_CUDA(cudaEventCreateWithFlags(&c->ev_temp, cudaEventDisableTiming));
   c->dxf.assign(param->dxf, param->dxf + nx);
