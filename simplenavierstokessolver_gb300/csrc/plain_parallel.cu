@@ -340,9 +340,11 @@ __global__ void __launch_bounds__(32 * kParWarpsMax) k_par_tri(const ParTriArgs 
   for (int i = lane; i < n; i += 32) gline[i] = line[i];
 }
 
-// adjacent columns per block of the DFT kernels: kParCols (whole 32-byte
-// sectors of the velocity rows at 4) where the shared memory allows it
-constexpr int kParCols = 4;
+// adjacent columns per block of the DFT kernels, where the shared memory
+// allows it. Measured at 512 x 1024 (parallel-form step, CUDA events): 1, 2,
+// 4 and 8 columns 0.513, 0.511, 0.538 and 0.724 ms per step: whole sectors
+// of the velocity rows (4 and more) cost more in blocks per SM than they save
+constexpr int kParCols = 2;
 int par_cols(const DevGrid &g) {
   int c = kParCols;
   while (c > 1 && (size_t)c * g.ny * sizeof(double) > 128 * 1024) c /= 2;
