@@ -398,7 +398,7 @@ def large_instance(args, torch, nx=2048, ny=4096, Ra=1e10, steps=500, acc_steps=
                 schemes.append((dd["implicitx"], dd["implicity"]))
             c.synchronize()
             per = np.array([a.elapsed_time(b) for a, b in ev])
-            imp = np.array([x or y for x, y in schemes])
+            imp = np.array([bool(x or y) for x, y in schemes], dtype=bool)
             ms = float(per.sum())
             d = c.get_dt()
             sim = d["time"] - t0
