@@ -115,24 +115,28 @@ constexpr int kPartLevels = 5;  // log2(kPartSeg)
 // doubles per line of the factor block written by partition_factors
 inline size_t partition_stride(int n) { return 4 * (size_t)n + 2 * kPartLevels * kPartSeg + kPartSeg; }
 
-// Factors of one line: sub-diagonal a_i (a_0 = 0), super-diagonal c_i
-// (c_{n-1} = 0), diagonal d_i = -l_raw_i - u_raw_i + eig with the Poisson
-// lines' Neumann closure (src/fluid/compute_potential.c:116-127: the first
-// and last diagonal entries absorb l_raw_0 and u_raw_{n-1}). pin_last: the
-// singular mean mode, whose last unknown the reference's Thomas solve sets
-// to zero (its last pivot vanishes, src/linalg.c:36-38). Output (doubles):
-// inv[n] up[n] v[n] w[n] (interior Thomas factors and spikes by row)
-// alpha[kPartLevels][kPartSeg] beta[kPartLevels][kPartSeg] rD[kPartSeg].
+// Factors of one line of n rows with sub-diagonal a_i, diagonal d_i and
+// super-diagonal c_i. periodic: row 0 couples to row n-1 through a_0 and row
+// n-1 to row 0 through c_{n-1}, so the interface system is cyclic (lane k
+// couples to lanes k -+ 2^lev modulo kPartSeg at every level; after the last
+// level both couplings fold into the diagonal); otherwise a_0 and c_{n-1} are
+// ignored and the couplings past either end are zero. pin_last: the singular
+// mean mode of the Poisson lines, whose last unknown the reference's Thomas
+// solve sets to zero (its last pivot vanishes, src/linalg.c:36-38). Output
+// (doubles): inv[n] up[n] v[n] w[n] (interior Thomas factors and spikes by
+// row) alpha[kPartLevels][kPartSeg] beta[kPartLevels][kPartSeg] rD[kPartSeg].
 // interleave: the four row arrays hold row k m + r at index r kPartSeg + k,
 // so that the 32 lanes, each walking its own segment, touch 32 consecutive
 // words at every step.
-inline void partition_factors(int n, const double *a, const double *c, const double *l_raw, const double *u_raw,
-                              double eig, bool pin_last, bool interleave, double *out) {
+inline void partition_factors_tri(int n, const double *a_in, const double *d, const double *c_in, bool periodic,
+                                  bool pin_last, bool interleave, double *out) {
   const int m = n / kPartSeg;
-  std::vector<double> d(n), inv(n, 0.0), up(n, 0.0), v(n, 0.0), w(n, 0.0);
-  for (int i = 0; i < n; i++) d[i] = -l_raw[i] - u_raw[i] + eig;
-  d[0] += l_raw[0];
-  d[n - 1] += u_raw[n - 1];
+  std::vector<double> a(a_in, a_in + n), c(c_in, c_in + n);
+  if (!periodic) {
+    a[0] = 0.0;
+    c[n - 1] = 0.0;
+  }
+  std::vector<double> inv(n, 0.0), up(n, 0.0), v(n, 0.0), w(n, 0.0);
   double *alpha = out + 4 * (size_t)n, *beta = alpha + kPartLevels * kPartSeg, *rD = beta + kPartLevels * kPartSeg;
   std::vector<double> L(kPartSeg), D(kPartSeg), U(kPartSeg);
   for (int k = 0; k < kPartSeg; k++) {
@@ -165,8 +169,8 @@ inline void partition_factors(int n, const double *a, const double *c, const dou
     L[k] = ae * v[e - 1];
     D[k] = ae * w[e - 1] + d[e];
     U[k] = 0.0;
-    if (k < kPartSeg - 1) {
-      const int s1 = s + m;
+    if (periodic || k < kPartSeg - 1) {
+      const int s1 = (s + m) % n;  // the next segment's first interior row
       D[k] += ce * v[s1];
       U[k] = ce * w[s1];
     }
@@ -180,19 +184,22 @@ inline void partition_factors(int n, const double *a, const double *c, const dou
     const int dd = 1 << lev;
     std::vector<double> L2(kPartSeg), D2(kPartSeg), U2(kPartSeg);
     for (int k = 0; k < kPartSeg; k++) {
-      const double al = k - dd >= 0 ? -L[k] / D[k - dd] : 0.0;
-      const double be = k + dd < kPartSeg ? -U[k] / D[k + dd] : 0.0;
+      const bool has_m = periodic || k - dd >= 0, has_p = periodic || k + dd < kPartSeg;
+      const int km = (k - dd + kPartSeg) % kPartSeg, kp = (k + dd) % kPartSeg;
+      const double al = has_m ? -L[k] / D[km] : 0.0;
+      const double be = has_p ? -U[k] / D[kp] : 0.0;
       alpha[lev * kPartSeg + k] = al;
       beta[lev * kPartSeg + k] = be;
-      L2[k] = k - dd >= 0 ? al * L[k - dd] : 0.0;
-      U2[k] = k + dd < kPartSeg ? be * U[k + dd] : 0.0;
-      D2[k] = D[k] + (k - dd >= 0 ? al * U[k - dd] : 0.0) + (k + dd < kPartSeg ? be * L[k + dd] : 0.0);
+      L2[k] = has_m ? al * L[km] : 0.0;
+      U2[k] = has_p ? be * U[kp] : 0.0;
+      D2[k] = D[k] + (has_m ? al * U[km] : 0.0) + (has_p ? be * L[kp] : 0.0);
     }
     L = L2;
     D = D2;
     U = U2;
   }
-  for (int k = 0; k < kPartSeg; k++) rD[k] = 1.0 / D[k];
+  // cyclic: the last level leaves L and U on the unknown itself
+  for (int k = 0; k < kPartSeg; k++) rD[k] = periodic ? 1.0 / (D[k] + L[k] + U[k]) : 1.0 / D[k];
   for (int i = 0; i < n; i++) {
     const size_t o = interleave ? (size_t)(i % m) * kPartSeg + i / m : (size_t)i;
     out[o] = inv[i];
@@ -200,6 +207,18 @@ inline void partition_factors(int n, const double *a, const double *c, const dou
     out[2 * (size_t)n + o] = v[i];
     out[3 * (size_t)n + o] = w[i];
   }
+}
+
+// The Poisson lines: diagonal d_i = -l_raw_i - u_raw_i + eig with the
+// Neumann closure (src/fluid/compute_potential.c:116-127: the first and last
+// diagonal entries absorb l_raw_0 and u_raw_{n-1}), a_0 = c_{n-1} = 0.
+inline void partition_factors(int n, const double *a, const double *c, const double *l_raw, const double *u_raw,
+                              double eig, bool pin_last, bool interleave, double *out) {
+  std::vector<double> d(n);
+  for (int i = 0; i < n; i++) d[i] = -l_raw[i] - u_raw[i] + eig;
+  d[0] += l_raw[0];
+  d[n - 1] += u_raw[n - 1];
+  partition_factors_tri(n, a, d.data(), c, false, pin_last, interleave, out);
 }
 
 // stage layout of the length-jtot/2 complex FFT: radix 2 first when

@@ -340,6 +340,212 @@ __global__ void __launch_bounds__(32 * kParWarpsMax) k_par_tri(const ParTriArgs 
   for (int i = lane; i < n; i += 32) gline[i] = line[i];
 }
 
+// ------------------------------------------------------------------------
+// Crank-Nicolson lines by the partition method: src/linalg.c:9-30 along x
+// (rows of a field, wall-bounded: src/temperature/update.c:141-157,
+// src/fluid/update_velocity.c:249-280 and :500-520) and src/linalg.c:52-108
+// along y (columns, periodic: src/temperature/update.c:189-207,
+// src/fluid/update_velocity.c:404-430). One warp per line, one lane per
+// segment of m = n / 32 rows; the line is gathered into shared memory with
+// each segment at a stride s = m | 1 (odd, so that the 32 lanes' accesses at
+// one row fall on distinct bank pairs). The periodic lines' interface
+// system is cyclic: its PCR levels shuffle modulo 32. All RHS-independent
+// factors are computed on the host per substage (they depend on dt).
+
+constexpr int kCnWarpsMax = 8;
+constexpr int kCnLoad = 8;  // elements in flight per thread while gathering a line
+
+// a field's line block: inv g up v w (interleaved rows), alpha beta (PCR
+// levels), rD, then the interface rows' sub- and super-diagonals
+__device__ __forceinline__ int cn_pos(int e, int m, int s) {
+  const int k = e / m;
+  return k * s + (e - k * m);
+}
+
+// COLUMNS: periodic lines along y (element stride nx, adjacent lines
+// adjacent in memory: a block gathers its lines together, a 32-byte sector
+// holding 4 of them); otherwise lines along x (contiguous rows, gathered per
+// warp, coalesced).
+template <bool COLUMNS>
+__global__ void __launch_bounds__(32 * kCnWarpsMax) k_par_cn(const ParCnArgs a) {
+  extern __shared__ __align__(16) double cn_sm[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  // the field by a select, not an index into the parameter array (which
+  // would copy the array to the stack)
+  const ParCnField F = blockIdx.y == 0 ? a.f[0] : blockIdx.y == 1 ? a.f[1] : a.f[2];
+  const int n = a.n, m = a.m, s = a.s;
+  const int line0 = F.first + blockIdx.x * wpb, line = line0 + w;
+  const bool live = line < a.lines;
+  const size_t wstride = (size_t)kPartSeg * s + 8;  // per warp: 8 doubles apart in bank pairs
+  double *sl = cn_sm + (size_t)w * wstride;
+  if constexpr (COLUMNS) {
+    // block-wide gather: thread t takes line t % wpb, row t / wpb (+ rows
+    // per pass), so a warp reads whole sectors of wpb adjacent columns
+    const int per = blockDim.x / wpb;
+    const int c = threadIdx.x % wpb, r0 = threadIdx.x / wpb;
+    const bool lc = line0 + c < a.lines;
+    const double *src = F.q + (line0 + c);
+    double *dst = cn_sm + (size_t)c * wstride;
+    for (int e0 = r0; e0 < n; e0 += per * kCnLoad) {
+      double v[kCnLoad];
+#pragma unroll
+      for (int k = 0; k < kCnLoad; ++k) {
+        const int e = e0 + k * per;
+        v[k] = (lc && e < n) ? src[(size_t)e * a.es] : 0.0;
+      }
+#pragma unroll
+      for (int k = 0; k < kCnLoad; ++k) {
+        const int e = e0 + k * per;
+        if (lc && e < n) dst[cn_pos(e, m, s)] = v[k];
+      }
+    }
+    __syncthreads();
+  } else {
+    if (!live) return;  // the whole warp: rows are gathered per warp
+    const double *src = F.q + (size_t)line * a.ls;
+    for (int e0 = lane; e0 < n; e0 += 32 * kCnLoad) {
+      double v[kCnLoad];
+#pragma unroll
+      for (int k = 0; k < kCnLoad; ++k) {
+        const int e = e0 + 32 * k;
+        v[k] = e < n ? src[e] : 0.0;
+      }
+#pragma unroll
+      for (int k = 0; k < kCnLoad; ++k) {
+        const int e = e0 + 32 * k;
+        if (e < n) sl[cn_pos(e, m, s)] = v[k];
+      }
+    }
+    __syncwarp();
+  }
+  if (live) {
+    const double *inv = F.fac, *gg = inv + n, *up = inv + 2 * n, *vv = inv + 3 * n, *ww = inv + 4 * n;
+    const double *alpha = inv + 5 * (size_t)n, *beta = alpha + kPartLevels * kPartSeg;
+    const double *rD = beta + kPartLevels * kPartSeg, *ae = rD + kPartSeg, *ce = ae + kPartSeg;
+    double *seg = sl + lane * s;
+    // 1) interior rows r = 0 .. m-2 with zero interface values:
+    //    y_r = inv_r q_r - g_r y_{r-1}, then y_r -= up_r y_{r+1}
+    double y = seg[0] * __ldg(inv + lane);
+    seg[0] = y;
+    double ci[kParChunk], cg[kParChunk];
+#pragma unroll
+    for (int k = 0; k < kParChunk; ++k) {
+      const int r = 1 + k, i = r * kPartSeg + lane;
+      ci[k] = r < m - 1 ? __ldg(inv + i) : 0.0;
+      cg[k] = r < m - 1 ? __ldg(gg + i) : 0.0;
+    }
+#pragma unroll 1
+    for (int b = 1; b < m - 1; b += kParChunk) {
+      double ni[kParChunk], ng[kParChunk];
+#pragma unroll
+      for (int k = 0; k < kParChunk; ++k) {
+        const int r = b + kParChunk + k, i = r * kPartSeg + lane;
+        ni[k] = r < m - 1 ? __ldg(inv + i) : 0.0;
+        ng[k] = r < m - 1 ? __ldg(gg + i) : 0.0;
+      }
+#pragma unroll
+      for (int k = 0; k < kParChunk; ++k) {
+        const int r = b + k;
+        if (r < m - 1) {
+          y = fma(-cg[k], y, ci[k] * seg[r]);
+          seg[r] = y;
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < kParChunk; ++k) {
+        ci[k] = ni[k];
+        cg[k] = ng[k];
+      }
+    }
+    const double ylast = y;  // row m-2
+    double cu[kParChunk];
+#pragma unroll
+    for (int k = 0; k < kParChunk; ++k) {
+      const int r = m - 3 - k;
+      cu[k] = r >= 0 ? __ldg(up + r * kPartSeg + lane) : 0.0;
+    }
+#pragma unroll 1
+    for (int b = m - 3; b >= 0; b -= kParChunk) {
+      double nu[kParChunk];
+#pragma unroll
+      for (int k = 0; k < kParChunk; ++k) {
+        const int r = b - kParChunk - k;
+        nu[k] = r >= 0 ? __ldg(up + r * kPartSeg + lane) : 0.0;
+      }
+#pragma unroll
+      for (int k = 0; k < kParChunk; ++k) {
+        const int r = b - k;
+        if (r >= 0) {
+          y = fma(-cu[k], y, seg[r]);
+          seg[r] = y;
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < kParChunk; ++k) cu[k] = nu[k];
+    }
+    // 2) interface row e of segment k: q_e - a_e y_{e-1} - c_e y'_0 (the next
+    //    segment's first interior value; cyclically for periodic lines, and
+    //    c_e = 0 for the last segment of a wall-bounded line)
+    const double ynext = __shfl_sync(0xffffffffu, y, (lane + 1) & 31);
+    double R = fma(-__ldg(ce + lane), ynext, fma(-__ldg(ae + lane), ylast, seg[m - 1]));
+    // 3) PCR of the 32 interface equations; the host zeroes the couplings
+    //    past the ends of a wall-bounded line
+#pragma unroll
+    for (int lev = 0; lev < kPartLevels; ++lev) {
+      const int d = 1 << lev;
+      const double rm = __shfl_sync(0xffffffffu, R, (lane - d) & 31);
+      const double rp = __shfl_sync(0xffffffffu, R, (lane + d) & 31);
+      R = fma(__ldg(beta + lev * kPartSeg + lane), rp, fma(__ldg(alpha + lev * kPartSeg + lane), rm, R));
+    }
+    const double xe = R * __ldg(rD + lane);
+    seg[m - 1] = xe;
+    // 4) interiors: x_r = y_r + v_r x_{e(k-1)} + w_r x_{e(k)} (v = 0 in the
+    //    first segment of a wall-bounded line)
+    const double xl = __shfl_sync(0xffffffffu, xe, (lane - 1) & 31);
+#pragma unroll 1
+    for (int b = 0; b < m - 1; b += kParChunk) {
+      double cv[kParChunk], cw[kParChunk];
+#pragma unroll
+      for (int k = 0; k < kParChunk; ++k) {
+        const int r = b + k, i = r * kPartSeg + lane;
+        cv[k] = r < m - 1 ? __ldg(vv + i) : 0.0;
+        cw[k] = r < m - 1 ? __ldg(ww + i) : 0.0;
+      }
+#pragma unroll
+      for (int k = 0; k < kParChunk; ++k) {
+        const int r = b + k;
+        if (r < m - 1) seg[r] = fma(cw[k], xe, fma(cv[k], xl, seg[r]));
+      }
+    }
+  }
+  if constexpr (COLUMNS) {
+    __syncthreads();
+    const int per = blockDim.x / wpb;
+    const int c = threadIdx.x % wpb, r0 = threadIdx.x / wpb;
+    if (line0 + c < a.lines) {
+      double *dstq = F.q + (line0 + c);
+      const double *src = cn_sm + (size_t)c * wstride;
+      for (int e0 = r0; e0 < n; e0 += per * kCnLoad) {
+        double v[kCnLoad];
+#pragma unroll
+        for (int k = 0; k < kCnLoad; ++k) {
+          const int e = e0 + k * per;
+          v[k] = e < n ? src[cn_pos(e, m, s)] : 0.0;
+        }
+#pragma unroll
+        for (int k = 0; k < kCnLoad; ++k) {
+          const int e = e0 + k * per;
+          if (e < n) dstq[(size_t)e * a.es] = v[k];
+        }
+      }
+    }
+  } else {
+    __syncwarp();
+    double *dstq = F.q + (size_t)line * a.ls;
+    for (int e = lane; e < n; e += 32) dstq[e] = sl[cn_pos(e, m, s)];
+  }
+}
+
 // adjacent columns per block of the DFT kernels, where the shared memory
 // allows it. Measured at 512 x 1024 (parallel-form step, CUDA events): 1, 2,
 // 4 and 8 columns 0.513, 0.511, 0.538 and 0.724 ms per step: whole sectors
@@ -409,6 +615,41 @@ cudaError_t launch_par_tri(const DevGrid &g, double2 *spec, const ParFactors &pf
     k_par_tri<true><<<(g.nh + wpb - 1) / wpb, 32 * wpb, smem, st>>>(a);
   } else {
     k_par_tri<false><<<(g.nh + wpb - 1) / wpb, 32 * wpb, smem, st>>>(a);
+  }
+  count_launches(1);
+  return cudaGetLastError();
+}
+
+size_t par_cn_stride(int n) { return 5 * (size_t)n + 2 * kPartLevels * kPartSeg + 3 * kPartSeg; }
+
+namespace {
+// doubles of shared memory per warp (one line)
+size_t cn_warp_doubles(int n) { return (size_t)kPartSeg * ((n / kPartSeg) | 1) + 8; }
+}  // namespace
+
+bool parallel_cn_supported(int n) {
+  return n >= 2 * kPartSeg && n % kPartSeg == 0 && cn_warp_doubles(n) * sizeof(double) <= kParSmemMax;
+}
+
+cudaError_t launch_par_cn(bool columns, ParCnArgs a, cudaStream_t st) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_par_cn<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kParSmemMax);
+    cudaFuncSetAttribute(k_par_cn<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kParSmemMax);
+    attr = true;
+  }
+  if (!parallel_cn_supported(a.n) || a.nf < 1 || a.nf > 3) return cudaErrorInvalidValue;
+  a.m = a.n / kPartSeg;
+  a.s = a.m | 1;
+  const size_t per = cn_warp_doubles(a.n) * sizeof(double);
+  // warps (lines) per block: two blocks per SM where the lines fit
+  int wpb = (int)std::min<size_t>(kCnWarpsMax, (kParSmemMax / 2) / per);
+  if (wpb < 1) wpb = 1;
+  const dim3 grid((a.lines + wpb - 1) / wpb, a.nf);
+  if (columns) {
+    k_par_cn<true><<<grid, 32 * wpb, wpb * per, st>>>(a);
+  } else {
+    k_par_cn<false><<<grid, 32 * wpb, wpb * per, st>>>(a);
   }
   count_launches(1);
   return cudaGetLastError();

@@ -574,17 +574,21 @@ struct HostFactors {
   double d0 = 0;
 };
 
-static void x_system(const param_t *param, int rk, int kind, HostFactors &hf) {
-  // kind 0: temperature (src/temperature/update.c:141-149), n = itot
-  // kind 1: ux (src/fluid/update_velocity.c:249-264), n = itot+1 with identity end rows
-  // kind 2: uy (src/fluid/update_velocity.c:500-508), n = itot
+// the reference's tridiagonal l, d, u of the Crank-Nicolson solve along x
+// kind 0: temperature (src/temperature/update.c:141-149), n = itot
+// kind 1: ux (src/fluid/update_velocity.c:249-264), n = itot+1 with identity end rows
+// kind 2: uy (src/fluid/update_velocity.c:500-508), n = itot
+static void x_tri(const param_t *param, int rk, int kind, std::vector<double> &l, std::vector<double> &d,
+                  std::vector<double> &u) {
   const int nx = param->itot;
   const double *dxf = param->dxf, *dxc = param->dxc;
   auto DXF = [&](int i) { return dxf[i - 1]; };
   auto DXC = [&](int i) { return dxc[i - 1]; };
   const double gamma = param->rkcoefs[rk].gamma, dt = param->dt, Ra = param->Ra, Pr = param->Pr;
   const int n = kind == 1 ? nx + 1 : nx;
-  std::vector<double> l(n), d(n), u(n);
+  l.assign(n, 0.);
+  d.assign(n, 0.);
+  u.assign(n, 0.);
   for (int i = 1; i <= n; i++) {
     if (kind == 1 && (i == 1 || i == nx + 1)) {
       l[i - 1] = 0.;
@@ -611,6 +615,12 @@ static void x_system(const param_t *param, int rk, int kind, HostFactors &hf) {
     u[i - 1] = -pf * cp;
     d[i - 1] = 1. - pf * c0;
   }
+}
+
+static void x_system(const param_t *param, int rk, int kind, HostFactors &hf) {
+  std::vector<double> l, d, u;
+  x_tri(param, rk, kind, l, d, u);
+  const int n = (int)l.size();
   hf.l = l;
   hf.inv.assign(n, 0.);
   hf.up.assign(n, 0.);
@@ -618,14 +628,16 @@ static void x_system(const param_t *param, int rk, int kind, HostFactors &hf) {
   hf.d0 = d[0];
 }
 
-// src/linalg.c:52-108 with the constant y matrix of src/temperature/update.c:189-197
+// the reference's constant periodic y matrix: src/temperature/update.c:189-197
 // (temperature, is_temp) or src/fluid/update_velocity.c:404-412 (velocity)
-static void y_system(const param_t *param, int rk, int is_temp, HostFactors &sub, std::vector<double> &q1,
-                     double &l_last, double &u_last, double &den) {
+static void y_tri(const param_t *param, int rk, int is_temp, std::vector<double> &l, std::vector<double> &d,
+                  std::vector<double> &u) {
   const int n = param->jtot;
   const double gamma = param->rkcoefs[rk].gamma, dt = param->dt, Ra = param->Ra, Pr = param->Pr, dy = param->dy;
   const double pf = is_temp ? (gamma * dt) / (2. * sqrt(Pr) * sqrt(Ra)) : (gamma * dt * sqrt(Pr)) / (2. * sqrt(Ra));
-  std::vector<double> l(n), d(n), u(n);
+  l.assign(n, 0.);
+  d.assign(n, 0.);
+  u.assign(n, 0.);
   for (int j = 0; j < n; j++) {
     const double cm = 1. / dy / dy, cp = 1. / dy / dy;
     const double c0 = -cm - cp;
@@ -633,6 +645,14 @@ static void y_system(const param_t *param, int rk, int is_temp, HostFactors &sub
     u[j] = -pf * cp;
     d[j] = 1. - pf * c0;
   }
+}
+
+// src/linalg.c:52-108 on the y matrix of y_tri
+static void y_system(const param_t *param, int rk, int is_temp, HostFactors &sub, std::vector<double> &q1,
+                     double &l_last, double &u_last, double &den) {
+  const int n = param->jtot;
+  std::vector<double> l, d, u;
+  y_tri(param, rk, is_temp, l, d, u);
   const int m = n - 1;
   sub.l.assign(l.begin(), l.begin() + m);
   sub.inv.assign(m, 0.);
@@ -693,9 +713,15 @@ static int push_factors(Context *c, const HostFactors &hf, size_t off, LineFacto
 // (stride 4 ny) after 9(nx+2) for the merged sweeps of the fused step
 static size_t xset_off(const Context *c, int k) { return (size_t)k * 3 * (c->nx + 2); }
 static size_t yset_off(const Context *c, int k) { return 9 * (size_t)(c->nx + 2) + (size_t)k * 4 * c->ny; }
+// then the parallel form's line blocks: three x systems (temperature, ux,
+// uy) and two y systems (temperature, velocity)
+static size_t cnx_off(const Context *c, int k) {
+  return std::max(4 * (size_t)(c->nx + 1) + 5 * (size_t)c->ny, yset_off(c, 2)) + 16 + (size_t)k * par_cn_stride(c->nx);
+}
+static size_t cny_off(const Context *c, int k) { return cnx_off(c, 3) + (size_t)k * par_cn_stride(c->ny); }
 
 static int ensure_factor_buffer(Context *c) {
-  const size_t need = std::max(4 * (size_t)(c->nx + 1) + 5 * (size_t)c->ny, yset_off(c, 2)) + 16;
+  const size_t need = cny_off(c, 2) + 16;
   if (c->fac_words >= need) return SNS_OK;
   if (int rc = dev_alloc(c, &c->fac, need)) return rc;
   if (c->fac_host) cudaFreeHost(c->fac_host);
@@ -722,7 +748,98 @@ static int end_factor_uploads(Context *c) {
   return SNS_OK;
 }
 
+// ------------------------------------------ parallel form: Crank-Nicolson lines
+// The Crank-Nicolson lines of the parallel form run the partition method
+// (k_par_cn in plain_parallel.cu) where the line length allows it: results
+// differ from the reference's Thomas recurrences (src/linalg.c:9-108) by
+// rounding only.
+static bool cn_parallel(const Context *c, int n) {
+  return c->form == SNS_FORM_PARALLEL && parallel_cn_supported(n);
+}
+
+// the factor block of one line system: inv, g = a inv, up, v, w (rows
+// interleaved), the PCR coefficients, then the interface rows' sub- and
+// super-diagonals. a, d, c: the device line's rows; periodic: a_0 couples
+// row 0 to row n-1 and c_{n-1} row n-1 to row 0 (otherwise both are dropped)
+static void cn_block(int n, std::vector<double> a, const std::vector<double> &d, std::vector<double> c, bool periodic,
+                     std::vector<double> &out) {
+  if (!periodic) {
+    a[0] = 0.0;
+    c[n - 1] = 0.0;
+  }
+  const int m = n / kPartSeg;
+  std::vector<double> blk(partition_stride(n));
+  partition_factors_tri(n, a.data(), d.data(), c.data(), periodic, false, true, blk.data());
+  out.assign(par_cn_stride(n), 0.0);
+  std::copy(blk.begin(), blk.begin() + n, out.begin());  // inv
+  for (int i = 0; i < n; i++) {
+    const size_t o = (size_t)(i % m) * kPartSeg + i / m;
+    out[n + o] = a[i] * blk[o];  // g
+  }
+  std::copy(blk.begin() + n, blk.end(), out.begin() + 2 * (size_t)n);  // up v w alpha beta rD
+  double *ae = out.data() + par_cn_stride(n) - 2 * kPartSeg, *ce = ae + kPartSeg;
+  for (int k = 0; k < kPartSeg; k++) {
+    ae[k] = a[(size_t)k * m + m - 1];
+    ce[k] = c[(size_t)k * m + m - 1];
+  }
+}
+
+// the device rows x = 0..itot-1 of the x system of `kind` (x_tri); for ux
+// row 0 is the wall's identity row and the other wall's row itot is not
+// stored: both hold zero in the reference's solve, so their couplings to
+// rows 1 and itot-1 drop out
+static void cn_x_block(const param_t *param, int rk, int kind, std::vector<double> &out) {
+  std::vector<double> l, d, u;
+  x_tri(param, rk, kind, l, d, u);
+  const int nx = param->itot;
+  l.resize(nx);
+  d.resize(nx);
+  u.resize(nx);
+  if (kind == 1) {
+    l[1] = 0.0;
+    u[nx - 1] = 0.0;
+  }
+  cn_block(nx, l, d, u, false, out);
+}
+
+static void cn_y_block(const param_t *param, int rk, int is_temp, std::vector<double> &out) {
+  std::vector<double> l, d, u;
+  y_tri(param, rk, is_temp, l, d, u);
+  cn_block(param->jtot, l, d, u, true, out);
+}
+
+static ParCnArgs cn_x_args(const Context *c) {
+  ParCnArgs a{};
+  a.n = c->nx;
+  a.lines = c->ny;
+  a.es = 1;
+  a.ls = c->nx;
+  return a;
+}
+
+static ParCnArgs cn_y_args(const Context *c) {
+  ParCnArgs a{};
+  a.n = c->ny;
+  a.lines = c->nx;
+  a.es = c->nx;
+  a.ls = 1;
+  return a;
+}
+
 static int implicit_x(Context *c, const param_t *param, int rk, int kind, double *q) {
+  if (cn_parallel(c, c->nx)) {
+    std::vector<double> blk;
+    cn_x_block(param, rk, kind, blk);
+    if (int rc = begin_factor_uploads(c)) return rc;
+    if (int rc = stage_upload(c, cnx_off(c, 0), blk.data(), blk.size())) return rc;
+    if (int rc = end_factor_uploads(c)) return rc;
+    ParCnArgs a = cn_x_args(c);
+    a.f[0] = ParCnField{q, c->fac + cnx_off(c, 0), 0};
+    a.nf = 1;
+    Prof pf(c, K_SOLVE_X);
+    SNS_CUDA(launch_par_cn(false, a, c->stream));
+    return SNS_OK;
+  }
   HostFactors hf;
   x_system(param, rk, kind, hf);
   LineFactors lf{};
@@ -735,6 +852,19 @@ static int implicit_x(Context *c, const param_t *param, int rk, int kind, double
 }
 
 static int implicit_y(Context *c, const param_t *param, int rk, int is_temp, int first_col, double *q) {
+  if (cn_parallel(c, c->ny)) {
+    std::vector<double> blk;
+    cn_y_block(param, rk, is_temp, blk);
+    if (int rc = begin_factor_uploads(c)) return rc;
+    if (int rc = stage_upload(c, cny_off(c, 0), blk.data(), blk.size())) return rc;
+    if (int rc = end_factor_uploads(c)) return rc;
+    ParCnArgs a = cn_y_args(c);
+    a.f[0] = ParCnField{q, c->fac + cny_off(c, 0), first_col};
+    a.nf = 1;
+    Prof pf(c, K_SOLVE_Y);
+    SNS_CUDA(launch_par_cn(true, a, c->stream));
+    return SNS_OK;
+  }
   HostFactors sub;
   std::vector<double> q1;
   PeriodicFactors pf{};
@@ -855,7 +985,17 @@ static int implicit_updates(const param_t *param, int rk, FluidExt *fe, TempExt 
   double *qs[3] = {with_t ? te->f.qt : nullptr, f.qx, f.qy};
   if (impx || impy)
     if (int rc = begin_factor_uploads(c)) return rc;
-  if (impx) {
+  if (impx && cn_parallel(c, c->nx)) {
+    ParCnArgs a = cn_x_args(c);
+    for (int k = with_t ? 0 : 1; k < 3; k++) {
+      std::vector<double> blk;
+      cn_x_block(param, rk, kinds[k], blk);
+      if (int rc = stage_upload(c, cnx_off(c, k), blk.data(), blk.size())) return rc;
+      a.f[a.nf++] = ParCnField{qs[k], c->fac + cnx_off(c, k), 0};
+    }
+    Prof pf(c, K_SOLVE_X);
+    SNS_CUDA(launch_par_cn(false, a, c->stream));
+  } else if (impx) {
     SolveXSet set{};
     for (int k = with_t ? 0 : 1; k < 3; k++) {
       HostFactors hf;
@@ -868,7 +1008,23 @@ static int implicit_updates(const param_t *param, int rk, FluidExt *fe, TempExt 
     Prof pf(c, K_SOLVE_X);
     SNS_CUDA(FORM(c, launch_solve_x_set)(c->g, set, c->stream));
   }
-  if (impy) {
+  if (impy && cn_parallel(c, c->ny)) {
+    ParCnArgs a = cn_y_args(c);
+    for (int sys = with_t ? 0 : 1; sys < 2; sys++) {  // y systems: temperature, velocity
+      std::vector<double> blk;
+      cn_y_block(param, rk, sys == 0 ? 1 : 0, blk);
+      if (int rc = stage_upload(c, cny_off(c, sys), blk.data(), blk.size())) return rc;
+      const double *fac = c->fac + cny_off(c, sys);
+      if (sys == 0) {
+        a.f[a.nf++] = ParCnField{te->f.qt, fac, 0};
+      } else {
+        a.f[a.nf++] = ParCnField{f.qx, fac, 1};  // ux: columns 1..itot-1
+        a.f[a.nf++] = ParCnField{f.qy, fac, 0};
+      }
+    }
+    Prof pr(c, K_SOLVE_Y);
+    SNS_CUDA(launch_par_cn(true, a, c->stream));
+  } else if (impy) {
     SolveYSet set{};
     for (int sys = with_t ? 0 : 1; sys < 2; sys++) {  // y systems: temperature, velocity
       HostFactors sub;
@@ -1481,9 +1637,11 @@ int temperature_update_temp(const param_t *param, const parallel_t *parallel, co
     return fail(SNS_ERR_ARG, "temperature_update_temp: bad argument");
   Context *c = te->ctx;
   if (int rc = flush_pending(c)) return rc;
-  if (c->fused && c->form == SNS_FORM_EXACT && fe->ctx == c && !param->implicitx && !param->implicity) {
-    // explicit: launched inside the next fluid_compute_potential (it reads the
-    // velocity of now, which that call's velocity update leaves in place)
+  if ((c->form == SNS_FORM_PARALLEL || c->fused) && fe->ctx == c && !param->implicitx && !param->implicity) {
+    // explicit: launched by the next fluid_compute_potential, inside the
+    // fused launch (exact form) or beside the Poisson kernels (parallel
+    // form); it reads the velocity of now, which that call's velocity update
+    // leaves in place
     PendingTemp &pt = c->ptemp;
     pt.te = te;
     pt.rk = rkstep;
@@ -1528,6 +1686,25 @@ int fluid_compute_potential(const param_t *param, const parallel_t *parallel, co
     if (fused) {
       te->cur = pt.out;
       pt = PendingTemp{};
+      return SNS_OK;
+    }
+    if (c->form == SNS_FORM_PARALLEL && !c->pcorr.fe) {
+      // the parallel form: the deferred temperature update on the side
+      // stream beside the Poisson kernels, as sns_run runs it; the main
+      // stream waits for it before anything later in call order
+      const PendingTemp p = pt;
+      pt = PendingTemp{};
+      SNS_CUDA(cudaEventRecord(c->ev_fwd, c->stream));
+      SNS_CUDA(cudaStreamWaitEvent(c->side, c->ev_fwd, 0));
+      {
+        Prof pf(c, K_TEMP, c->side);
+        SNS_CUDA(FORM(c, launch_temp_update)(c->g, p.s, 0, 0, te->f.t[te->cur], te->f.t[p.out], te->f.at, nullptr, p.ux_k,
+                                             p.uy_k, c->side));
+      }
+      SNS_CUDA(cudaEventRecord(c->ev_temp, c->side));
+      te->cur = p.out;
+      if (int rc = poisson(c, s, fe->f)) return rc;
+      SNS_CUDA(cudaStreamWaitEvent(c->stream, c->ev_temp, 0));
       return SNS_OK;
     }
   }
@@ -2386,19 +2563,13 @@ void *sns_stream(const fluid_t *fluid) {
 
 // One time step's substages (src/main.c:80-99) with fused kernels. With the
 // explicit scheme the temperature update of a substage, which reads only the
-// substage's starting T and u, runs on a side stream while the Poisson
-// tridiagonal sweep (a serial recurrence that occupies few SMs) runs on the
-// main stream; the velocity kernel has already taken its buoyancy from the
-// starting T, and the next substage waits for the new T. Same kernels, same
-// inputs, same bits as the sequential order.
-// One time step's substages (src/main.c:80-99) with fused kernels. With the
-// explicit scheme the temperature update of a substage, which reads only the
 // substage's starting T and u, runs inside the fused Poisson launch on the
-// SMs that the latency-bound tridiagonal sweeps leave free (or, when the
-// Poisson solve runs as three kernels, on a side stream during the sweep);
-// the velocity kernel has already taken its buoyancy from the starting T, and
-// the next substage reads the new T. Same kernels' arithmetic, same inputs,
-// same bits as the sequential order.
+// SMs that the latency-bound tridiagonal sweeps leave free (exact form), or
+// on a side stream beside the tridiagonal solve and the inverse DFT (Poisson
+// solve as separate kernels, either form); the velocity kernel has already
+// taken its buoyancy from the starting T, and the next substage reads the
+// new T. Same kernels' arithmetic, same inputs, same bits as the sequential
+// order.
 static int integrate_impl(const param_t *param, FluidExt *fe, TempExt *te, bool reduce_last) {
   Context *c = fe->ctx;
   Fields &f = fe->f;
@@ -2424,7 +2595,14 @@ static int integrate_impl(const param_t *param, FluidExt *fe, TempExt *te, bool 
     }
     if (!fused) {
       if (overlap) {
-        if (int rc = poisson_forward(c, s, f)) return rc;
+        // the temperature update on the side stream: in the parallel form
+        // from the end of the velocity update on, beside the forward DFT,
+        // whose 2 columns per block leave SMs unevenly loaded (512 x 1024:
+        // 0.502 against 0.511 ms per step with it beside the tridiagonal
+        // solve); in the exact form beside the serial tridiagonal sweeps
+        const bool early = c->form == SNS_FORM_PARALLEL;
+        if (!early)
+          if (int rc = poisson_forward(c, s, f)) return rc;
         SNS_CUDA(cudaEventRecord(c->ev_fwd, c->stream));
         SNS_CUDA(cudaStreamWaitEvent(c->side, c->ev_fwd, 0));
         {
@@ -2434,6 +2612,8 @@ static int integrate_impl(const param_t *param, FluidExt *fe, TempExt *te, bool 
         }
         SNS_CUDA(cudaEventRecord(c->ev_temp, c->side));
         te->cur = out;
+        if (early)
+          if (int rc = poisson_forward(c, s, f)) return rc;
         if (int rc = poisson_rest(c, s, f)) return rc;
       } else {
         if (int rc = poisson(c, s, f)) return rc;

@@ -180,6 +180,27 @@ cudaError_t launch_par_tri(const DevGrid &g, double2 *spec, const ParFactors &pf
 cudaError_t launch_par_bwd(const DevGrid &g, const StageScalars &s, const double2 *spec, double *psi,
                            cudaStream_t st);
 
+// Partition-method form of the Crank-Nicolson solves (plain_parallel.cu):
+// per field the right-hand sides (solved in place), the line factor block
+// (par_cn_stride doubles, shared by all lines of the field) and the first
+// line solved; one launch covers up to three fields of one direction
+struct ParCnField {
+  double *q = nullptr;
+  const double *fac = nullptr;
+  int first = 0;
+};
+struct ParCnArgs {
+  ParCnField f[3];
+  int nf = 0;
+  int n = 0, m = 0, s = 0;  // rows per line, per segment, shared-memory stride of a segment
+  int lines = 0;            // lines per field (a field's lines are first .. lines-1)
+  long long es = 0, ls = 0; // strides of a line's elements and of consecutive lines in q
+};
+size_t par_cn_stride(int n);
+bool parallel_cn_supported(int n);
+// columns: periodic lines along y; otherwise wall-bounded rows along x
+cudaError_t launch_par_cn(bool columns, ParCnArgs a, cudaStream_t st);
+
 // kernel kinds for the optional per-launch event timing (sns_profile_*)
 enum KernelKind {
   K_TEMP = 0, K_VEL, K_POI_FWD, K_POI_TRI, K_POI_BWD, K_CORR_PRES, K_CORR, K_PRES, K_UMAX, K_SOLVE_X, K_SOLVE_Y,

@@ -1,9 +1,10 @@
-"""The plain FP64 path with the Poisson lines solved by the partition method
-and parallel cyclic reduction (sns_set_form(SNS_FORM_PARALLEL))
-against the CPU oracle, whose Thomas recurrence is the reference's
-(src/linalg.c:32-50). The two differ by rounding only, so the bar is the
-path's stated tolerance: 1e-12 relative L2 per field (ux, uy, T, p) after the
-stated step counts of the Rayleigh-Benard workloads.
+"""The plain FP64 path with the Poisson lines and the Crank-Nicolson lines
+solved by the partition method and parallel cyclic reduction
+(sns_set_form(SNS_FORM_PARALLEL)) against the CPU oracle, whose Thomas
+recurrences are the reference's (src/linalg.c:9-108). The two differ by
+rounding only, so the bar is the path's stated tolerance: 1e-12 relative L2
+per field (ux, uy, T, p) after the stated step counts of the Rayleigh-Benard
+workloads.
 
 Also here: the bounded device waits of the fused Poisson launch and of the
 parallel tridiagonal launch. A test makes a wait run out (a completion flag
@@ -106,6 +107,75 @@ def test_reference_named_calls_within_tolerance(costs):
         c.set_form(True)
         c.run_calls(20)
         o.run(20)
+        errs = _errors(c, o)
+        assert all(e <= REL_TOL for e in errs.values()), errs
+
+
+@pytest.mark.parametrize("scheme", [(1, 0), (0, 1), (1, 1)], ids=["imp_x", "imp_y", "imp_imp"])
+@pytest.mark.parametrize("nx,ny", [(64, 128), (256, 64)], ids=["64x128", "256x64"])
+def test_crank_nicolson_calls_within_round_off(scheme, nx, ny):
+    """The Crank-Nicolson solves of the parallel form (partition method: one
+    lane per segment of itot/32 rows along x, of jtot/32 rows along y, whose
+    periodic lines give a cyclic interface system) against the oracle's
+    Thomas recurrences (src/linalg.c:9-108), call by call on seeded fields
+    with non-zero previous sources: segments of 2 and 8 rows along x, 4 and 2
+    along y (the form needs the mean mode's last pivot to vanish, which on
+    the reference's unit-length x means a power-of-two itot). Each substage
+    starts from the oracle's state, and the increments that
+    temperature_update_temp and fluid_update_velocity add are compared: a
+    wrong coupling anywhere in a line changes them at O(1)."""
+    cfg = Config(nx, ny, ly=1.0, Ra=2e5, Pr=0.8)
+    rng = np.random.default_rng(17)
+    su, sc = (cfg.jtot + 2, cfg.itot + 1), (cfg.jtot + 2, cfg.itot + 2)
+    state = (0.2 * rng.uniform(-1, 1, su), 0.2 * rng.uniform(-1, 1, sc), 0.05 * rng.uniform(-1, 1, sc),
+             rng.uniform(-0.5, 0.5, sc))
+    src = {"srcuxa": rng.uniform(-1, 1, (cfg.jtot, cfg.itot - 1)), "srcuya": rng.uniform(-1, 1, (cfg.jtot, cfg.itot)),
+           "srctempa": rng.uniform(-1, 1, (cfg.jtot, cfg.itot))}
+    o = OracleCase(cfg)
+    o.set_state(*state)
+    o.set_sources(src["srcuxa"], src["srcuya"], src["srctempa"])
+    o.call("update_boundaries")
+    with _case(cfg) as c:
+        c.set_form(True)
+        c.set_state(*state, sources=src)
+        for x in (c, o):
+            x.set_dt(2e-3, *scheme)
+        for rk in range(3):
+            s0 = o.get_state()
+            c.temperature_compute_force()
+            c.temperature_update_temp(rk)
+            o.call("temperature_force_and_update", rk)
+            g, r = c.get_state(), o.get_state()
+            inc = rel_l2(g["temp"][1:-1, 1:-1] - s0["temp"][1:-1, 1:-1], r["temp"][1:-1, 1:-1] - s0["temp"][1:-1, 1:-1])
+            assert inc <= 1e-12, ("temperature increment", rk, inc)
+            c.fluid_update_velocity(rk)
+            o.call("fluid_update_velocity", rk)
+            g, r = c.get_state(), o.get_state()
+            for k in ("ux", "uy"):
+                inc = rel_l2(g[k][1:-1, 1:-1] - s0[k][1:-1, 1:-1], r[k][1:-1, 1:-1] - s0[k][1:-1, 1:-1])
+                assert inc <= 1e-12, (k, "increment", rk, inc)
+            for name in ("fluid_compute_potential", "fluid_correct_velocity", "fluid_update_pressure"):
+                getattr(c, name)(rk)
+                o.call(name, rk)
+            # the next substage from the oracle's state
+            r, rs = o.get_state(), o.get_sources()
+            c.set_state(r["ux"], r["uy"], r["p"], r["temp"], sources=rs)
+
+
+def test_rayleigh_benard_2048x4096_50_steps_within_tolerance():
+    """The 2048 x 4096, Ra 1e10 instance, whose cost table picks
+    Crank-Nicolson in x and y: the partition-method solves along both
+    directions (segments of 64 and 128 rows) and the parallel Poisson lines,
+    50 steps against the oracle."""
+    cfg = Config(2048, 4096, ly=2.0, Ra=1e10, Pr=1.0)
+    o = OracleCase(cfg, threads=16)
+    o.set_costs([1, 2, 2, 3])
+    with _case(cfg) as c:
+        c.set_form(True)
+        c.run(50)
+        o.run(50)
+        d = c.get_dt()
+        assert (d["implicitx"], d["implicity"]) == (1, 1)
         errs = _errors(c, o)
         assert all(e <= REL_TOL for e in errs.values()), errs
 
