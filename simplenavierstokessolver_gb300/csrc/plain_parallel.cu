@@ -18,14 +18,19 @@
 // mode line in the interleaved order p = (x % m) * 32 + x / m (m = nx / 32):
 // lane k walks segment k, and at every step the 32 lanes touch 32
 // consecutive elements, in global and in shared memory alike. The forward
-// and inverse DFTs (the same FFT as the Thomas form) write and read that
-// order.
+// and inverse DFTs write and read that order: a radix-8 Stockham FFT in
+// registers for 16 <= jtot <= 8192 (fft_stockham.cuh), the Thomas form's
+// radix-2/4 FFT otherwise.
+//
+// The Crank-Nicolson lines (src/linalg.c:9-108) are solved by the same
+// partition method, one warp per row or column (k_par_cn).
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstdint>
 
 #include "fft_dev.cuh"
+#include "fft_stockham.cuh"
 #include "host_common.h"
 #include "sns_gpu.h"
 #include "sns_internal.h"
@@ -105,6 +110,112 @@ __global__ void __launch_bounds__(256) k_par_bwd(const ParArgs a) {
     const int c = e % C, y = e / C, x = x0 + c;
     if (x >= nx) continue;
     a.psi[(size_t)y * nx + x] = zd[2 * (c * M + (y >> 1)) + (y & 1)] * a.s.rny;
+  }
+}
+
+// ---- the same two transforms by the radix-8 Stockham FFT (fft_stockham.cuh),
+// for 16 <= jtot <= 8192. The solve is linear, so this pair moves two
+// constant factors to the inverse's final scale: the forward transforms
+// div u* without the factor 1/(gamma dt) and leaves the real FFT's split
+// step unhalved (2 X), and the inverse multiplies by 1/(gamma dt) / (2 jtot)
+// (an exact power-of-two scaling of 1/(gamma dt)). Both kernels run C
+// columns per block on C jtot / 16 threads, 8 complex values per thread.
+
+// src/fluid/compute_potential.c:69-92: div u* along two rows per complex
+// element (z[m] = d[2m] + i d[2m+1]), its FFT, and 2 X[k] of the real
+// transform at the columns' line positions
+__global__ void __launch_bounds__(512) k_par_fwd8(const ParArgs a) {
+  extern __shared__ double2 z[];
+  const int nx = a.g.nx, ny = a.g.ny, M = ny / 2, C = a.cols;
+  const int x0 = blockIdx.x * C;
+  const double rdy = a.g.rdy;
+  const double2 *tw = reinterpret_cast<const double2 *>(a.g.tw);
+  for (int e = threadIdx.x; e < C * M; e += blockDim.x) {
+    const int c = e % C, mm = e / C, x = x0 + c;
+    double2 d = make_double2(0.0, 0.0);
+    if (x < nx) {
+      const size_t r0 = (size_t)(2 * mm) * nx + x, r1 = r0 + nx;
+      const size_t r2 = (size_t)(2 * mm + 2 == ny ? 0 : 2 * mm + 2) * nx + x;
+      const bool right = x == nx - 1;
+      const double rdx = a.g.rdxf[x];
+      const double u0m = a.ux[r0], u0p = right ? 0.0 : a.ux[r0 + 1];
+      const double u1m = a.ux[r1], u1p = right ? 0.0 : a.ux[r1 + 1];
+      const double v0 = a.uy[r0], v1 = a.uy[r1], v2 = a.uy[r2];
+      d.x = (u0p - u0m) * rdx + (v1 - v0) * rdy;
+      d.y = (u1p - u1m) * rdx + (v2 - v1) * rdy;
+    }
+    z[c * M + fft8::swz(mm)] = d;
+  }
+  __syncthreads();
+  fft8::transform<true>(z, M, tw);
+  // split step for the bin pair (k, M-k): 2 X[k] = (Z[k] + conj Z[M-k]) +
+  // w^k (Z[k] - conj Z[M-k]) / i, w = exp(-2 pi i / jtot)
+  const int half = M / 2 + 1;
+  for (int e = threadIdx.x; e < C * half; e += blockDim.x) {
+    const int c = e % C, k = e / C, x = x0 + c;
+    if (x >= nx) continue;
+    const double2 *zc = z + c * M;
+    double2 *out = a.spec + par_p(x, a.m);
+    const size_t os = (size_t)nx;
+    if (k == 0) {
+      const double2 z0 = zc[0];
+      const double s = z0.x + z0.y, t = z0.x - z0.y;
+      out[0] = make_double2(s + s, 0.0);
+      out[(size_t)M * os] = make_double2(t + t, 0.0);
+    } else {
+      const double2 A = zc[fft8::swz(k)], B = zc[fft8::swz(M - k)];
+      const double sre = A.x + B.x, dim = A.y - B.y, dre = A.x - B.x, sim = A.y + B.y;
+      const double2 w = tw[k];
+      const double wor = w.x * sim + w.y * dre;
+      const double woi = w.y * sim - w.x * dre;
+      out[(size_t)k * os] = make_double2(sre + wor, dim + woi);
+      if (2 * k != M) out[(size_t)(M - k) * os] = make_double2(sre - wor, woi - dim);
+    }
+  }
+}
+
+// src/fluid/compute_potential.c:146-157: the inverse (2 Z[k] from the bin
+// pair, FFT, psi rows 2m and 2m+1 from element m) and the final scale
+__global__ void __launch_bounds__(512) k_par_bwd8(const ParArgs a) {
+  extern __shared__ double2 z[];
+  const int nx = a.g.nx, ny = a.g.ny, M = ny / 2, C = a.cols;
+  const int x0 = blockIdx.x * C;
+  const double2 *tw = reinterpret_cast<const double2 *>(a.g.tw);
+  const int half = M / 2 + 1;
+  for (int e = threadIdx.x; e < C * half; e += blockDim.x) {
+    const int c = e % C, k = e / C, x = x0 + c;
+    double2 *zc = z + c * M;
+    if (x >= nx) {
+      zc[fft8::swz(k)] = make_double2(0.0, 0.0);
+      if (k > 0) zc[fft8::swz(M - k)] = make_double2(0.0, 0.0);
+      continue;
+    }
+    const double2 *in = a.spec + par_p(x, a.m);
+    const size_t is = (size_t)nx;
+    if (k == 0) {
+      // imaginary parts of X[0] and X[M] ignored (FFTW's c2r convention)
+      const double x0r = in[0].x, xmr = in[(size_t)M * is].x;
+      zc[0] = make_double2(x0r + xmr, x0r - xmr);
+    } else {
+      const double2 A = in[(size_t)k * is], B = in[(size_t)(M - k) * is];
+      const double er = A.x + B.x, ei = A.y - B.y, dr = A.x - B.x, di = A.y + B.y;
+      const double2 w = tw[k];
+      const double orr = dr * w.x + di * w.y;
+      const double oi = di * w.x - dr * w.y;
+      zc[fft8::swz(k)] = make_double2(er - oi, ei + orr);
+      if (2 * k != M) zc[fft8::swz(M - k)] = make_double2(er + oi, orr - ei);
+    }
+  }
+  __syncthreads();
+  fft8::transform<false>(z, M, tw);
+  const double scale = a.s.rgdt * (0.5 * a.s.rny);
+  for (int e = threadIdx.x; e < C * M; e += blockDim.x) {
+    const int c = e % C, mm = e / C, x = x0 + c;
+    if (x >= nx) continue;
+    const double2 v = z[c * M + fft8::swz(mm)];
+    const size_t r0 = (size_t)(2 * mm) * nx + x;
+    a.psi[r0] = v.x * scale;
+    a.psi[r0 + nx] = v.y * scale;
   }
 }
 
@@ -582,17 +693,41 @@ bool parallel_tri_supported(int nx, int ny) {
   return nx >= 2 * kPartSeg && nx % kPartSeg == 0 && ny >= 4 && 16 * (size_t)nx + 128 <= kParSmemMax;
 }
 
-cudaError_t launch_par_fwd(const DevGrid &g, const StageScalars &s, const double *ux, const double *uy,
-                           double2 *spec, cudaStream_t st) {
+namespace {
+// the radix-8 Stockham pair: 16 <= jtot <= 8192 (at most 512 threads a block)
+bool par_fft8(const DevGrid &g) { return g.ny >= 16 && g.ny <= 8192; }
+
+void par_dft_attributes() {
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(k_par_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
     cudaFuncSetAttribute(k_par_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(k_par_fwd8, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+    cudaFuncSetAttribute(k_par_bwd8, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
     attr = true;
   }
-  const int C = par_cols(g);
-  const ParArgs a{g, s, ux, uy, spec, nullptr, C, g.nx / kPartSeg};
-  k_par_fwd<<<(g.nx + C - 1) / C, par_threads(g, C), (size_t)C * g.ny * sizeof(double), st>>>(a);
+}
+
+// columns per block of the radix-8 pair: C jtot / 16 threads, C jtot 8 bytes
+int par_cols8(const DevGrid &g) {
+  int c = kParCols;
+  while (c > 1 && ((size_t)c * g.ny * sizeof(double) > 128 * 1024 || c * g.ny / 16 > 512)) c /= 2;
+  return c;
+}
+}  // namespace
+
+cudaError_t launch_par_fwd(const DevGrid &g, const StageScalars &s, const double *ux, const double *uy,
+                           double2 *spec, cudaStream_t st) {
+  par_dft_attributes();
+  if (par_fft8(g)) {
+    const int C = par_cols8(g);
+    const ParArgs a{g, s, ux, uy, spec, nullptr, C, g.nx / kPartSeg};
+    k_par_fwd8<<<(g.nx + C - 1) / C, C * g.ny / 16, (size_t)C * g.ny * sizeof(double), st>>>(a);
+  } else {
+    const int C = par_cols(g);
+    const ParArgs a{g, s, ux, uy, spec, nullptr, C, g.nx / kPartSeg};
+    k_par_fwd<<<(g.nx + C - 1) / C, par_threads(g, C), (size_t)C * g.ny * sizeof(double), st>>>(a);
+  }
   count_launches(1);
   return cudaGetLastError();
 }
@@ -657,9 +792,16 @@ cudaError_t launch_par_cn(bool columns, ParCnArgs a, cudaStream_t st) {
 
 cudaError_t launch_par_bwd(const DevGrid &g, const StageScalars &s, const double2 *spec, double *psi,
                            cudaStream_t st) {
-  const int C = par_cols(g);
-  const ParArgs a{g, s, nullptr, nullptr, const_cast<double2 *>(spec), psi, C, g.nx / kPartSeg};
-  k_par_bwd<<<(g.nx + C - 1) / C, par_threads(g, C), (size_t)C * g.ny * sizeof(double), st>>>(a);
+  par_dft_attributes();
+  if (par_fft8(g)) {
+    const int C = par_cols8(g);
+    const ParArgs a{g, s, nullptr, nullptr, const_cast<double2 *>(spec), psi, C, g.nx / kPartSeg};
+    k_par_bwd8<<<(g.nx + C - 1) / C, C * g.ny / 16, (size_t)C * g.ny * sizeof(double), st>>>(a);
+  } else {
+    const int C = par_cols(g);
+    const ParArgs a{g, s, nullptr, nullptr, const_cast<double2 *>(spec), psi, C, g.nx / kPartSeg};
+    k_par_bwd<<<(g.nx + C - 1) / C, par_threads(g, C), (size_t)C * g.ny * sizeof(double), st>>>(a);
+  }
   count_launches(1);
   return cudaGetLastError();
 }
