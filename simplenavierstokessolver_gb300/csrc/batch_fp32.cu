@@ -25,6 +25,7 @@
 
 #include "batch_internal.h"
 #include "fft_dev.cuh"
+#include "fft_stockham.cuh"
 
 namespace sns {
 namespace {
@@ -369,6 +370,12 @@ __global__ void __launch_bounds__(kBTileXMax) k_b_stencil(const BCase *__restric
 }
 
 // ------------------------------------------------------------------- Poisson
+// The column DFTs run the radix-8 Stockham FFT (fft_stockham.cuh, 8 values
+// per thread) where the block's threads cover the column group that way, the
+// radix-2/4 stages otherwise (the block size is set by the largest case of
+// the batch)
+__device__ __forceinline__ bool stockham8(int M, int nc) { return M >= 8 && nc * M <= 8 * (int)blockDim.x; }
+
 // FP64 divergence of the FP32 predicted velocity (src/fluid/compute_potential.c:74-86)
 // and the forward real DFT along y of `fcols` columns.
 // the block's column group x0 .. x0+fcols-1 (every thread of the block)
@@ -382,6 +389,7 @@ __device__ __forceinline__ void fwd_cols(const BCase &C, int x0, int rk, double2
   const double rgdt = C.rgdt[rk], rdy = C.rdy;
   const F2 rg2 = ff(rgdt);
   double *zd = reinterpret_cast<double *>(zs);
+  const bool s8 = stockham8(M, nc);
   for (int e = threadIdx.x; e < nc * ny; e += blockDim.x) {
     const int c = e % nc, y = e / nc, x = x0 + c;
     double d = 0.0;
@@ -400,15 +408,25 @@ __device__ __forceinline__ void fwd_cols(const BCase &C, int x0, int rk, double2
         d = rgdt * ((double)dux * C.rdxf[x] + (double)duy * rdy);
       }
     }
-    zd[2 * (c * M + fft::fft_slot(y >> 1, M, C.fft_nst, C.fft_first2)) + (y & 1)] = d;
+    const int m = y >> 1;
+    zd[2 * (c * M + (s8 ? fft8::swz(m) : fft::fft_slot(m, M, C.fft_nst, C.fft_first2))) + (y & 1)] = d;
   }
   __syncthreads();
   const double2 *tw = reinterpret_cast<const double2 *>(C.tw);
-  fft::fft_stages<true>(zs, nc, M, ny, C.fft_nst, C.fft_first2, tw);
+  if (s8) {
+    fft8::transform<true, 1>(zs, nc, M, tw);
+  } else {
+    fft::fft_stages<true>(zs, nc, M, ny, C.fft_nst, C.fft_first2, tw);
+  }
   const int half = M / 2 + 1;
   for (int e = threadIdx.x; e < nc * half; e += blockDim.x) {
     const int c = e % nc, k = e / nc, x = x0 + c;
-    if (x < nx) fft::rfft_post(zs + c * M, C.spec + x, M, k, tw, (size_t)nx);
+    if (x >= nx) continue;
+    if (s8) {
+      fft8::rfft_post(zs + c * M, C.spec + x, M, k, tw, (size_t)nx);
+    } else {
+      fft::rfft_post(zs + c * M, C.spec + x, M, k, tw, (size_t)nx);
+    }
   }
 }
 
@@ -425,24 +443,34 @@ __global__ void __launch_bounds__(256) k_b_fwd(const BCase *__restrict__ cases, 
 __device__ __forceinline__ void bwd_cols(const BCase &C, int x0, double2 *zs) {
   const int nx = C.nx, ny = C.ny, M = ny / 2, nc = C.fcols;
   const double2 *tw = reinterpret_cast<const double2 *>(C.tw);
+  const bool s8 = stockham8(M, nc);
   const int half = M / 2 + 1;
   for (int e = threadIdx.x; e < nc * half; e += blockDim.x) {
     const int c = e % nc, k = e / nc, x = x0 + c;
     double2 *zc = zs + c * M;
     if (x >= nx) {
-      zc[fft::fft_slot(k, M, C.fft_nst, C.fft_first2)] = make_double2(0.0, 0.0);
-      if (k > 0) zc[fft::fft_slot(M - k, M, C.fft_nst, C.fft_first2)] = make_double2(0.0, 0.0);
+      zc[s8 ? fft8::swz(k) : fft::fft_slot(k, M, C.fft_nst, C.fft_first2)] = make_double2(0.0, 0.0);
+      if (k > 0) zc[s8 ? fft8::swz(M - k) : fft::fft_slot(M - k, M, C.fft_nst, C.fft_first2)] = make_double2(0.0, 0.0);
       continue;
     }
-    fft::rfft_pre(C.spec + x, zc, M, k, tw, C.fft_nst, C.fft_first2, (size_t)nx);
+    if (s8) {
+      fft8::rfft_pre(C.spec + x, zc, M, k, tw, (size_t)nx);
+    } else {
+      fft::rfft_pre(C.spec + x, zc, M, k, tw, C.fft_nst, C.fft_first2, (size_t)nx);
+    }
   }
   __syncthreads();
-  fft::fft_stages<false>(zs, nc, M, ny, C.fft_nst, C.fft_first2, tw);
+  if (s8) {
+    fft8::transform<false, 1>(zs, nc, M, tw);
+  } else {
+    fft::fft_stages<false>(zs, nc, M, ny, C.fft_nst, C.fft_first2, tw);
+  }
   const double *zd = reinterpret_cast<const double *>(zs);
   const double rny = 1.0 / ny;
   for (int e = threadIdx.x; e < nc * ny; e += blockDim.x) {
     const int c = e % nc, y = e / nc, x = x0 + c;
-    if (x < nx) C.psi[(size_t)y * nx + x] = zd[2 * (c * M + (y >> 1)) + (y & 1)] * rny;
+    const int m = y >> 1;
+    if (x < nx) C.psi[(size_t)y * nx + x] = zd[2 * (c * M + (s8 ? fft8::swz(m) : m)) + (y & 1)] * rny;
   }
 }
 

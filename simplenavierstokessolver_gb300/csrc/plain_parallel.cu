@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(512) k_par_fwd8(const ParArgs a) {
     z[c * M + fft8::swz(mm)] = d;
   }
   __syncthreads();
-  fft8::transform<true>(z, M, tw);
+  fft8::transform<true, 1>(z, C, M, tw);
   // split step for the bin pair (k, M-k): 2 X[k] = (Z[k] + conj Z[M-k]) +
   // w^k (Z[k] - conj Z[M-k]) / i, w = exp(-2 pi i / jtot)
   const int half = M / 2 + 1;
@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(512) k_par_bwd8(const ParArgs a) {
     }
   }
   __syncthreads();
-  fft8::transform<false>(z, M, tw);
+  fft8::transform<false, 1>(z, C, M, tw);
   const double scale = a.s.rgdt * (0.5 * a.s.rny);
   for (int e = threadIdx.x; e < C * M; e += blockDim.x) {
     const int c = e % C, mm = e / C, x = x0 + c;
