@@ -84,10 +84,11 @@ PROFILED_TRAFFIC = {
 
 # FP64 instructions per cell of the parallel form's kernels on a uniform
 # power-of-two grid (DADD + DMUL + DFMA thread instructions counted by ncu at
-# 512 x 1024: profiles/plain_parallel_fp64_counts_512x1024.md; the DFT
-# counts grow with log2(jtot))
-PARALLEL_FP64_OPS = {"velocity_update": 47.5, "temperature_update": 17.0, "poisson_forward_fft": 23.5,
-                     "poisson_pcr": 5.4, "poisson_inverse_fft": 19.0, "correct_and_pressure": 9.0}
+# 512 x 1024: profiles/plain_parallel_fp64_counts_512x1024.md; the temperature
+# update's mean over the three substages, the first of which has no previous
+# source; the DFT counts grow with log2(jtot))
+PARALLEL_FP64_OPS = {"velocity_update": 47.45, "temperature_update": 17.17, "poisson_forward_fft": 20.63,
+                     "poisson_pcr": 5.39, "poisson_inverse_fft": 17.75, "correct_and_pressure": 9.0}
 
 # algorithmic DRAM bytes per cell of the plain path's implicit-scheme
 # launches (2048 x 4096 at Ra 1e10): each Crank-Nicolson launch solves the
