@@ -412,6 +412,23 @@ def large_instance(args, torch, nx=2048, ny=4096, Ra=1e10, steps=500, acc_steps=
             lib.sns_profile(c.fluid, 0)
             kernels = {lib.sns_profile_kind_name(k).decode(): round(1e3 * kms[k] / kcnt[k], 1)
                        for k in range(n) if kcnt[k]}
+        # per-kernel times of implicit steps (Crank-Nicolson in x and y): the
+        # first steps of a fresh case, profiled; the timed run above is not touched
+        with Case(nx, ny, ly=2.0, Ra=Ra, Pr=1.0) as c:
+            lib = c.lib
+            c.set_form(form == "parallel")
+            c.run(3)
+            lib.sns_profile(c.fluid, 1)
+            c.run(2)
+            c.synchronize()
+            dimp = c.get_dt()
+            kms = (ctypes.c_double * 32)()
+            kcnt = (ctypes.c_longlong * 32)()
+            n = lib.sns_profile_read(c.fluid, kms, kcnt, 32)
+            lib.sns_profile(c.fluid, 0)
+            kernels_imp = {lib.sns_profile_kind_name(k).decode(): round(1e3 * kms[k] / kcnt[k], 1)
+                           for k in range(n) if kcnt[k]}
+            scheme_imp = (dimp["implicitx"], dimp["implicity"])
         kgbs = {}
         for k, us in kernels.items():
             bpc = IMPLICIT_MODEL.get(k, KERNEL_MODEL.get(k, (None,))[0])
@@ -427,7 +444,9 @@ def large_instance(args, torch, nx=2048, ny=4096, Ra=1e10, steps=500, acc_steps=
             "implicit_steps": int(imp.sum()), "explicit_steps": int((~imp).sum()),
             "ms_step_implicit_median": float(np.median(per[imp])) if imp.any() else None,
             "ms_step_explicit_median": float(np.median(per[~imp])) if (~imp).any() else None,
-            "kernel_avg_us": kernels, "kernel_hbm": kgbs, "hbm_peak_gbs": peak}
+            "kernel_avg_us": kernels, "kernel_hbm": kgbs, "hbm_peak_gbs": peak,
+            "kernel_avg_us_implicit": {"scheme_xy": list(scheme_imp), "steps": "4 and 5 of a fresh case",
+                                       "kernels": kernels_imp}}
     for name, comp in (("fp32_stencil", False), ("fp32_compensated", True)):
         with Batch(16 << 30) as b:
             s = b.add(Desc(nx, ny, ly=2.0, Ra=Ra, Pr=1.0, compensated=comp))
