@@ -456,204 +456,236 @@ __global__ void __launch_bounds__(32 * kParWarpsMax) k_par_tri(const ParTriArgs 
 // (rows of a field, wall-bounded: src/temperature/update.c:141-157,
 // src/fluid/update_velocity.c:249-280 and :500-520) and src/linalg.c:52-108
 // along y (columns, periodic: src/temperature/update.c:189-207,
-// src/fluid/update_velocity.c:404-430). One warp per line, one lane per
-// segment of m = n / 32 rows; the line is gathered into shared memory with
-// each segment at a stride s = m | 1 (odd, so that the 32 lanes' accesses at
-// one row fall on distinct bank pairs). The periodic lines' interface
-// system is cyclic: its PCR levels shuffle modulo 32. All RHS-independent
-// factors are computed on the host per substage (they depend on dt).
+// src/fluid/update_velocity.c:404-430). A line of n rows is cut into 32
+// segments of m = n / 32 rows; a periodic line's interface system is
+// cyclic (its PCR levels couple modulo 32). All RHS-independent factors are
+// computed on the host per substage (they depend on dt). Both kernels do
+// the same operations on every element, in the same order.
 
 constexpr int kCnWarpsMax = 8;
-constexpr int kCnLoad = 8;  // elements in flight per thread while gathering a line
+constexpr int kCnLoad = 8;  // elements in flight per thread while gathering a row
 
-// a field's line block: inv g up v w (interleaved rows), alpha beta (PCR
-// levels), rD, then the interface rows' sub- and super-diagonals
+// factor block of a field's lines: inv g up v w (rows interleaved: row r of
+// segment k at r * 32 + k), alpha beta (PCR levels), rD, then the interface
+// rows' sub- and super-diagonals
+struct CnFac {
+  const double *inv, *gg, *up, *vv, *ww, *alpha, *beta, *rD, *ae, *ce;
+  __device__ __forceinline__ CnFac(const double *f, int n)
+      : inv(f), gg(f + n), up(f + 2 * n), vv(f + 3 * n), ww(f + 4 * n), alpha(f + 5 * (size_t)n),
+        beta(alpha + kPartLevels * kPartSeg), rD(beta + kPartLevels * kPartSeg), ae(rD + kPartSeg),
+        ce(ae + kPartSeg) {}
+};
+
+__device__ __forceinline__ ParCnField cn_field(const ParCnArgs &a) {
+  // a select, not an index into the parameter array (which would copy the
+  // array to the stack)
+  return blockIdx.y == 0 ? a.f[0] : blockIdx.y == 1 ? a.f[1] : a.f[2];
+}
+
 __device__ __forceinline__ int cn_pos(int e, int m, int s) {
   const int k = e / m;
   return k * s + (e - k * m);
 }
 
-// COLUMNS: periodic lines along y (element stride nx, adjacent lines
-// adjacent in memory: a block gathers its lines together, a 32-byte sector
-// holding 4 of them); otherwise lines along x (contiguous rows, gathered per
-// warp, coalesced).
-template <bool COLUMNS>
+// Rows along x (wall-bounded): one warp per row, one lane per segment; the
+// row is gathered into shared memory with each segment at a stride s = m | 1
+// (odd, so that the 32 lanes' accesses at one row fall on distinct bank
+// pairs), solved there and written back, coalesced both ways.
 __global__ void __launch_bounds__(32 * kCnWarpsMax) k_par_cn(const ParCnArgs a) {
   extern __shared__ __align__(16) double cn_sm[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-  // the field by a select, not an index into the parameter array (which
-  // would copy the array to the stack)
-  const ParCnField F = blockIdx.y == 0 ? a.f[0] : blockIdx.y == 1 ? a.f[1] : a.f[2];
+  const ParCnField F = cn_field(a);
   const int n = a.n, m = a.m, s = a.s;
-  const int line0 = F.first + blockIdx.x * wpb, line = line0 + w;
-  const bool live = line < a.lines;
-  const size_t wstride = (size_t)kPartSeg * s + 8;  // per warp: 8 doubles apart in bank pairs
-  double *sl = cn_sm + (size_t)w * wstride;
-  if constexpr (COLUMNS) {
-    // block-wide gather: thread t takes line t % wpb, row t / wpb (+ rows
-    // per pass), so a warp reads whole sectors of wpb adjacent columns
-    const int per = blockDim.x / wpb;
-    const int c = threadIdx.x % wpb, r0 = threadIdx.x / wpb;
-    const bool lc = line0 + c < a.lines;
-    const double *src = F.q + (line0 + c);
-    double *dst = cn_sm + (size_t)c * wstride;
-    for (int e0 = r0; e0 < n; e0 += per * kCnLoad) {
-      double v[kCnLoad];
+  const int line = F.first + blockIdx.x * wpb + w;
+  if (line >= a.lines) return;  // the whole warp
+  double *sl = cn_sm + (size_t)w * ((size_t)kPartSeg * s + 8);
+  const double *src = F.q + (size_t)line * a.ls;
+  for (int e0 = lane; e0 < n; e0 += 32 * kCnLoad) {
+    double v[kCnLoad];
 #pragma unroll
-      for (int k = 0; k < kCnLoad; ++k) {
-        const int e = e0 + k * per;
-        v[k] = (lc && e < n) ? src[(size_t)e * a.es] : 0.0;
-      }
-#pragma unroll
-      for (int k = 0; k < kCnLoad; ++k) {
-        const int e = e0 + k * per;
-        if (lc && e < n) dst[cn_pos(e, m, s)] = v[k];
-      }
+    for (int k = 0; k < kCnLoad; ++k) {
+      const int e = e0 + 32 * k;
+      v[k] = e < n ? src[e] : 0.0;
     }
-    __syncthreads();
-  } else {
-    if (!live) return;  // the whole warp: rows are gathered per warp
-    const double *src = F.q + (size_t)line * a.ls;
-    for (int e0 = lane; e0 < n; e0 += 32 * kCnLoad) {
-      double v[kCnLoad];
 #pragma unroll
-      for (int k = 0; k < kCnLoad; ++k) {
-        const int e = e0 + 32 * k;
-        v[k] = e < n ? src[e] : 0.0;
-      }
-#pragma unroll
-      for (int k = 0; k < kCnLoad; ++k) {
-        const int e = e0 + 32 * k;
-        if (e < n) sl[cn_pos(e, m, s)] = v[k];
-      }
+    for (int k = 0; k < kCnLoad; ++k) {
+      const int e = e0 + 32 * k;
+      if (e < n) sl[cn_pos(e, m, s)] = v[k];
     }
-    __syncwarp();
   }
+  __syncwarp();
+  const CnFac f(F.fac, n);
+  double *seg = sl + lane * s;
+  // 1) interior rows r = 0 .. m-2 with zero interface values:
+  //    y_r = inv_r q_r - g_r y_{r-1}, then y_r -= up_r y_{r+1}
+  double y = seg[0] * __ldg(f.inv + lane);
+  seg[0] = y;
+  double ci[kParChunk], cg[kParChunk];
+#pragma unroll
+  for (int k = 0; k < kParChunk; ++k) {
+    const int r = 1 + k, i = r * kPartSeg + lane;
+    ci[k] = r < m - 1 ? __ldg(f.inv + i) : 0.0;
+    cg[k] = r < m - 1 ? __ldg(f.gg + i) : 0.0;
+  }
+#pragma unroll 1
+  for (int b = 1; b < m - 1; b += kParChunk) {
+    double ni[kParChunk], ng[kParChunk];
+#pragma unroll
+    for (int k = 0; k < kParChunk; ++k) {
+      const int r = b + kParChunk + k, i = r * kPartSeg + lane;
+      ni[k] = r < m - 1 ? __ldg(f.inv + i) : 0.0;
+      ng[k] = r < m - 1 ? __ldg(f.gg + i) : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < kParChunk; ++k) {
+      const int r = b + k;
+      if (r < m - 1) {
+        y = fma(-cg[k], y, ci[k] * seg[r]);
+        seg[r] = y;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kParChunk; ++k) {
+      ci[k] = ni[k];
+      cg[k] = ng[k];
+    }
+  }
+  const double ylast = y;  // row m-2
+  double cu[kParChunk];
+#pragma unroll
+  for (int k = 0; k < kParChunk; ++k) {
+    const int r = m - 3 - k;
+    cu[k] = r >= 0 ? __ldg(f.up + r * kPartSeg + lane) : 0.0;
+  }
+#pragma unroll 1
+  for (int b = m - 3; b >= 0; b -= kParChunk) {
+    double nu[kParChunk];
+#pragma unroll
+    for (int k = 0; k < kParChunk; ++k) {
+      const int r = b - kParChunk - k;
+      nu[k] = r >= 0 ? __ldg(f.up + r * kPartSeg + lane) : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < kParChunk; ++k) {
+      const int r = b - k;
+      if (r >= 0) {
+        y = fma(-cu[k], y, seg[r]);
+        seg[r] = y;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kParChunk; ++k) cu[k] = nu[k];
+  }
+  // 2) interface row e of segment k: q_e - a_e y_{e-1} - c_e y'_0 (the next
+  //    segment's first interior value; c_e = 0 for the last segment)
+  const double ynext = __shfl_sync(0xffffffffu, y, (lane + 1) & 31);
+  double R = fma(-__ldg(f.ce + lane), ynext, fma(-__ldg(f.ae + lane), ylast, seg[m - 1]));
+  // 3) PCR of the 32 interface equations; the host zeroes the couplings
+  //    past the ends of the line
+#pragma unroll
+  for (int lev = 0; lev < kPartLevels; ++lev) {
+    const int d = 1 << lev;
+    const double rm = __shfl_sync(0xffffffffu, R, (lane - d) & 31);
+    const double rp = __shfl_sync(0xffffffffu, R, (lane + d) & 31);
+    R = fma(__ldg(f.beta + lev * kPartSeg + lane), rp, fma(__ldg(f.alpha + lev * kPartSeg + lane), rm, R));
+  }
+  const double xe = R * __ldg(f.rD + lane);
+  seg[m - 1] = xe;
+  // 4) interiors: x_r = y_r + v_r x_{e(k-1)} + w_r x_{e(k)} (v = 0 in the
+  //    first segment)
+  const double xl = __shfl_sync(0xffffffffu, xe, (lane - 1) & 31);
+#pragma unroll 1
+  for (int b = 0; b < m - 1; b += kParChunk) {
+    double cv[kParChunk], cw[kParChunk];
+#pragma unroll
+    for (int k = 0; k < kParChunk; ++k) {
+      const int r = b + k, i = r * kPartSeg + lane;
+      cv[k] = r < m - 1 ? __ldg(f.vv + i) : 0.0;
+      cw[k] = r < m - 1 ? __ldg(f.ww + i) : 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < kParChunk; ++k) {
+      const int r = b + k;
+      if (r < m - 1) seg[r] = fma(cw[k], xe, fma(cv[k], xl, seg[r]));
+    }
+  }
+  __syncwarp();
+  double *dstq = F.q + (size_t)line * a.ls;
+  for (int e = lane; e < n; e += 32) dstq[e] = sl[cn_pos(e, m, s)];
+}
+
+// Columns along y (periodic): a block takes kCnCols adjacent columns and
+// all 32 segments of each, thread t column t % kCnCols and segment
+// t / kCnCols, and walks its segment in place in global memory; a warp's
+// access covers 8 rows of kCnCols columns (whole 32-byte sectors). The
+// first interior values, the interface right-hand sides and the interface
+// solutions pass between the threads of a column through shared memory;
+// warp c solves column c's cyclic interface system with lane = segment.
+// Same operations on every element as k_par_cn.
+constexpr int kCnCols = 4;
+
+__global__ void __launch_bounds__(32 * kCnCols) k_par_cn_cols(const ParCnArgs a) {
+  __shared__ double ex[3][kCnCols][kPartSeg];
+  const ParCnField F = cn_field(a);
+  const int n = a.n, m = a.m;
+  const int c = threadIdx.x % kCnCols, k = threadIdx.x / kCnCols;
+  const int col = F.first + blockIdx.x * kCnCols + c;
+  const bool live = col < a.lines;
+  const size_t es = (size_t)a.es;
+  double *q = F.q + (live ? col : 0);
+  const CnFac f(F.fac, n);
+  const size_t e0 = (size_t)k * m;  // first row of the segment
+  double y = 0.0, ylast = 0.0;
   if (live) {
-    const double *inv = F.fac, *gg = inv + n, *up = inv + 2 * n, *vv = inv + 3 * n, *ww = inv + 4 * n;
-    const double *alpha = inv + 5 * (size_t)n, *beta = alpha + kPartLevels * kPartSeg;
-    const double *rD = beta + kPartLevels * kPartSeg, *ae = rD + kPartSeg, *ce = ae + kPartSeg;
-    double *seg = sl + lane * s;
-    // 1) interior rows r = 0 .. m-2 with zero interface values:
-    //    y_r = inv_r q_r - g_r y_{r-1}, then y_r -= up_r y_{r+1}
-    double y = seg[0] * __ldg(inv + lane);
-    seg[0] = y;
-    double ci[kParChunk], cg[kParChunk];
-#pragma unroll
-    for (int k = 0; k < kParChunk; ++k) {
-      const int r = 1 + k, i = r * kPartSeg + lane;
-      ci[k] = r < m - 1 ? __ldg(inv + i) : 0.0;
-      cg[k] = r < m - 1 ? __ldg(gg + i) : 0.0;
+    // 1) interior rows r = 0 .. m-2: forward elimination, back substitution
+    y = q[e0 * es] * __ldg(f.inv + k);
+    q[e0 * es] = y;
+#pragma unroll 4
+    for (int r = 1; r < m - 1; ++r) {
+      const size_t o = (e0 + r) * es;
+      y = fma(-__ldg(f.gg + r * kPartSeg + k), y, __ldg(f.inv + r * kPartSeg + k) * q[o]);
+      q[o] = y;
     }
-#pragma unroll 1
-    for (int b = 1; b < m - 1; b += kParChunk) {
-      double ni[kParChunk], ng[kParChunk];
-#pragma unroll
-      for (int k = 0; k < kParChunk; ++k) {
-        const int r = b + kParChunk + k, i = r * kPartSeg + lane;
-        ni[k] = r < m - 1 ? __ldg(inv + i) : 0.0;
-        ng[k] = r < m - 1 ? __ldg(gg + i) : 0.0;
-      }
-#pragma unroll
-      for (int k = 0; k < kParChunk; ++k) {
-        const int r = b + k;
-        if (r < m - 1) {
-          y = fma(-cg[k], y, ci[k] * seg[r]);
-          seg[r] = y;
-        }
-      }
-#pragma unroll
-      for (int k = 0; k < kParChunk; ++k) {
-        ci[k] = ni[k];
-        cg[k] = ng[k];
-      }
+    ylast = y;
+#pragma unroll 4
+    for (int r = m - 3; r >= 0; --r) {
+      const size_t o = (e0 + r) * es;
+      y = fma(-__ldg(f.up + r * kPartSeg + k), y, q[o]);
+      q[o] = y;
     }
-    const double ylast = y;  // row m-2
-    double cu[kParChunk];
-#pragma unroll
-    for (int k = 0; k < kParChunk; ++k) {
-      const int r = m - 3 - k;
-      cu[k] = r >= 0 ? __ldg(up + r * kPartSeg + lane) : 0.0;
-    }
-#pragma unroll 1
-    for (int b = m - 3; b >= 0; b -= kParChunk) {
-      double nu[kParChunk];
-#pragma unroll
-      for (int k = 0; k < kParChunk; ++k) {
-        const int r = b - kParChunk - k;
-        nu[k] = r >= 0 ? __ldg(up + r * kPartSeg + lane) : 0.0;
-      }
-#pragma unroll
-      for (int k = 0; k < kParChunk; ++k) {
-        const int r = b - k;
-        if (r >= 0) {
-          y = fma(-cu[k], y, seg[r]);
-          seg[r] = y;
-        }
-      }
-#pragma unroll
-      for (int k = 0; k < kParChunk; ++k) cu[k] = nu[k];
-    }
-    // 2) interface row e of segment k: q_e - a_e y_{e-1} - c_e y'_0 (the next
-    //    segment's first interior value; cyclically for periodic lines, and
-    //    c_e = 0 for the last segment of a wall-bounded line)
-    const double ynext = __shfl_sync(0xffffffffu, y, (lane + 1) & 31);
-    double R = fma(-__ldg(ce + lane), ynext, fma(-__ldg(ae + lane), ylast, seg[m - 1]));
-    // 3) PCR of the 32 interface equations; the host zeroes the couplings
-    //    past the ends of a wall-bounded line
+  }
+  ex[0][c][k] = y;  // the segment's first interior value
+  __syncthreads();
+  // 2) interface row e of segment k (the next segment cyclically)
+  double R = 0.0;
+  if (live) {
+    const double ynext = ex[0][c][(k + 1) & 31];
+    R = fma(-__ldg(f.ce + k), ynext, fma(-__ldg(f.ae + k), ylast, q[(e0 + m - 1) * es]));
+  }
+  ex[1][c][k] = R;
+  __syncthreads();
+  // 3) PCR: warp w takes column w, lane = segment
+  {
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double Rw = ex[1][w][lane];
 #pragma unroll
     for (int lev = 0; lev < kPartLevels; ++lev) {
       const int d = 1 << lev;
-      const double rm = __shfl_sync(0xffffffffu, R, (lane - d) & 31);
-      const double rp = __shfl_sync(0xffffffffu, R, (lane + d) & 31);
-      R = fma(__ldg(beta + lev * kPartSeg + lane), rp, fma(__ldg(alpha + lev * kPartSeg + lane), rm, R));
+      const double rm = __shfl_sync(0xffffffffu, Rw, (lane - d) & 31);
+      const double rp = __shfl_sync(0xffffffffu, Rw, (lane + d) & 31);
+      Rw = fma(__ldg(f.beta + lev * kPartSeg + lane), rp, fma(__ldg(f.alpha + lev * kPartSeg + lane), rm, Rw));
     }
-    const double xe = R * __ldg(rD + lane);
-    seg[m - 1] = xe;
-    // 4) interiors: x_r = y_r + v_r x_{e(k-1)} + w_r x_{e(k)} (v = 0 in the
-    //    first segment of a wall-bounded line)
-    const double xl = __shfl_sync(0xffffffffu, xe, (lane - 1) & 31);
-#pragma unroll 1
-    for (int b = 0; b < m - 1; b += kParChunk) {
-      double cv[kParChunk], cw[kParChunk];
-#pragma unroll
-      for (int k = 0; k < kParChunk; ++k) {
-        const int r = b + k, i = r * kPartSeg + lane;
-        cv[k] = r < m - 1 ? __ldg(vv + i) : 0.0;
-        cw[k] = r < m - 1 ? __ldg(ww + i) : 0.0;
-      }
-#pragma unroll
-      for (int k = 0; k < kParChunk; ++k) {
-        const int r = b + k;
-        if (r < m - 1) seg[r] = fma(cw[k], xe, fma(cv[k], xl, seg[r]));
-      }
-    }
+    ex[2][w][lane] = Rw * __ldg(f.rD + lane);
   }
-  if constexpr (COLUMNS) {
-    __syncthreads();
-    const int per = blockDim.x / wpb;
-    const int c = threadIdx.x % wpb, r0 = threadIdx.x / wpb;
-    if (line0 + c < a.lines) {
-      double *dstq = F.q + (line0 + c);
-      const double *src = cn_sm + (size_t)c * wstride;
-      for (int e0 = r0; e0 < n; e0 += per * kCnLoad) {
-        double v[kCnLoad];
-#pragma unroll
-        for (int k = 0; k < kCnLoad; ++k) {
-          const int e = e0 + k * per;
-          v[k] = e < n ? src[cn_pos(e, m, s)] : 0.0;
-        }
-#pragma unroll
-        for (int k = 0; k < kCnLoad; ++k) {
-          const int e = e0 + k * per;
-          if (e < n) dstq[(size_t)e * a.es] = v[k];
-        }
-      }
-    }
-  } else {
-    __syncwarp();
-    double *dstq = F.q + (size_t)line * a.ls;
-    for (int e = lane; e < n; e += 32) dstq[e] = sl[cn_pos(e, m, s)];
+  __syncthreads();
+  if (!live) return;
+  // 4) interiors from the spikes
+  const double xe = ex[2][c][k], xl = ex[2][c][(k - 1) & 31];
+  q[(e0 + m - 1) * es] = xe;
+#pragma unroll 4
+  for (int r = 0; r < m - 1; ++r) {
+    const size_t o = (e0 + r) * es;
+    q[o] = fma(__ldg(f.ww + r * kPartSeg + k), xe, fma(__ldg(f.vv + r * kPartSeg + k), xl, q[o]));
   }
 }
 
@@ -769,22 +801,22 @@ bool parallel_cn_supported(int n) {
 cudaError_t launch_par_cn(bool columns, ParCnArgs a, cudaStream_t st) {
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(k_par_cn<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kParSmemMax);
-    cudaFuncSetAttribute(k_par_cn<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kParSmemMax);
+    cudaFuncSetAttribute(k_par_cn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kParSmemMax);
     attr = true;
   }
   if (!parallel_cn_supported(a.n) || a.nf < 1 || a.nf > 3) return cudaErrorInvalidValue;
   a.m = a.n / kPartSeg;
   a.s = a.m | 1;
-  const size_t per = cn_warp_doubles(a.n) * sizeof(double);
-  // warps (lines) per block: two blocks per SM where the lines fit
-  int wpb = (int)std::min<size_t>(kCnWarpsMax, (kParSmemMax / 2) / per);
-  if (wpb < 1) wpb = 1;
-  const dim3 grid((a.lines + wpb - 1) / wpb, a.nf);
   if (columns) {
-    k_par_cn<true><<<grid, 32 * wpb, wpb * per, st>>>(a);
+    const dim3 grid((a.lines + kCnCols - 1) / kCnCols, a.nf);
+    k_par_cn_cols<<<grid, 32 * kCnCols, 0, st>>>(a);
   } else {
-    k_par_cn<false><<<grid, 32 * wpb, wpb * per, st>>>(a);
+    const size_t per = cn_warp_doubles(a.n) * sizeof(double);
+    // warps (rows) per block: two blocks per SM where the rows fit
+    int wpb = (int)std::min<size_t>(kCnWarpsMax, (kParSmemMax / 2) / per);
+    if (wpb < 1) wpb = 1;
+    const dim3 grid((a.lines + wpb - 1) / wpb, a.nf);
+    k_par_cn<<<grid, 32 * wpb, wpb * per, st>>>(a);
   }
   count_launches(1);
   return cudaGetLastError();
