@@ -337,14 +337,19 @@ extern int sns_set_fused(const fluid_t *fluid, int on);
  * critical path.
  * SNS_FORM_PARALLEL: the Poisson lines by the partition method with
  * warp-shuffle parallel cyclic reduction (one warp per Fourier mode, one lane
- * per segment of itot/32 rows), and every kernel compiled with fused
- * multiply-adds (fewer FP64 instructions, shorter Crank-Nicolson chains).
- * Results differ from the reference's by rounding, held to 1e-12 relative L2
- * per field after the stated step counts. Needs itot a multiple of 32 in
- * [64, 14048] and a grid on which the mean mode's last Thomas pivot vanishes
- * (uniform grids), otherwise SNS_ERR_UNSUPPORTED and the form is unchanged.
- * The first switch to it computes the factors (host, O(itot * jtot)) and
- * allocates them on the device. */
+ * per segment of itot/32 rows), the Crank-Nicolson lines (src/linalg.c:9-108)
+ * by the same method (32 segments per row or column, the periodic y lines
+ * with a cyclic interface system; the serial sweep where a line is not a
+ * multiple of 32 rows of at least 64), the DFTs by a radix-8 Stockham FFT,
+ * and every other kernel compiled with fused multiply-adds. Results differ
+ * from the reference's by rounding, held to 1e-12 relative L2 per field
+ * after the stated step counts. Needs itot in [64, 14048] and a grid on
+ * which the mean mode's last Thomas pivot vanishes (uniform grids with a
+ * power-of-two itot), otherwise SNS_ERR_UNSUPPORTED and the form is
+ * unchanged. The first switch to it computes the Poisson factors (host,
+ * O(itot * jtot)) and allocates them on the device; the Crank-Nicolson
+ * factors are recomputed on the host every implicit substage (they depend
+ * on dt). */
 #define SNS_FORM_EXACT 0
 #define SNS_FORM_PARALLEL 1
 extern int sns_set_form(const fluid_t *fluid, int form);
