@@ -251,44 +251,50 @@ __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)_
 // while the current chunk is eliminated, off the dependent chain
 constexpr int kParChunk = 8;
 
-// src/fluid/compute_potential.c:109-136 by the partition method: one warp per
-// mode line. The warp's lane 0 moves the line (16 nx bytes) into shared
-// memory with a bulk asynchronous copy (completion on an mbarrier, bounded
-// wait), STAGED: also the mode's factor block; otherwise the factors are read
-// from global memory, coalesced by the interleaved row order, a chunk ahead.
-// The warp solves in shared memory and writes the line back with coalesced
-// stores. Real and imaginary parts see the same real matrix.
+// src/fluid/compute_potential.c:109-136 by the partition method: two warps
+// per mode line, one for its real and one for its imaginary part (both see
+// the same real matrix and never mix, so each part takes the operations it
+// took when one warp carried both). The first warp's lane 0 moves the line
+// (16 nx bytes) into shared memory with a bulk asynchronous copy (completion
+// on an mbarrier both warps wait on, bounded), STAGED: also the mode's factor
+// block; otherwise the factors are read from global memory, coalesced by the
+// interleaved row order, a chunk ahead. Each warp solves its part in shared
+// memory and writes it back.
 template <bool STAGED>
 __global__ void __launch_bounds__(32 * kParWarpsMax) k_par_tri(const ParTriArgs a) {
   extern __shared__ __align__(128) unsigned char sm[];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int J = blockIdx.x * (blockDim.x >> 5) + w;
-  if (J >= a.nh) return;  // the whole warp
+  const int li = w >> 1, comp = w & 1;  // line of the block, part (0 real, 1 imaginary)
+  const int J = blockIdx.x * (blockDim.x >> 6) + li;
+  if (J >= a.nh) return;  // both warps of the line
   const int n = a.nx, m = a.m;
-  const size_t per_warp = 16 * (size_t)n + (STAGED ? 8 * a.stride : 0);
-  double2 *line = reinterpret_cast<double2 *>(sm + 128 + (size_t)w * per_warp);
+  const size_t per_line = 16 * (size_t)n + (STAGED ? 8 * a.stride : 0);
+  double2 *line = reinterpret_cast<double2 *>(sm + 128 + (size_t)li * per_line);
+  double *lc = reinterpret_cast<double *>(line) + comp;  // this part of element i at lc[2 i]
   double *fs = reinterpret_cast<double *>(line + n);
   double2 *gline = a.spec + (size_t)J * n;
   const double *gfac = a.fac + (size_t)J * a.stride;
-  const unsigned bar = smem_u32(reinterpret_cast<unsigned long long *>(sm) + w);
+  const unsigned bar = smem_u32(reinterpret_cast<unsigned long long *>(sm) + li);
   const unsigned line_bytes = 16u * (unsigned)n, fac_bytes = STAGED ? 8u * (unsigned)a.stride : 0u;
-  if (lane == 0) {
+  if (comp == 0 && lane == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(line_bytes + fac_bytes)
                  : "memory");
-  }
-  if (lane == 0 && !a.stale) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(line)),
-                 "l"(__cvta_generic_to_global(gline)), "r"(line_bytes), "r"(bar)
-                 : "memory");
-    if (STAGED)
+    if (!a.stale) {
       asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                       smem_u32(fs)),
-                   "l"(__cvta_generic_to_global(gfac)), "r"(fac_bytes), "r"(bar)
+                       smem_u32(line)),
+                   "l"(__cvta_generic_to_global(gline)), "r"(line_bytes), "r"(bar)
                    : "memory");
+      if (STAGED)
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                         smem_u32(fs)),
+                     "l"(__cvta_generic_to_global(gfac)), "r"(fac_bytes), "r"(bar)
+                     : "memory");
+    }
   }
+  // the line's two warps: the mbarrier is initialised before either waits on it
+  asm volatile("bar.sync %0, 64;" ::"r"(1 + li) : "memory");
   const double *f = STAGED ? fs : gfac;
   auto ld = [&](const double *p) -> double {
     if constexpr (STAGED) {
@@ -310,13 +316,12 @@ __global__ void __launch_bounds__(32 * kParWarpsMax) k_par_tri(const ParTriArgs 
       cg[k] = r < m - 1 ? ld(gg + i) : 0.0;
     }
   }
-  __syncwarp();
   bool done = false;
   for (unsigned k = 0; k < a.spin_limit && !done; ++k) done = mbar_try(bar, 0u);
   if (!done) {
     if (lane == 0) atomicOr(a.err, 1u);
     // leave the line unsolved, but only once the copies issued into this
-    // warp's shared memory have landed (bounded as well)
+    // line's shared memory have landed (bounded as well)
     if (!a.stale)
       for (unsigned k = 0; k < kParDrainSpins && !mbar_try(bar, 0u); ++k) {
       }
@@ -334,13 +339,12 @@ __global__ void __launch_bounds__(32 * kParWarpsMax) k_par_tri(const ParTriArgs 
   //    with zero boundary values: forward elimination and back substitution.
   //    y_r = inv_r q_r - g_r y_{r-1} with g_r = a_r inv_r: one FMA per row on
   //    the dependent chain, the product inv_r q_r off it
-  double2 y = line[lane];
+  double y = lc[2 * lane];
   {
     const double i0 = STAGED ? ld(inv + lane) : inv0;
-    y.x *= i0;
-    y.y *= i0;
+    y *= i0;
   }
-  line[lane] = y;
+  lc[2 * lane] = y;
 #pragma unroll 1
   for (int b = 1; b < m - 1; b += kParChunk) {
     double ni[kParChunk], ng[kParChunk];
@@ -354,10 +358,8 @@ __global__ void __launch_bounds__(32 * kParWarpsMax) k_par_tri(const ParTriArgs 
     for (int k = 0; k < kParChunk; ++k) {
       const int r = b + k, i = r * kPartSeg + lane;
       if (r < m - 1) {
-        double2 q = line[i];
-        q.x = fma(-cg[k], y.x, ci[k] * q.x);
-        q.y = fma(-cg[k], y.y, ci[k] * q.y);
-        line[i] = q;
+        const double q = fma(-cg[k], y, ci[k] * lc[2 * i]);
+        lc[2 * i] = q;
         y = q;
       }
     }
@@ -367,7 +369,7 @@ __global__ void __launch_bounds__(32 * kParWarpsMax) k_par_tri(const ParTriArgs 
       cg[k] = ng[k];
     }
   }
-  const double2 ylast = y;  // row m-2
+  const double ylast = y;  // row m-2
   double cu[kParChunk];
 #pragma unroll
   for (int k = 0; k < kParChunk; ++k) {
@@ -386,10 +388,8 @@ __global__ void __launch_bounds__(32 * kParWarpsMax) k_par_tri(const ParTriArgs 
     for (int k = 0; k < kParChunk; ++k) {
       const int r = b - k, i = r * kPartSeg + lane;
       if (r >= 0) {
-        double2 q = line[i];
-        q.x = fma(-cu[k], y.x, q.x);
-        q.y = fma(-cu[k], y.y, q.y);
-        line[i] = q;
+        const double q = fma(-cu[k], y, lc[2 * i]);
+        lc[2 * i] = q;
         y = q;
       }
     }
@@ -399,34 +399,27 @@ __global__ void __launch_bounds__(32 * kParWarpsMax) k_par_tri(const ParTriArgs 
   // y: the first interior value (row 0). 2) right-hand side of the interface
   // row e: r_e - a_e y_{e-1} - c_e y'_0 (y'_0 of the next segment)
   const int ie = (m - 1) * kPartSeg + lane;
-  const double ynx = __shfl_down_sync(0xffffffffu, y.x, 1);
-  const double yny = __shfl_down_sync(0xffffffffu, y.y, 1);
-  const double2 re = line[ie];
+  const double yn = __shfl_down_sync(0xffffffffu, y, 1);
+  const double re = lc[2 * ie];
   const double ae = __ldg(a.lo + ie), ce = lane < kPartSeg - 1 ? __ldg(a.hi + ie) : 0.0;
-  double Rx = re.x - ae * ylast.x - ce * (lane < kPartSeg - 1 ? ynx : 0.0);
-  double Ry = re.y - ae * ylast.y - ce * (lane < kPartSeg - 1 ? yny : 0.0);
-  if (J == 0 && lane == kPartSeg - 1) {  // the mean mode: last unknown pinned to 0
-    Rx = 0.0;
-    Ry = 0.0;
-  }
+  double R = re - ae * ylast - ce * (lane < kPartSeg - 1 ? yn : 0.0);
+  if (J == 0 && lane == kPartSeg - 1) R = 0.0;  // the mean mode: last unknown pinned to 0
   // 3) parallel cyclic reduction of the 32 interface equations
 #pragma unroll
   for (int lev = 0; lev < kPartLevels; ++lev) {
     const int d = 1 << lev;
-    const double mx = __shfl_up_sync(0xffffffffu, Rx, d), my = __shfl_up_sync(0xffffffffu, Ry, d);
-    const double px = __shfl_down_sync(0xffffffffu, Rx, d), py = __shfl_down_sync(0xffffffffu, Ry, d);
+    const double mv = __shfl_up_sync(0xffffffffu, R, d);
+    const double pv = __shfl_down_sync(0xffffffffu, R, d);
     const double al = ld(alpha + lev * kPartSeg + lane), be = ld(beta + lev * kPartSeg + lane);
-    const double lmx = lane >= d ? mx : 0.0, lmy = lane >= d ? my : 0.0;
-    const double lpx = lane + d < kPartSeg ? px : 0.0, lpy = lane + d < kPartSeg ? py : 0.0;
-    Rx = fma(be, lpx, fma(al, lmx, Rx));
-    Ry = fma(be, lpy, fma(al, lmy, Ry));
+    const double lm = lane >= d ? mv : 0.0;
+    const double lp = lane + d < kPartSeg ? pv : 0.0;
+    R = fma(be, lp, fma(al, lm, R));
   }
-  const double rd = ld(rD + lane);
-  const double xe_x = Rx * rd, xe_y = Ry * rd;
-  line[ie] = make_double2(xe_x, xe_y);
+  const double xe = R * ld(rD + lane);
+  lc[2 * ie] = xe;
   // 4) interiors from the spikes: x_i = y_i + v_i x_{e(k-1)} + w_i x_{e(k)}
-  const double xl_x = __shfl_up_sync(0xffffffffu, xe_x, 1), xl_y = __shfl_up_sync(0xffffffffu, xe_y, 1);
-  const double lx = lane > 0 ? xl_x : 0.0, ly = lane > 0 ? xl_y : 0.0;
+  const double xl = __shfl_up_sync(0xffffffffu, xe, 1);
+  const double lx = lane > 0 ? xl : 0.0;
 #pragma unroll 1
   for (int b = 0; b < m - 1; b += kParChunk) {
     double cv[kParChunk], cw[kParChunk];
@@ -439,16 +432,12 @@ __global__ void __launch_bounds__(32 * kParWarpsMax) k_par_tri(const ParTriArgs 
 #pragma unroll
     for (int k = 0; k < kParChunk; ++k) {
       const int r = b + k, i = r * kPartSeg + lane;
-      if (r < m - 1) {
-        double2 q = line[i];
-        q.x = fma(cw[k], xe_x, fma(cv[k], lx, q.x));
-        q.y = fma(cw[k], xe_y, fma(cv[k], ly, q.y));
-        line[i] = q;
-      }
+      if (r < m - 1) lc[2 * i] = fma(cw[k], xe, fma(cv[k], lx, lc[2 * i]));
     }
   }
   __syncwarp();
-  for (int i = lane; i < n; i += 32) gline[i] = line[i];
+  double *gc = reinterpret_cast<double *>(gline) + comp;
+  for (int i = lane; i < n; i += 32) gc[2 * i] = lc[2 * i];
 }
 
 // ------------------------------------------------------------------------
@@ -772,16 +761,17 @@ cudaError_t launch_par_tri(const DevGrid &g, double2 *spec, const ParFactors &pf
     attr = true;
   }
   const bool staged = par_staged(g.nx, pf.stride);
-  const size_t per_warp = 16 * (size_t)g.nx + (staged ? 8 * pf.stride : 0);
-  const int wpb = par_warps(g.nx, per_warp, g.nh);
-  if (wpb < 1) return cudaErrorInvalidValue;
+  const size_t per_line = 16 * (size_t)g.nx + (staged ? 8 * pf.stride : 0);
+  // mode lines per block, two warps each
+  const int lpb = std::min(par_warps(g.nx, per_line, g.nh), kParWarpsMax / 2);
+  if (lpb < 1) return cudaErrorInvalidValue;
   const ParTriArgs a{spec,  pf.fac, pf.lo, pf.hi, pf.stride, g.nx, g.nh, g.nx / kPartSeg, pf.err, pf.spin_limit,
                      pf.stale};
-  const size_t smem = 128 + (size_t)wpb * per_warp;
+  const size_t smem = 128 + (size_t)lpb * per_line;
   if (staged) {
-    k_par_tri<true><<<(g.nh + wpb - 1) / wpb, 32 * wpb, smem, st>>>(a);
+    k_par_tri<true><<<(g.nh + lpb - 1) / lpb, 64 * lpb, smem, st>>>(a);
   } else {
-    k_par_tri<false><<<(g.nh + wpb - 1) / wpb, 32 * wpb, smem, st>>>(a);
+    k_par_tri<false><<<(g.nh + lpb - 1) / lpb, 64 * lpb, smem, st>>>(a);
   }
   count_launches(1);
   return cudaGetLastError();
