@@ -91,6 +91,7 @@ def test_rayleigh_benard_within_tolerance(nx, ny, Ra, steps):
             o.run(k)
             done += k
         errs = _errors(c, o)
+        print(f"{nx}x{ny} after {steps} steps, relative L2 against the oracle: {errs}")
         assert all(e <= REL_TOL for e in errs.values()), errs
         # dt follows from the velocity, so it agrees to round-off as well
         assert abs(c.get_dt()["dt"] - o.get_dt()["dt"]) <= 1e-12 * o.get_dt()["dt"]
@@ -177,6 +178,7 @@ def test_rayleigh_benard_2048x4096_50_steps_within_tolerance():
         d = c.get_dt()
         assert (d["implicitx"], d["implicity"]) == (1, 1)
         errs = _errors(c, o)
+        print(f"2048x4096 after 50 steps, relative L2 against the oracle: {errs}")
         assert all(e <= REL_TOL for e in errs.values()), errs
 
 
