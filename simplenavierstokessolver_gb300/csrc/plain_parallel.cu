@@ -1,4 +1,4 @@
-// Parallel tridiagonal form of the plain FP64 Poisson solve on GB300.
+// Parallel form of the plain FP64 step's line solves and DFTs on GB300.
 //
 // The reference solves each Fourier mode's x-line with a serial Thomas
 // recurrence (src/fluid/compute_potential.c:109-136, src/linalg.c:32-50).
@@ -6,13 +6,14 @@
 // operations per x, which on GB300 (~70 cycles per dependent FP64 operation)
 // bounds the plain step no matter how many lines run side by side. This
 // form solves the same lines by the partition method with warp-shuffle
-// parallel cyclic reduction (PCR): one warp per mode, one lane per segment of
-// nx/32 rows, a 32-unknown interface system reduced in 5 shuffle levels. All
-// RHS-independent factors (interior Thomas factors, spikes, PCR coefficients)
-// are computed once on the host. Its results differ from the Thomas
-// recurrence by rounding only, so the form is held to the path's tolerance
-// (1e-12 relative L2 per field after the stated step counts) rather than to
-// bit identity, and this unit is compiled with floating-point contraction.
+// parallel cyclic reduction (PCR): a warp per part (real, imaginary) of a
+// mode line, one lane per segment of nx/32 rows, a 32-unknown interface
+// system reduced in 5 shuffle levels. All RHS-independent factors (interior
+// Thomas factors, spikes, PCR coefficients) are computed once on the host.
+// Its results differ from the Thomas recurrence by rounding only, so the
+// form is held to the path's tolerance (1e-12 relative L2 per field after
+// the stated step counts) rather than to bit identity, and this unit is
+// compiled with floating-point contraction.
 //
 // Layout: the spectrum is mode-major, spec[J * nx + p], with the rows of a
 // mode line in the interleaved order p = (x % m) * 32 + x / m (m = nx / 32):
@@ -23,7 +24,8 @@
 // radix-2/4 FFT otherwise.
 //
 // The Crank-Nicolson lines (src/linalg.c:9-108) are solved by the same
-// partition method, one warp per row or column (k_par_cn).
+// partition method: one warp per row along x (k_par_cn), one thread per
+// segment of a column along y (k_par_cn_cols).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -38,7 +40,7 @@
 namespace sns {
 namespace {
 
-constexpr int kParWarpsMax = 8;  // mode lines per block of the PCR kernel
+constexpr int kParWarpsMax = 8;  // warps per block of the PCR kernel (two per mode line)
 constexpr size_t kParSmemMax = 220 * 1024;
 
 struct ParArgs {
@@ -696,9 +698,9 @@ int par_threads(const DevGrid &g, int cols) {
 
 // mode lines per block: enough blocks to spread over the SMs twice, and at
 // least two blocks per SM where the lines' shared memory allows it
-int par_warps(int nx, size_t per_warp, int nh) {
-  const size_t room = 2 * per_warp + 256 <= kParSmemMax ? kParSmemMax / 2 - 128 : kParSmemMax - 128;
-  const int by_smem = (int)std::min<size_t>(kParWarpsMax, room / per_warp);
+int par_lines(int nx, size_t per_line, int nh) {
+  const size_t room = 2 * per_line + 256 <= kParSmemMax ? kParSmemMax / 2 - 128 : kParSmemMax - 128;
+  const int by_smem = (int)std::min<size_t>(kParWarpsMax / 2, room / per_line);
   const int spread = (nh + 2 * 152 - 1) / (2 * 152);
   return std::max(0, std::min(by_smem, std::max(1, spread)));
 }
@@ -763,7 +765,7 @@ cudaError_t launch_par_tri(const DevGrid &g, double2 *spec, const ParFactors &pf
   const bool staged = par_staged(g.nx, pf.stride);
   const size_t per_line = 16 * (size_t)g.nx + (staged ? 8 * pf.stride : 0);
   // mode lines per block, two warps each
-  const int lpb = std::min(par_warps(g.nx, per_line, g.nh), kParWarpsMax / 2);
+  const int lpb = par_lines(g.nx, per_line, g.nh);
   if (lpb < 1) return cudaErrorInvalidValue;
   const ParTriArgs a{spec,  pf.fac, pf.lo, pf.hi, pf.stride, g.nx, g.nh, g.nx / kPartSeg, pf.err, pf.spin_limit,
                      pf.stale};
