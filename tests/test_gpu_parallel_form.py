@@ -49,12 +49,15 @@ def _errors(c, o):
     return {k: rel_l2(g[k], r[k]) for k in STATE}
 
 
-@pytest.mark.parametrize("nx,ny", [(256, 128), (64, 32), (2048, 64)], ids=["256x128", "64x32", "2048x64"])
+@pytest.mark.parametrize("nx,ny", [(256, 128), (64, 32), (2048, 64), (64, 16), (64, 8)],
+                         ids=["256x128", "64x32", "2048x64", "64x16", "64x8"])
 def test_poisson_solve_alone_matches_oracle(nx, ny):
     """one fluid_compute_potential on a seeded divergent velocity: psi
     within round-off of the Thomas solution (segments of 8, 2 and 64 rows;
     itot 2048 reads its factors from global memory, the others stage them
-    in shared memory). The mean mode's line is the Neumann Laplacian, whose
+    in shared memory). The DFTs: radix-8 Stockham passes 8x8 (jtot 128),
+    8x2 (32), 8x4 (64), one radix-8 pass (16), and the radix-2/4 stages
+    below jtot 16 (8). The mean mode's line is the Neumann Laplacian, whose
     condition number grows as itot^2: two solution methods differ by that
     times the rounding, hence the bound (an indexing fault is O(1))."""
     cfg = Config(nx, ny, ly=1.0, Ra=1e7, Pr=1.0)
