@@ -8,16 +8,25 @@ one solver time step: the device max-|u| reduction and dt decision plus the
 three RK substages (temperature, momentum, Poisson, projection, pressure).
 
 Arms:
-  default          the plain FP64 GPU path of libsns_gpu.so (bit-identical to the
-                   reference); inputs resident in HBM; per-step CUDA events on the
-                   solver's stream; L2 flushed (256 MiB write) between timed steps.
+  default          the plain FP64 GPU path of libsns_gpu.so in the form --form
+                   names (default parallel: partition-method line solves and
+                   radix-8 DFTs, within 1e-12 of the reference; exact: the
+                   reference's operations, bit-identical), the other form's
+                   figure beside it; inputs resident in HBM; per-step CUDA
+                   events on the solver's stream; L2 flushed (256 MiB write)
+                   between timed steps.
   --impl reference the CPU oracle (the reference's algorithm restated in C, bit
                    identical to it) on all host cores, same workload and metric.
 
 The JSON line also carries the per-kernel roofline of the dominant kernel
-(CUDA events around each launch, a second pass of the same steps), the CPU
-baseline, an end-to-end number through the C ABI with host buffers, kernel
-launch counts and the SM clocks sampled during the timed region.
+(CUDA events around each launch, a second pass of the same steps) against
+HBM and against the FP64 issue rate measured in the run, the CPU baseline,
+an end-to-end number through the C ABI with host buffers, kernel launch
+counts and the SM clocks sampled during the timed region; beyond the
+headline, the batched FP32 and compensated forms (one case, the 64-case
+ensemble, with accuracy against FP64), the serving stream and the
+2048 x 4096 instance over 500 steps (--plain-only, --large-only and
+--serving-only run parts alone).
 """
 from __future__ import annotations
 
