@@ -75,18 +75,19 @@ KERNEL_MODEL = {
 
 
 # DRAM bytes (read + write) per launch from ncu captures of the default
-# workload; the parallel form's velocity update reads 16.8-25.2 MB per launch
-# (profiles/plain_parallel_fp64_counts_512x1024.md), as the exact form's does
-# workload (profiles/plain_fp64_fused_512x1024_ncu.md for the fused launch and
-# the velocity update, the three-kernel form's from an earlier capture of the
-# same size); keyed by kernel and size
+# workload, keyed by kernel and size: the fused launch from
+# profiles/plain_fp64_fused_512x1024_ncu.md; the velocity update (16.8-25.2 MB
+# per launch in either form; the larger figure is used) and the parallel
+# form's kernels from profiles/plain_parallel_fp64_counts_512x1024.md; the
+# exact form's three-kernel Poisson solve from an earlier capture of the same
+# size
 PROFILED_TRAFFIC = {
     ("poisson_fused", 512, 1024): 29699840 + 19200,  # profiles/plain_fp64_fused_512x1024_ncu.md
     ("poisson_tridiagonal", 512, 1024): 8665344,
     ("velocity_update", 512, 1024): 25210880,
-    ("poisson_forward_fft", 512, 1024): 8429056,
+    ("poisson_forward_fft", 512, 1024): 8440064,
     ("temperature_update", 512, 1024): 12647168,
-    ("poisson_inverse_fft", 512, 1024): 4314880,
+    ("poisson_inverse_fft", 512, 1024): 4249088,
     ("correct_and_pressure", 512, 1024): 16805376,
 }
 
